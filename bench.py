@@ -1,0 +1,295 @@
+"""Benchmark of the quasi-static slice loop (one JSON line on rank 0).
+
+A step is one 3D step of the c2 deck: beam charge deposit, 1024 xi slices with the full
+B-perp predictor-corrector (iter_reltol 1e-6), beam push, and the plasma renewal that
+the reference performs after every 3D step.  The metric's first half, plasma
+particle-pushes/s, is the headline value (one plasma particle advanced through one
+slice, all of its predictor-corrector deposits included); B-perp iterations per slice
+are reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--deck c2] [--precision fp64|mixed]
+
+--impl reference times the reference algorithm's CPU implementation (the project's C
+restatement of it, OpenMP over particles, every host core) on a bounded sample of the
+same deck; the Fortran reference itself cannot be built on these machines.
+Multi-GPU runs are independent replicas (one simulation per GPU, different seeds).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-pushes/s & B⊥ iters/slice: mixed+learned vs plain FP64 @1e-4 err"
+UNIT = "particle-pushes/s"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def _deck(args):
+    from qpad_gb300 import decks
+    return decks.DECKS[args.deck]()
+
+
+def cpu_sample(deck, nslices, steps=1, nthreads=None):
+    """Times the oracle (C restatement of the reference loop, OpenMP over particles) on the
+    first `nslices` slices of the deck with every plasma particle; the beam charge of the
+    whole deck is deposited before the clock starts.  Returns pushes/s and details."""
+    import numpy as np
+
+    import qpad_gb300 as Q
+    from oracle import oracle as O
+    nthreads = nthreads or os.cpu_count()
+    pl, beams = Q.deck_inputs(deck)
+    g = O.grid(deck.nr, deck.nz, deck.max_mode, deck.dr, deck.dxi)
+    x, p, gam, ps, q = pl
+    opl = O.Plasma(len(q))
+    opl.x[:], opl.y[:], opl.px[:], opl.py[:], opl.pz[:] = x[:, 0], x[:, 1], p[:, 0], p[:, 1], p[:, 2]
+    opl.gamma[:], opl.psi[:], opl.q[:] = gam, ps, q
+    sim = O.Sim(g, iter_max=deck.iter_max, iter_reltol=deck.iter_reltol, iter_abstol=deck.iter_abstol,
+                dt3d=deck.dt, sp_npmax=len(q), beams=[(-1.0, O.PUSH3_REDUCED, len(b[2])) for b in beams],
+                nthreads=nthreads)
+    for k, (bx, bp, bq) in enumerate(beams):
+        bm = O.Beam(len(bq))
+        bm.x[:], bm.y[:], bm.z[:], bm.px[:], bm.py[:], bm.pz[:], bm.q[:] = (bx[:, 0], bx[:, 1], bx[:, 2],
+                                                                               bp[:, 0], bp[:, 1], bp[:, 2], bq)
+        sim.set_beam(k, bm)
+    best, iters = None, []
+    for _ in range(steps):
+        sim.set_plasma(opl)
+        sim.begin_3dstep()
+        t0 = time.perf_counter()
+        its = [sim.slice(j)[0] for j in range(1, nslices + 1)]
+        t = time.perf_counter() - t0
+        if best is None or t < best:
+            best, iters = t, its
+    pushes = len(q) * nslices
+    return {"value": pushes / best, "seconds": best, "iters_per_slice": float(np.mean(iters)),
+            "cores": nthreads, "slices": nslices, "particles_per_slice": len(q)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    deck = _deck(args)
+    nslices = args.cpu_slices
+    vals = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        info = cpu_sample(deck, nslices)
+        if k >= args.warmup:
+            vals.append(info["value"])
+    v = statistics.median(vals)
+    sample = (f"first {info['slices']} of {deck.nz} slices of {deck.name}, all {info['particles_per_slice']} "
+              f"plasma particles, full predictor-corrector, beam charge precomputed")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": deck.name, "sample_slices": info["slices"]},
+            "iters_per_slice": info["iters_per_slice"],
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+
+    import qpad_gb300 as Q
+    from qpad_gb300 import _capi as K
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        torch.cuda.set_device(local)
+    deck = _deck(args)
+    deck.seed = deck.seed + 17 * rank          # independent replica per GPU
+    prec = K.PREC_FP64 if args.precision == "fp64" else K.PREC_MIXED
+    inputs = Q.deck_inputs(deck)
+    sim = Q.build_simulation(deck, precision=prec, device=local, inputs=inputs)
+    sp = sim.species[0]
+    npl = len(inputs[0][4])
+    nbeam = sum(len(b[2]) for b in inputs[1])
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up (also fills the caches of the allocator and the factor tables)
+    for _ in range(args.warmup):
+        sp.reset()
+        sim.run_3d_step()
+    barrier()
+    sim.synchronize()
+    sim.profile(True)
+    l0 = sim.launch_count()
+    iters_tot = 0
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            sp.reset()
+            it, _ = sim.run_3d_step()
+            iters_tot += int(it.sum())
+        sim.synchronize()
+        wall = time.perf_counter() - t0
+    launches = sim.launch_count() - l0
+    step_ms, nstep = sim.profile_read("step")
+    amj_ms, namj = sim.profile_read("amjdp")
+    sim.profile(False)
+    dev_s = step_ms / 1e3 if nstep else wall
+    barrier()
+    if dist is not None:
+        import torch
+        tt = torch.tensor([dev_s], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_s = float(tt.item())
+    pushes_step = npl * deck.nz
+    value = world * pushes_step * args.steps / dev_s
+    iters_per_slice = iters_tot / (args.steps * deck.nz)
+
+    # end to end through the C ABI with host buffers: renew from host arrays every step
+    x, p, g, ps, q = inputs[0]
+    h2d = sum(a.nbytes for a in (x, p, g, ps, q))
+    e2e_t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(max(1, args.steps)):
+        sp.renew(x, p, g, ps, q)
+        it, _ = sim.run_3d_step()
+        d2h += int(it.sum()) * 24 + 8
+    e2e_s = time.perf_counter() - e2e_t0
+    e2e_steps = max(1, args.steps)
+    e2e = world * pushes_step * e2e_steps / e2e_s
+
+    peak, peak_kind = _peaks()
+    bytes_per_particle = 64   # FP64 amjdp: reads x, y, px, py, pz, q; writes gamma, psi
+    amj_avg_s = (amj_ms / 1e3) / max(namj, 1)
+    achieved = bytes_per_particle * npl / amj_avg_s / 1e9 if namj else None
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "amjdp_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(args.precision)
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32/f64",
+        "data": "synthetic (seeded deck, no dataset)",
+        "config": {"workload": deck.name, "nr": deck.nr, "nz": deck.nz, "max_mode": deck.max_mode,
+                   "plasma_particles_per_slice": npl, "beam_particles": nbeam, "path": args.precision,
+                   "iter_reltol": deck.iter_reltol, "iter_max": deck.iter_max,
+                   "l2": "step working set above L2 (beam arrays and 3D field stores); per-slice data L2-resident",
+                   "parallelism": f"replicas x{world}"},
+        "iters_per_slice": iters_per_slice,
+        "slices_per_s": world * deck.nz * args.steps / dev_s,
+        "beam_pushes_per_s": world * nbeam * args.steps / dev_s,
+        "wall_s": wall,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h // e2e_steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "k_amjdp", "peak_kind": peak_kind,
+                     "bytes_per_launch": bytes_per_particle * npl, "avg_launch_us": amj_avg_s * 1e6},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_sample(deck, args.cpu_slices)
+        line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": "port",
+                                "sample": f"first {cb['slices']} of {deck.nz} slices of {deck.name}, all "
+                                          f"{cb['particles_per_slice']} plasma particles, OpenMP oracle"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--deck", default="c2")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-slices", type=int, default=48)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

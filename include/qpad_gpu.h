@@ -1,0 +1,210 @@
+/*
+ * qpad_gpu.h -- C ABI of the GB300 (sm_103a) implementation of QPAD's per-xi-slice
+ * quasi-static loop.
+ *
+ * The reference plugs alternative algorithms in by Fortran type extension: a
+ * `simulation_gpu extends simulation` project overrides the type-bound procedures
+ * that run_simulation calls (source/simulation_class.f03:283-510).  Each entry point
+ * below is what such an extension would bind through ISO_C_BINDING in place of one
+ * reference procedure; the procedure it replaces is cited beside it.
+ *
+ * Conventions
+ *  - Every function returns 0 on success or a positive QPAD_E_* code; nothing aborts
+ *    or traps.  qpad_last_error() gives the message for the last failure on a context.
+ *  - The library owns all device memory.  Host buffers stay owned by the caller and
+ *    are only read or written during the call.
+ *  - Host array layouts are the reference's Fortran layouts:
+ *      particles   x(2,np) / x(3,nb) and p(3,np), component fastest; gamma, psi, q (np)
+ *      slice field f1(dim, 0:nr+1) of one mode part, component fastest
+ *    Mode parts are numbered p = 0 (m=0), 2m-1 (Re m), 2m (Im m): the reference's
+ *    rf_re(0:M) / rf_im(1:M) (source/fields/field_class.f03:136-142).
+ *  - One context = one simulation on one GPU and one CUDA stream; a context is used
+ *    from one host thread at a time, like one reference MPI rank.
+ */
+#ifndef QPAD_GPU_H
+#define QPAD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------------- */
+enum {
+  QPAD_OK = 0,
+  QPAD_E_ARG = 1,        /* invalid argument / size */
+  QPAD_E_CUDA = 2,       /* CUDA runtime error (message has the CUDA error string) */
+  QPAD_E_NOMEM = 3,      /* device or host allocation failed */
+  QPAD_E_CAPACITY = 4,   /* particle buffer too small */
+  QPAD_E_STATE = 5       /* call order / missing object */
+};
+
+/* ---- enums mirroring source/param.f03 ------------------------------------------- */
+enum { QPAD_BND_ZERO = 2, QPAD_BND_OPEN = 3 };                     /* param.f03:72-74 */
+enum { QPAD_PUSH2_STD = 0, QPAD_PUSH2_ROBUST = 1 };                /* param.f03:63-64 */
+enum { QPAD_PUSH3_REDUCED = 1, QPAD_PUSH3_BORIS = 2 };             /* param.f03:62 */
+enum { QPAD_COPY_1TO2 = 1, QPAD_COPY_2TO1 = -1 };                  /* param.f03:125 */
+enum { QPAD_PREC_FP64 = 0, QPAD_PREC_MIXED = 1 };
+
+/* Field objects of sim_fields (source/sim_fields_class.f03:45-89). */
+enum {
+  QPAD_F_PSI = 0, QPAD_F_E, QPAD_F_E_SPE, QPAD_F_B, QPAD_F_B_SPE, QPAD_F_B_BEAM,
+  QPAD_F_CU, QPAD_F_AMU, QPAD_F_ACU, QPAD_F_DCU, QPAD_F_Q_SPE, QPAD_F_Q_BEAM,
+  QPAD_NFIELDS
+};
+
+/* ---- context ------------------------------------------------------------------- */
+typedef struct qpad_ctx qpad_ctx;
+typedef struct qpad_species qpad_species;
+typedef struct qpad_beam qpad_beam;
+
+typedef struct qpad_grid_desc {
+  int32_t nr, nz, max_mode;   /* simulation.grid(1:2), simulation.max_mode */
+  int32_t bnd;                /* simulation.field_boundary */
+  double dr, dxi;             /* options_class.f03:82-94 */
+  double relax_fac;           /* < 0: default 1e-3*(dr/0.02)^2, sim_fields_class.f03:137-140 */
+  int32_t iter_max;           /* simulation.iter_max */
+  double iter_reltol, iter_abstol;
+  double dt;                  /* simulation.dt (3D step, beam push) */
+  int32_t precision;          /* QPAD_PREC_FP64 (reference arithmetic) or QPAD_PREC_MIXED */
+  int32_t device;             /* CUDA device ordinal */
+} qpad_grid_desc;
+
+/* simulation::new + sim_fields::new (simulation_class.f03:105-199, sim_fields_class.f03:91-160) */
+int qpad_ctx_create(const qpad_grid_desc* desc, qpad_ctx** out);
+int qpad_ctx_destroy(qpad_ctx* ctx);
+const char* qpad_last_error(const qpad_ctx* ctx);
+int qpad_synchronize(qpad_ctx* ctx);
+/* Components and radial line length (nr+2) of a slice field's device layout
+ * [part][component][node]. */
+int qpad_field_layout(const qpad_ctx* ctx, int field, int* ncomp, int64_t* ld);
+/* Number of visible CUDA devices (no context needed; 0 when there is no GPU). */
+int qpad_device_count(int* count);
+/* Kernel launches issued on this context so far (all kernels of this library). */
+int qpad_launch_count(const qpad_ctx* ctx, int64_t* count);
+/* Per-kernel CUDA-event timing on the context's stream: enable/disable, then read the
+ * accumulated device time (ms) and launch count of one kernel family by name
+ * ("amjdp", "qdeposit", "push", "field", "beam_push", "beam_qdeposit"). */
+int qpad_profile_enable(qpad_ctx* ctx, int on);
+int qpad_profile_read(qpad_ctx* ctx, const char* name, double* total_ms, int64_t* launches);
+
+/* ---- fields (source/fields/) ------------------------------------------------------ */
+/* ufield f1 host mirror <-> device, one mode part; f1 is (dim, 0:nr+1) */
+int qpad_field_upload(qpad_ctx* ctx, int field, int part, const double* f1);
+int qpad_field_download(qpad_ctx* ctx, int field, int part, double* f1);
+/* 3D store f2(dim, 0:nr+1, slice) of one slice and part (slice 1..nz+1) */
+int qpad_store_download(qpad_ctx* ctx, int field, int slice, int part, double* f1);
+int qpad_store_upload(qpad_ctx* ctx, int field, int slice, int part, const double* f1);
+/* field = value (assign_f1, field_class.f03:917-950) and field%as (f2) */
+int qpad_field_fill(qpad_ctx* ctx, int field, double value);
+int qpad_store_fill(qpad_ctx* ctx, int field, double value);
+/* c = a + b (add_f1_binary, field_class.f03:1031-1050) */
+int qpad_field_add(qpad_ctx* ctx, int a, int b, int c);
+/* b(bdim(k),:) += a(adim(k),:) (add_f1_unitary_dim, field_class.f03:1009-1029); dims 1-based */
+int qpad_field_add_dim(qpad_ctx* ctx, int a, int b, const int32_t* adim, const int32_t* bdim, int n);
+/* field *= s (dot_f1_unitary, field_class.f03:1159-1178) */
+int qpad_field_scale(qpad_ctx* ctx, int field, double s);
+/* ufield%copy_slice (ufield_class.f03:341-383): dir = QPAD_COPY_1TO2 / QPAD_COPY_2TO1 */
+int qpad_field_copy_slice(qpad_ctx* ctx, int field, int slice, int dir);
+
+/* field solves; the ids name the sim_fields objects taking part */
+int qpad_solve_psi(qpad_ctx* ctx, int psi, int q);                  /* field_psi_class.f03:218-254 */
+int qpad_solve_bz(qpad_ctx* ctx, int b, int cu);                    /* field_b_class.f03:760-796 */
+int qpad_solve_bt_beam(qpad_ctx* ctx, int b, int q);                /* field_b_class.f03:798-834 */
+int qpad_solve_bt_iter(qpad_ctx* ctx, int b, int dcu, int cu);      /* field_b_class.f03:836-879 */
+int qpad_solve_ez(qpad_ctx* ctx, int e, int cu);                    /* field_e_class.f03:298-334 */
+int qpad_solve_et(qpad_ctx* ctx, int e, int b, int psi);            /* field_e_class.f03:412-514 */
+int qpad_solve_djdxi(qpad_ctx* ctx, int dcu, int acu, int amu);     /* field_src_class.f03:273-405 */
+/* convergence_tester (simulation_class.f03:522-606) on component dim of field b:
+ * op 0 = 'record', op 1 = 'compare' (writes rel_res, abs_res). */
+int qpad_conv_test(qpad_ctx* ctx, int b, int dim, int op, double* rel_res, double* abs_res);
+
+/* ---- plasma species (source/species/) -------------------------------------------- */
+typedef struct qpad_species_desc {
+  double qbm;            /* q/m */
+  int32_t push_type;     /* QPAD_PUSH2_* (sim_plasma_class.f03:123-137) */
+  int32_t neutralized;   /* species(k).neutralized */
+  int64_t npmax;         /* particle capacity */
+  int32_t sort_freq;     /* species(k).sort_freq: sort every n slices, 0 = never */
+} qpad_species_desc;
+
+/* species2d::new (species2d_class.f03:75-134): uploads the loaded particles and sets
+ * the neutralising background qn = -(their charge deposit). */
+int qpad_species_create(qpad_ctx* ctx, const qpad_species_desc* desc, const double* x,
+                        const double* p, const double* gamma, const double* psi,
+                        const double* q, int64_t np, qpad_species** out);
+int qpad_species_destroy(qpad_species* sp);
+/* species2d::renew (species2d_class.f03:154-184) with freshly loaded particles */
+int qpad_species_renew(qpad_species* sp, const double* x, const double* p, const double* gamma,
+                       const double* psi, const double* q, int64_t np);
+int qpad_species_download(qpad_species* sp, double* x, double* p, double* gamma, double* psi,
+                          double* q, int64_t* np);
+/* renew from the device-resident copy of the last uploaded particles (no host traffic);
+ * equivalent to qpad_species_renew with the same arrays. */
+int qpad_species_reset(qpad_species* sp);
+int qpad_species_count(qpad_species* sp, int64_t* np);
+/* species2d::qdp (species2d_class.f03:186-208): q += deposit (+ qn if neutralized) */
+int qpad_species_qdp(qpad_species* sp, int q);
+/* species2d::amjdp (species2d_class.f03:233-280): cu, amu, dcu += deposits */
+int qpad_species_amjdp(qpad_species* sp, int ef, int bf, int cu, int amu, int dcu, double dt);
+/* species2d::push_u (species2d_class.f03:282-309) */
+int qpad_species_push_u(qpad_species* sp, int ef, int bf, double dt);
+/* species2d::push_x (species2d_class.f03:311-327): push_x + update_bound */
+int qpad_species_push_x(qpad_species* sp, double dt);
+/* species2d::interp_psi (species2d_class.f03:437-452) */
+int qpad_species_interp_psi(qpad_species* sp, int psi);
+/* part2d::sort (part2d_class.f03:2498-2579): exact reference permutation */
+int qpad_species_sort(qpad_species* sp);
+
+/* ---- beams (source/beam/) -------------------------------------------------------- */
+typedef struct qpad_beam_desc {
+  double qbm;
+  int32_t push_type;     /* QPAD_PUSH3_* (beam3d_class.f03:139-154) */
+  int32_t evolution;     /* beam(k).evolution */
+  int64_t npmax;
+} qpad_beam_desc;
+
+int qpad_beam_create(qpad_ctx* ctx, const qpad_beam_desc* desc, const double* x, const double* p,
+                     const double* q, int64_t nb, qpad_beam** out);       /* beam3d_class.f03:121-177 */
+int qpad_beam_destroy(qpad_beam* bm);
+int qpad_beam_download(qpad_beam* bm, double* x, double* p, double* q, int64_t* nb);
+int qpad_beam_count(qpad_beam* bm, int64_t* nb);
+/* beam3d::qdp (beam3d_class.f03:193-221): q (3D store) += beam charge */
+int qpad_beam_qdp(qpad_beam* bm, int q);
+/* beam3d::push (beam3d_class.f03:223-254): push + update_bound with the e, b 3D stores */
+int qpad_beam_push(qpad_beam* bm, int ef, int bf);
+
+/* ---- fused drivers --------------------------------------------------------------- */
+typedef struct qpad_slice_stats {
+  int32_t iters;         /* predictor-corrector iterations taken */
+  double rel_res, abs_res;
+} qpad_slice_stats;
+
+/* One xi slice j (1..nz) of run_simulation (simulation_class.f03:342-469) over all
+ * species and the stored beam charge. */
+int qpad_slice_step(qpad_ctx* ctx, int j, qpad_slice_stats* stats);
+/* One whole 3D step (simulation_class.f03:294-512 without diagnostics): beam deposit,
+ * slices 1..nz, beam push; per-slice stats into stats[nz] (may be NULL). */
+int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* stats);
+
+/* ---- loaders (host; project RNG substituting gfortran random_number) ------------- */
+typedef struct qpad_rng { uint64_t s; int32_t have; double next; } qpad_rng;
+void qpad_rng_seed(qpad_rng* r, uint64_t seed);
+/* fdist2d::inject (fdist2d_class.f03:289-357), uniform profile; returns the count or -1 */
+int64_t qpad_load_plasma(int nr, double dr, qpad_rng* r, int ppc1, int ppc2, int num_theta,
+                         double qm, double density, const double uth[3], double* x, double* p,
+                         double* gamma, double* psi, double* q, int64_t cap);
+typedef struct qpad_beam_load_desc {
+  int64_t tot_num; double tot_charge, qm, gamma;
+  double center[3], sigma[3], range_lo[3], range_hi[3];
+  double uth[3]; int32_t quiet;
+} qpad_beam_load_desc;
+/* fdist3d_rnd::inject (fdist3d_rnd_class.f03:360-514), Gaussian profiles */
+int64_t qpad_load_beam(int nr, int nz, double dr, double dxi, qpad_rng* r,
+                       const qpad_beam_load_desc* d, double* x, double* p, double* q, int64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1481 @@
+/*
+ * qpad_oracle.c -- CPU FP64 restatement of QPAD's per-xi-slice quasi-static loop.
+ *
+ * TEST INFRASTRUCTURE ONLY (the oracle and the timed CPU baseline).  Parity is
+ * UNPINNED against the reference itself: the reference cannot be built here and its
+ * tests hold no golden vectors.  It is pinned by the project's own known-answer
+ * tests instead.  See qpad_oracle.h for the layouts.
+ *
+ * Each function names the reference routine (file:line within QPAD's source/) that it
+ * restates, with single-rank semantics (noff = 0, idproc = 0 = nvp-1, no pipeline).
+ * Operation order follows the Fortran expressions; compile with -ffp-contract=off.
+ */
+#include "qpad_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NR2 (g->nr + 2)
+/* slice-field element: part p, component c, node i (0..nr+1) */
+#define F(f, nc, p, c, i) ((f)[((size_t)(p) * (nc) + (c)) * (size_t)NR2 + (size_t)(i)])
+#define PRE(m) (2 * (m) - 1)  /* part holding Re of mode m >= 1 */
+#define PIM(m) (2 * (m))      /* part holding Im of mode m >= 1 */
+
+static const double ORC_PI = 3.141592653589793; /* 4*atan(1.0), param.f03:29 */
+
+static int nparts(const orc_grid* g) { return 2 * g->max_mode + 1; }
+
+/* =============================================================================
+ * Tridiagonal operators: field_solver_class.f03:256-561 (set_struct_matrix)
+ * ============================================================================= */
+void orc_build_matrix(const orc_grid* g, int kind, int m, double* a, double* b, double* c) {
+  const int nr = g->nr;
+  const double dr = g->dr, dr2 = dr * dr, m2 = (double)(m * m), rf = g->relax_fac;
+  /* rows 2..nr: j = row-1 (field_solver_class.f03:301-307, 335-342, 370-377) */
+  for (int k = 2; k <= nr; ++k) {
+    double j = (double)(k - 1);
+    a[k - 1] = 1.0 - 0.5 / j;
+    c[k - 1] = 1.0 + 0.5 / j;
+    if (kind == ORC_FK_BPLUS) {
+      double t = (double)(m + 1) / j;
+      b[k - 1] = -2.0 - t * t - rf;
+    } else if (kind == ORC_FK_BMINUS) {
+      double t = (double)(m - 1) / j;
+      b[k - 1] = -2.0 - t * t - rf;
+    } else {
+      b[k - 1] = -2.0 - m2 / (j * j);
+    }
+  }
+  /* first row (axis) */
+  int identity_axis = 1;
+  if (kind == ORC_FK_BPLUS) {
+    identity_axis = 1;                                   /* :346-356 */
+  } else if (kind == ORC_FK_BMINUS) {
+    if (m == 1) {                                        /* :383-389 */
+      a[0] = 0.0; b[0] = -4.0 - rf; c[0] = 4.0; identity_axis = 0;
+    }
+  } else if (m == 0) {                                   /* :312-315 */
+    a[0] = 0.0; b[0] = -4.0; c[0] = 4.0; identity_axis = 0;
+  }
+  if (identity_axis) {                                   /* :316-322 */
+    a[0] = 0.0; b[0] = 1.0; c[0] = 0.0;
+    if (nr >= 2) a[1] = 0.0;
+  }
+  /* outer boundary (:484-545) */
+  if (g->bnd == ORC_BND_ZERO) {
+    c[nr - 1] = 0.0;
+  } else {
+    double jmax = (double)nr;
+    double fac;
+    int dirichlet = 0;
+    switch (kind) {
+      case ORC_FK_PSI: case ORC_FK_EZ: case ORC_FK_BZ:
+        if (m == 0) dirichlet = 1; else fac = 1.0 - (double)m / jmax;
+        break;
+      case ORC_FK_BT:
+        if (m == 0) fac = 1.0 + 1.0 / (jmax * log(jmax * dr));
+        else fac = 1.0 - (double)m / jmax;
+        break;
+      default: /* BPLUS, BMINUS both use (m+1) */
+        fac = 1.0 - (double)(m + 1) / jmax;
+        break;
+    }
+    if (!dirichlet) b[nr - 1] = b[nr - 1] + fac * c[nr - 1];
+    c[nr - 1] = 0.0;
+  }
+  for (int k = 0; k < nr; ++k) { a[k] /= dr2; b[k] /= dr2; c[k] /= dr2; }  /* :552 */
+}
+
+void orc_thomas(int n, const double* a, const double* b, const double* c, double* d) {
+  double* cp = (double*)malloc(sizeof(double) * (size_t)n);
+  cp[0] = c[0] / b[0];
+  d[0] = d[0] / b[0];
+  for (int k = 1; k < n; ++k) {
+    double den = b[k] - a[k] * cp[k - 1];
+    cp[k] = c[k] / den;
+    d[k] = (d[k] - a[k] * d[k - 1]) / den;
+  }
+  for (int k = n - 2; k >= 0; --k) d[k] = d[k] - cp[k] * d[k + 1];
+  free(cp);
+}
+
+/* HYPRE StructCycRedSolve stand-in (field_solver_class.f03:145-196): solve in place.
+ * buf is 1-based in the reference (buf(1..nr)); here buf[0..nr-1]. */
+static void solve_sys(const orc_grid* g, int kind, int m, double* buf) {
+  int nr = g->nr;
+  double* a = (double*)malloc(sizeof(double) * 3 * (size_t)nr);
+  double* b = a + nr;
+  double* c = b + nr;
+  orc_build_matrix(g, kind, m, a, b, c);
+  orc_thomas(nr, a, b, c, buf);
+  free(a);
+}
+
+/* =============================================================================
+ * psi: field_psi_class.f03:131-254
+ * ============================================================================= */
+void orc_solve_psi(const orc_grid* g, const double* q, double* psi) {
+  const int nr = g->nr, M = g->max_mode;
+  double* bre = (double*)malloc(sizeof(double) * 2 * (size_t)nr);
+  double* bim = bre + nr;
+  for (int m = 0; m <= M; ++m) {
+    int pr = m == 0 ? 0 : PRE(m), pi = m == 0 ? 0 : PIM(m);
+    for (int i = 1; i <= nr; ++i) {                                  /* set_source 131-176 */
+      bre[i - 1] = -1.0 * F(q, 1, pr, 0, i);
+      if (m > 0) bim[i - 1] = -1.0 * F(q, 1, pi, 0, i);
+    }
+    solve_sys(g, ORC_FK_PSI, m, bre);
+    if (m > 0) solve_sys(g, ORC_FK_PSI, m, bim);
+    for (int i = 1; i <= nr; ++i) {                                  /* get_solution 178-216 */
+      F(psi, 1, pr, 0, i) = bre[i - 1];
+      if (m > 0) F(psi, 1, pi, 0, i) = bim[i - 1];
+    }
+    if (m > 0) { F(psi, 1, pr, 0, 1) = 0.0; F(psi, 1, pi, 0, 1) = 0.0; }
+  }
+  free(bre);
+}
+
+/* =============================================================================
+ * Bz: field_b_class.f03:205-307 (set_source_bz), 508-543, 760-796
+ * ============================================================================= */
+void orc_solve_bz(const orc_grid* g, const double* cu, double* b) {
+  const int nr = g->nr, M = g->max_mode;
+  const double idr = 1.0 / g->dr, idrh = 0.5 * idr;
+  double* bre = (double*)calloc(2 * (size_t)nr + 2, sizeof(double));
+  double* bim = bre + nr + 1;   /* 1-based buffers: bre[1..nr] */
+  for (int m = 0; m <= M; ++m) {
+    memset(bre, 0, sizeof(double) * (2 * (size_t)nr + 2));
+    if (m == 0) {
+      for (int i = 2; i <= nr; ++i) {
+        double ir = idr / (double)(i - 1);
+        bre[i] = -idrh * (F(cu, 3, 0, 1, i + 1) - F(cu, 3, 0, 1, i - 1)) - ir * F(cu, 3, 0, 1, i);
+      }
+      bre[1] = -2.0 * idr * F(cu, 3, 0, 1, 2);
+      {
+        double ir = idr / (double)(nr - 1);
+        bre[nr] = -idrh * (3.0 * F(cu, 3, 0, 1, nr) - 4.0 * F(cu, 3, 0, 1, nr - 1) + F(cu, 3, 0, 1, nr - 2))
+                  - ir * F(cu, 3, 0, 1, nr);
+      }
+    } else {
+      const int pr = PRE(m), pi = PIM(m);
+      for (int i = 2; i <= nr; ++i) {
+        double ir = idr / (double)(i - 1);
+        bre[i] = -idrh * (F(cu, 3, pr, 1, i + 1) - F(cu, 3, pr, 1, i - 1)) - ir * F(cu, 3, pr, 1, i)
+                 - m * ir * F(cu, 3, pi, 0, i);
+        bim[i] = -idrh * (F(cu, 3, pi, 1, i + 1) - F(cu, 3, pi, 1, i - 1)) - ir * F(cu, 3, pi, 1, i)
+                 + m * ir * F(cu, 3, pr, 0, i);
+      }
+      if (m % 2 == 0) {
+        bre[1] = -2.0 * idr * F(cu, 3, pr, 1, 2) - m * idr * F(cu, 3, pi, 0, 2);
+        bim[1] = -2.0 * idr * F(cu, 3, pi, 1, 2) + m * idr * F(cu, 3, pr, 0, 2);
+      } else {
+        bre[1] = 0.0;
+        bim[1] = 0.0;
+        if (m == 1) {
+          double ir = idr;
+          bre[2] = -idr * (F(cu, 3, pr, 1, 3) - F(cu, 3, pr, 1, 2)) - ir * F(cu, 3, pr, 1, 2)
+                   - m * ir * F(cu, 3, pi, 0, 2);
+          bim[2] = -idr * (F(cu, 3, pi, 1, 3) - F(cu, 3, pi, 1, 2)) - ir * F(cu, 3, pi, 1, 2)
+                   + m * ir * F(cu, 3, pr, 0, 2);
+        }
+      }
+      {
+        double ir = idr / (double)(nr - 1);
+        bre[nr] = -idrh * (3.0 * F(cu, 3, pr, 1, nr) - 4.0 * F(cu, 3, pr, 1, nr - 1) + F(cu, 3, pr, 1, nr - 2))
+                  - ir * F(cu, 3, pr, 1, nr) - m * ir * F(cu, 3, pi, 0, nr);
+        bim[nr] = -idrh * (3.0 * F(cu, 3, pi, 1, nr) - 4.0 * F(cu, 3, pi, 1, nr - 1) + F(cu, 3, pi, 1, nr - 2))
+                  - ir * F(cu, 3, pi, 1, nr) + m * ir * F(cu, 3, pr, 0, nr);
+      }
+    }
+    solve_sys(g, ORC_FK_BZ, m, bre + 1);
+    if (m > 0) solve_sys(g, ORC_FK_BZ, m, bim + 1);
+    int pr = m == 0 ? 0 : PRE(m), pi = m == 0 ? 0 : PIM(m);
+    for (int i = 1; i <= nr; ++i) {
+      F(b, 3, pr, 2, i) = bre[i];
+      if (m > 0) F(b, 3, pi, 2, i) = bim[i];
+    }
+    if (m > 0) { F(b, 3, pr, 2, 1) = 0.0; F(b, 3, pi, 2, 1) = 0.0; }
+  }
+  free(bre);
+}
+
+/* =============================================================================
+ * Beam B-perp: field_b_class.f03:309-358 (set_source_bt), 545-701, 798-834
+ * ============================================================================= */
+void orc_solve_bt_beam(const orc_grid* g, const double* q, double* b) {
+  const int nr = g->nr, M = g->max_mode;
+  const double idr = 1.0 / g->dr, idrh = 0.5 * idr;
+  double* bre = (double*)calloc(2 * (size_t)nr + 2, sizeof(double));
+  double* bim = bre + nr + 1;
+  for (int m = 0; m <= M; ++m) {
+    int pr = m == 0 ? 0 : PRE(m), pi = m == 0 ? 0 : PIM(m);
+    for (int i = 1; i <= nr; ++i) {
+      bre[i] = -1.0 * F(q, 1, pr, 0, i);
+      if (m > 0) bim[i] = -1.0 * F(q, 1, pi, 0, i);
+    }
+    solve_sys(g, ORC_FK_BT, m, bre + 1);
+    if (m > 0) solve_sys(g, ORC_FK_BT, m, bim + 1);
+    if (m == 0) {
+      for (int i = 2; i <= nr - 1; ++i) {
+        F(b, 3, 0, 0, i) = 0.0;
+        F(b, 3, 0, 1, i) = -idrh * (bre[i + 1] - bre[i - 1]);
+      }
+      F(b, 3, 0, 0, 1) = 0.0;
+      F(b, 3, 0, 1, 1) = 0.0;
+      F(b, 3, 0, 0, nr) = 0.0;
+      F(b, 3, 0, 1, nr) = -idrh * (3.0 * bre[nr] - 4.0 * bre[nr - 1] + bre[nr - 2]);
+    } else {
+      for (int i = 2; i <= nr - 1; ++i) {
+        double ir = idr / (double)(i - 1);
+        F(b, 3, pr, 0, i) = -ir * m * bim[i];
+        F(b, 3, pi, 0, i) = ir * m * bre[i];
+        F(b, 3, pr, 1, i) = -idrh * (bre[i + 1] - bre[i - 1]);
+        F(b, 3, pi, 1, i) = -idrh * (bim[i + 1] - bim[i - 1]);
+      }
+      if (m == 1) {
+        F(b, 3, pr, 0, 1) = -idr * m * bim[2];
+        F(b, 3, pi, 0, 1) = idr * m * bre[2];
+        F(b, 3, pr, 1, 1) = -idr * bre[2];
+        F(b, 3, pi, 1, 1) = -idr * bim[2];
+      } else {
+        F(b, 3, pr, 0, 1) = 0.0;
+        F(b, 3, pi, 0, 1) = 0.0;
+        F(b, 3, pr, 1, 1) = 0.0;
+        F(b, 3, pi, 1, 1) = 0.0;
+      }
+      {
+        double ir = idr / (double)(nr - 1);
+        F(b, 3, pr, 0, nr) = -ir * m * bim[nr];
+        F(b, 3, pi, 0, nr) = ir * m * bre[nr];
+        F(b, 3, pr, 1, nr) = -idrh * (3.0 * bre[nr] - 4.0 * bre[nr - 1] + bre[nr - 2]);
+        F(b, 3, pi, 1, nr) = -idrh * (3.0 * bim[nr] - 4.0 * bim[nr - 1] + bim[nr - 2]);
+      }
+    }
+  }
+  free(bre);
+}
+
+/* =============================================================================
+ * Plasma B-perp predictor-corrector: field_b_class.f03:360-506, 703-758, 836-879
+ * b holds B_old on entry (components 1:2), receives the new B_perp.
+ * ============================================================================= */
+void orc_solve_bt_iter(const orc_grid* g, const double* dcu, const double* cu, double* b) {
+  const int nr = g->nr, M = g->max_mode;
+  const double idr = 1.0 / g->dr, idrh = 0.5 * idr;
+  const double relax_idr2 = g->relax_fac * (idr * idr);
+  double* buf = (double*)calloc(4 * ((size_t)nr + 1), sizeof(double));
+  double *b1re = buf, *b1im = buf + (nr + 1), *b2re = buf + 2 * (nr + 1), *b2im = buf + 3 * (nr + 1);
+  for (int m = 0; m <= M; ++m) {
+    memset(buf, 0, sizeof(double) * 4 * ((size_t)nr + 1));
+    if (m == 0) {
+      /* f1 = djdxi, f2 = jay, f3 = b (old) */
+      for (int i = 2; i <= nr; ++i) {
+        b1re[i] = -F(dcu, 2, 0, 1, i) - F(b, 3, 0, 0, i) * relax_idr2;
+        b2re[i] = F(dcu, 2, 0, 0, i) + idrh * (F(cu, 3, 0, 2, i + 1) - F(cu, 3, 0, 2, i - 1))
+                  - F(b, 3, 0, 1, i) * relax_idr2;
+      }
+      b1re[1] = 0.0;
+      b2re[1] = 0.0;
+      b2re[2] = F(dcu, 2, 0, 0, 2) + idr * (F(cu, 3, 0, 2, 3) - F(cu, 3, 0, 2, 2)) - F(b, 3, 0, 1, 2) * relax_idr2;
+      b1re[nr] = -F(dcu, 2, 0, 1, nr) - F(b, 3, 0, 0, nr) * relax_idr2;
+      b2re[nr] = F(dcu, 2, 0, 0, nr) + idrh * (3.0 * F(cu, 3, 0, 2, nr) - 4.0 * F(cu, 3, 0, 2, nr - 1) + F(cu, 3, 0, 2, nr - 2))
+                 - F(b, 3, 0, 1, nr) * relax_idr2;
+      solve_sys(g, ORC_FK_BPLUS, 0, b1re + 1);
+      solve_sys(g, ORC_FK_BMINUS, 0, b2re + 1);
+      for (int i = 1; i <= nr; ++i) {
+        F(b, 3, 0, 0, i) = b1re[i];
+        F(b, 3, 0, 1, i) = b2re[i];
+      }
+      F(b, 3, 0, 0, 1) = 0.0;
+      F(b, 3, 0, 1, 1) = 0.0;
+    } else {
+      const int pr = PRE(m), pi = PIM(m);
+      double s1re, s1im, s2re, s2im;
+#define BT_ITER_FILL(I)                                                                           \
+  b1re[I] = s1re - s2im - (F(b, 3, pr, 0, I) - F(b, 3, pi, 1, I)) * relax_idr2;                   \
+  b1im[I] = s1im + s2re - (F(b, 3, pi, 0, I) + F(b, 3, pr, 1, I)) * relax_idr2;                   \
+  b2re[I] = s1re + s2im - (F(b, 3, pr, 0, I) + F(b, 3, pi, 1, I)) * relax_idr2;                   \
+  b2im[I] = s1im - s2re - (F(b, 3, pi, 0, I) - F(b, 3, pr, 1, I)) * relax_idr2;
+      for (int i = 2; i <= nr; ++i) {
+        double ir = idr / (double)(i - 1);
+        s1re = -F(dcu, 2, pr, 1, i) + m * F(cu, 3, pi, 2, i) * ir;
+        s1im = -F(dcu, 2, pi, 1, i) - m * F(cu, 3, pr, 2, i) * ir;
+        s2re = F(dcu, 2, pr, 0, i) + idrh * (F(cu, 3, pr, 2, i + 1) - F(cu, 3, pr, 2, i - 1));
+        s2im = F(dcu, 2, pi, 0, i) + idrh * (F(cu, 3, pi, 2, i + 1) - F(cu, 3, pi, 2, i - 1));
+        BT_ITER_FILL(i)
+      }
+      if (m == 1) {
+        s1re = -F(dcu, 2, pr, 1, 1) + idr * m * F(cu, 3, pi, 2, 2);
+        s1im = -F(dcu, 2, pi, 1, 1) - idr * m * F(cu, 3, pr, 2, 2);
+        s2re = F(dcu, 2, pr, 0, 1) + idr * F(cu, 3, pr, 2, 2);
+        s2im = F(dcu, 2, pi, 0, 1) + idr * F(cu, 3, pi, 2, 2);
+      } else if (m % 2 == 0) {
+        s1re = 0.0; s1im = 0.0; s2re = 0.0; s2im = 0.0;
+      } else {
+        s1re = idr * m * F(cu, 3, pi, 2, 2);
+        s1im = idr * m * F(cu, 3, pr, 2, 2);
+        s2re = idr * F(cu, 3, pr, 2, 2);
+        s2im = idr * F(cu, 3, pi, 2, 2);
+      }
+      BT_ITER_FILL(1)
+      {
+        double ir = idr / (double)(nr - 1);
+        s1re = -F(dcu, 2, pr, 1, nr) + m * F(cu, 3, pi, 2, nr) * ir;
+        s1im = -F(dcu, 2, pi, 1, nr) - m * F(cu, 3, pr, 2, nr) * ir;
+        s2re = F(dcu, 2, pr, 0, nr) + idrh * (3.0 * F(cu, 3, pr, 2, nr) - 4.0 * F(cu, 3, pr, 2, nr - 1) + F(cu, 3, pr, 2, nr - 2));
+        s2im = F(dcu, 2, pi, 0, nr) + idrh * (3.0 * F(cu, 3, pi, 2, nr) - 4.0 * F(cu, 3, pi, 2, nr - 1) + F(cu, 3, pi, 2, nr - 2));
+        BT_ITER_FILL(nr)
+      }
+#undef BT_ITER_FILL
+      solve_sys(g, ORC_FK_BPLUS, m, b1re + 1);
+      solve_sys(g, ORC_FK_BPLUS, m, b1im + 1);
+      solve_sys(g, ORC_FK_BMINUS, m, b2re + 1);
+      solve_sys(g, ORC_FK_BMINUS, m, b2im + 1);
+      for (int i = 1; i <= nr; ++i) {
+        F(b, 3, pr, 0, i) = 0.5 * (b1re[i] + b2re[i]);
+        F(b, 3, pi, 0, i) = 0.5 * (b1im[i] + b2im[i]);
+        F(b, 3, pr, 1, i) = 0.5 * (b1im[i] - b2im[i]);
+        F(b, 3, pi, 1, i) = 0.5 * (-b1re[i] + b2re[i]);
+      }
+      if (m != 1) {
+        F(b, 3, pr, 0, 1) = 0.0; F(b, 3, pi, 0, 1) = 0.0;
+        F(b, 3, pr, 1, 1) = 0.0; F(b, 3, pi, 1, 1) = 0.0;
+      }
+    }
+  }
+  free(buf);
+}
+
+/* =============================================================================
+ * Ez: field_e_class.f03:148-259 (set_source_ez), 261-296, 298-334
+ * ============================================================================= */
+void orc_solve_ez(const orc_grid* g, const double* cu, double* e) {
+  const int nr = g->nr, M = g->max_mode;
+  const double idr = 1.0 / g->dr, idrh = 0.5 * idr;
+  double* bre = (double*)calloc(2 * (size_t)nr + 2, sizeof(double));
+  double* bim = bre + nr + 1;
+  for (int m = 0; m <= M; ++m) {
+    memset(bre, 0, sizeof(double) * (2 * (size_t)nr + 2));
+    if (m == 0) {
+      double div = 0.0;
+      for (int i = 2; i <= nr - 2; ++i) {
+        double ir = idr / (double)(i - 1);
+        bre[i] = idrh * (F(cu, 3, 0, 0, i + 1) - F(cu, 3, 0, 0, i - 1)) + ir * F(cu, 3, 0, 0, i);
+        div = div + bre[i] * (double)(i - 1);
+      }
+      {
+        double ir = idr / (double)(nr - 2);
+        bre[nr - 1] = idrh * (F(cu, 3, 0, 0, nr) - F(cu, 3, 0, 0, nr - 2)) + ir * F(cu, 3, 0, 0, nr - 1);
+        ir = idr / (double)(nr - 1);
+        bre[nr] = idr * (F(cu, 3, 0, 0, nr) - F(cu, 3, 0, 0, nr - 1)) + ir * F(cu, 3, 0, 0, nr);
+        div = div - idrh * (F(cu, 3, 0, 0, nr - 2) + F(cu, 3, 0, 0, nr - 1)) * ((double)nr - 2.5);
+      }
+      bre[1] = div;                 /* MPI_REDUCE on one rank */
+      bre[1] = -8.0 * bre[1];
+    } else {
+      const int pr = PRE(m), pi = PIM(m);
+      for (int i = 2; i <= nr; ++i) {
+        double ir = idr / (double)(i - 1);
+        bre[i] = idrh * (F(cu, 3, pr, 0, i + 1) - F(cu, 3, pr, 0, i - 1)) + ir * F(cu, 3, pr, 0, i)
+                 - m * ir * F(cu, 3, pi, 1, i);
+        bim[i] = idrh * (F(cu, 3, pi, 0, i + 1) - F(cu, 3, pi, 0, i - 1)) + ir * F(cu, 3, pi, 0, i)
+                 + m * ir * F(cu, 3, pr, 1, i);
+      }
+      if (m % 2 == 0) {
+        bre[1] = 2.0 * idr * F(cu, 3, pr, 0, 2) - m * idr * F(cu, 3, pi, 1, 2);
+        bim[1] = 2.0 * idr * F(cu, 3, pi, 0, 2) + m * idr * F(cu, 3, pr, 1, 2);
+      } else {
+        bre[1] = 0.0;
+        bim[1] = 0.0;
+        if (m == 1) {
+          double ir = idr;
+          bre[2] = idr * (F(cu, 3, pr, 0, 3) - F(cu, 3, pr, 0, 2)) + ir * F(cu, 3, pr, 0, 2) - m * ir * F(cu, 3, pi, 1, 2);
+          bim[2] = idr * (F(cu, 3, pi, 0, 3) - F(cu, 3, pi, 0, 2)) + ir * F(cu, 3, pi, 0, 2) + m * ir * F(cu, 3, pr, 1, 2);
+        }
+      }
+      {
+        double ir = idr / (double)(nr - 1);
+        bre[nr] = idrh * (3.0 * F(cu, 3, pr, 0, nr) - 4.0 * F(cu, 3, pr, 0, nr - 1) + F(cu, 3, pr, 0, nr - 2))
+                  + ir * F(cu, 3, pr, 0, nr) - m * ir * F(cu, 3, pi, 1, nr);
+        bim[nr] = idrh * (3.0 * F(cu, 3, pi, 0, nr) - 4.0 * F(cu, 3, pi, 0, nr - 1) + F(cu, 3, pi, 0, nr - 2))
+                  + ir * F(cu, 3, pi, 0, nr) + m * ir * F(cu, 3, pr, 1, nr);
+      }
+    }
+    solve_sys(g, ORC_FK_EZ, m, bre + 1);
+    if (m > 0) solve_sys(g, ORC_FK_EZ, m, bim + 1);
+    int pr = m == 0 ? 0 : PRE(m), pi = m == 0 ? 0 : PIM(m);
+    for (int i = 1; i <= nr; ++i) {
+      F(e, 3, pr, 2, i) = bre[i];
+      if (m > 0) F(e, 3, pi, 2, i) = bim[i];
+    }
+    if (m > 0) { F(e, 3, pr, 2, 1) = 0.0; F(e, 3, pi, 2, 1) = 0.0; }
+  }
+  free(bre);
+}
+
+/* =============================================================================
+ * E-perp from B and psi: field_e_class.f03:412-514
+ * ============================================================================= */
+void orc_solve_et(const orc_grid* g, const double* b, const double* psi, double* e) {
+  const int nr = g->nr, M = g->max_mode;
+  const double idr = 1.0 / g->dr, idrh = idr * 0.5;
+  for (int i = 1; i <= nr; ++i) {
+    F(e, 3, 0, 0, i) = F(b, 3, 0, 1, i) - idrh * (F(psi, 1, 0, 0, i + 1) - F(psi, 1, 0, 0, i - 1));
+    F(e, 3, 0, 1, i) = -F(b, 3, 0, 0, i);
+  }
+  F(e, 3, 0, 0, 1) = 0.0;
+  F(e, 3, 0, 1, 1) = 0.0;
+  F(e, 3, 0, 0, nr) = F(b, 3, 0, 1, nr) + idrh * (4.0 * F(psi, 1, 0, 0, nr - 1) - F(psi, 1, 0, 0, nr - 2) - 3.0 * F(psi, 1, 0, 0, nr));
+  for (int m = 1; m <= M; ++m) {
+    const int pr = PRE(m), pi = PIM(m);
+    for (int i = 2; i <= nr; ++i) {
+      double ir = idr / (double)(i - 1);
+      F(e, 3, pr, 0, i) = F(b, 3, pr, 1, i) - idrh * (F(psi, 1, pr, 0, i + 1) - F(psi, 1, pr, 0, i - 1));
+      F(e, 3, pi, 0, i) = F(b, 3, pi, 1, i) - idrh * (F(psi, 1, pi, 0, i + 1) - F(psi, 1, pi, 0, i - 1));
+      F(e, 3, pr, 1, i) = -F(b, 3, pr, 0, i) + ir * m * F(psi, 1, pi, 0, i);
+      F(e, 3, pi, 1, i) = -F(b, 3, pi, 0, i) - ir * m * F(psi, 1, pr, 0, i);
+    }
+    if (m == 1) {
+      F(e, 3, pr, 0, 1) = F(b, 3, pr, 1, 1) - idr * F(psi, 1, pr, 0, 2);
+      F(e, 3, pi, 0, 1) = F(b, 3, pi, 1, 1) - idr * F(psi, 1, pi, 0, 2);
+      F(e, 3, pr, 1, 1) = -F(b, 3, pr, 0, 1) + idr * F(psi, 1, pi, 0, 2);
+      F(e, 3, pi, 1, 1) = -F(b, 3, pi, 0, 1) - idr * F(psi, 1, pr, 0, 2);
+    } else {
+      F(e, 3, pr, 0, 1) = 0.0; F(e, 3, pi, 0, 1) = 0.0;
+      F(e, 3, pr, 1, 1) = 0.0; F(e, 3, pi, 1, 1) = 0.0;
+    }
+    F(e, 3, pr, 0, nr) = F(b, 3, pr, 1, nr) + idrh * (4.0 * F(psi, 1, pr, 0, nr - 1) - F(psi, 1, pr, 0, nr - 2) - 3.0 * F(psi, 1, pr, 0, nr));
+    F(e, 3, pi, 0, nr) = F(b, 3, pi, 1, nr) + idrh * (4.0 * F(psi, 1, pi, 0, nr - 1) - F(psi, 1, pi, 0, nr - 2) - 3.0 * F(psi, 1, pi, 0, nr));
+  }
+}
+
+/* =============================================================================
+ * dJ_perp/dxi = acu - div(amu): field_src_class.f03:273-405
+ * ============================================================================= */
+void orc_solve_djdxi(const orc_grid* g, const double* acu, const double* amu, double* dcu) {
+  const int nr = g->nr, M = g->max_mode;
+  const double idr = 1.0 / g->dr, idrh = idr * 0.5;
+#define A(p, c, i) F(acu, 2, p, c, i)
+#define U(p, c, i) F(amu, 3, p, c, i)
+#define D(p, c, i) F(dcu, 2, p, c, i)
+  for (int i = 2; i <= nr; ++i) {
+    double ir = idr / (double)(i - 1);
+    D(0, 0, i) = A(0, 0, i) - idrh * (U(0, 0, i + 1) - U(0, 0, i - 1)) - ir * U(0, 0, i);
+    D(0, 1, i) = A(0, 1, i) - idrh * (U(0, 1, i + 1) - U(0, 1, i - 1)) - ir * U(0, 1, i);
+  }
+  D(0, 0, 1) = 0.0;
+  D(0, 1, 1) = 0.0;
+  {
+    double ir = idr / (double)(nr - 1);
+    D(0, 0, nr) = A(0, 0, nr) + idrh * (4.0 * U(0, 0, nr - 1) - U(0, 0, nr - 2) - 3.0 * U(0, 0, nr)) - ir * U(0, 0, nr);
+    D(0, 1, nr) = A(0, 1, nr) + idrh * (4.0 * U(0, 1, nr - 1) - U(0, 1, nr - 2) - 3.0 * U(0, 1, nr)) - ir * U(0, 1, nr);
+  }
+  for (int m = 1; m <= M; ++m) {
+    const int r = PRE(m), s = PIM(m);
+    for (int i = 2; i <= nr; ++i) {
+      double ir = idr / (double)(i - 1);
+      D(r, 0, i) = A(r, 0, i) - idrh * (U(r, 0, i + 1) - U(r, 0, i - 1)) - ir * U(r, 0, i) + m * ir * U(s, 1, i);
+      D(r, 1, i) = A(r, 1, i) - idrh * (U(r, 1, i + 1) - U(r, 1, i - 1)) - ir * U(r, 1, i) + m * ir * U(s, 2, i);
+      D(s, 0, i) = A(s, 0, i) - idrh * (U(s, 0, i + 1) - U(s, 0, i - 1)) - ir * U(s, 0, i) - m * ir * U(r, 1, i);
+      D(s, 1, i) = A(s, 1, i) - idrh * (U(s, 1, i + 1) - U(s, 1, i - 1)) - ir * U(s, 1, i) - m * ir * U(r, 2, i);
+    }
+    if (m == 1) {
+      D(r, 0, 1) = A(r, 0, 1) - 2.0 * idr * U(r, 0, 2) + m * idr * U(s, 1, 2);
+      D(r, 1, 1) = A(r, 1, 1) - 2.0 * idr * U(r, 1, 2) + m * idr * U(s, 2, 2);
+      D(s, 0, 1) = A(s, 0, 1) - 2.0 * idr * U(s, 0, 2) - m * idr * U(r, 1, 2);
+      D(s, 1, 1) = A(s, 1, 1) - 2.0 * idr * U(s, 1, 2) - m * idr * U(r, 2, 2);
+    } else {
+      D(r, 0, 1) = 0.0; D(r, 1, 1) = 0.0; D(s, 0, 1) = 0.0; D(s, 1, 1) = 0.0;
+      if (m == 2) {
+        double ir = idr;
+        D(r, 0, 2) = A(r, 0, 2) - idr * (U(r, 0, 3) - U(r, 0, 2)) - ir * U(r, 0, 2) + m * ir * U(s, 1, 2);
+        D(r, 1, 2) = A(r, 1, 2) - idr * (U(r, 1, 3) - U(r, 1, 2)) - ir * U(r, 1, 2) + m * ir * U(s, 2, 2);
+        D(s, 0, 2) = A(s, 0, 2) - idr * (U(s, 0, 3) - U(s, 0, 2)) - ir * U(s, 0, 2) - m * ir * U(r, 1, 2);
+        D(s, 1, 2) = A(s, 1, 2) - idr * (U(s, 1, 3) - U(s, 1, 2)) - ir * U(s, 1, 2) - m * ir * U(r, 2, 2);
+      }
+    }
+    {
+      double ir = idr / (double)(nr - 1);
+      D(r, 0, nr) = A(r, 0, nr) + idrh * (4.0 * U(r, 0, nr - 1) - U(r, 0, nr - 2) - 3.0 * U(r, 0, nr)) - ir * U(r, 0, nr) + m * ir * U(s, 1, nr);
+      D(r, 1, nr) = A(r, 1, nr) + idrh * (4.0 * U(r, 1, nr - 1) - U(r, 1, nr - 2) - 3.0 * U(r, 1, nr)) - ir * U(r, 1, nr) + m * ir * U(s, 2, nr);
+      D(s, 0, nr) = A(s, 0, nr) + idrh * (4.0 * U(s, 0, nr - 1) - U(s, 0, nr - 2) - 3.0 * U(s, 0, nr)) - ir * U(s, 0, nr) - m * ir * U(r, 1, nr);
+      D(s, 1, nr) = A(s, 1, nr) + idrh * (4.0 * U(s, 1, nr - 1) - U(s, 1, nr - 2) - 3.0 * U(s, 1, nr)) - ir * U(s, 1, nr) - m * ir * U(r, 2, nr);
+    }
+  }
+#undef A
+#undef U
+#undef D
+}
+
+/* =============================================================================
+ * convergence_tester: simulation_class.f03:522-606 (dim = 2, infinity norm)
+ * ============================================================================= */
+void orc_conv_record(const orc_grid* g, const double* b, double* s_re, double* s_im) {
+  const int nr = g->nr, M = g->max_mode;
+  for (int i = 1; i <= nr; ++i) { s_re[i - 1] = 0.0; s_im[i - 1] = 0.0; }
+  for (int m = 0; m <= M; ++m) {
+    int pr = m == 0 ? 0 : PRE(m);
+    for (int i = 1; i <= nr; ++i) s_re[i - 1] = s_re[i - 1] + fabs(F(b, 3, pr, 1, i));
+    if (m == 0) continue;
+    for (int i = 1; i <= nr; ++i) s_im[i - 1] = s_im[i - 1] + fabs(F(b, 3, PIM(m), 1, i));
+  }
+}
+
+void orc_conv_compare(const orc_grid* g, const double* b, double* s_re, double* s_im,
+                      double* rel_res, double* abs_res) {
+  const int nr = g->nr, M = g->max_mode;
+  double mx = 0.0;
+  for (int i = 0; i < nr; ++i) {
+    double v = s_re[i] * s_re[i] + s_im[i] * s_im[i];
+    if (i == 0 || v > mx) mx = v;
+  }
+  double old_norm = sqrt(mx);
+  for (int m = 0; m <= M; ++m) {
+    int pr = m == 0 ? 0 : PRE(m);
+    for (int i = 1; i <= nr; ++i) s_re[i - 1] = s_re[i - 1] - fabs(F(b, 3, pr, 1, i));
+    if (m == 0) continue;
+    for (int i = 1; i <= nr; ++i) s_im[i - 1] = s_im[i - 1] - fabs(F(b, 3, PIM(m), 1, i));
+  }
+  mx = 0.0;
+  for (int i = 0; i < nr; ++i) {
+    double v = s_re[i] * s_re[i] + s_im[i] * s_im[i];
+    if (i == 0 || v > mx) mx = v;
+  }
+  *abs_res = sqrt(mx);
+  if (old_norm > 2.220446049250313e-16) *rel_res = *abs_res / old_norm;   /* epsilon(1.0d0) */
+  else *rel_res = 1.7976931348623157e308;                                 /* huge(1.0) */
+}
+
+/* =============================================================================
+ * Plasma charge deposit: part2d_class.f03:231-359 (accumulates into qf)
+ * ============================================================================= */
+static void qdeposit_axis_scale(const orc_grid* g, double* qf) {
+  const int nr = g->nr, M = g->max_mode;
+  F(qf, 1, 0, 0, 0) = 0.0;
+  F(qf, 1, 0, 0, 1) = 8.0 * F(qf, 1, 0, 0, 1);
+  for (int j = 2; j <= nr + 1; ++j) {
+    double ir = 1.0 / (double)(j - 1);
+    F(qf, 1, 0, 0, j) = F(qf, 1, 0, 0, j) * ir;
+  }
+  for (int m = 1; m <= M; ++m) {
+    F(qf, 1, PRE(m), 0, 0) = 0.0; F(qf, 1, PIM(m), 0, 0) = 0.0;
+    F(qf, 1, PRE(m), 0, 1) = 0.0; F(qf, 1, PIM(m), 0, 1) = 0.0;
+    for (int j = 2; j <= nr + 1; ++j) {
+      double ir = 1.0 / (double)(j - 1);
+      F(qf, 1, PRE(m), 0, j) = F(qf, 1, PRE(m), 0, j) * ir;
+      F(qf, 1, PIM(m), 0, j) = F(qf, 1, PIM(m), 0, j) * ir;
+    }
+  }
+}
+
+void orc_qdeposit(const orc_grid* g, int64_t np, const double* x, const double* y,
+                  const double* q, double* qf) {
+  const int M = g->max_mode;
+  const double idr = 1.0 / g->dr;
+  for (int64_t pp = 0; pp < np; ++pp) {
+    double pos = sqrt(x[pp] * x[pp] + y[pp] * y[pp]) * idr;
+    double ph0r = x[pp] / pos * idr, ph0i = -y[pp] / pos * idr;
+    if (!(pos >= 0.0 && pos < 1.0e9)) continue;
+    int nn = (int)floor(pos);
+    pos = pos - (double)nn;
+    nn = nn + 1;
+    if (nn < 1 || nn > g->nr) continue;  /* radius rounds onto/over the edge: nothing deposited */
+    double wt0 = 1.0 - pos, wt1 = pos;
+    double phr = 1.0 * q[pp], phi = 0.0 * q[pp];
+    F(qf, 1, 0, 0, nn) = F(qf, 1, 0, 0, nn) + wt0 * phr;
+    F(qf, 1, 0, 0, nn + 1) = F(qf, 1, 0, 0, nn + 1) + wt1 * phr;
+    for (int m = 1; m <= M; ++m) {
+      double t = phr * ph0r - phi * ph0i;
+      phi = phr * ph0i + phi * ph0r;
+      phr = t;
+      F(qf, 1, PRE(m), 0, nn) = F(qf, 1, PRE(m), 0, nn) + wt0 * phr;
+      F(qf, 1, PIM(m), 0, nn) = F(qf, 1, PIM(m), 0, nn) + wt0 * phi;
+      F(qf, 1, PRE(m), 0, nn + 1) = F(qf, 1, PRE(m), 0, nn + 1) + wt1 * phr;
+      F(qf, 1, PIM(m), 0, nn + 1) = F(qf, 1, PIM(m), 0, nn + 1) + wt1 * phi;
+    }
+  }
+  qdeposit_axis_scale(g, qf);
+}
+
+/* =============================================================================
+ * Field gather helpers: interp_part2d.f03:28-171
+ * ============================================================================= */
+/* idx outside 1..nr (a radius that rounds onto the outer edge, or a NaN) marks a
+ * particle that gathers zero fields and deposits nothing: the reference would read
+ * and write past the upper guard cell there. */
+typedef struct { double w0, w1, pcos, psin; int idx; } interp_info;
+#define II_OK(g, ii) ((ii).idx >= 1 && (ii).idx <= (g)->nr)
+
+static inline interp_info gen_interp_info(double x, double y, double idr) {  /* :28-65 */
+  interp_info ii;
+  double pos = sqrt(x * x + y * y);
+  ii.pcos = x / pos;
+  ii.psin = y / pos;
+  pos = pos * idr;
+  if (!(pos >= 0.0 && pos < 1.0e9)) { ii.idx = 0; ii.w0 = ii.w1 = 0.0; return ii; }
+  int ip = (int)pos;
+  ii.idx = ip + 1;
+  pos = pos - (double)ip;
+  ii.w0 = 1.0 - pos;
+  ii.w1 = pos;
+  return ii;
+}
+
+/* vector gather of a 3-component field (:67-109) */
+static inline void interp_vec(const orc_grid* g, const double* f, const interp_info* ii, double fp[3]) {
+  const int M = g->max_mode;
+  const int i0 = ii->idx, i1 = ii->idx + 1;
+  if (!II_OK(g, *ii)) { fp[0] = fp[1] = fp[2] = 0.0; return; }
+  for (int c = 0; c < 3; ++c) {
+    fp[c] = 0.0;
+    fp[c] = fp[c] + F(f, 3, 0, c, i0) * ii->w0;
+    fp[c] = fp[c] + F(f, 3, 0, c, i1) * ii->w1;
+  }
+  double phr = 1.0, phi = 0.0;
+  for (int m = 1; m <= M; ++m) {
+    double t = phr * ii->pcos - phi * ii->psin;
+    phi = phr * ii->psin + phi * ii->pcos;
+    phr = t;
+    double pre = 2.0 * phr, pim = 2.0 * phi;
+    for (int c = 0; c < 3; ++c) {
+      fp[c] = fp[c] + (F(f, 3, PRE(m), c, i0) * pre - F(f, 3, PIM(m), c, i0) * pim) * ii->w0;
+      fp[c] = fp[c] + (F(f, 3, PRE(m), c, i1) * pre - F(f, 3, PIM(m), c, i1) * pim) * ii->w1;
+    }
+  }
+}
+
+static inline double interp_scalar(const orc_grid* g, const double* f, const interp_info* ii) {  /* :111-153 */
+  const int M = g->max_mode;
+  const int i0 = ii->idx, i1 = ii->idx + 1;
+  double fp = 0.0;
+  if (!II_OK(g, *ii)) return 0.0;
+  fp = fp + F(f, 1, 0, 0, i0) * ii->w0;
+  fp = fp + F(f, 1, 0, 0, i1) * ii->w1;
+  double phr = 1.0, phi = 0.0;
+  for (int m = 1; m <= M; ++m) {
+    double t = phr * ii->pcos - phi * ii->psin;
+    phi = phr * ii->psin + phi * ii->pcos;
+    phr = t;
+    double pre = 2.0 * phr, pim = 2.0 * phi;
+    fp = fp + (F(f, 1, PRE(m), 0, i0) * pre - F(f, 1, PIM(m), 0, i0) * pim) * ii->w0;
+    fp = fp + (F(f, 1, PRE(m), 0, i1) * pre - F(f, 1, PIM(m), 0, i1) * pim) * ii->w1;
+  }
+  return fp;
+}
+
+/* =============================================================================
+ * Current / acceleration / momentum-flux deposit:
+ *   amjdeposit_robust part2d_class.f03:746-1010, amjdeposit_std 478-744
+ * cu (3 comps), amu (3), dcu (2) accumulate; the axis fix and 1/(j-1) scaling follow.
+ * ============================================================================= */
+static void amj_one(const orc_grid* g, int push_type, double qbm, double qtmh, double idt,
+                    double idr, int64_t pp, const double* x, const double* y, const double* px,
+                    const double* py, const double* pz, const double* q, double* gamma, double* psi,
+                    const double* ef, const double* bf, double* cu, double* amu, double* dcu) {
+  const int M = g->max_mode;
+  interp_info ii = gen_interp_info(x[pp], y[pp], idr);
+  double ep[3], bp[3], wp[3], u0[3], u[3], utmp[3], du[3], u2[3];
+  interp_vec(g, ef, &ii, ep);
+  interp_vec(g, bf, &ii, bp);
+  wp[0] = ep[0] - bp[1];
+  wp[1] = ep[1] + bp[0];
+  wp[2] = ep[2];
+  u0[0] = px[pp] * ii.pcos + py[pp] * ii.psin;
+  u0[1] = py[pp] * ii.pcos - px[pp] * ii.psin;
+  u0[2] = pz[pp];
+  double ipsi;
+  if (push_type == ORC_PUSH_ROBUST) {
+    double gam = sqrt(1.0 + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
+    double qtmh1 = qtmh * gam / (gam - u0[2]);
+    for (int c = 0; c < 3; ++c) { ep[c] = ep[c] * qtmh1; utmp[c] = u0[c] + ep[c]; }
+    gam = sqrt(1.0 + utmp[0] * utmp[0] + utmp[1] * utmp[1] + utmp[2] * utmp[2]);
+    double qtmh2 = qtmh / (gam - utmp[2]);
+    for (int c = 0; c < 3; ++c) bp[c] = bp[c] * qtmh2;
+  } else {
+    double gam = sqrt(1.0 + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
+    double qtmh2 = qtmh / (1.0 - qbm * psi[pp]);
+    double qtmh1 = qtmh2 * gam;
+    for (int c = 0; c < 3; ++c) bp[c] = bp[c] * qtmh2;
+    for (int c = 0; c < 3; ++c) utmp[c] = u0[c] + ep[c] * qtmh1;
+  }
+  u[0] = utmp[0] + utmp[1] * bp[2] - utmp[2] * bp[1];
+  u[1] = utmp[1] + utmp[2] * bp[0] - utmp[0] * bp[2];
+  u[2] = utmp[2] + utmp[0] * bp[1] - utmp[1] * bp[0];
+  double ostq = 2.0 / (1.0 + bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2]);
+  for (int c = 0; c < 3; ++c) bp[c] = bp[c] * ostq;
+  {
+    double t0 = utmp[0] + u[1] * bp[2] - u[2] * bp[1];
+    double t1 = utmp[1] + u[2] * bp[0] - u[0] * bp[2];
+    double t2 = utmp[2] + u[0] * bp[1] - u[1] * bp[0];
+    utmp[0] = t0; utmp[1] = t1; utmp[2] = t2;
+  }
+  if (push_type == ORC_PUSH_ROBUST) {
+    for (int c = 0; c < 3; ++c) u[c] = utmp[c] + ep[c];
+  } else {
+    double gam = sqrt(1.0 + utmp[0] * utmp[0] + utmp[1] * utmp[1] + utmp[2] * utmp[2]);
+    double qtmh2 = qtmh / (1.0 - qbm * psi[pp]);
+    double qtmh1 = qtmh2 * gam;
+    for (int c = 0; c < 3; ++c) u[c] = utmp[c] + ep[c] * qtmh1;
+  }
+  /* time-centred values and deposit (robust :857-909, std :602-662) */
+  du[0] = idt * (u[0] - u0[0]);
+  du[1] = idt * (u[1] - u0[1]);
+  for (int c = 0; c < 3; ++c) u[c] = 0.5 * (u[c] + u0[c]);
+  gamma[pp] = sqrt(1.0 + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  if (push_type == ORC_PUSH_ROBUST) {
+    ipsi = 1.0 / (gamma[pp] - u[2]);
+    psi[pp] = (1.0 - 1.0 / ipsi) / qbm;
+  } else {
+    ipsi = 1.0 / (1.0 - qbm * psi[pp]);
+  }
+  double dpsi = qbm * (wp[2] - (wp[0] * u[0] + wp[1] * u[1]) * ipsi);
+  du[0] = du[0] + u[0] * dpsi * ipsi;
+  du[1] = du[1] + u[1] * dpsi * ipsi;
+  u2[0] = u[0] * u[0] * ipsi;
+  u2[1] = u[0] * u[1] * ipsi;
+  u2[2] = u[1] * u[1] * ipsi;
+  double ph0r = ii.pcos, ph0i = -ii.psin;
+  double phr = 1.0 * q[pp] * ipsi, phi = 0.0 * q[pp] * ipsi;
+  const double wj[2] = {ii.w0, ii.w1};
+  if (!II_OK(g, ii)) return;
+  for (int j = 0; j < 2; ++j) {
+    int n = ii.idx + j;
+    double w = wj[j] * phr;
+    for (int c = 0; c < 3; ++c) F(cu, 3, 0, c, n) = F(cu, 3, 0, c, n) + w * u[c];
+    for (int c = 0; c < 2; ++c) F(dcu, 2, 0, c, n) = F(dcu, 2, 0, c, n) + w * du[c];
+    for (int c = 0; c < 3; ++c) F(amu, 3, 0, c, n) = F(amu, 3, 0, c, n) + w * u2[c];
+  }
+  for (int m = 1; m <= M; ++m) {
+    double t = phr * ph0r - phi * ph0i;
+    phi = phr * ph0i + phi * ph0r;
+    phr = t;
+    const int r = PRE(m), s = PIM(m);
+    for (int j = 0; j < 2; ++j) {
+      int n = ii.idx + j;
+      double w = wj[j] * phr;
+      for (int c = 0; c < 3; ++c) F(cu, 3, r, c, n) = F(cu, 3, r, c, n) + w * u[c];
+      for (int c = 0; c < 2; ++c) F(dcu, 2, r, c, n) = F(dcu, 2, r, c, n) + w * du[c];
+      for (int c = 0; c < 3; ++c) F(amu, 3, r, c, n) = F(amu, 3, r, c, n) + w * u2[c];
+      w = wj[j] * phi;
+      for (int c = 0; c < 3; ++c) F(cu, 3, s, c, n) = F(cu, 3, s, c, n) + w * u[c];
+      for (int c = 0; c < 2; ++c) F(dcu, 2, s, c, n) = F(dcu, 2, s, c, n) + w * du[c];
+      for (int c = 0; c < 3; ++c) F(amu, 3, s, c, n) = F(amu, 3, s, c, n) + w * u2[c];
+    }
+  }
+}
+
+/* axis fixes and 1/(j-1) scaling: part2d_class.f03:914-1005 (robust), 658-740 (std) */
+static void amj_axis_scale(const orc_grid* g, double* cu, double* amu, double* dcu) {
+  const int nr = g->nr, M = g->max_mode;
+  for (int c = 0; c < 3; ++c) { F(cu, 3, 0, c, 0) = 0.0; F(amu, 3, 0, c, 0) = 0.0; }
+  for (int c = 0; c < 2; ++c) F(dcu, 2, 0, c, 0) = 0.0;
+  F(cu, 3, 0, 0, 1) = 0.0; F(cu, 3, 0, 1, 1) = 0.0; F(cu, 3, 0, 2, 1) = 8.0 * F(cu, 3, 0, 2, 1);
+  F(dcu, 2, 0, 0, 1) = 0.0; F(dcu, 2, 0, 1, 1) = 0.0;
+  for (int c = 0; c < 3; ++c) F(amu, 3, 0, c, 1) = 0.0;
+  for (int m = 1; m <= M; ++m) {
+    for (int h = 0; h < 2; ++h) {
+      int p = h == 0 ? PRE(m) : PIM(m);
+      for (int c = 0; c < 3; ++c) { F(cu, 3, p, c, 0) = 0.0; F(amu, 3, p, c, 0) = 0.0; }
+      for (int c = 0; c < 2; ++c) F(dcu, 2, p, c, 0) = 0.0;
+      if (m == 1) {
+        F(cu, 3, p, 0, 1) = 8.0 * F(cu, 3, p, 0, 1);
+        F(cu, 3, p, 1, 1) = 8.0 * F(cu, 3, p, 1, 1);
+        F(cu, 3, p, 2, 1) = 0.0;
+        F(dcu, 2, p, 0, 1) = 8.0 * F(dcu, 2, p, 0, 1);
+        F(dcu, 2, p, 1, 1) = 8.0 * F(dcu, 2, p, 1, 1);
+        for (int c = 0; c < 3; ++c) F(amu, 3, p, c, 1) = 0.0;
+      } else if (m == 2) {
+        for (int c = 0; c < 3; ++c) F(cu, 3, p, c, 1) = 0.0;
+        for (int c = 0; c < 2; ++c) F(dcu, 2, p, c, 1) = 0.0;
+        for (int c = 0; c < 3; ++c) F(amu, 3, p, c, 1) = 8.0 * F(amu, 3, p, c, 1);
+      } else {
+        for (int c = 0; c < 3; ++c) F(cu, 3, p, c, 1) = 0.0;
+        for (int c = 0; c < 2; ++c) F(dcu, 2, p, c, 1) = 0.0;
+        for (int c = 0; c < 3; ++c) F(amu, 3, p, c, 1) = 0.0;
+      }
+    }
+  }
+  for (int p = 0; p < nparts(g); ++p) {
+    for (int j = 2; j <= nr + 1; ++j) {
+      double ir = 1.0 / (double)(j - 1);
+      for (int c = 0; c < 3; ++c) F(cu, 3, p, c, j) = F(cu, 3, p, c, j) * ir;
+      for (int c = 0; c < 2; ++c) F(dcu, 2, p, c, j) = F(dcu, 2, p, c, j) * ir;
+      for (int c = 0; c < 3; ++c) F(amu, 3, p, c, j) = F(amu, 3, p, c, j) * ir;
+    }
+  }
+}
+
+void orc_amjdeposit(const orc_grid* g, int push_type, double qbm, double dt, int64_t np,
+                    const double* x, const double* y, const double* px, const double* py,
+                    const double* pz, const double* q, double* gamma, double* psi,
+                    const double* ef, const double* bf, double* cu, double* amu, double* dcu,
+                    int nthreads) {
+  const double idt = 1.0 / dt, qtmh = 0.5 * qbm * dt, idr = 1.0 / g->dr;
+  if (nthreads <= 1) {
+    for (int64_t pp = 0; pp < np; ++pp)
+      amj_one(g, push_type, qbm, qtmh, idt, idr, pp, x, y, px, py, pz, q, gamma, psi, ef, bf, cu, amu, dcu);
+  } else {
+    /* thread-private deposit arrays summed afterwards (CPU baseline only) */
+    const size_t n3 = (size_t)nparts(g) * 3 * NR2, n2 = (size_t)nparts(g) * 2 * NR2;
+    double* priv = (double*)calloc((size_t)nthreads * (2 * n3 + n2), sizeof(double));
+#pragma omp parallel num_threads(nthreads)
+    {
+#ifdef _OPENMP
+      int t = omp_get_thread_num();
+#else
+      int t = 0;
+#endif
+      double* pc = priv + (size_t)t * (2 * n3 + n2);
+      double* pa = pc + n3;
+      double* pd = pa + n3;
+#pragma omp for schedule(static)
+      for (int64_t pp = 0; pp < np; ++pp)
+        amj_one(g, push_type, qbm, qtmh, idt, idr, pp, x, y, px, py, pz, q, gamma, psi, ef, bf, pc, pa, pd);
+#pragma omp for schedule(static)
+      for (int64_t k = 0; k < (int64_t)n3; ++k) {
+        double sc = 0.0, sa = 0.0;
+        for (int u = 0; u < nthreads; ++u) {
+          sc += priv[(size_t)u * (2 * n3 + n2) + (size_t)k];
+          sa += priv[(size_t)u * (2 * n3 + n2) + n3 + (size_t)k];
+        }
+        cu[k] += sc;
+        amu[k] += sa;
+      }
+#pragma omp for schedule(static)
+      for (int64_t k = 0; k < (int64_t)n2; ++k) {
+        double sd = 0.0;
+        for (int u = 0; u < nthreads; ++u) sd += priv[(size_t)u * (2 * n3 + n2) + 2 * n3 + (size_t)k];
+        dcu[k] += sd;
+      }
+    }
+    free(priv);
+  }
+  amj_axis_scale(g, cu, amu, dcu);
+}
+
+/* =============================================================================
+ * Momentum push: push_u_robust part2d_class.f03:1879-1965, push_u_std 1790-1877
+ * ============================================================================= */
+static inline void push_u_one(const orc_grid* g, int push_type, double qbm, double qtmh, double idr,
+                              int64_t pp, const double* x, const double* y, double* px, double* py,
+                              double* pz, double* gamma, const double* psi, const double* ef,
+                              const double* bf) {
+  interp_info ii = gen_interp_info(x[pp], y[pp], idr);
+  double ep[3], bp[3], utmp[3], p[3];
+  interp_vec(g, ef, &ii, ep);
+  interp_vec(g, bf, &ii, bp);
+  /* transform_to_cartesian, interp_part2d.f03:155-171 */
+  double t = ep[0] * ii.pcos - ep[1] * ii.psin;
+  ep[1] = ep[0] * ii.psin + ep[1] * ii.pcos;
+  ep[0] = t;
+  t = bp[0] * ii.pcos - bp[1] * ii.psin;
+  bp[1] = bp[0] * ii.psin + bp[1] * ii.pcos;
+  bp[0] = t;
+  p[0] = px[pp]; p[1] = py[pp]; p[2] = pz[pp];
+  double qtmh1, qtmh2;
+  if (push_type == ORC_PUSH_ROBUST) {
+    double gam = sqrt(1.0 + p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    qtmh1 = qtmh / (gam - p[2]);
+    qtmh2 = qtmh1 * gam;
+  } else {
+    qtmh1 = qtmh / (1.0 - qbm * psi[pp]);
+    qtmh2 = qtmh1 * gamma[pp];
+  }
+  for (int c = 0; c < 3; ++c) { ep[c] = ep[c] * qtmh2; bp[c] = bp[c] * qtmh1; }
+  for (int c = 0; c < 3; ++c) utmp[c] = p[c] + ep[c];
+  p[0] = utmp[0] + utmp[1] * bp[2] - utmp[2] * bp[1];
+  p[1] = utmp[1] + utmp[2] * bp[0] - utmp[0] * bp[2];
+  p[2] = utmp[2] + utmp[0] * bp[1] - utmp[1] * bp[0];
+  double ostq = 2.0 / (1.0 + bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2]);
+  for (int c = 0; c < 3; ++c) bp[c] = bp[c] * ostq;
+  {
+    double t0 = utmp[0] + p[1] * bp[2] - p[2] * bp[1];
+    double t1 = utmp[1] + p[2] * bp[0] - p[0] * bp[2];
+    double t2 = utmp[2] + p[0] * bp[1] - p[1] * bp[0];
+    utmp[0] = t0; utmp[1] = t1; utmp[2] = t2;
+  }
+  for (int c = 0; c < 3; ++c) p[c] = utmp[c] + ep[c];
+  px[pp] = p[0]; py[pp] = p[1]; pz[pp] = p[2];
+  gamma[pp] = sqrt(1.0 + p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+}
+
+void orc_push_u(const orc_grid* g, int push_type, double qbm, double dt, int64_t np,
+                const double* x, const double* y, double* px, double* py, double* pz,
+                double* gamma, const double* psi, const double* ef, const double* bf, int nthreads) {
+  const double qtmh = qbm * dt * 0.5, idr = 1.0 / g->dr;
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+  for (int64_t pp = 0; pp < np; ++pp)
+    push_u_one(g, push_type, qbm, qtmh, idr, pp, x, y, px, py, pz, gamma, psi, ef, bf);
+}
+
+void orc_push_x(int64_t np, double dt, double* x, double* y, const double* px, const double* py,
+                const double* pz, const double* gamma) {                  /* :2221-2262 */
+  for (int64_t pp = 0; pp < np; ++pp) {
+    double dtc = dt / (gamma[pp] - pz[pp]);
+    x[pp] = x[pp] + px[pp] * dtc;
+    y[pp] = y[pp] + py[pp] * dtc;
+  }
+}
+
+int64_t orc_update_bound(const orc_grid* g, int64_t np, double* x, double* y, double* px,
+                         double* py, double* pz, double* gamma, double* psi, double* q) {  /* :2307-2353 */
+  if (np == 0) return 0;
+  const double edge = (double)g->nr * g->dr;
+  int64_t i = 0, n = np;       /* 0-based: i < n-1 mirrors Fortran i < npp */
+  while (i < n - 1) {
+    double pos = sqrt(x[i] * x[i] + y[i] * y[i]);
+    if (pos >= edge) {
+      int64_t l = n - 1;
+      x[i] = x[l]; y[i] = y[l]; px[i] = px[l]; py[i] = py[l]; pz[i] = pz[l];
+      gamma[i] = gamma[l]; psi[i] = psi[l]; q[i] = q[l];
+      n = n - 1;
+      continue;
+    }
+    i = i + 1;
+  }
+  double pos = sqrt(x[n - 1] * x[n - 1] + y[n - 1] * y[n - 1]);
+  if (pos >= edge) n = n - 1;
+  return n;
+}
+
+void orc_interp_psi(const orc_grid* g, int64_t np, const double* x, const double* y,
+                    const double* psif, double* psi) {                      /* :2264-2305 */
+  const double idr = 1.0 / g->dr;
+  for (int64_t pp = 0; pp < np; ++pp) {
+    interp_info ii = gen_interp_info(x[pp], y[pp], idr);
+    psi[pp] = interp_scalar(g, psif, &ii);
+  }
+}
+
+/* counting sort: sort_module.f03:10-41, part2d_class.f03:2498-2579 */
+void orc_sort(const orc_grid* g, int64_t np, double* x, double* y, double* px, double* py,
+              double* pz, double* gamma, double* psi, double* q, int32_t* keys, int32_t* sort_idx) {
+  const int nr = g->nr;
+  const double idr = 1.0 / g->dr;
+  for (int64_t i = 0; i < np; ++i) {
+    double pos = sqrt(x[i] * x[i] + y[i] * y[i]) * idr;
+    keys[i] = (int32_t)floor(pos) + 1;
+  }
+  int64_t* counter = (int64_t*)calloc((size_t)nr + 2, sizeof(int64_t));
+  for (int64_t i = 0; i < np; ++i) counter[keys[i]] += 1;
+  for (int k = 2; k <= nr; ++k) counter[k] += counter[k - 1];
+  for (int64_t i = 0; i < np; ++i) {
+    int k = keys[i];
+    sort_idx[i] = (int32_t)counter[k];       /* 1-based destination */
+    counter[k] -= 1;
+  }
+  free(counter);
+  double* buf = (double*)malloc(sizeof(double) * (size_t)(np > 0 ? np : 1));
+  double* arrs[8] = {x, y, px, py, pz, gamma, q, psi};
+  for (int a = 0; a < 8; ++a) {
+    memcpy(buf, arrs[a], sizeof(double) * (size_t)np);
+    for (int64_t i = 0; i < np; ++i) arrs[a][sort_idx[i] - 1] = buf[i];
+  }
+  free(buf);
+}
+
+/* =============================================================================
+ * Beam: part3d_class.f03
+ * q2 and e2/b2 are f2 stores: slices 1..nz+1.
+ * ============================================================================= */
+#define F2(f, nc, s, p, c, i) \
+  ((f)[((((size_t)(s) - 1) * (size_t)P + (size_t)(p)) * (nc) + (c)) * (size_t)NR2 + (size_t)(i)])
+
+void orc_beam_qdeposit(const orc_grid* g, int64_t nb, const double* x, const double* y,
+                       const double* z, const double* q, double* q2) {    /* :221-356 */
+  const int M = g->max_mode, P = nparts(g), nr = g->nr, nz = g->nz;
+  const double idr = 1.0 / g->dr, idz = 1.0 / g->dxi;
+  for (int64_t pp = 0; pp < nb; ++pp) {
+    double pr = sqrt(x[pp] * x[pp] + y[pp] * y[pp]) * idr;
+    double pzs = z[pp] * idz;
+    double ph0r = x[pp] / pr * idr, ph0i = -y[pp] / pr * idr;
+    if (!(pr >= 0.0 && pr < 1.0e9 && pzs >= 0.0 && pzs < 1.0e9)) continue;
+    int nn = (int)floor(pr), mm = (int)floor(pzs);
+    pr = pr - (double)nn;
+    pzs = pzs - (double)mm;
+    nn = nn + 1;
+    mm = mm + 1;
+    if (mm < 1 || mm > nz || nn < 1 || nn > nr) continue;   /* outside the stored box */
+    double wr[2] = {1.0 - pr, pr}, wz[2] = {1.0 - pzs, pzs};
+    double phr = 1.0 * q[pp], phi = 0.0 * q[pp];
+    for (int k = 0; k < 2; ++k)
+      for (int j = 0; j < 2; ++j)
+        F2(q2, 1, mm + k, 0, 0, nn + j) = F2(q2, 1, mm + k, 0, 0, nn + j) + wr[j] * wz[k] * phr;
+    for (int m = 1; m <= M; ++m) {
+      double t = phr * ph0r - phi * ph0i;
+      phi = phr * ph0i + phi * ph0r;
+      phr = t;
+      for (int k = 0; k < 2; ++k)
+        for (int j = 0; j < 2; ++j) {
+          F2(q2, 1, mm + k, PRE(m), 0, nn + j) = F2(q2, 1, mm + k, PRE(m), 0, nn + j) + wr[j] * wz[k] * phr;
+          F2(q2, 1, mm + k, PIM(m), 0, nn + j) = F2(q2, 1, mm + k, PIM(m), 0, nn + j) + wr[j] * wz[k] * phi;
+        }
+    }
+  }
+  for (int s = 1; s <= nz; ++s) {
+    F2(q2, 1, s, 0, 0, 0) = 0.0;
+    F2(q2, 1, s, 0, 0, 1) = 8.0 * F2(q2, 1, s, 0, 0, 1);
+    for (int m = 1; m <= M; ++m) {
+      F2(q2, 1, s, PRE(m), 0, 0) = 0.0; F2(q2, 1, s, PIM(m), 0, 0) = 0.0;
+      F2(q2, 1, s, PRE(m), 0, 1) = 0.0; F2(q2, 1, s, PIM(m), 0, 1) = 0.0;
+    }
+    for (int j = 2; j <= nr + 1; ++j) {
+      double ir = 1.0 / (double)(j - 1);
+      for (int p = 0; p < P; ++p) F2(q2, 1, s, p, 0, j) = F2(q2, 1, s, p, 0, j) * ir;
+    }
+  }
+}
+
+/* interp_emf_part3d :691-790 */
+static inline void beam_interp(const orc_grid* g, const double* e2, const double* b2, double x,
+                               double y, double z, double ep[3], double bp[3]) {
+  const int M = g->max_mode, P = nparts(g);
+  const double idr = 1.0 / g->dr, idz = 1.0 / g->dxi;
+  double pr = sqrt(x * x + y * y) * idr;
+  double pzs = z * idz;
+  double cc = x / pr * idr, ss = y / pr * idr;
+  for (int c = 0; c < 3; ++c) { ep[c] = 0.0; bp[c] = 0.0; }
+  if (!(pr >= 0.0 && pr < 1.0e9 && pzs > -1.0 && pzs < 1.0e9)) return;
+  int nn = (int)pr, mm = (int)pzs;
+  pr = pr - (double)nn;
+  pzs = pzs - (double)mm;
+  nn = nn + 1;
+  mm = mm + 1;
+  double wr[2] = {1.0 - pr, pr}, wz[2] = {1.0 - pzs, pzs};
+  for (int c = 0; c < 3; ++c) { ep[c] = 0.0; bp[c] = 0.0; }
+  if (nn < 1 || nn > g->nr || mm < 1 || mm > g->nz) return;  /* outside the stored box */
+  for (int k = 0; k < 2; ++k)
+    for (int j = 0; j < 2; ++j) {
+      double wt = wr[j] * wz[k];
+      for (int c = 0; c < 3; ++c) {
+        ep[c] = ep[c] + F2(e2, 3, mm + k, 0, c, nn + j) * wt;
+        bp[c] = bp[c] + F2(b2, 3, mm + k, 0, c, nn + j) * wt;
+      }
+    }
+  double phr = 1.0, phi = 0.0;
+  for (int m = 1; m <= M; ++m) {
+    double t = phr * cc - phi * ss;
+    phi = phr * ss + phi * cc;
+    phr = t;
+    double ph_r = 2.0 * phr, ph_i = 2.0 * phi;
+    for (int k = 0; k < 2; ++k)
+      for (int j = 0; j < 2; ++j) {
+        double wt = wr[j] * wz[k];
+        for (int c = 0; c < 3; ++c) {
+          ep[c] = ep[c] + (F2(e2, 3, mm + k, PRE(m), c, nn + j) * ph_r - F2(e2, 3, mm + k, PIM(m), c, nn + j) * ph_i) * wt;
+          bp[c] = bp[c] + (F2(b2, 3, mm + k, PRE(m), c, nn + j) * ph_r - F2(b2, 3, mm + k, PIM(m), c, nn + j) * ph_i) * wt;
+        }
+      }
+  }
+  double a = ep[0] * cc - ep[1] * ss, b = ep[0] * ss + ep[1] * cc;
+  ep[0] = a; ep[1] = b;
+  a = bp[0] * cc - bp[1] * ss; b = bp[0] * ss + bp[1] * cc;
+  bp[0] = a; bp[1] = b;
+}
+
+void orc_beam_push(const orc_grid* g, int push_type, double qbm, double dt, int64_t nb,
+                   double* x, double* y, double* z, double* px, double* py, double* pz,
+                   const double* e2, const double* b2, int nthreads) {
+  const double qtmh = qbm * dt * 0.5;
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+  for (int64_t pp = 0; pp < nb; ++pp) {
+    double ep[3], bp[3], p[3] = {px[pp], py[pp], pz[pp]};
+    beam_interp(g, e2, b2, x[pp], y[pp], z[pp], ep, bp);
+    if (push_type == ORC_PUSH3_REDUCED) {                     /* :477-576 */
+      double wp[3];
+      for (int c = 0; c < 3; ++c) { ep[c] = ep[c] * qtmh; bp[c] = bp[c] * qtmh; }
+      wp[0] = ep[0] - bp[1];
+      wp[1] = ep[1] + bp[0];
+      wp[2] = ep[2];
+      for (int c = 0; c < 3; ++c) p[c] = p[c] + wp[c];
+      for (int c = 0; c < 3; ++c) p[c] = p[c] + wp[c];
+    } else {                                                  /* :358-475 */
+      double utmp[3];
+      for (int c = 0; c < 3; ++c) { ep[c] = ep[c] * qtmh; utmp[c] = p[c] + ep[c]; }
+      double u2 = utmp[0] * utmp[0] + utmp[1] * utmp[1] + utmp[2] * utmp[2];
+      double gam = sqrt(1.0 + u2);
+      double gq = qtmh / gam;
+      for (int c = 0; c < 3; ++c) bp[c] = bp[c] * gq;
+      p[0] = utmp[0] + utmp[1] * bp[2] - utmp[2] * bp[1];
+      p[1] = utmp[1] + utmp[2] * bp[0] - utmp[0] * bp[2];
+      p[2] = utmp[2] + utmp[0] * bp[1] - utmp[1] * bp[0];
+      double ostq = 2.0 / (1.0 + bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2]);
+      for (int c = 0; c < 3; ++c) bp[c] = bp[c] * ostq;
+      double t0 = utmp[0] + p[1] * bp[2] - p[2] * bp[1];
+      double t1 = utmp[1] + p[2] * bp[0] - p[0] * bp[2];
+      double t2 = utmp[2] + p[0] * bp[1] - p[1] * bp[0];
+      p[0] = t0 + ep[0]; p[1] = t1 + ep[1]; p[2] = t2 + ep[2];
+    }
+    double dt_gam = dt / sqrt(1.0 + p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    x[pp] = x[pp] + p[0] * dt_gam;
+    y[pp] = y[pp] + p[1] * dt_gam;
+    z[pp] = z[pp] - p[2] * dt_gam + dt;
+    px[pp] = p[0]; py[pp] = p[1]; pz[pp] = p[2];
+  }
+}
+
+int64_t orc_beam_update_bound(const orc_grid* g, int64_t nb, double* x, double* y, double* z,
+                              double* px, double* py, double* pz, double* q) {  /* :640-689 */
+  if (nb == 0) return 0;
+  const double er = (double)g->nr * g->dr, ez = (double)g->nz * g->dxi;
+  int64_t i = 0, n = nb;
+  while (i < n - 1) {
+    double pr = sqrt(x[i] * x[i] + y[i] * y[i]);
+    if (pr >= er || z[i] >= ez) {
+      int64_t l = n - 1;
+      x[i] = x[l]; y[i] = y[l]; z[i] = z[l]; px[i] = px[l]; py[i] = py[l]; pz[i] = pz[l]; q[i] = q[l];
+      n = n - 1;
+      continue;
+    }
+    i = i + 1;
+  }
+  double pr = sqrt(x[n - 1] * x[n - 1] + y[n - 1] * y[n - 1]);
+  if (pr >= er || z[n - 1] >= ez) n = n - 1;
+  return n;
+}
+
+/* =============================================================================
+ * Loaders.  The reference draws from gfortran's random_number through rand_norm
+ * (math_module.f03:77-102), which cannot be reproduced without gfortran; the
+ * project substitutes a SplitMix64 stream (Steele, Lea & Flood 2014) feeding the
+ * same Box-Muller pairing.  Product and oracle implement the identical generator.
+ * ============================================================================= */
+void orc_rng_seed(orc_rng* r, uint64_t seed) { r->s = seed; r->have = 0; r->next = 0.0; }
+
+static uint64_t splitmix64(uint64_t* s) {
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+double orc_rand_uniform(orc_rng* r) {
+  return ((double)(splitmix64(&r->s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+double orc_rand_norm(orc_rng* r) {
+  if (!r->have) {
+    double u1 = orc_rand_uniform(r), u2 = orc_rand_uniform(r);
+    double theta = 2.0 * ORC_PI * u1;
+    double amp = sqrt(-2.0 * log(u2));
+    r->next = amp * sin(theta);
+    r->have = 1;
+    return amp * cos(theta);
+  }
+  r->have = 0;
+  double v = r->next;
+  r->next = 0.0;
+  return v;
+}
+
+int64_t orc_load_plasma(const orc_grid* g, orc_rng* r, int ppc1, int ppc2, int num_theta,
+                        double qm, double density, const double uth[3], double* x, double* y,
+                        double* px, double* py, double* pz, double* gamma, double* psi, double* q) {
+  /* fdist2d_class.f03:289-357 with uniform transverse and longitudinal profiles */
+  const int nr = g->nr;
+  const double dr = g->dr, dtheta = 2.0 * ORC_PI / num_theta;
+  const int ppc_tot = ppc1 * ppc2;
+  const double coef = (qm >= 0.0 ? 1.0 : -1.0) / ((double)ppc_tot * (double)num_theta);
+  const double den_lon = 1.0, den_perp = 1.0, den_min = 1.0e-10;
+  int64_t ip = 0;
+  for (int j = 1; j <= num_theta; ++j)
+    for (int i = 1; i <= nr; ++i)
+      for (int i1 = 1; i1 <= ppc1; ++i1) {
+        double rn = (i1 - 0.5) / ppc1 + (double)(i - 1);
+        for (int i2 = 1; i2 <= ppc2; ++i2) {
+          double theta = ((i2 - 0.5) / ppc2 + j - 1.0) * dtheta;
+          double xt = rn * dr * cos(theta), yt = rn * dr * sin(theta);
+          if (den_lon * den_perp * density < den_min) continue;
+          x[ip] = xt;
+          y[ip] = yt;
+          q[ip] = rn * den_perp * den_lon * density * coef;
+          px[ip] = uth[0] * orc_rand_norm(r);
+          py[ip] = uth[1] * orc_rand_norm(r);
+          pz[ip] = uth[2] * orc_rand_norm(r);
+          gamma[ip] = sqrt(1.0 + px[ip] * px[ip] + py[ip] * py[ip] + pz[ip] * pz[ip]);
+          psi[ip] = (1.0 - gamma[ip] + pz[ip]) / qm;
+          ++ip;
+        }
+      }
+  return ip;
+}
+
+int64_t orc_load_beam(const orc_grid* g, orc_rng* r, const orc_beam_desc* d, double* x, double* y,
+                      double* z, double* px, double* py, double* pz, double* q) {
+  /* fdist3d_rnd_class.f03:360-514, Gaussian profiles, cartesian geometry */
+  const double dr = g->dr, dz = g->dxi;
+  const double er = (double)g->nr * dr, ez = (double)g->nz * dz;
+  const double q_per_part = (d->qm >= 0.0 ? 1.0 : -1.0) * d->tot_charge /
+                            (2.0 * ORC_PI * (double)d->tot_num * (dr * dr) * dz);
+  int64_t n = 0;
+  for (int64_t i = 0; i < d->tot_num; ++i) {
+    double xt[3];
+    for (;;) {
+      xt[0] = orc_rand_norm(r) * d->sigma[0] + d->center[0];
+      if (xt[0] < d->range_lo[0] || xt[0] >= d->range_hi[0]) continue;
+      xt[1] = orc_rand_norm(r) * d->sigma[1] + d->center[1];
+      if (xt[1] < d->range_lo[1] || xt[1] >= d->range_hi[1]) continue;
+      xt[2] = orc_rand_norm(r) * d->sigma[2] + d->center[2];
+      if (xt[2] < d->range_lo[2] || xt[2] >= d->range_hi[2]) continue;
+      break;
+    }
+    double rt = sqrt(xt[0] * xt[0] + xt[1] * xt[1]);
+    if (rt < 0.0 || rt >= er) continue;
+    if (xt[2] < 0.0 || xt[2] >= ez) continue;
+    x[n] = xt[0]; y[n] = xt[1]; z[n] = xt[2];
+    q[n] = q_per_part;
+    px[n] = d->uth[0] * orc_rand_norm(r);
+    py[n] = d->uth[1] * orc_rand_norm(r);
+    pz[n] = d->uth[2] * orc_rand_norm(r) + d->gamma;
+    pz[n] = sqrt(pz[n] * pz[n] - px[n] * px[n] - py[n] * py[n] - 1);
+    ++n;
+  }
+  if (d->quiet) {
+    int64_t ip = n;
+    for (int64_t i = 0; i < ip; ++i) {
+      x[ip + i] = -x[i]; y[ip + i] = -y[i]; z[ip + i] = z[i];
+      px[ip + i] = -px[i]; py[ip + i] = -py[i]; pz[ip + i] = pz[i];
+      q[i] = 0.5 * q[i];
+      q[ip + i] = q[i];
+    }
+    n *= 2;
+  }
+  return n;
+}
+
+/* =============================================================================
+ * Whole-loop driver: simulation_class.f03:294-512 (one 3D step)
+ * ============================================================================= */
+struct orc_sim {
+  orc_sim_desc d;
+  int P;
+  size_t n1, n2;  /* doubles per 1-component f1 / f2 */
+  /* slice fields */
+  double *psi, *e, *e_spe, *b, *b_spe, *b_beam, *cu, *amu, *acu, *dcu, *q_spe, *q_beam, *qsp, *qn;
+  /* 3D stores */
+  double *q_beam2, *e2, *b2, *psi2, *b_spe2, *e_spe2, *cu2, *q_spe2;
+  /* plasma */
+  int64_t np;
+  double *x, *y, *px, *py, *pz, *gamma, *ppsi, *q;
+  /* beams */
+  int64_t nb[4];
+  double *bx[4], *by[4], *bz[4], *bpx[4], *bpy[4], *bpz[4], *bq[4];
+  double *s_re, *s_im;
+};
+
+static double* zalloc(size_t n) { return (double*)calloc(n ? n : 1, sizeof(double)); }
+
+orc_sim* orc_sim_create(const orc_sim_desc* d) {
+  orc_sim* s = (orc_sim*)calloc(1, sizeof(orc_sim));
+  s->d = *d;
+  const orc_grid* g = &s->d.g;
+  s->P = nparts(g);
+  s->n1 = (size_t)s->P * NR2;
+  s->n2 = s->n1 * (size_t)(g->nz + 1);
+  s->psi = zalloc(s->n1); s->e = zalloc(3 * s->n1); s->e_spe = zalloc(3 * s->n1);
+  s->b = zalloc(3 * s->n1); s->b_spe = zalloc(3 * s->n1); s->b_beam = zalloc(3 * s->n1);
+  s->cu = zalloc(3 * s->n1); s->amu = zalloc(3 * s->n1); s->acu = zalloc(2 * s->n1);
+  s->dcu = zalloc(2 * s->n1); s->q_spe = zalloc(s->n1); s->q_beam = zalloc(s->n1);
+  s->qsp = zalloc(s->n1); s->qn = zalloc(s->n1);
+  s->q_beam2 = zalloc(s->n2); s->e2 = zalloc(3 * s->n2); s->b2 = zalloc(3 * s->n2);
+  s->psi2 = zalloc(s->n2); s->b_spe2 = zalloc(3 * s->n2); s->e_spe2 = zalloc(3 * s->n2);
+  s->cu2 = zalloc(3 * s->n2); s->q_spe2 = zalloc(s->n2);
+  int64_t npm = d->sp_npmax;
+  s->x = zalloc(npm); s->y = zalloc(npm); s->px = zalloc(npm); s->py = zalloc(npm);
+  s->pz = zalloc(npm); s->gamma = zalloc(npm); s->ppsi = zalloc(npm); s->q = zalloc(npm);
+  for (int k = 0; k < d->nbeams; ++k) {
+    int64_t n = d->beam_npmax[k];
+    s->bx[k] = zalloc(n); s->by[k] = zalloc(n); s->bz[k] = zalloc(n);
+    s->bpx[k] = zalloc(n); s->bpy[k] = zalloc(n); s->bpz[k] = zalloc(n); s->bq[k] = zalloc(n);
+  }
+  s->s_re = zalloc((size_t)g->nr);
+  s->s_im = zalloc((size_t)g->nr);
+  return s;
+}
+
+void orc_sim_destroy(orc_sim* s) {
+  if (!s) return;
+  double* all[] = {s->psi, s->e, s->e_spe, s->b, s->b_spe, s->b_beam, s->cu, s->amu, s->acu, s->dcu,
+                   s->q_spe, s->q_beam, s->qsp, s->qn, s->q_beam2, s->e2, s->b2, s->psi2, s->b_spe2,
+                   s->e_spe2, s->cu2, s->q_spe2, s->x, s->y, s->px, s->py, s->pz, s->gamma, s->ppsi,
+                   s->q, s->s_re, s->s_im};
+  for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); ++i) free(all[i]);
+  for (int k = 0; k < s->d.nbeams; ++k) {
+    free(s->bx[k]); free(s->by[k]); free(s->bz[k]); free(s->bpx[k]); free(s->bpy[k]);
+    free(s->bpz[k]); free(s->bq[k]);
+  }
+  free(s);
+}
+
+void orc_sim_set_plasma(orc_sim* s, int64_t np, const double* x, const double* y,
+                        const double* px, const double* py, const double* pz,
+                        const double* gamma, const double* psi, const double* q) {
+  const orc_grid* g = &s->d.g;
+  s->np = np;
+  size_t b = sizeof(double) * (size_t)np;
+  memcpy(s->x, x, b); memcpy(s->y, y, b); memcpy(s->px, px, b); memcpy(s->py, py, b);
+  memcpy(s->pz, pz, b); memcpy(s->gamma, gamma, b); memcpy(s->ppsi, psi, b); memcpy(s->q, q, b);
+  /* species2d_class.f03:114-129 / 171-180: qn = -(deposit of the fresh particles) */
+  memset(s->qsp, 0, sizeof(double) * s->n1);
+  orc_qdeposit(g, s->np, s->x, s->y, s->q, s->qsp);
+  for (size_t i = 0; i < s->n1; ++i) s->qn[i] = s->qsp[i] * -1.0;
+}
+
+void orc_sim_set_beam(orc_sim* s, int k, int64_t nb, const double* x, const double* y,
+                      const double* z, const double* px, const double* py, const double* pz,
+                      const double* q) {
+  s->nb[k] = nb;
+  size_t b = sizeof(double) * (size_t)nb;
+  memcpy(s->bx[k], x, b); memcpy(s->by[k], y, b); memcpy(s->bz[k], z, b);
+  memcpy(s->bpx[k], px, b); memcpy(s->bpy[k], py, b); memcpy(s->bpz[k], pz, b);
+  memcpy(s->bq[k], q, b);
+}
+
+static void copy_1to2(orc_sim* s, const double* f1, double* f2, int nc, int j) {
+  size_t n = s->n1 * (size_t)nc;
+  memcpy(f2 + (size_t)(j - 1) * n, f1, sizeof(double) * n);
+}
+
+void orc_sim_begin_3dstep(orc_sim* s) {
+  const orc_grid* g = &s->d.g;
+  const size_t n1 = s->n1;
+  /* simulation_class.f03:309-317 */
+  memset(s->q_beam2, 0, sizeof(double) * s->n2);
+  memset(s->q_spe2, 0, sizeof(double) * s->n2);
+  for (int k = 0; k < s->d.nbeams; ++k)
+    orc_beam_qdeposit(g, s->nb[k], s->bx[k], s->by[k], s->bz[k], s->bq[k], s->q_beam2);
+  /* :332-341 */
+  memset(s->b, 0, 3 * n1 * sizeof(double)); memset(s->e, 0, 3 * n1 * sizeof(double));
+  memset(s->b_spe, 0, 3 * n1 * sizeof(double)); memset(s->e_spe, 0, 3 * n1 * sizeof(double));
+  memset(s->psi, 0, n1 * sizeof(double)); memset(s->cu, 0, 3 * n1 * sizeof(double));
+  memset(s->acu, 0, 2 * n1 * sizeof(double)); memset(s->amu, 0, 3 * n1 * sizeof(double));
+}
+
+/* one xi slice j: simulation_class.f03:342-469 */
+void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
+  const orc_grid* g = &s->d.g;
+  const int nt = s->d.nthreads;
+  const double dxi = g->dxi;
+  const size_t n1 = s->n1;
+  {
+    /* :344-345 q_beam%copy_slice(j, 2->1); b_beam%solve(q_beam) */
+    memcpy(s->q_beam, s->q_beam2 + (size_t)(j - 1) * n1, n1 * sizeof(double));
+    orc_solve_bt_beam(g, s->q_beam, s->b_beam);
+    /* :346-349 q_spe = 0; spe%qdp(q_spe) (species2d_class.f03:186-208) */
+    memset(s->q_spe, 0, n1 * sizeof(double));
+    memset(s->qsp, 0, n1 * sizeof(double));
+    orc_qdeposit(g, s->np, s->x, s->y, s->q, s->qsp);
+    for (size_t i = 0; i < n1; ++i) s->q_spe[i] = s->q_spe[i] + s->qsp[i];
+    if (s->d.sp_neutralized) for (size_t i = 0; i < n1; ++i) s->q_spe[i] = s->q_spe[i] + s->qn[i];
+    /* :356-360 */
+    orc_solve_psi(g, s->q_spe, s->psi);
+    if (s->d.sp_push_type == ORC_PUSH_STD) orc_interp_psi(g, s->np, s->x, s->y, s->psi, s->ppsi);
+    orc_solve_bz(g, s->cu, s->b_spe);
+    /* :370-398 predictor-corrector */
+    int l;
+    double rel_res = 0.0, abs_res = 0.0;
+    for (l = 1; l <= s->d.iter_max; ++l) {
+      orc_conv_record(g, s->b_spe, s->s_re, s->s_im);
+      for (size_t i = 0; i < 3 * n1; ++i) s->b[i] = s->b_spe[i] + s->b_beam[i];
+      orc_solve_ez(g, s->cu, s->e);
+      orc_solve_et(g, s->b, s->psi, s->e);
+      memset(s->cu, 0, 3 * n1 * sizeof(double));
+      memset(s->acu, 0, 2 * n1 * sizeof(double));
+      memset(s->amu, 0, 3 * n1 * sizeof(double));
+      orc_amjdeposit(g, s->d.sp_push_type, s->d.sp_qbm, dxi, s->np, s->x, s->y, s->px, s->py, s->pz,
+                     s->q, s->gamma, s->ppsi, s->e, s->b, s->cu, s->amu, s->acu, nt);
+      orc_solve_djdxi(g, s->acu, s->amu, s->dcu);
+      orc_solve_bt_iter(g, s->dcu, s->cu, s->b_spe);
+      orc_solve_bz(g, s->cu, s->b_spe);
+      orc_conv_compare(g, s->b_spe, s->s_re, s->s_im, &rel_res, &abs_res);
+      if (rel_res < s->d.iter_reltol || abs_res < s->d.iter_abstol) break;
+    }
+    if (iters) *iters = l > s->d.iter_max ? s->d.iter_max : l;
+    if (rel) *rel = rel_res;
+    /* :403-416 cbq, stores */
+    copy_1to2(s, s->cu, s->cu2, 3, j);
+    for (int i = 0; i < NR2 * s->P; ++i) {
+      int p = i / NR2, n = i % NR2;
+      F(s->q_spe, 1, p, 0, n) = F(s->q_spe, 1, p, 0, n) + F(s->cu, 3, p, 2, n);
+    }
+    copy_1to2(s, s->q_spe, s->q_spe2, 1, j);
+    for (size_t i = 0; i < 3 * n1; ++i) s->b[i] = s->b_spe[i] + s->b_beam[i];
+    orc_solve_et(g, s->b_spe, s->psi, s->e_spe);
+    orc_solve_ez(g, s->cu, s->e);
+    orc_solve_et(g, s->b, s->psi, s->e);
+    /* :425-426 dcu *= dxi; cu(1:2) += dcu(1:2) */
+    for (size_t i = 0; i < 2 * n1; ++i) s->dcu[i] = s->dcu[i] * dxi;
+    for (int p = 0; p < s->P; ++p)
+      for (int c = 0; c < 2; ++c)
+        for (int n = 0; n < NR2; ++n) F(s->cu, 3, p, c, n) = F(s->cu, 3, p, c, n) + F(s->dcu, 2, p, c, n);
+    /* :437-441 push_u, push_x (+update_bound) */
+    orc_push_u(g, s->d.sp_push_type, s->d.sp_qbm, dxi, s->np, s->x, s->y, s->px, s->py, s->pz,
+               s->gamma, s->ppsi, s->e, s->b, nt);
+    orc_push_x(s->np, dxi, s->x, s->y, s->px, s->py, s->pz, s->gamma);
+    s->np = orc_update_bound(g, s->np, s->x, s->y, s->px, s->py, s->pz, s->gamma, s->ppsi, s->q);
+    /* :452-456 copy slices */
+    copy_1to2(s, s->e, s->e2, 3, j);
+    copy_1to2(s, s->b, s->b2, 3, j);
+    copy_1to2(s, s->psi, s->psi2, 1, j);
+    copy_1to2(s, s->b_spe, s->b_spe2, 3, j);
+    copy_1to2(s, s->e_spe, s->e_spe2, 3, j);
+  }
+}
+
+/* :487-492 beam push (slice nz+1 of e2/b2 stays zero on one stage) */
+void orc_sim_end_3dstep(orc_sim* s, int push_beams) {
+  const orc_grid* g = &s->d.g;
+  const int nt = s->d.nthreads;
+  if (push_beams) {
+    for (int k = 0; k < s->d.nbeams; ++k) {
+      orc_beam_push(g, s->d.beam_push_type[k], s->d.beam_qbm[k], s->d.dt3d, s->nb[k], s->bx[k], s->by[k],
+                    s->bz[k], s->bpx[k], s->bpy[k], s->bpz[k], s->e2, s->b2, nt);
+      s->nb[k] = orc_beam_update_bound(g, s->nb[k], s->bx[k], s->by[k], s->bz[k], s->bpx[k], s->bpy[k],
+                                       s->bpz[k], s->bq[k]);
+    }
+  }
+}
+
+void orc_sim_run_3dstep(orc_sim* s, int push_beams, int* iters, double* rel) {
+  orc_sim_begin_3dstep(s);
+  for (int j = 1; j <= s->d.g.nz; ++j) orc_sim_slice(s, j, iters ? iters + (j - 1) : NULL, rel ? rel + (j - 1) : NULL);
+  orc_sim_end_3dstep(s, push_beams);
+}
+
+double* orc_sim_field(orc_sim* s, const char* name, int* nc) {
+  struct { const char* n; double* p; int c; } t[] = {
+      {"psi", s->psi, 1}, {"e", s->e, 3}, {"e_spe", s->e_spe, 3}, {"b", s->b, 3},
+      {"b_spe", s->b_spe, 3}, {"b_beam", s->b_beam, 3}, {"cu", s->cu, 3}, {"amu", s->amu, 3},
+      {"acu", s->acu, 2}, {"dcu", s->dcu, 2}, {"q_spe", s->q_spe, 1}, {"q_beam", s->q_beam, 1},
+      {"qn", s->qn, 1}};
+  for (size_t i = 0; i < sizeof(t) / sizeof(t[0]); ++i)
+    if (!strcmp(t[i].n, name)) { if (nc) *nc = t[i].c; return t[i].p; }
+  return NULL;
+}
+
+double* orc_sim_store(orc_sim* s, const char* name, int* nc) {
+  struct { const char* n; double* p; int c; } t[] = {
+      {"q_beam", s->q_beam2, 1}, {"e", s->e2, 3}, {"b", s->b2, 3}, {"psi", s->psi2, 1},
+      {"b_spe", s->b_spe2, 3}, {"e_spe", s->e_spe2, 3}, {"cu", s->cu2, 3}, {"q_spe", s->q_spe2, 1}};
+  for (size_t i = 0; i < sizeof(t) / sizeof(t[0]); ++i)
+    if (!strcmp(t[i].n, name)) { if (nc) *nc = t[i].c; return t[i].p; }
+  return NULL;
+}
+
+int64_t orc_sim_plasma(orc_sim* s, double** x, double** y, double** px, double** py, double** pz,
+                       double** gamma, double** psi, double** q) {
+  *x = s->x; *y = s->y; *px = s->px; *py = s->py; *pz = s->pz; *gamma = s->gamma; *psi = s->ppsi; *q = s->q;
+  return s->np;
+}
+
+int64_t orc_sim_beam(orc_sim* s, int k, double** x, double** y, double** z, double** px, double** py,
+                     double** pz, double** q) {
+  *x = s->bx[k]; *y = s->by[k]; *z = s->bz[k]; *px = s->bpx[k]; *py = s->bpy[k]; *pz = s->bpz[k]; *q = s->bq[k];
+  return s->nb[k];
+}

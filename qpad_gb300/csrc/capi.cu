@@ -1,0 +1,893 @@
+// capi.cu -- the C ABI (include/qpad_gpu.h): contexts, fields, species, beams and the
+// fused slice / 3D-step drivers of run_simulation (simulation_class.f03:294-512).
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "particles.cuh"
+
+using namespace qpad;
+
+namespace qpad {
+
+int set_err(qpad_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int cuda_check(qpad_ctx* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return QPAD_OK;
+  return set_err(ctx, QPAD_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int check_launch(qpad_ctx* ctx, const char* what, int nlaunch) {
+  if (ctx) ctx->launches += nlaunch;
+  return cuda_check(ctx, cudaGetLastError(), what);
+}
+
+static cudaEvent_t ev_get(qpad_ctx* ctx) {
+  if (!ctx->ev_pool.empty()) {
+    cudaEvent_t e = ctx->ev_pool.back();
+    ctx->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void prof_begin(qpad_ctx* ctx, const char* name) {
+  if (!ctx->prof_on) return;
+  cudaEvent_t e = ev_get(ctx);
+  cudaEventRecord(e, ctx->stream);
+  ctx->prof[name].pending.push_back(e);
+}
+
+void prof_end(qpad_ctx* ctx, const char* name) {
+  if (!ctx->prof_on) return;
+  cudaEvent_t e = ev_get(ctx);
+  cudaEventRecord(e, ctx->stream);
+  ctx->prof[name].pending.push_back(e);
+}
+
+void prof_collect(qpad_ctx* ctx) {
+  for (auto& kv : ctx->prof) {
+    auto& pr = kv.second;
+    const size_t npair = pr.pending.size() / 2;
+    for (size_t k = 0; k < npair; ++k) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, pr.pending[2 * k], pr.pending[2 * k + 1]) == cudaSuccess) {
+        pr.ms += ms;
+        pr.n += 1;
+      }
+      ctx->ev_pool.push_back(pr.pending[2 * k]);
+      ctx->ev_pool.push_back(pr.pending[2 * k + 1]);
+    }
+    pr.pending.erase(pr.pending.begin(), pr.pending.begin() + 2 * npair);
+  }
+  cudaGetLastError();
+}
+
+}  // namespace qpad
+
+namespace {
+
+static thread_local std::string g_create_err;
+
+bool has_store(int f) {
+  switch (f) {
+    case QPAD_F_Q_BEAM: case QPAD_F_E: case QPAD_F_B: case QPAD_F_PSI: case QPAD_F_B_SPE:
+    case QPAD_F_E_SPE: case QPAD_F_CU: case QPAD_F_Q_SPE: return true;
+    default: return false;
+  }
+}
+
+size_t f1_elems(const qpad_ctx* c, int f) { return (size_t)c->g.P * field_ncomp(f) * c->g.ld; }
+size_t f2_elems(const qpad_ctx* c, int f) { return f1_elems(c, f) * (size_t)(c->g.nz + 1); }
+
+int dmalloc(qpad_ctx* ctx, void** p, size_t bytes, const char* what) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, e == cudaErrorMemoryAllocation ? QPAD_E_NOMEM : QPAD_E_CUDA,
+                   std::string("cudaMalloc(") + what + "): " + cudaGetErrorString(e));
+  }
+  return cudaMemsetAsync(*p, 0, bytes ? bytes : 8, ctx->stream) == cudaSuccess ? 0 : QPAD_E_CUDA;
+}
+
+bool valid_field(int f) { return f >= 0 && f < QPAD_NFIELDS; }
+
+// ---- small elementwise kernels over whole slice fields ------------------------------
+__global__ void k_fill(double* a, size_t n, double v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a[i] = v;
+}
+__global__ void k_add(const double* a, const double* b, double* c, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    c[i] = a[i] + b[i];
+}
+__global__ void k_add2(double* q, const double* a, const double* b, size_t n) {   // q = (q + a) + b
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double v = q[i] + a[i];
+    if (b) v = v + b[i];
+    q[i] = v;
+  }
+}
+__global__ void k_scale(double* a, size_t n, double s) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    a[i] = a[i] * s;
+}
+// b(bdim,:) += a(adim,:) for every mode part
+__global__ void k_add_dim(const double* a, int nca, int ca, double* b, int ncb, int cb, int P, int ld) {
+  const int p = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ld; i += gridDim.x * blockDim.x) {
+    double* d = b + ((size_t)p * ncb + cb) * ld + i;
+    *d = *d + a[((size_t)p * nca + ca) * ld + i];
+  }
+}
+__global__ void k_neg(const double* a, double* b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = a[i] * -1.0;
+}
+__global__ void k_deinterleave(const double* __restrict__ src, int64_t n, int nc, double* d0, double* d1,
+                               double* d2) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  d0[i] = src[nc * i];
+  d1[i] = src[nc * i + 1];
+  if (nc == 3) d2[i] = src[nc * i + 2];
+}
+__global__ void k_interleave(double* __restrict__ dst, int64_t n, int nc, const double* d0, const double* d1,
+                             const double* d2) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dst[nc * i] = d0[i];
+  dst[nc * i + 1] = d1[i];
+  if (nc == 3) dst[nc * i + 2] = d2[i];
+}
+
+int elem_grid(size_t n) {
+  size_t b = (n + 255) / 256;
+  return (int)(b < 1 ? 1 : (b > 4096 ? 4096 : b));
+}
+
+// ---- particle upload / download (Fortran layouts x(nc,np), p(3,np)) ------------------
+int upload_vec(qpad_ctx* ctx, double* staging, const double* host, int64_t n, int nc, double* d0, double* d1,
+               double* d2) {
+  if (n == 0) return 0;
+  cudaError_t e = cudaMemcpyAsync(staging, host, sizeof(double) * nc * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "upload");
+  k_deinterleave<<<(int)((n + 255) / 256), 256, 0, ctx->stream>>>(staging, n, nc, d0, d1, d2);
+  return check_launch(ctx, "deinterleave");
+}
+
+int download_vec(qpad_ctx* ctx, double* staging, double* host, int64_t n, int nc, const double* d0, const double* d1,
+                 const double* d2) {
+  if (n == 0) return 0;
+  k_interleave<<<(int)((n + 255) / 256), 256, 0, ctx->stream>>>(staging, n, nc, d0, d1, d2);
+  if (int r = check_launch(ctx, "interleave")) return r;
+  cudaError_t e = cudaMemcpyAsync(host, staging, sizeof(double) * nc * n, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "download");
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "download sync");
+}
+
+int h2d(qpad_ctx* ctx, double* d, const double* h, int64_t n) {
+  if (n == 0) return 0;
+  return cuda_check(ctx, cudaMemcpyAsync(d, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream), "h2d");
+}
+int d2h(qpad_ctx* ctx, double* h, const double* d, int64_t n) {
+  if (n == 0) return 0;
+  return cuda_check(ctx, cudaMemcpyAsync(h, d, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "d2h");
+}
+
+// neutralising background of one species: qn = -(finished charge deposit) (species2d_class.f03:114-129)
+int species_set_background(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  const size_t n1 = f1_elems(ctx, QPAD_F_Q_SPE);
+  if (cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "memset qraw");
+  if (int r = species_qdeposit_raw(sp, ctx->qraw)) return r;
+  if (int r = launch_finish_q(ctx, ctx->qraw, sp->qf, 0)) return r;
+  k_neg<<<elem_grid(n1), 256, 0, ctx->stream>>>(sp->qf, sp->qn, n1);
+  return check_launch(ctx, "qn");
+}
+
+// ctx->qn = sum of the neutralised species' backgrounds
+int rebuild_total_background(qpad_ctx* ctx) {
+  const size_t n1 = f1_elems(ctx, QPAD_F_Q_SPE);
+  if (cudaMemsetAsync(ctx->qn, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "memset qn");
+  for (qpad_species* s : ctx->species)
+    if (s->neutralized) {
+      k_add<<<elem_grid(n1), 256, 0, ctx->stream>>>(ctx->qn, s->qn, ctx->qn, n1);
+      if (int r = check_launch(ctx, "qn sum")) return r;
+    }
+  return 0;
+}
+
+int save_pristine(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  const double* src[8] = {sp->x[0], sp->y[0], sp->px[0], sp->py[0], sp->pz[0], sp->gamma[0], sp->psi[0], sp->q[0]};
+  for (int a = 0; a < 8; ++a)
+    if (sp->np > 0 && cudaMemcpyAsync(sp->pristine + (size_t)a * sp->npmax, src[a], sizeof(double) * sp->np,
+                                      cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+      return check_launch(ctx, "pristine copy");
+  sp->np_pristine = sp->np;
+  return 0;
+}
+
+int species_load(qpad_species* sp, const double* x, const double* p, const double* gamma, const double* psi,
+                 const double* q, int64_t np) {
+  qpad_ctx* ctx = sp->ctx;
+  if (np < 0 || np > sp->npmax) return set_err(ctx, QPAD_E_CAPACITY, "particle count exceeds npmax");
+  if (np > 0 && (!x || !p || !gamma || !psi || !q)) return set_err(ctx, QPAD_E_ARG, "null particle array");
+  sp->np = np;
+  double* staging = sp->x[1];   // scratch buffers are 8 * npmax doubles in total (contiguous)
+  if (int r = upload_vec(ctx, staging, x, np, 2, sp->x[0], sp->y[0], nullptr)) return r;
+  if (int r = upload_vec(ctx, staging + 2 * np, p, np, 3, sp->px[0], sp->py[0], sp->pz[0])) return r;
+  if (int r = h2d(ctx, sp->gamma[0], gamma, np)) return r;
+  if (int r = h2d(ctx, sp->psi[0], psi, np)) return r;
+  if (int r = h2d(ctx, sp->q[0], q, np)) return r;
+  *sp->h_count = np;
+  if (cudaMemcpyAsync(sp->d_count, sp->h_count, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "count upload");
+  if (int r = save_pristine(sp)) return r;
+  if (int r = species_set_background(sp)) return r;
+  if (int r = rebuild_total_background(ctx)) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "species load");
+}
+
+int beam_load(qpad_beam* bm, const double* x, const double* p, const double* q, int64_t nb) {
+  qpad_ctx* ctx = bm->ctx;
+  if (nb < 0 || nb > bm->npmax) return set_err(ctx, QPAD_E_CAPACITY, "beam particle count exceeds npmax");
+  if (nb > 0 && (!x || !p || !q)) return set_err(ctx, QPAD_E_ARG, "null beam array");
+  bm->nb = nb;
+  double* staging = bm->x[1];
+  if (int r = upload_vec(ctx, staging, x, nb, 3, bm->x[0], bm->y[0], bm->z[0])) return r;
+  if (int r = upload_vec(ctx, staging + 3 * nb, p, nb, 3, bm->px[0], bm->py[0], bm->pz[0])) return r;
+  if (int r = h2d(ctx, bm->q[0], q, nb)) return r;
+  *bm->h_count = nb;
+  if (cudaMemcpyAsync(bm->d_count, bm->h_count, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "count upload");
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "beam load");
+}
+
+int beam_sync_count(qpad_beam* bm) {
+  qpad_ctx* ctx = bm->ctx;
+  cudaError_t e = cudaMemcpyAsync(bm->h_count, bm->d_count, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "beam count");
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "beam count sync");
+  bm->nb = *bm->h_count;
+  return 0;
+}
+
+}  // namespace
+
+// =====================================================================================
+// context
+// =====================================================================================
+extern "C" int qpad_ctx_create(const qpad_grid_desc* d, qpad_ctx** out) {
+  if (!d || !out) return QPAD_E_ARG;
+  *out = nullptr;
+  if (d->nr < 8 || d->nr > 4096 || d->nz < 1 || d->max_mode < 0 || d->max_mode > QPAD_MAX_MODE || !(d->dr > 0) ||
+      !(d->dxi > 0) || d->iter_max < 1 || (d->bnd != QPAD_BND_OPEN && d->bnd != QPAD_BND_ZERO)) {
+    g_create_err = "invalid grid descriptor (8 <= nr <= 4096, 0 <= max_mode <= 8, dr, dxi > 0, iter_max >= 1)";
+    return QPAD_E_ARG;
+  }
+  qpad_ctx* ctx = new (std::nothrow) qpad_ctx();
+  if (!ctx) return QPAD_E_NOMEM;
+  GridDev& g = ctx->g;
+  g.nr = d->nr; g.nz = d->nz; g.M = d->max_mode; g.P = 2 * d->max_mode + 1; g.ld = d->nr + 2; g.bnd = d->bnd;
+  g.dr = d->dr; g.dxi = d->dxi; g.idr = 1.0 / d->dr;
+  g.relax_fac = d->relax_fac >= 0.0 ? d->relax_fac : 1.0e-3 * ((d->dr / 0.02) * (d->dr / 0.02));
+  ctx->iter_max = d->iter_max; ctx->reltol = d->iter_reltol; ctx->abstol = d->iter_abstol; ctx->dt = d->dt;
+  ctx->precision = d->precision; ctx->device = d->device;
+  int r = cuda_check(ctx, cudaSetDevice(d->device), "cudaSetDevice");
+  if (!r) r = cuda_check(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream");
+  for (int f = 0; f < QPAD_NFIELDS && !r; ++f) {
+    r = dmalloc(ctx, (void**)&ctx->f[f], f1_elems(ctx, f) * sizeof(double), "field");
+    if (!r && has_store(f)) r = dmalloc(ctx, (void**)&ctx->f2[f], f2_elems(ctx, f) * sizeof(double), "store");
+  }
+  if (!r) r = dmalloc(ctx, (void**)&ctx->qn, f1_elems(ctx, QPAD_F_Q_SPE) * sizeof(double), "qn");
+  if (!r) r = dmalloc(ctx, (void**)&ctx->qraw, f1_elems(ctx, QPAD_F_Q_SPE) * sizeof(double), "qraw");
+  if (!r) r = dmalloc(ctx, (void**)&ctx->conv, (2 * (size_t)g.nr + 8) * sizeof(double), "conv");
+  if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->h_res, 8 * sizeof(double)), "pinned");
+  if (!r) r = build_factors(ctx);
+  if (!r) r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "create sync");
+  if (r) {
+    g_create_err = ctx->err;
+    qpad_ctx_destroy(ctx);
+    return r;
+  }
+  *out = ctx;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_ctx_destroy(qpad_ctx* ctx) {
+  if (!ctx) return QPAD_OK;
+  std::vector<qpad_species*> sps = ctx->species;
+  for (auto* s : sps) qpad_species_destroy(s);
+  std::vector<qpad_beam*> bms = ctx->beams;
+  for (auto* b : bms) qpad_beam_destroy(b);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (int f = 0; f < QPAD_NFIELDS; ++f) {
+    if (ctx->f[f]) cudaFree(ctx->f[f]);
+    if (ctx->f2[f]) cudaFree(ctx->f2[f]);
+  }
+  if (ctx->fac) cudaFree(ctx->fac);
+  if (ctx->qn) cudaFree(ctx->qn);
+  if (ctx->qraw) cudaFree(ctx->qraw);
+  if (ctx->conv) cudaFree(ctx->conv);
+  if (ctx->scratch) cudaFree(ctx->scratch);
+  if (ctx->h_res) cudaFreeHost(ctx->h_res);
+  prof_collect(ctx);
+  for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return QPAD_OK;
+}
+
+extern "C" const char* qpad_last_error(const qpad_ctx* ctx) {
+  if (!ctx) return g_create_err.c_str();
+  return ctx->err.c_str();
+}
+
+extern "C" int qpad_synchronize(qpad_ctx* ctx) {
+  if (!ctx) return QPAD_E_ARG;
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "synchronize");
+}
+
+extern "C" int qpad_field_layout(const qpad_ctx* ctx, int field, int* ncomp, int64_t* ld) {
+  if (!ctx || !valid_field(field)) return QPAD_E_ARG;
+  if (ncomp) *ncomp = field_ncomp(field);
+  if (ld) *ld = ctx->g.ld;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_device_count(int* count) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  if (count) *count = n;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_launch_count(const qpad_ctx* ctx, int64_t* count) {
+  if (!ctx || !count) return QPAD_E_ARG;
+  *count = ctx->launches;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_profile_enable(qpad_ctx* ctx, int on) {
+  if (!ctx) return QPAD_E_ARG;
+  if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "profile sync")) return r;
+  prof_collect(ctx);
+  ctx->prof_on = on != 0;
+  if (on) ctx->prof.clear();
+  return QPAD_OK;
+}
+
+extern "C" int qpad_profile_read(qpad_ctx* ctx, const char* name, double* total_ms, int64_t* launches) {
+  if (!ctx || !name) return QPAD_E_ARG;
+  if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "profile sync")) return r;
+  prof_collect(ctx);
+  auto it = ctx->prof.find(name);
+  if (total_ms) *total_ms = it == ctx->prof.end() ? 0.0 : it->second.ms;
+  if (launches) *launches = it == ctx->prof.end() ? 0 : it->second.n;
+  return QPAD_OK;
+}
+
+// =====================================================================================
+// fields
+// =====================================================================================
+namespace {
+int part_ok(const qpad_ctx* ctx, int part) { return part >= 0 && part < ctx->g.P; }
+
+// host f1(dim, 0:nr+1) <-> device [c][i] line block of one part
+int f1_transfer(qpad_ctx* ctx, double* dev_part, int nc, double* host, bool upload) {
+  const int ld = ctx->g.ld;
+  std::vector<double> tmp((size_t)nc * ld);
+  if (upload) {
+    for (int i = 0; i < ld; ++i)
+      for (int c = 0; c < nc; ++c) tmp[(size_t)c * ld + i] = host[(size_t)i * nc + c];
+    if (int r = h2d(ctx, dev_part, tmp.data(), (int64_t)nc * ld)) return r;
+    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "upload sync");
+  }
+  if (int r = d2h(ctx, tmp.data(), dev_part, (int64_t)nc * ld)) return r;
+  if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "download sync")) return r;
+  for (int i = 0; i < ld; ++i)
+    for (int c = 0; c < nc; ++c) host[(size_t)i * nc + c] = tmp[(size_t)c * ld + i];
+  return 0;
+}
+}  // namespace
+
+extern "C" int qpad_field_upload(qpad_ctx* ctx, int field, int part, const double* f1) {
+  if (!ctx || !valid_field(field) || !part_ok(ctx, part) || !f1) return ctx ? set_err(ctx, QPAD_E_ARG, "bad args") : QPAD_E_ARG;
+  const int nc = field_ncomp(field);
+  return f1_transfer(ctx, ctx->f[field] + (size_t)part * nc * ctx->g.ld, nc, const_cast<double*>(f1), true);
+}
+
+extern "C" int qpad_field_download(qpad_ctx* ctx, int field, int part, double* f1) {
+  if (!ctx || !valid_field(field) || !part_ok(ctx, part) || !f1) return ctx ? set_err(ctx, QPAD_E_ARG, "bad args") : QPAD_E_ARG;
+  const int nc = field_ncomp(field);
+  return f1_transfer(ctx, ctx->f[field] + (size_t)part * nc * ctx->g.ld, nc, f1, false);
+}
+
+extern "C" int qpad_store_download(qpad_ctx* ctx, int field, int slice, int part, double* f1) {
+  if (!ctx || !valid_field(field) || !has_store(field) || !part_ok(ctx, part) || !f1 || slice < 1 ||
+      slice > ctx->g.nz + 1)
+    return ctx ? set_err(ctx, QPAD_E_ARG, "bad store args") : QPAD_E_ARG;
+  const int nc = field_ncomp(field);
+  double* dev = ctx->f2[field] + ((size_t)(slice - 1) * ctx->g.P + part) * nc * ctx->g.ld;
+  return f1_transfer(ctx, dev, nc, f1, false);
+}
+
+extern "C" int qpad_store_upload(qpad_ctx* ctx, int field, int slice, int part, const double* f1) {
+  if (!ctx || !valid_field(field) || !has_store(field) || !part_ok(ctx, part) || !f1 || slice < 1 ||
+      slice > ctx->g.nz + 1)
+    return ctx ? set_err(ctx, QPAD_E_ARG, "bad store args") : QPAD_E_ARG;
+  const int nc = field_ncomp(field);
+  double* dev = ctx->f2[field] + ((size_t)(slice - 1) * ctx->g.P + part) * nc * ctx->g.ld;
+  return f1_transfer(ctx, dev, nc, const_cast<double*>(f1), true);
+}
+
+extern "C" int qpad_field_fill(qpad_ctx* ctx, int field, double v) {
+  if (!ctx || !valid_field(field)) return QPAD_E_ARG;
+  const size_t n = f1_elems(ctx, field);
+  k_fill<<<elem_grid(n), 256, 0, ctx->stream>>>(ctx->f[field], n, v);
+  return check_launch(ctx, "fill");
+}
+
+extern "C" int qpad_store_fill(qpad_ctx* ctx, int field, double v) {
+  if (!ctx || !valid_field(field) || !has_store(field)) return ctx ? set_err(ctx, QPAD_E_ARG, "no store") : QPAD_E_ARG;
+  const size_t n = f2_elems(ctx, field);
+  k_fill<<<elem_grid(n), 256, 0, ctx->stream>>>(ctx->f2[field], n, v);
+  return check_launch(ctx, "store fill");
+}
+
+extern "C" int qpad_field_add(qpad_ctx* ctx, int a, int b, int c) {
+  if (!ctx || !valid_field(a) || !valid_field(b) || !valid_field(c) || field_ncomp(a) != field_ncomp(c) ||
+      field_ncomp(b) != field_ncomp(c))
+    return ctx ? set_err(ctx, QPAD_E_ARG, "field_add: mismatched fields") : QPAD_E_ARG;
+  const size_t n = f1_elems(ctx, c);
+  k_add<<<elem_grid(n), 256, 0, ctx->stream>>>(ctx->f[a], ctx->f[b], ctx->f[c], n);
+  return check_launch(ctx, "add");
+}
+
+extern "C" int qpad_field_add_dim(qpad_ctx* ctx, int a, int b, const int32_t* adim, const int32_t* bdim, int n) {
+  if (!ctx || !valid_field(a) || !valid_field(b) || !adim || !bdim || n < 0) return QPAD_E_ARG;
+  for (int k = 0; k < n; ++k) {
+    if (adim[k] < 1 || adim[k] > field_ncomp(a) || bdim[k] < 1 || bdim[k] > field_ncomp(b))
+      return set_err(ctx, QPAD_E_ARG, "add_dim: component out of range");
+    dim3 grid((ctx->g.ld + 255) / 256, ctx->g.P);
+    k_add_dim<<<grid, 256, 0, ctx->stream>>>(ctx->f[a], field_ncomp(a), adim[k] - 1, ctx->f[b], field_ncomp(b),
+                                             bdim[k] - 1, ctx->g.P, ctx->g.ld);
+    if (int r = check_launch(ctx, "add_dim")) return r;
+  }
+  return QPAD_OK;
+}
+
+extern "C" int qpad_field_scale(qpad_ctx* ctx, int field, double s) {
+  if (!ctx || !valid_field(field)) return QPAD_E_ARG;
+  const size_t n = f1_elems(ctx, field);
+  k_scale<<<elem_grid(n), 256, 0, ctx->stream>>>(ctx->f[field], n, s);
+  return check_launch(ctx, "scale");
+}
+
+extern "C" int qpad_field_copy_slice(qpad_ctx* ctx, int field, int slice, int dir) {
+  if (!ctx || !valid_field(field) || !has_store(field) || slice < 1 || slice > ctx->g.nz + 1 ||
+      (dir != QPAD_COPY_1TO2 && dir != QPAD_COPY_2TO1))
+    return ctx ? set_err(ctx, QPAD_E_ARG, "copy_slice: bad args") : QPAD_E_ARG;
+  const size_t n = f1_elems(ctx, field);
+  double* s2 = ctx->f2[field] + (size_t)(slice - 1) * n;
+  double* dst = dir == QPAD_COPY_1TO2 ? s2 : ctx->f[field];
+  const double* src = dir == QPAD_COPY_1TO2 ? ctx->f[field] : s2;
+  return cuda_check(ctx, cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream),
+                    "copy_slice");
+}
+
+namespace {
+int solve_checked(qpad_ctx* ctx, int op, int out, int in0, int in1, int nc_out, int nc0, int nc1) {
+  if (!ctx) return QPAD_E_ARG;
+  if (!valid_field(out) || !valid_field(in0) || (in1 >= 0 && !valid_field(in1)) || field_ncomp(out) != nc_out ||
+      field_ncomp(in0) != nc0 || (in1 >= 0 && field_ncomp(in1) != nc1))
+    return set_err(ctx, QPAD_E_ARG, "solve: field ids do not match the operation");
+  FieldArgs a{ctx->f[out], ctx->f[in0], in1 >= 0 ? ctx->f[in1] : nullptr};
+  return launch_field_op(ctx, op, a);
+}
+}  // namespace
+
+extern "C" int qpad_solve_psi(qpad_ctx* ctx, int psi, int q) { return solve_checked(ctx, FOP_PSI, psi, q, -1, 1, 1, 0); }
+extern "C" int qpad_solve_bz(qpad_ctx* ctx, int b, int cu) { return solve_checked(ctx, FOP_BZ, b, cu, -1, 3, 3, 0); }
+extern "C" int qpad_solve_bt_beam(qpad_ctx* ctx, int b, int q) {
+  return solve_checked(ctx, FOP_BT_BEAM, b, q, -1, 3, 1, 0);
+}
+extern "C" int qpad_solve_bt_iter(qpad_ctx* ctx, int b, int dcu, int cu) {
+  return solve_checked(ctx, FOP_BT_ITER, b, dcu, cu, 3, 2, 3);
+}
+extern "C" int qpad_solve_ez(qpad_ctx* ctx, int e, int cu) { return solve_checked(ctx, FOP_EZ, e, cu, -1, 3, 3, 0); }
+extern "C" int qpad_solve_et(qpad_ctx* ctx, int e, int b, int psi) {
+  return solve_checked(ctx, FOP_ET, e, b, psi, 3, 3, 1);
+}
+extern "C" int qpad_solve_djdxi(qpad_ctx* ctx, int dcu, int acu, int amu) {
+  return solve_checked(ctx, FOP_DJDXI, dcu, acu, amu, 2, 2, 3);
+}
+
+extern "C" int qpad_conv_test(qpad_ctx* ctx, int b, int dim, int op, double* rel_res, double* abs_res) {
+  if (!ctx || !valid_field(b) || field_ncomp(b) != 3 || dim < 1 || dim > 3 || (op != 0 && op != 1))
+    return ctx ? set_err(ctx, QPAD_E_ARG, "conv_test: bad args") : QPAD_E_ARG;
+  if (int r = launch_conv(ctx, ctx->f[b], dim - 1, op)) return r;
+  if (op == 1) {
+    if (int r = d2h(ctx, ctx->h_res, ctx->conv + 2 * ctx->g.nr, 3)) return r;
+    if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "conv sync")) return r;
+    if (rel_res) *rel_res = ctx->h_res[0];
+    if (abs_res) *abs_res = ctx->h_res[1];
+  }
+  return QPAD_OK;
+}
+
+// =====================================================================================
+// species
+// =====================================================================================
+extern "C" int qpad_species_create(qpad_ctx* ctx, const qpad_species_desc* d, const double* x, const double* p,
+                                   const double* gamma, const double* psi, const double* q, int64_t np,
+                                   qpad_species** out) {
+  if (!ctx || !d || !out) return QPAD_E_ARG;
+  *out = nullptr;
+  if (d->npmax < 1 || d->npmax > (int64_t)1 << 30 || np > d->npmax || np < 0 ||
+      (d->push_type != QPAD_PUSH2_STD && d->push_type != QPAD_PUSH2_ROBUST) || d->qbm == 0.0)
+    return set_err(ctx, QPAD_E_ARG, "invalid species descriptor");
+  qpad_species* sp = new (std::nothrow) qpad_species();
+  if (!sp) return set_err(ctx, QPAD_E_NOMEM, "species");
+  sp->ctx = ctx;
+  sp->qbm = d->qbm; sp->push_type = d->push_type; sp->neutralized = d->neutralized; sp->sort_freq = d->sort_freq;
+  sp->npmax = d->npmax;
+  const int64_t cap = d->npmax;
+  double* block = nullptr;
+  int r = dmalloc(ctx, (void**)&block, sizeof(double) * 16 * (size_t)cap, "particles");
+  if (!r) {
+    double** arrs[8] = {sp->x, sp->y, sp->px, sp->py, sp->pz, sp->gamma, sp->psi, sp->q};
+    for (int b = 0; b < 2; ++b)
+      for (int a = 0; a < 8; ++a) arrs[a][b] = block + ((size_t)b * 8 + a) * cap;
+  }
+  if (!r) r = dmalloc(ctx, (void**)&sp->pristine, sizeof(double) * 8 * (size_t)cap, "pristine");
+  if (!r) r = dmalloc(ctx, (void**)&sp->key, sizeof(int32_t) * cap, "keys");
+  if (!r) r = dmalloc(ctx, (void**)&sp->aux, sizeof(int32_t) * cap, "aux");
+  const int64_t ntiles = (cap + 1023) / 1024;
+  const int64_t nh = ntiles * ctx->g.nr;
+  int64_t need = 2 * nh + scan_tmp_elems(nh);
+  if (scan_tmp_elems(cap) > need) need = scan_tmp_elems(cap);
+  sp->blk_cap = need + 64;
+  if (!r) r = dmalloc(ctx, (void**)&sp->blk, sizeof(int32_t) * sp->blk_cap, "blocks");
+  if (!r) r = dmalloc(ctx, (void**)&sp->d_count, sizeof(int64_t), "count");
+  if (!r) r = dmalloc(ctx, (void**)&sp->d_total, sizeof(int64_t), "total");
+  if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&sp->h_count, sizeof(int64_t)), "pinned count");
+  if (!r) r = dmalloc(ctx, (void**)&sp->qf, f1_elems(ctx, QPAD_F_Q_SPE) * sizeof(double), "species q");
+  if (!r) r = dmalloc(ctx, (void**)&sp->qn, f1_elems(ctx, QPAD_F_Q_SPE) * sizeof(double), "species qn");
+  if (!r) {
+    ctx->species.push_back(sp);
+    r = species_load(sp, x, p, gamma, psi, q, np);
+  }
+  if (r) {
+    qpad_species_destroy(sp);
+    return r;
+  }
+  *out = sp;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_species_destroy(qpad_species* sp) {
+  if (!sp) return QPAD_OK;
+  qpad_ctx* ctx = sp->ctx;
+  cudaStreamSynchronize(ctx->stream);
+  if (sp->x[0]) cudaFree(sp->x[0] < sp->x[1] ? sp->x[0] : sp->x[1]);
+  if (sp->key) cudaFree(sp->key);
+  if (sp->aux) cudaFree(sp->aux);
+  if (sp->blk) cudaFree(sp->blk);
+  if (sp->d_count) cudaFree(sp->d_count);
+  if (sp->d_total) cudaFree(sp->d_total);
+  if (sp->h_count) cudaFreeHost(sp->h_count);
+  if (sp->qf) cudaFree(sp->qf);
+  if (sp->qn) cudaFree(sp->qn);
+  if (sp->pristine) cudaFree(sp->pristine);
+  for (size_t i = 0; i < ctx->species.size(); ++i)
+    if (ctx->species[i] == sp) { ctx->species.erase(ctx->species.begin() + i); break; }
+  delete sp;
+  rebuild_total_background(ctx);
+  return QPAD_OK;
+}
+
+extern "C" int qpad_species_renew(qpad_species* sp, const double* x, const double* p, const double* gamma,
+                                  const double* psi, const double* q, int64_t np) {
+  if (!sp) return QPAD_E_ARG;
+  return species_load(sp, x, p, gamma, psi, q, np);
+}
+
+extern "C" int qpad_species_reset(qpad_species* sp) {
+  if (!sp) return QPAD_E_ARG;
+  qpad_ctx* ctx = sp->ctx;
+  sp->np = sp->np_pristine;
+  double* dst[8] = {sp->x[0], sp->y[0], sp->px[0], sp->py[0], sp->pz[0], sp->gamma[0], sp->psi[0], sp->q[0]};
+  for (int a = 0; a < 8; ++a)
+    if (sp->np > 0 && cudaMemcpyAsync(dst[a], sp->pristine + (size_t)a * sp->npmax, sizeof(double) * sp->np,
+                                      cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+      return check_launch(ctx, "reset copy");
+  *sp->h_count = sp->np;
+  return cuda_check(ctx, cudaMemcpyAsync(sp->d_count, sp->h_count, sizeof(int64_t), cudaMemcpyHostToDevice,
+                                         ctx->stream), "reset count");
+}
+
+extern "C" int qpad_species_count(qpad_species* sp, int64_t* np) {
+  if (!sp) return QPAD_E_ARG;
+  if (int r = species_sync_count(sp)) return r;
+  if (np) *np = sp->np;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_species_download(qpad_species* sp, double* x, double* p, double* gamma, double* psi, double* q,
+                                     int64_t* np) {
+  if (!sp) return QPAD_E_ARG;
+  qpad_ctx* ctx = sp->ctx;
+  if (int r = species_sync_count(sp)) return r;
+  const int64_t n = sp->np;
+  if (np) *np = n;
+  double* staging = sp->x[1];
+  if (x) if (int r = download_vec(ctx, staging, x, n, 2, sp->x[0], sp->y[0], nullptr)) return r;
+  if (p) if (int r = download_vec(ctx, staging, p, n, 3, sp->px[0], sp->py[0], sp->pz[0])) return r;
+  if (gamma) if (int r = d2h(ctx, gamma, sp->gamma[0], n)) return r;
+  if (psi) if (int r = d2h(ctx, psi, sp->psi[0], n)) return r;
+  if (q) if (int r = d2h(ctx, q, sp->q[0], n)) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "species download");
+}
+
+extern "C" int qpad_species_qdp(qpad_species* sp, int q) {
+  if (!sp || !valid_field(q) || field_ncomp(q) != 1) return sp ? set_err(sp->ctx, QPAD_E_ARG, "qdp: bad field") : QPAD_E_ARG;
+  qpad_ctx* ctx = sp->ctx;
+  const size_t n1 = f1_elems(ctx, QPAD_F_Q_SPE);
+  if (cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess) return check_launch(ctx, "memset");
+  if (int r = species_qdeposit_raw(sp, ctx->qraw)) return r;
+  if (int r = launch_finish_q(ctx, ctx->qraw, sp->qf, 0)) return r;
+  k_add2<<<elem_grid(n1), 256, 0, ctx->stream>>>(ctx->f[q], sp->qf, sp->neutralized ? sp->qn : nullptr, n1);
+  return check_launch(ctx, "qdp add");
+}
+
+namespace {
+int ensure_scratch(qpad_ctx* ctx) {
+  if (ctx->scratch) return 0;
+  const size_t n = (size_t)ctx->g.P * 8 * ctx->g.ld;
+  return dmalloc(ctx, (void**)&ctx->scratch, n * sizeof(double), "scratch");
+}
+}  // namespace
+
+extern "C" int qpad_species_amjdp(qpad_species* sp, int ef, int bf, int cu, int amu, int dcu, double dt) {
+  if (!sp || !valid_field(ef) || !valid_field(bf) || !valid_field(cu) || !valid_field(amu) || !valid_field(dcu) ||
+      field_ncomp(ef) != 3 || field_ncomp(bf) != 3 || field_ncomp(cu) != 3 || field_ncomp(amu) != 3 ||
+      field_ncomp(dcu) != 2 || !(dt > 0))
+    return sp ? set_err(sp->ctx, QPAD_E_ARG, "amjdp: bad args") : QPAD_E_ARG;
+  qpad_ctx* ctx = sp->ctx;
+  if (int r = ensure_scratch(ctx)) return r;
+  const size_t n3 = f1_elems(ctx, QPAD_F_CU), n2 = f1_elems(ctx, QPAD_F_ACU);
+  double* scu = ctx->scratch;
+  double* samu = scu + n3;
+  double* sacu = samu + n3;
+  if (cudaMemsetAsync(scu, 0, (2 * n3 + n2) * sizeof(double), ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "memset");
+  if (int r = species_amjdp_raw(sp, ctx->f[ef], ctx->f[bf], scu, samu, sacu, dt)) return r;
+  if (int r = launch_finish_amj(ctx, scu, samu, sacu)) return r;
+  k_add<<<elem_grid(n3), 256, 0, ctx->stream>>>(ctx->f[cu], scu, ctx->f[cu], n3);
+  k_add<<<elem_grid(n3), 256, 0, ctx->stream>>>(ctx->f[amu], samu, ctx->f[amu], n3);
+  k_add<<<elem_grid(n2), 256, 0, ctx->stream>>>(ctx->f[dcu], sacu, ctx->f[dcu], n2);
+  return check_launch(ctx, "amjdp add", 3);
+}
+
+extern "C" int qpad_species_push_u(qpad_species* sp, int ef, int bf, double dt) {
+  if (!sp || !valid_field(ef) || !valid_field(bf) || field_ncomp(ef) != 3 || field_ncomp(bf) != 3)
+    return sp ? set_err(sp->ctx, QPAD_E_ARG, "push_u: bad args") : QPAD_E_ARG;
+  return species_push_u(sp, sp->ctx->f[ef], sp->ctx->f[bf], dt, 0);
+}
+
+extern "C" int qpad_species_push_x(qpad_species* sp, double dt) {
+  if (!sp) return QPAD_E_ARG;
+  return species_push_x(sp, dt);
+}
+
+extern "C" int qpad_species_interp_psi(qpad_species* sp, int psi) {
+  if (!sp || !valid_field(psi) || field_ncomp(psi) != 1) return sp ? set_err(sp->ctx, QPAD_E_ARG, "interp_psi") : QPAD_E_ARG;
+  return species_interp_psi(sp, sp->ctx->f[psi]);
+}
+
+extern "C" int qpad_species_sort(qpad_species* sp) {
+  if (!sp) return QPAD_E_ARG;
+  return species_sort(sp);
+}
+
+// =====================================================================================
+// beams
+// =====================================================================================
+extern "C" int qpad_beam_create(qpad_ctx* ctx, const qpad_beam_desc* d, const double* x, const double* p,
+                                const double* q, int64_t nb, qpad_beam** out) {
+  if (!ctx || !d || !out) return QPAD_E_ARG;
+  *out = nullptr;
+  if (d->npmax < 1 || d->npmax > (int64_t)1 << 31 || nb < 0 || nb > d->npmax ||
+      (d->push_type != QPAD_PUSH3_REDUCED && d->push_type != QPAD_PUSH3_BORIS))
+    return set_err(ctx, QPAD_E_ARG, "invalid beam descriptor");
+  qpad_beam* bm = new (std::nothrow) qpad_beam();
+  if (!bm) return set_err(ctx, QPAD_E_NOMEM, "beam");
+  bm->ctx = ctx;
+  bm->qbm = d->qbm; bm->push_type = d->push_type; bm->evolution = d->evolution; bm->npmax = d->npmax;
+  const int64_t cap = d->npmax;
+  double* block = nullptr;
+  int r = dmalloc(ctx, (void**)&block, sizeof(double) * 14 * (size_t)cap, "beam particles");
+  if (!r) {
+    double** arrs[7] = {bm->x, bm->y, bm->z, bm->px, bm->py, bm->pz, bm->q};
+    for (int b = 0; b < 2; ++b)
+      for (int a = 0; a < 7; ++a) arrs[a][b] = block + ((size_t)b * 7 + a) * cap;
+  }
+  if (!r) r = dmalloc(ctx, (void**)&bm->key, sizeof(int32_t) * cap, "beam keys");
+  if (!r) r = dmalloc(ctx, (void**)&bm->aux, sizeof(int32_t) * cap, "beam aux");
+  bm->blk_cap = scan_tmp_elems(cap) + 64;
+  if (!r) r = dmalloc(ctx, (void**)&bm->blk, sizeof(int32_t) * bm->blk_cap, "beam blocks");
+  if (!r) r = dmalloc(ctx, (void**)&bm->d_count, sizeof(int64_t), "beam count");
+  if (!r) r = dmalloc(ctx, (void**)&bm->d_total, sizeof(int64_t), "beam total");
+  if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&bm->h_count, sizeof(int64_t)), "pinned");
+  if (!r) {
+    ctx->beams.push_back(bm);
+    r = beam_load(bm, x, p, q, nb);
+  }
+  if (r) {
+    qpad_beam_destroy(bm);
+    return r;
+  }
+  *out = bm;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_beam_destroy(qpad_beam* bm) {
+  if (!bm) return QPAD_OK;
+  qpad_ctx* ctx = bm->ctx;
+  cudaStreamSynchronize(ctx->stream);
+  if (bm->x[0]) cudaFree(bm->x[0] < bm->x[1] ? bm->x[0] : bm->x[1]);
+  if (bm->key) cudaFree(bm->key);
+  if (bm->aux) cudaFree(bm->aux);
+  if (bm->blk) cudaFree(bm->blk);
+  if (bm->d_count) cudaFree(bm->d_count);
+  if (bm->d_total) cudaFree(bm->d_total);
+  if (bm->h_count) cudaFreeHost(bm->h_count);
+  for (size_t i = 0; i < ctx->beams.size(); ++i)
+    if (ctx->beams[i] == bm) { ctx->beams.erase(ctx->beams.begin() + i); break; }
+  delete bm;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_beam_count(qpad_beam* bm, int64_t* nb) {
+  if (!bm) return QPAD_E_ARG;
+  if (int r = beam_sync_count(bm)) return r;
+  if (nb) *nb = bm->nb;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_beam_download(qpad_beam* bm, double* x, double* p, double* q, int64_t* nb) {
+  if (!bm) return QPAD_E_ARG;
+  qpad_ctx* ctx = bm->ctx;
+  if (int r = beam_sync_count(bm)) return r;
+  const int64_t n = bm->nb;
+  if (nb) *nb = n;
+  double* staging = bm->x[1];
+  if (x) if (int r = download_vec(ctx, staging, x, n, 3, bm->x[0], bm->y[0], bm->z[0])) return r;
+  if (p) if (int r = download_vec(ctx, staging, p, n, 3, bm->px[0], bm->py[0], bm->pz[0])) return r;
+  if (q) if (int r = d2h(ctx, q, bm->q[0], n)) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "beam download");
+}
+
+extern "C" int qpad_beam_qdp(qpad_beam* bm, int q) {
+  if (!bm || !valid_field(q) || field_ncomp(q) != 1 || !has_store(q))
+    return bm ? set_err(bm->ctx, QPAD_E_ARG, "beam qdp: field needs a 3D store") : QPAD_E_ARG;
+  qpad_ctx* ctx = bm->ctx;
+  // this%q = 0; deposit; corrections; q += this%q   (beam3d_class.f03:193-221)
+  if (!ctx->beam_scratch) {
+    if (int r = dmalloc(ctx, (void**)&ctx->beam_scratch, f2_elems(ctx, QPAD_F_Q_BEAM) * sizeof(double), "beam q"))
+      return r;
+  }
+  const size_t n2 = f2_elems(ctx, QPAD_F_Q_BEAM);
+  if (cudaMemsetAsync(ctx->beam_scratch, 0, n2 * sizeof(double), ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "memset beam q");
+  if (int r = beam_qdeposit(bm, ctx->beam_scratch)) return r;
+  if (int r = beam_finish_q(ctx, ctx->beam_scratch)) return r;
+  k_add<<<elem_grid(n2), 256, 0, ctx->stream>>>(ctx->f2[q], ctx->beam_scratch, ctx->f2[q], n2);
+  return check_launch(ctx, "beam qdp add");
+}
+
+extern "C" int qpad_beam_push(qpad_beam* bm, int ef, int bf) {
+  if (!bm || !valid_field(ef) || !valid_field(bf) || !has_store(ef) || !has_store(bf) || field_ncomp(ef) != 3 ||
+      field_ncomp(bf) != 3)
+    return bm ? set_err(bm->ctx, QPAD_E_ARG, "beam push: fields need 3D stores") : QPAD_E_ARG;
+  return beam_push(bm, bm->ctx->f2[ef], bm->ctx->f2[bf]);
+}
+
+// =====================================================================================
+// fused drivers
+// =====================================================================================
+namespace {
+
+int slice_step(qpad_ctx* ctx, int j, qpad_slice_stats* st) {
+  const GridDev& g = ctx->g;
+  const size_t n1 = f1_elems(ctx, QPAD_F_Q_SPE);
+  int any_ntd = 0, any_std = 0;
+  for (auto* s : ctx->species) { any_ntd |= s->neutralized; any_std |= (s->push_type == QPAD_PUSH2_STD); }
+  // q_spe = 0; spe%qdp(q_spe)  -> raw deposit, finished in k_slice_begin
+  if (cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess) return check_launch(ctx, "qraw");
+  for (auto* s : ctx->species)
+    if (int r = species_qdeposit_raw(s, ctx->qraw)) return r;
+  if (int r = launch_slice_begin(ctx, j, any_ntd)) return r;
+  if (any_std)
+    for (auto* s : ctx->species)
+      if (s->push_type == QPAD_PUSH2_STD)
+        if (int r = species_interp_psi(s, ctx->f[QPAD_F_PSI])) return r;
+  if (int r = launch_conv(ctx, ctx->f[QPAD_F_B_SPE], 1, 0)) return r;
+  int l;
+  double rel = 0.0, ab = 0.0;
+  for (l = 1; l <= ctx->iter_max; ++l) {
+    if (int r = launch_iter_e(ctx)) return r;
+    for (auto* s : ctx->species)
+      if (int r = species_amjdp_raw(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], ctx->f[QPAD_F_CU], ctx->f[QPAD_F_AMU],
+                                    ctx->f[QPAD_F_ACU], g.dxi))
+        return r;
+    if (int r = launch_iter_b(ctx)) return r;
+    if (int r = launch_conv(ctx, ctx->f[QPAD_F_B_SPE], 1, 1)) return r;
+    if (int r = d2h(ctx, ctx->h_res, ctx->conv + 2 * g.nr, 3)) return r;
+    if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "iteration sync")) return r;
+    if (ctx->prof_on) prof_collect(ctx);
+    rel = ctx->h_res[0];
+    ab = ctx->h_res[1];
+    if (ctx->h_res[2] != 0.0) break;
+  }
+  if (st) {
+    st->iters = l > ctx->iter_max ? ctx->iter_max : l;
+    st->rel_res = rel;
+    st->abs_res = ab;
+  }
+  if (int r = launch_slice_end(ctx, j)) return r;
+  for (auto* s : ctx->species) {
+    if (int r = species_push_u(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], g.dxi, 1)) return r;
+    if (s->sort_freq > 0 && (j % s->sort_freq) == 0)
+      if (int r = species_sort(s)) return r;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int qpad_slice_step(qpad_ctx* ctx, int j, qpad_slice_stats* stats) {
+  if (!ctx || j < 1 || j > ctx->g.nz) return ctx ? set_err(ctx, QPAD_E_ARG, "slice index out of range") : QPAD_E_ARG;
+  return slice_step(ctx, j, stats);
+}
+
+extern "C" int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* stats) {
+  if (!ctx) return QPAD_E_ARG;
+  prof_begin(ctx, "step");
+  // simulation_class.f03:309-341
+  if (int r = qpad_store_fill(ctx, QPAD_F_Q_BEAM, 0.0)) return r;
+  if (int r = qpad_store_fill(ctx, QPAD_F_Q_SPE, 0.0)) return r;
+  for (auto* b : ctx->beams)
+    if (int r = beam_qdeposit(b, ctx->f2[QPAD_F_Q_BEAM])) return r;
+  if (!ctx->beams.empty())
+    if (int r = beam_finish_q(ctx, ctx->f2[QPAD_F_Q_BEAM])) return r;
+  const int zero_fields[] = {QPAD_F_B, QPAD_F_E, QPAD_F_B_SPE, QPAD_F_E_SPE, QPAD_F_PSI,
+                             QPAD_F_CU, QPAD_F_ACU, QPAD_F_AMU};
+  for (int f : zero_fields)
+    if (cudaMemsetAsync(ctx->f[f], 0, f1_elems(ctx, f) * sizeof(double), ctx->stream) != cudaSuccess)
+      return check_launch(ctx, "zero fields");
+  for (int j = 1; j <= ctx->g.nz; ++j)
+    if (int r = slice_step(ctx, j, stats ? stats + (j - 1) : nullptr)) return r;
+  if (push_beams)
+    for (auto* b : ctx->beams)
+      if (int r = beam_push(b, ctx->f2[QPAD_F_E], ctx->f2[QPAD_F_B])) return r;
+  prof_end(ctx, "step");
+  for (auto* s : ctx->species)
+    if (int r = species_sync_count(s)) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "3d step");
+}

@@ -1,0 +1,1036 @@
+// fields.cu -- per-mode radial field solves of the quasi-static slice loop (FP64).
+//
+// Every solve of the reference goes through HYPRE's struct cyclic-reduction solver with a
+// tridiagonal matrix that is analytic in (kind, mode) (field_solver_class.f03:256-561).
+// Here the matrices are factorised once per context (Thomas LU, host, FP64) and each
+// solve is a forward and a backward substitution.  Both substitutions are first-order
+// affine recurrences, evaluated by one CTA as a parallel scan of affine maps
+// (y_k = a_k + b_k * y_{k-1}): each thread composes a contiguous chunk of rows, a warp
+// shuffle scan plus a cross-warp scan combine the chunks, and each thread then replays
+// its chunk.  One CTA owns one azimuthal mode, so the Re/Im right-hand sides of that mode
+// (which share the matrix) are solved together, and the source construction
+// (set_source_*), the solve and the recovery of the field (get_solution_*) are fused into
+// the same kernel with the radial lines held in shared memory.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "qpad_internal.cuh"
+
+namespace qpad {
+
+#define FULLMASK 0xffffffffu
+static constexpr int kFieldThreads = 256;
+
+int field_ncomp(int field) {
+  switch (field) {
+    case QPAD_F_PSI: case QPAD_F_Q_SPE: case QPAD_F_Q_BEAM: return 1;
+    case QPAD_F_ACU: case QPAD_F_DCU: return 2;
+    default: return 3;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Host: tridiagonal matrices (field_solver_class.f03:256-561) and their factorisation
+// ------------------------------------------------------------------------------------
+static void build_matrix(const GridDev& g, int kind, int m, double* a, double* b, double* c) {
+  const int nr = g.nr;
+  const double dr = g.dr, dr2 = dr * dr, m2 = (double)(m * m), rf = g.relax_fac;
+  for (int k = 2; k <= nr; ++k) {                      // rows 2..nr, j = row - 1
+    double j = (double)(k - 1);
+    a[k - 1] = 1.0 - 0.5 / j;
+    c[k - 1] = 1.0 + 0.5 / j;
+    if (kind == OK_BPLUS) {
+      double t = (double)(m + 1) / j;
+      b[k - 1] = -2.0 - t * t - rf;
+    } else if (kind == OK_BMINUS) {
+      double t = (double)(m - 1) / j;
+      b[k - 1] = -2.0 - t * t - rf;
+    } else {
+      b[k - 1] = -2.0 - m2 / (j * j);
+    }
+  }
+  bool identity_axis = true;                           // axis row
+  if (kind == OK_BMINUS && m == 1) {
+    a[0] = 0.0; b[0] = -4.0 - rf; c[0] = 4.0; identity_axis = false;
+  } else if ((kind == OK_GEN || kind == OK_BT) && m == 0) {
+    a[0] = 0.0; b[0] = -4.0; c[0] = 4.0; identity_axis = false;
+  }
+  if (identity_axis) {
+    a[0] = 0.0; b[0] = 1.0; c[0] = 0.0;
+    if (nr >= 2) a[1] = 0.0;
+  }
+  if (g.bnd == QPAD_BND_ZERO) {                        // outer row
+    c[nr - 1] = 0.0;
+  } else {
+    const double jmax = (double)nr;
+    bool dirichlet = false;
+    double fac = 0.0;
+    if (kind == OK_GEN) {
+      if (m == 0) dirichlet = true; else fac = 1.0 - (double)m / jmax;
+    } else if (kind == OK_BT) {
+      fac = (m == 0) ? 1.0 + 1.0 / (jmax * std::log(jmax * dr)) : 1.0 - (double)m / jmax;
+    } else {
+      fac = 1.0 - (double)(m + 1) / jmax;              // B+ and B- both use (m+1)
+    }
+    if (!dirichlet) b[nr - 1] = b[nr - 1] + fac * c[nr - 1];
+    c[nr - 1] = 0.0;
+  }
+  for (int k = 0; k < nr; ++k) { a[k] /= dr2; b[k] /= dr2; c[k] /= dr2; }
+}
+
+int build_factors(qpad_ctx* ctx) {
+  const GridDev& g = ctx->g;
+  const int nr = g.nr, M = g.M;
+  std::vector<double> h((size_t)OK_NKINDS * (M + 1) * 3 * nr);
+  std::vector<double> a(nr), b(nr), c(nr);
+  for (int kind = 0; kind < OK_NKINDS; ++kind)
+    for (int m = 0; m <= M; ++m) {
+      build_matrix(g, kind, m, a.data(), b.data(), c.data());
+      double* w = h.data() + fac_off(nr, M, kind, m);
+      double* ib = w + nr;
+      double* gg = ib + nr;
+      double piv = b[0];
+      w[0] = 0.0;
+      ib[0] = 1.0 / piv;
+      for (int k = 1; k < nr; ++k) {
+        w[k] = a[k] / piv;
+        piv = b[k] - w[k] * c[k - 1];
+        ib[k] = 1.0 / piv;
+      }
+      for (int k = 0; k < nr; ++k) gg[k] = c[k] * ib[k];
+      for (int k = 0; k < nr; ++k)
+        if (!std::isfinite(ib[k]) || !std::isfinite(w[k]))
+          return set_err(ctx, QPAD_E_ARG, "singular tridiagonal operator (check nr, dr, relax_fac)");
+    }
+  cudaError_t e = cudaMalloc(&ctx->fac, h.size() * sizeof(double));
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(factors)");
+  return cuda_check(ctx, cudaMemcpy(ctx->fac, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice),
+                    "upload factors");
+}
+
+// ------------------------------------------------------------------------------------
+// Device: CTA-wide scan of affine maps and the substitution passes
+// ------------------------------------------------------------------------------------
+// Composition convention: map (B, A) sends y -> A + B*y.  Later-after-earlier composes as
+// (B_l*B_e, A_l + B_l*A_e).  `reverse` walks the threads (and their chunks) downward.
+template <int NV>
+__device__ __forceinline__ void affine_scan(double& B, double (&A)[NV], bool reverse, double* sc) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    double Bo = reverse ? __shfl_down_sync(FULLMASK, B, off) : __shfl_up_sync(FULLMASK, B, off);
+    double Ao[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      Ao[v] = reverse ? __shfl_down_sync(FULLMASK, A[v], off) : __shfl_up_sync(FULLMASK, A[v], off);
+    const bool valid = reverse ? (lane + off < 32) : (lane >= off);
+    if (valid) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) A[v] = A[v] + B * Ao[v];
+      B = B * Bo;
+    }
+  }
+  double Be = reverse ? __shfl_down_sync(FULLMASK, B, 1) : __shfl_up_sync(FULLMASK, B, 1);
+  double Ae[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    Ae[v] = reverse ? __shfl_down_sync(FULLMASK, A[v], 1) : __shfl_up_sync(FULLMASK, A[v], 1);
+  if (reverse ? (lane == 31) : (lane == 0)) {
+    Be = 1.0;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) Ae[v] = 0.0;
+  }
+  double* tot = sc;
+  double* pre = sc + 32 * (NV + 1);
+  if (reverse ? (lane == 0) : (lane == 31)) {
+    tot[warp * (NV + 1)] = B;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) tot[warp * (NV + 1) + 1 + v] = A[v];
+  }
+  __syncthreads();
+  if (t == 0) {
+    double Bc = 1.0, Ac[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) Ac[v] = 0.0;
+    for (int k = 0; k < nw; ++k) {
+      const int w = reverse ? nw - 1 - k : k;
+      pre[w * (NV + 1)] = Bc;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) pre[w * (NV + 1) + 1 + v] = Ac[v];
+      const double Bw = tot[w * (NV + 1)];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) Ac[v] = tot[w * (NV + 1) + 1 + v] + Bw * Ac[v];
+      Bc = Bw * Bc;
+    }
+  }
+  __syncthreads();
+  const double Bp = pre[warp * (NV + 1)];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) A[v] = Ae[v] + Be * pre[warp * (NV + 1) + 1 + v];
+  B = Be * Bp;
+  __syncthreads();
+}
+
+// Solve the factored system in place for NV right-hand sides d0 (and d1) of length n.
+template <int NV>
+__device__ void tri_solve(int n, const double* __restrict__ fw, const double* __restrict__ fib,
+                          const double* __restrict__ fg, double* d0, double* d1, double* sc) {
+  const int T = blockDim.x, t = threadIdx.x;
+  const int C = (n + T - 1) / T;
+  const int k0 = min(t * C, n), k1 = min(k0 + C, n);
+  double* d[2] = {d0, d1};
+  double B = 1.0, A[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) A[v] = 0.0;
+  for (int k = k0; k < k1; ++k) {                       // forward: y_k = d_k - w_k y_{k-1}
+    const double beta = -fw[k];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) A[v] = d[v][k] + beta * A[v];
+    B = B * beta;
+  }
+  affine_scan<NV>(B, A, false, sc);
+  for (int k = k0; k < k1; ++k) {
+    const double wk = fw[k];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      A[v] = d[v][k] - wk * A[v];
+      d[v][k] = A[v];
+    }
+  }
+  __syncthreads();
+  B = 1.0;
+#pragma unroll
+  for (int v = 0; v < NV; ++v) A[v] = 0.0;
+  for (int k = k1 - 1; k >= k0; --k) {                  // backward: x_k = y_k ib_k - g_k x_{k+1}
+    const double beta = -fg[k], ibk = fib[k];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) A[v] = d[v][k] * ibk + beta * A[v];
+    B = B * beta;
+  }
+  affine_scan<NV>(B, A, true, sc);
+  for (int k = k1 - 1; k >= k0; --k) {
+    const double ibk = fib[k], gk = fg[k];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      A[v] = d[v][k] * ibk - gk * A[v];
+      d[v][k] = A[v];
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void solve_mode(const GridDev& G, const double* fac, int kind, int m,
+                                           double* d0, double* d1, double* sc) {
+  const double* w = fac + fac_off(G.nr, G.M, kind, m);
+  if (m == 0 && d1 == nullptr)
+    tri_solve<1>(G.nr, w, w + G.nr, w + 2 * G.nr, d0, d0, sc);
+  else
+    tri_solve<2>(G.nr, w, w + G.nr, w + 2 * G.nr, d0, d1, sc);
+}
+
+// ------------------------------------------------------------------------------------
+// Device: per-mode operations.  Shared-memory vectors are 1-based (index i = node i).
+// Each op is executed by a whole CTA for one mode m and ends with __syncthreads().
+// ------------------------------------------------------------------------------------
+#define FLD(f, nc, p, c, i) (f)[fidx(G.ld, nc, p, c, i)]
+
+// psi: field_psi_class.f03:131-254
+__device__ void op_psi(const GridDev& G, int m, const double* fac, double* sm, double* sc,
+                       const double* __restrict__ q, double* __restrict__ psi) {
+  const int nr = G.nr, pr = part_re(m), pi = part_im(m);
+  double* d0 = sm;
+  double* d1 = sm + (nr + 2);
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    d0[i] = -1.0 * FLD(q, 1, pr, 0, i);
+    if (m > 0) d1[i] = -1.0 * FLD(q, 1, pi, 0, i);
+  }
+  __syncthreads();
+  solve_mode(G, fac, OK_GEN, m, d0 + 1, m > 0 ? d1 + 1 : nullptr, sc);
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    FLD(psi, 1, pr, 0, i) = (m > 0 && i == 1) ? 0.0 : d0[i];
+    if (m > 0) FLD(psi, 1, pi, 0, i) = (i == 1) ? 0.0 : d1[i];
+  }
+  __syncthreads();
+}
+
+// Bz source: field_b_class.f03:205-307
+__device__ __forceinline__ void src_bz_row(const GridDev& G, int m, int i, const double* __restrict__ cu,
+                                           double& re, double& im) {
+  const int nr = G.nr;
+  const double idr = G.idr, idrh = 0.5 * idr;
+  if (m == 0) {
+    if (i == 1) {
+      re = -2.0 * idr * FLD(cu, 3, 0, 1, 2);
+    } else if (i == nr) {
+      const double ir = idr / (double)(nr - 1);
+      re = -idrh * (3.0 * FLD(cu, 3, 0, 1, nr) - 4.0 * FLD(cu, 3, 0, 1, nr - 1) + FLD(cu, 3, 0, 1, nr - 2)) -
+           ir * FLD(cu, 3, 0, 1, nr);
+    } else {
+      const double ir = idr / (double)(i - 1);
+      re = -idrh * (FLD(cu, 3, 0, 1, i + 1) - FLD(cu, 3, 0, 1, i - 1)) - ir * FLD(cu, 3, 0, 1, i);
+    }
+    im = 0.0;
+    return;
+  }
+  const int pr = part_re(m), pi = part_im(m);
+  const double dm = (double)m;
+  if (i == nr) {
+    const double ir = idr / (double)(nr - 1);
+    re = -idrh * (3.0 * FLD(cu, 3, pr, 1, nr) - 4.0 * FLD(cu, 3, pr, 1, nr - 1) + FLD(cu, 3, pr, 1, nr - 2)) -
+         ir * FLD(cu, 3, pr, 1, nr) - dm * ir * FLD(cu, 3, pi, 0, nr);
+    im = -idrh * (3.0 * FLD(cu, 3, pi, 1, nr) - 4.0 * FLD(cu, 3, pi, 1, nr - 1) + FLD(cu, 3, pi, 1, nr - 2)) -
+         ir * FLD(cu, 3, pi, 1, nr) + dm * ir * FLD(cu, 3, pr, 0, nr);
+  } else if (i == 1) {
+    if (m % 2 == 0) {
+      re = -2.0 * idr * FLD(cu, 3, pr, 1, 2) - dm * idr * FLD(cu, 3, pi, 0, 2);
+      im = -2.0 * idr * FLD(cu, 3, pi, 1, 2) + dm * idr * FLD(cu, 3, pr, 0, 2);
+    } else {
+      re = 0.0;
+      im = 0.0;
+    }
+  } else if (i == 2 && m == 1) {
+    const double ir = idr;
+    re = -idr * (FLD(cu, 3, pr, 1, 3) - FLD(cu, 3, pr, 1, 2)) - ir * FLD(cu, 3, pr, 1, 2) -
+         dm * ir * FLD(cu, 3, pi, 0, 2);
+    im = -idr * (FLD(cu, 3, pi, 1, 3) - FLD(cu, 3, pi, 1, 2)) - ir * FLD(cu, 3, pi, 1, 2) +
+         dm * ir * FLD(cu, 3, pr, 0, 2);
+  } else {
+    const double ir = idr / (double)(i - 1);
+    re = -idrh * (FLD(cu, 3, pr, 1, i + 1) - FLD(cu, 3, pr, 1, i - 1)) - ir * FLD(cu, 3, pr, 1, i) -
+         dm * ir * FLD(cu, 3, pi, 0, i);
+    im = -idrh * (FLD(cu, 3, pi, 1, i + 1) - FLD(cu, 3, pi, 1, i - 1)) - ir * FLD(cu, 3, pi, 1, i) +
+         dm * ir * FLD(cu, 3, pr, 0, i);
+  }
+}
+
+// Bz: field_b_class.f03:508-543, 760-796
+__device__ void op_bz(const GridDev& G, int m, const double* fac, double* sm, double* sc,
+                      const double* __restrict__ cu, double* __restrict__ b) {
+  const int nr = G.nr, pr = part_re(m), pi = part_im(m);
+  double* d0 = sm;
+  double* d1 = sm + (nr + 2);
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    double re, im;
+    src_bz_row(G, m, i, cu, re, im);
+    d0[i] = re;
+    d1[i] = im;
+  }
+  __syncthreads();
+  solve_mode(G, fac, OK_GEN, m, d0 + 1, m > 0 ? d1 + 1 : nullptr, sc);
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    FLD(b, 3, pr, 2, i) = (m > 0 && i == 1) ? 0.0 : d0[i];
+    if (m > 0) FLD(b, 3, pi, 2, i) = (i == 1) ? 0.0 : d1[i];
+  }
+  __syncthreads();
+}
+
+// Beam B-perp: field_b_class.f03:309-358, 545-701, 798-834 (q read from q, which may be
+// a slice of a 3D store with the same per-slice layout)
+__device__ void op_bt_beam(const GridDev& G, int m, const double* fac, double* sm, double* sc,
+                           const double* __restrict__ q, double* __restrict__ b) {
+  const int nr = G.nr, pr = part_re(m), pi = part_im(m);
+  const double idr = G.idr, idrh = 0.5 * idr, dm = (double)m;
+  double* d0 = sm;
+  double* d1 = sm + (nr + 2);
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    d0[i] = -1.0 * FLD(q, 1, pr, 0, i);
+    if (m > 0) d1[i] = -1.0 * FLD(q, 1, pi, 0, i);
+  }
+  __syncthreads();
+  solve_mode(G, fac, OK_BT, m, d0 + 1, m > 0 ? d1 + 1 : nullptr, sc);
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    if (m == 0) {
+      double br = 0.0, bp;
+      if (i == 1) bp = 0.0;
+      else if (i == nr) bp = -idrh * (3.0 * d0[nr] - 4.0 * d0[nr - 1] + d0[nr - 2]);
+      else bp = -idrh * (d0[i + 1] - d0[i - 1]);
+      FLD(b, 3, 0, 0, i) = br;
+      FLD(b, 3, 0, 1, i) = bp;
+    } else {
+      double rr, ri, pr_, pi_;
+      if (i == 1) {
+        if (m == 1) {
+          rr = -idr * dm * d1[2];
+          ri = idr * dm * d0[2];
+          pr_ = -idr * d0[2];
+          pi_ = -idr * d1[2];
+        } else {
+          rr = ri = pr_ = pi_ = 0.0;
+        }
+      } else if (i == nr) {
+        const double ir = idr / (double)(nr - 1);
+        rr = -ir * dm * d1[nr];
+        ri = ir * dm * d0[nr];
+        pr_ = -idrh * (3.0 * d0[nr] - 4.0 * d0[nr - 1] + d0[nr - 2]);
+        pi_ = -idrh * (3.0 * d1[nr] - 4.0 * d1[nr - 1] + d1[nr - 2]);
+      } else {
+        const double ir = idr / (double)(i - 1);
+        rr = -ir * dm * d1[i];
+        ri = ir * dm * d0[i];
+        pr_ = -idrh * (d0[i + 1] - d0[i - 1]);
+        pi_ = -idrh * (d1[i + 1] - d1[i - 1]);
+      }
+      FLD(b, 3, pr, 0, i) = rr;
+      FLD(b, 3, pi, 0, i) = ri;
+      FLD(b, 3, pr, 1, i) = pr_;
+      FLD(b, 3, pi, 1, i) = pi_;
+    }
+  }
+  __syncthreads();
+}
+
+// Plasma B-perp predictor-corrector: field_b_class.f03:360-506, 703-758, 836-879.
+// b holds B_old in components 1:2 on entry.
+__device__ void op_bt_iter(const GridDev& G, int m, const double* fac, double* sm, double* sc,
+                           const double* __restrict__ dcu, const double* __restrict__ cu, double* __restrict__ b) {
+  const int nr = G.nr;
+  const double idr = G.idr, idrh = 0.5 * idr, rix = G.relax_fac * (idr * idr), dm = (double)m;
+  double* b1re = sm;
+  double* b1im = sm + (nr + 2);
+  double* b2re = sm + 2 * (nr + 2);
+  double* b2im = sm + 3 * (nr + 2);
+  if (m == 0) {
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+      double v1, v2;
+      if (i == 1) {
+        v1 = 0.0;
+        v2 = 0.0;
+      } else if (i == nr) {
+        v1 = -FLD(dcu, 2, 0, 1, nr) - FLD(b, 3, 0, 0, nr) * rix;
+        v2 = FLD(dcu, 2, 0, 0, nr) +
+             idrh * (3.0 * FLD(cu, 3, 0, 2, nr) - 4.0 * FLD(cu, 3, 0, 2, nr - 1) + FLD(cu, 3, 0, 2, nr - 2)) -
+             FLD(b, 3, 0, 1, nr) * rix;
+      } else if (i == 2) {
+        v1 = -FLD(dcu, 2, 0, 1, 2) - FLD(b, 3, 0, 0, 2) * rix;
+        v2 = FLD(dcu, 2, 0, 0, 2) + idr * (FLD(cu, 3, 0, 2, 3) - FLD(cu, 3, 0, 2, 2)) - FLD(b, 3, 0, 1, 2) * rix;
+      } else {
+        v1 = -FLD(dcu, 2, 0, 1, i) - FLD(b, 3, 0, 0, i) * rix;
+        v2 = FLD(dcu, 2, 0, 0, i) + idrh * (FLD(cu, 3, 0, 2, i + 1) - FLD(cu, 3, 0, 2, i - 1)) -
+             FLD(b, 3, 0, 1, i) * rix;
+      }
+      b1re[i] = v1;
+      b2re[i] = v2;
+    }
+    __syncthreads();
+    const double* w = fac + fac_off(nr, G.M, OK_BPLUS, 0);
+    tri_solve<1>(nr, w, w + nr, w + 2 * nr, b1re + 1, b1re + 1, sc);
+    w = fac + fac_off(nr, G.M, OK_BMINUS, 0);
+    tri_solve<1>(nr, w, w + nr, w + 2 * nr, b2re + 1, b2re + 1, sc);
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+      FLD(b, 3, 0, 0, i) = (i == 1) ? 0.0 : b1re[i];
+      FLD(b, 3, 0, 1, i) = (i == 1) ? 0.0 : b2re[i];
+    }
+    __syncthreads();
+    return;
+  }
+  const int pr = part_re(m), pi = part_im(m);
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    double s1re, s1im, s2re, s2im;
+    if (i == 1) {
+      if (m == 1) {
+        s1re = -FLD(dcu, 2, pr, 1, 1) + idr * dm * FLD(cu, 3, pi, 2, 2);
+        s1im = -FLD(dcu, 2, pi, 1, 1) - idr * dm * FLD(cu, 3, pr, 2, 2);
+        s2re = FLD(dcu, 2, pr, 0, 1) + idr * FLD(cu, 3, pr, 2, 2);
+        s2im = FLD(dcu, 2, pi, 0, 1) + idr * FLD(cu, 3, pi, 2, 2);
+      } else if (m % 2 == 0) {
+        s1re = s1im = s2re = s2im = 0.0;
+      } else {
+        s1re = idr * dm * FLD(cu, 3, pi, 2, 2);
+        s1im = idr * dm * FLD(cu, 3, pr, 2, 2);
+        s2re = idr * FLD(cu, 3, pr, 2, 2);
+        s2im = idr * FLD(cu, 3, pi, 2, 2);
+      }
+    } else if (i == nr) {
+      const double ir = idr / (double)(nr - 1);
+      s1re = -FLD(dcu, 2, pr, 1, nr) + dm * FLD(cu, 3, pi, 2, nr) * ir;
+      s1im = -FLD(dcu, 2, pi, 1, nr) - dm * FLD(cu, 3, pr, 2, nr) * ir;
+      s2re = FLD(dcu, 2, pr, 0, nr) +
+             idrh * (3.0 * FLD(cu, 3, pr, 2, nr) - 4.0 * FLD(cu, 3, pr, 2, nr - 1) + FLD(cu, 3, pr, 2, nr - 2));
+      s2im = FLD(dcu, 2, pi, 0, nr) +
+             idrh * (3.0 * FLD(cu, 3, pi, 2, nr) - 4.0 * FLD(cu, 3, pi, 2, nr - 1) + FLD(cu, 3, pi, 2, nr - 2));
+    } else {
+      const double ir = idr / (double)(i - 1);
+      s1re = -FLD(dcu, 2, pr, 1, i) + dm * FLD(cu, 3, pi, 2, i) * ir;
+      s1im = -FLD(dcu, 2, pi, 1, i) - dm * FLD(cu, 3, pr, 2, i) * ir;
+      s2re = FLD(dcu, 2, pr, 0, i) + idrh * (FLD(cu, 3, pr, 2, i + 1) - FLD(cu, 3, pr, 2, i - 1));
+      s2im = FLD(dcu, 2, pi, 0, i) + idrh * (FLD(cu, 3, pi, 2, i + 1) - FLD(cu, 3, pi, 2, i - 1));
+    }
+    const double br0 = FLD(b, 3, pr, 0, i), bi0 = FLD(b, 3, pi, 0, i);
+    const double br1 = FLD(b, 3, pr, 1, i), bi1 = FLD(b, 3, pi, 1, i);
+    b1re[i] = s1re - s2im - (br0 - bi1) * rix;
+    b1im[i] = s1im + s2re - (bi0 + br1) * rix;
+    b2re[i] = s1re + s2im - (br0 + bi1) * rix;
+    b2im[i] = s1im - s2re - (bi0 - br1) * rix;
+  }
+  __syncthreads();
+  const double* w = fac + fac_off(nr, G.M, OK_BPLUS, m);
+  tri_solve<2>(nr, w, w + nr, w + 2 * nr, b1re + 1, b1im + 1, sc);
+  w = fac + fac_off(nr, G.M, OK_BMINUS, m);
+  tri_solve<2>(nr, w, w + nr, w + 2 * nr, b2re + 1, b2im + 1, sc);
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    const bool zero = (i == 1 && m != 1);
+    FLD(b, 3, pr, 0, i) = zero ? 0.0 : 0.5 * (b1re[i] + b2re[i]);
+    FLD(b, 3, pi, 0, i) = zero ? 0.0 : 0.5 * (b1im[i] + b2im[i]);
+    FLD(b, 3, pr, 1, i) = zero ? 0.0 : 0.5 * (b1im[i] - b2im[i]);
+    FLD(b, 3, pi, 1, i) = zero ? 0.0 : 0.5 * (-b1re[i] + b2re[i]);
+  }
+  __syncthreads();
+}
+
+// CTA-wide sum (all threads return the total)
+__device__ double block_sum(double v, double* sc) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULLMASK, v, off);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) sc[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < nw; ++w) s += sc[w];
+    sc[32] = s;
+  }
+  __syncthreads();
+  s = sc[32];
+  __syncthreads();
+  return s;
+}
+
+// Ez: field_e_class.f03:148-259, 261-296, 298-334
+__device__ void op_ez(const GridDev& G, int m, const double* fac, double* sm, double* sc,
+                      const double* __restrict__ cu, double* __restrict__ e) {
+  const int nr = G.nr, pr = part_re(m), pi = part_im(m);
+  const double idr = G.idr, idrh = 0.5 * idr, dm = (double)m;
+  double* d0 = sm;
+  double* d1 = sm + (nr + 2);
+  if (m == 0) {
+    double div = 0.0;
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+      double v;
+      if (i == 1) {
+        v = 0.0;   // set after the reduction
+      } else if (i == nr - 1) {
+        const double ir = idr / (double)(nr - 2);
+        v = idrh * (FLD(cu, 3, 0, 0, nr) - FLD(cu, 3, 0, 0, nr - 2)) + ir * FLD(cu, 3, 0, 0, nr - 1);
+      } else if (i == nr) {
+        const double ir = idr / (double)(nr - 1);
+        v = idr * (FLD(cu, 3, 0, 0, nr) - FLD(cu, 3, 0, 0, nr - 1)) + ir * FLD(cu, 3, 0, 0, nr);
+      } else {
+        const double ir = idr / (double)(i - 1);
+        v = idrh * (FLD(cu, 3, 0, 0, i + 1) - FLD(cu, 3, 0, 0, i - 1)) + ir * FLD(cu, 3, 0, 0, i);
+        div += v * (double)(i - 1);
+      }
+      d0[i] = v;
+    }
+    div = block_sum(div, sc);
+    if (threadIdx.x == 0) {
+      div = div - idrh * (FLD(cu, 3, 0, 0, nr - 2) + FLD(cu, 3, 0, 0, nr - 1)) * ((double)nr - 2.5);
+      d0[1] = -8.0 * div;
+    }
+  } else {
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+      double re, im;
+      if (i == nr) {
+        const double ir = idr / (double)(nr - 1);
+        re = idrh * (3.0 * FLD(cu, 3, pr, 0, nr) - 4.0 * FLD(cu, 3, pr, 0, nr - 1) + FLD(cu, 3, pr, 0, nr - 2)) +
+             ir * FLD(cu, 3, pr, 0, nr) - dm * ir * FLD(cu, 3, pi, 1, nr);
+        im = idrh * (3.0 * FLD(cu, 3, pi, 0, nr) - 4.0 * FLD(cu, 3, pi, 0, nr - 1) + FLD(cu, 3, pi, 0, nr - 2)) +
+             ir * FLD(cu, 3, pi, 0, nr) + dm * ir * FLD(cu, 3, pr, 1, nr);
+      } else if (i == 1) {
+        if (m % 2 == 0) {
+          re = 2.0 * idr * FLD(cu, 3, pr, 0, 2) - dm * idr * FLD(cu, 3, pi, 1, 2);
+          im = 2.0 * idr * FLD(cu, 3, pi, 0, 2) + dm * idr * FLD(cu, 3, pr, 1, 2);
+        } else {
+          re = 0.0;
+          im = 0.0;
+        }
+      } else if (i == 2 && m == 1) {
+        const double ir = idr;
+        re = idr * (FLD(cu, 3, pr, 0, 3) - FLD(cu, 3, pr, 0, 2)) + ir * FLD(cu, 3, pr, 0, 2) -
+             dm * ir * FLD(cu, 3, pi, 1, 2);
+        im = idr * (FLD(cu, 3, pi, 0, 3) - FLD(cu, 3, pi, 0, 2)) + ir * FLD(cu, 3, pi, 0, 2) +
+             dm * ir * FLD(cu, 3, pr, 1, 2);
+      } else {
+        const double ir = idr / (double)(i - 1);
+        re = idrh * (FLD(cu, 3, pr, 0, i + 1) - FLD(cu, 3, pr, 0, i - 1)) + ir * FLD(cu, 3, pr, 0, i) -
+             dm * ir * FLD(cu, 3, pi, 1, i);
+        im = idrh * (FLD(cu, 3, pi, 0, i + 1) - FLD(cu, 3, pi, 0, i - 1)) + ir * FLD(cu, 3, pi, 0, i) +
+             dm * ir * FLD(cu, 3, pr, 1, i);
+      }
+      d0[i] = re;
+      d1[i] = im;
+    }
+  }
+  __syncthreads();
+  solve_mode(G, fac, OK_GEN, m, d0 + 1, m > 0 ? d1 + 1 : nullptr, sc);
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    FLD(e, 3, pr, 2, i) = (m > 0 && i == 1) ? 0.0 : d0[i];
+    if (m > 0) FLD(e, 3, pi, 2, i) = (i == 1) ? 0.0 : d1[i];
+  }
+  __syncthreads();
+}
+
+// E-perp from B and psi: field_e_class.f03:412-514 (no solve)
+__device__ void op_et(const GridDev& G, int m, const double* __restrict__ b, const double* __restrict__ psi,
+                      double* __restrict__ e) {
+  const int nr = G.nr;
+  const double idr = G.idr, idrh = idr * 0.5, dm = (double)m;
+  if (m == 0) {
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+      double e0, e1;
+      if (i == 1) {
+        e0 = 0.0;
+        e1 = 0.0;
+      } else if (i == nr) {
+        e0 = FLD(b, 3, 0, 1, nr) + idrh * (4.0 * FLD(psi, 1, 0, 0, nr - 1) - FLD(psi, 1, 0, 0, nr - 2) -
+                                           3.0 * FLD(psi, 1, 0, 0, nr));
+        e1 = -FLD(b, 3, 0, 0, nr);
+      } else {
+        e0 = FLD(b, 3, 0, 1, i) - idrh * (FLD(psi, 1, 0, 0, i + 1) - FLD(psi, 1, 0, 0, i - 1));
+        e1 = -FLD(b, 3, 0, 0, i);
+      }
+      FLD(e, 3, 0, 0, i) = e0;
+      FLD(e, 3, 0, 1, i) = e1;
+    }
+  } else {
+    const int pr = part_re(m), pi = part_im(m);
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+      double r0, i0, r1, i1;
+      if (i == 1) {
+        if (m == 1) {
+          r0 = FLD(b, 3, pr, 1, 1) - idr * FLD(psi, 1, pr, 0, 2);
+          i0 = FLD(b, 3, pi, 1, 1) - idr * FLD(psi, 1, pi, 0, 2);
+          r1 = -FLD(b, 3, pr, 0, 1) + idr * FLD(psi, 1, pi, 0, 2);
+          i1 = -FLD(b, 3, pi, 0, 1) - idr * FLD(psi, 1, pr, 0, 2);
+        } else {
+          r0 = i0 = r1 = i1 = 0.0;
+        }
+      } else {
+        const double ir = idr / (double)(i - 1);
+        if (i == nr) {
+          r0 = FLD(b, 3, pr, 1, nr) + idrh * (4.0 * FLD(psi, 1, pr, 0, nr - 1) - FLD(psi, 1, pr, 0, nr - 2) -
+                                              3.0 * FLD(psi, 1, pr, 0, nr));
+          i0 = FLD(b, 3, pi, 1, nr) + idrh * (4.0 * FLD(psi, 1, pi, 0, nr - 1) - FLD(psi, 1, pi, 0, nr - 2) -
+                                              3.0 * FLD(psi, 1, pi, 0, nr));
+        } else {
+          r0 = FLD(b, 3, pr, 1, i) - idrh * (FLD(psi, 1, pr, 0, i + 1) - FLD(psi, 1, pr, 0, i - 1));
+          i0 = FLD(b, 3, pi, 1, i) - idrh * (FLD(psi, 1, pi, 0, i + 1) - FLD(psi, 1, pi, 0, i - 1));
+        }
+        r1 = -FLD(b, 3, pr, 0, i) + ir * dm * FLD(psi, 1, pi, 0, i);
+        i1 = -FLD(b, 3, pi, 0, i) - ir * dm * FLD(psi, 1, pr, 0, i);
+      }
+      FLD(e, 3, pr, 0, i) = r0;
+      FLD(e, 3, pi, 0, i) = i0;
+      FLD(e, 3, pr, 1, i) = r1;
+      FLD(e, 3, pi, 1, i) = i1;
+    }
+  }
+  __syncthreads();
+}
+
+// dJ_perp/dxi: field_src_class.f03:273-405 (no solve)
+__device__ void op_djdxi(const GridDev& G, int m, const double* __restrict__ acu, const double* __restrict__ amu,
+                         double* __restrict__ dcu) {
+  const int nr = G.nr;
+  const double idr = G.idr, idrh = idr * 0.5, dm = (double)m;
+#define A_(p, c, i) FLD(acu, 2, p, c, i)
+#define U_(p, c, i) FLD(amu, 3, p, c, i)
+  if (m == 0) {
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+      double v0, v1;
+      if (i == 1) {
+        v0 = 0.0;
+        v1 = 0.0;
+      } else if (i == nr) {
+        const double ir = idr / (double)(nr - 1);
+        v0 = A_(0, 0, nr) + idrh * (4.0 * U_(0, 0, nr - 1) - U_(0, 0, nr - 2) - 3.0 * U_(0, 0, nr)) - ir * U_(0, 0, nr);
+        v1 = A_(0, 1, nr) + idrh * (4.0 * U_(0, 1, nr - 1) - U_(0, 1, nr - 2) - 3.0 * U_(0, 1, nr)) - ir * U_(0, 1, nr);
+      } else {
+        const double ir = idr / (double)(i - 1);
+        v0 = A_(0, 0, i) - idrh * (U_(0, 0, i + 1) - U_(0, 0, i - 1)) - ir * U_(0, 0, i);
+        v1 = A_(0, 1, i) - idrh * (U_(0, 1, i + 1) - U_(0, 1, i - 1)) - ir * U_(0, 1, i);
+      }
+      FLD(dcu, 2, 0, 0, i) = v0;
+      FLD(dcu, 2, 0, 1, i) = v1;
+    }
+  } else {
+    const int r = part_re(m), s = part_im(m);
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+      double a0, a1, b0, b1;
+      if (i == 1) {
+        if (m == 1) {
+          a0 = A_(r, 0, 1) - 2.0 * idr * U_(r, 0, 2) + dm * idr * U_(s, 1, 2);
+          a1 = A_(r, 1, 1) - 2.0 * idr * U_(r, 1, 2) + dm * idr * U_(s, 2, 2);
+          b0 = A_(s, 0, 1) - 2.0 * idr * U_(s, 0, 2) - dm * idr * U_(r, 1, 2);
+          b1 = A_(s, 1, 1) - 2.0 * idr * U_(s, 1, 2) - dm * idr * U_(r, 2, 2);
+        } else {
+          a0 = a1 = b0 = b1 = 0.0;
+        }
+      } else if (i == nr) {
+        const double ir = idr / (double)(nr - 1);
+        a0 = A_(r, 0, nr) + idrh * (4.0 * U_(r, 0, nr - 1) - U_(r, 0, nr - 2) - 3.0 * U_(r, 0, nr)) - ir * U_(r, 0, nr) + dm * ir * U_(s, 1, nr);
+        a1 = A_(r, 1, nr) + idrh * (4.0 * U_(r, 1, nr - 1) - U_(r, 1, nr - 2) - 3.0 * U_(r, 1, nr)) - ir * U_(r, 1, nr) + dm * ir * U_(s, 2, nr);
+        b0 = A_(s, 0, nr) + idrh * (4.0 * U_(s, 0, nr - 1) - U_(s, 0, nr - 2) - 3.0 * U_(s, 0, nr)) - ir * U_(s, 0, nr) - dm * ir * U_(r, 1, nr);
+        b1 = A_(s, 1, nr) + idrh * (4.0 * U_(s, 1, nr - 1) - U_(s, 1, nr - 2) - 3.0 * U_(s, 1, nr)) - ir * U_(s, 1, nr) - dm * ir * U_(r, 2, nr);
+      } else if (i == 2 && m == 2) {
+        const double ir = idr;
+        a0 = A_(r, 0, 2) - idr * (U_(r, 0, 3) - U_(r, 0, 2)) - ir * U_(r, 0, 2) + dm * ir * U_(s, 1, 2);
+        a1 = A_(r, 1, 2) - idr * (U_(r, 1, 3) - U_(r, 1, 2)) - ir * U_(r, 1, 2) + dm * ir * U_(s, 2, 2);
+        b0 = A_(s, 0, 2) - idr * (U_(s, 0, 3) - U_(s, 0, 2)) - ir * U_(s, 0, 2) - dm * ir * U_(r, 1, 2);
+        b1 = A_(s, 1, 2) - idr * (U_(s, 1, 3) - U_(s, 1, 2)) - ir * U_(s, 1, 2) - dm * ir * U_(r, 2, 2);
+      } else {
+        const double ir = idr / (double)(i - 1);
+        a0 = A_(r, 0, i) - idrh * (U_(r, 0, i + 1) - U_(r, 0, i - 1)) - ir * U_(r, 0, i) + dm * ir * U_(s, 1, i);
+        a1 = A_(r, 1, i) - idrh * (U_(r, 1, i + 1) - U_(r, 1, i - 1)) - ir * U_(r, 1, i) + dm * ir * U_(s, 2, i);
+        b0 = A_(s, 0, i) - idrh * (U_(s, 0, i + 1) - U_(s, 0, i - 1)) - ir * U_(s, 0, i) - dm * ir * U_(r, 1, i);
+        b1 = A_(s, 1, i) - idrh * (U_(s, 1, i + 1) - U_(s, 1, i - 1)) - ir * U_(s, 1, i) - dm * ir * U_(r, 2, i);
+      }
+      FLD(dcu, 2, r, 0, i) = a0;
+      FLD(dcu, 2, r, 1, i) = a1;
+      FLD(dcu, 2, s, 0, i) = b0;
+      FLD(dcu, 2, s, 1, i) = b1;
+    }
+  }
+#undef A_
+#undef U_
+  __syncthreads();
+}
+
+// Raw charge deposit -> density (part2d_class.f03:314-335): axis guard 0, axis x8 for
+// m=0 and 0 for m>0, 1/(j-1) beyond.  out = raw finished (+ qn when add_qn, which is the
+// species2d::qdp accumulation q_spe = 0 + q_species + qn).
+__device__ void op_finish_q(const GridDev& G, int m, const double* __restrict__ raw, const double* __restrict__ qn,
+                            double* __restrict__ out) {
+  const int np_ = m == 0 ? 1 : 2;
+  for (int h = 0; h < np_; ++h) {
+    const int p = h == 0 ? part_re(m) : part_im(m);
+    for (int i = threadIdx.x; i <= G.nr + 1; i += blockDim.x) {
+      const double r = FLD(raw, 1, p, 0, i);
+      double v;
+      if (i == 0) v = 0.0;
+      else if (i == 1) v = (m == 0) ? 8.0 * r : 0.0;
+      else v = r * (1.0 / (double)(i - 1));
+      if (qn) v = (0.0 + v) + FLD(qn, 1, p, 0, i);
+      FLD(out, 1, p, 0, i) = v;
+    }
+  }
+  __syncthreads();
+}
+
+// Axis fixes and 1/(j-1) scaling of the current, momentum-flux and acceleration deposits,
+// in place (part2d_class.f03:914-1005).
+__device__ void op_finish_amj(const GridDev& G, int m, double* __restrict__ cu, double* __restrict__ amu,
+                              double* __restrict__ acu) {
+  const int np_ = m == 0 ? 1 : 2;
+  for (int h = 0; h < np_; ++h) {
+    const int p = h == 0 ? part_re(m) : part_im(m);
+    for (int i = threadIdx.x; i <= G.nr + 1; i += blockDim.x) {
+      if (i == 0) {
+        for (int c = 0; c < 3; ++c) { FLD(cu, 3, p, c, 0) = 0.0; FLD(amu, 3, p, c, 0) = 0.0; }
+        for (int c = 0; c < 2; ++c) FLD(acu, 2, p, c, 0) = 0.0;
+      } else if (i == 1) {
+        const double fcu0 = (m == 1) ? 8.0 : 0.0;   // J_r, J_phi
+        const double fcu2 = (m == 0) ? 8.0 : 0.0;   // J_z
+        const double fac_ = (m == 1) ? 8.0 : 0.0;   // acu
+        const double fam = (m == 2) ? 8.0 : 0.0;    // amu
+        FLD(cu, 3, p, 0, 1) = fcu0 == 0.0 ? 0.0 : fcu0 * FLD(cu, 3, p, 0, 1);
+        FLD(cu, 3, p, 1, 1) = fcu0 == 0.0 ? 0.0 : fcu0 * FLD(cu, 3, p, 1, 1);
+        FLD(cu, 3, p, 2, 1) = fcu2 == 0.0 ? 0.0 : fcu2 * FLD(cu, 3, p, 2, 1);
+        for (int c = 0; c < 2; ++c) FLD(acu, 2, p, c, 1) = fac_ == 0.0 ? 0.0 : fac_ * FLD(acu, 2, p, c, 1);
+        for (int c = 0; c < 3; ++c) FLD(amu, 3, p, c, 1) = fam == 0.0 ? 0.0 : fam * FLD(amu, 3, p, c, 1);
+      } else {
+        const double ir = 1.0 / (double)(i - 1);
+        for (int c = 0; c < 3; ++c) {
+          FLD(cu, 3, p, c, i) = FLD(cu, 3, p, c, i) * ir;
+          FLD(amu, 3, p, c, i) = FLD(amu, 3, p, c, i) * ir;
+        }
+        for (int c = 0; c < 2; ++c) FLD(acu, 2, p, c, i) = FLD(acu, 2, p, c, i) * ir;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// c = a + b over all components and nodes of mode m (add_f1_binary)
+__device__ void op_add(const GridDev& G, int m, int nc, const double* a, const double* b, double* c) {
+  const int np_ = m == 0 ? 1 : 2;
+  for (int h = 0; h < np_; ++h) {
+    const int p = h == 0 ? part_re(m) : part_im(m);
+    for (int k = threadIdx.x; k < nc * G.ld; k += blockDim.x) {
+      const size_t o = (size_t)p * nc * G.ld + k;
+      c[o] = a[o] + b[o];
+    }
+  }
+  __syncthreads();
+}
+
+__device__ void op_fill(const GridDev& G, int m, int nc, double* a, double v) {
+  const int np_ = m == 0 ? 1 : 2;
+  for (int h = 0; h < np_; ++h) {
+    const int p = h == 0 ? part_re(m) : part_im(m);
+    for (int k = threadIdx.x; k < nc * G.ld; k += blockDim.x) a[(size_t)p * nc * G.ld + k] = v;
+  }
+  __syncthreads();
+}
+
+__device__ void op_copy(const GridDev& G, int m, int nc, const double* a, double* b) {
+  const int np_ = m == 0 ? 1 : 2;
+  for (int h = 0; h < np_; ++h) {
+    const int p = h == 0 ? part_re(m) : part_im(m);
+    for (int k = threadIdx.x; k < nc * G.ld; k += blockDim.x) {
+      const size_t o = (size_t)p * nc * G.ld + k;
+      b[o] = a[o];
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------------------
+// Kernels
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kFieldThreads) k_field_op(GridDev G, int op, const double* __restrict__ fac,
+                                                            FieldArgs a) {
+  extern __shared__ double sm[];
+  __shared__ double sc[6 * 32 + 8];
+  const int m = blockIdx.x;
+  switch (op) {
+    case FOP_PSI: op_psi(G, m, fac, sm, sc, a.in0, a.out); break;
+    case FOP_BZ: op_bz(G, m, fac, sm, sc, a.in0, a.out); break;
+    case FOP_BT_BEAM: op_bt_beam(G, m, fac, sm, sc, a.in0, a.out); break;
+    case FOP_BT_ITER: op_bt_iter(G, m, fac, sm, sc, a.in0, a.in1, a.out); break;
+    case FOP_EZ: op_ez(G, m, fac, sm, sc, a.in0, a.out); break;
+    case FOP_ET: op_et(G, m, a.in0, a.in1, a.out); break;
+    case FOP_DJDXI: op_djdxi(G, m, a.in0, a.in1, a.out); break;
+  }
+}
+
+struct SliceFields {
+  double* f[QPAD_NFIELDS];
+  double* f2[QPAD_NFIELDS];
+  const double* qraw;
+  const double* qn;
+};
+
+static SliceFields slice_fields(qpad_ctx* ctx) {
+  SliceFields s;
+  for (int k = 0; k < QPAD_NFIELDS; ++k) { s.f[k] = ctx->f[k]; s.f2[k] = ctx->f2[k]; }
+  s.qraw = ctx->qraw;
+  s.qn = ctx->qn;
+  return s;
+}
+
+__device__ __forceinline__ double* store_slice(const GridDev& G, double* f2, int nc, int j) {
+  return f2 + (size_t)(j - 1) * G.P * nc * G.ld;
+}
+
+// Start of slice j (simulation_class.f03:344-360): beam B-perp from the stored beam
+// charge; species charge (+ background) and psi; Bz from the carried current.
+__global__ void __launch_bounds__(kFieldThreads) k_slice_begin(GridDev G, const double* __restrict__ fac,
+                                                               SliceFields F, int j, int use_qn) {
+  extern __shared__ double sm[];
+  __shared__ double sc[6 * 32 + 8];
+  const int job = blockIdx.x / (G.M + 1), m = blockIdx.x % (G.M + 1);
+  if (job == 0) {
+    const double* qs = store_slice(G, F.f2[QPAD_F_Q_BEAM], 1, j);
+    op_copy(G, m, 1, qs, F.f[QPAD_F_Q_BEAM]);                      // q_beam%copy_slice(j, 2->1)
+    op_bt_beam(G, m, fac, sm, sc, F.f[QPAD_F_Q_BEAM], F.f[QPAD_F_B_BEAM]);
+  } else if (job == 1) {
+    op_finish_q(G, m, F.qraw, use_qn ? F.qn : nullptr, F.f[QPAD_F_Q_SPE]);
+    op_psi(G, m, fac, sm, sc, F.f[QPAD_F_Q_SPE], F.f[QPAD_F_PSI]);
+  } else {
+    op_bz(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_B_SPE]);
+  }
+}
+
+// Iteration phase 1 (simulation_class.f03:375-380): b = b_spe + b_beam, Ez(cu), E-perp(b,psi);
+// then cu = acu = amu = 0 for the deposit that follows.
+__global__ void __launch_bounds__(kFieldThreads) k_iter_e(GridDev G, const double* __restrict__ fac, SliceFields F) {
+  extern __shared__ double sm[];
+  __shared__ double sc[6 * 32 + 8];
+  const int m = blockIdx.x;
+  op_add(G, m, 3, F.f[QPAD_F_B_SPE], F.f[QPAD_F_B_BEAM], F.f[QPAD_F_B]);
+  op_ez(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_E]);
+  op_et(G, m, F.f[QPAD_F_B], F.f[QPAD_F_PSI], F.f[QPAD_F_E]);
+  op_fill(G, m, 3, F.f[QPAD_F_CU], 0.0);
+  op_fill(G, m, 2, F.f[QPAD_F_ACU], 0.0);
+  op_fill(G, m, 3, F.f[QPAD_F_AMU], 0.0);
+}
+
+// Iteration phase 2 (simulation_class.f03:386-392): finish the deposits, dJ/dxi, B-perp
+// predictor-corrector solve and Bz.
+__global__ void __launch_bounds__(kFieldThreads) k_iter_b(GridDev G, const double* __restrict__ fac, SliceFields F) {
+  extern __shared__ double sm[];
+  __shared__ double sc[6 * 32 + 8];
+  const int m = blockIdx.x;
+  op_finish_amj(G, m, F.f[QPAD_F_CU], F.f[QPAD_F_AMU], F.f[QPAD_F_ACU]);
+  op_djdxi(G, m, F.f[QPAD_F_ACU], F.f[QPAD_F_AMU], F.f[QPAD_F_DCU]);
+  op_bt_iter(G, m, fac, sm, sc, F.f[QPAD_F_DCU], F.f[QPAD_F_CU], F.f[QPAD_F_B_SPE]);
+  op_bz(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_B_SPE]);
+}
+
+// End of slice j (simulation_class.f03:403-456 without the particle push): cbq and the
+// stores of cu and rho, total and species fields, the J-perp predictor for slice j+1.
+__global__ void __launch_bounds__(kFieldThreads) k_slice_end(GridDev G, const double* __restrict__ fac,
+                                                             SliceFields F, int j) {
+  extern __shared__ double sm[];
+  __shared__ double sc[6 * 32 + 8];
+  const int m = blockIdx.x;
+  const int npart = m == 0 ? 1 : 2;
+  double* cu = F.f[QPAD_F_CU];
+  double* qs = F.f[QPAD_F_Q_SPE];
+  // q_spe(1,:) += cu(3,:) over all nodes, then the stores of cu and q_spe
+  for (int h = 0; h < npart; ++h) {
+    const int p = h == 0 ? part_re(m) : part_im(m);
+    for (int i = threadIdx.x; i < G.ld; i += blockDim.x) FLD(qs, 1, p, 0, i) = FLD(qs, 1, p, 0, i) + FLD(cu, 3, p, 2, i);
+  }
+  __syncthreads();
+  op_copy(G, m, 3, cu, store_slice(G, F.f2[QPAD_F_CU], 3, j));
+  op_copy(G, m, 1, qs, store_slice(G, F.f2[QPAD_F_Q_SPE], 1, j));
+  op_add(G, m, 3, F.f[QPAD_F_B_SPE], F.f[QPAD_F_B_BEAM], F.f[QPAD_F_B]);
+  op_et(G, m, F.f[QPAD_F_B_SPE], F.f[QPAD_F_PSI], F.f[QPAD_F_E_SPE]);
+  op_ez(G, m, fac, sm, sc, cu, F.f[QPAD_F_E]);
+  op_et(G, m, F.f[QPAD_F_B], F.f[QPAD_F_PSI], F.f[QPAD_F_E]);
+  // dcu *= dxi ; cu(1:2) += dcu(1:2)   (simulation_class.f03:425-426)
+  double* dcu = F.f[QPAD_F_DCU];
+  for (int h = 0; h < npart; ++h) {
+    const int p = h == 0 ? part_re(m) : part_im(m);
+    for (int i = threadIdx.x; i < G.ld; i += blockDim.x)
+      for (int c = 0; c < 2; ++c) {
+        const double d = FLD(dcu, 2, p, c, i) * G.dxi;
+        FLD(dcu, 2, p, c, i) = d;
+        FLD(cu, 3, p, c, i) = FLD(cu, 3, p, c, i) + d;
+      }
+  }
+  __syncthreads();
+  op_copy(G, m, 3, F.f[QPAD_F_E], store_slice(G, F.f2[QPAD_F_E], 3, j));
+  op_copy(G, m, 3, F.f[QPAD_F_B], store_slice(G, F.f2[QPAD_F_B], 3, j));
+  op_copy(G, m, 1, F.f[QPAD_F_PSI], store_slice(G, F.f2[QPAD_F_PSI], 1, j));
+  op_copy(G, m, 3, F.f[QPAD_F_B_SPE], store_slice(G, F.f2[QPAD_F_B_SPE], 3, j));
+  op_copy(G, m, 3, F.f[QPAD_F_E_SPE], store_slice(G, F.f2[QPAD_F_E_SPE], 3, j));
+}
+
+__global__ void __launch_bounds__(kFieldThreads) k_finish_q(GridDev G, const double* raw, const double* qn,
+                                                            double* out) {
+  op_finish_q(G, blockIdx.x, raw, qn, out);
+}
+
+__global__ void __launch_bounds__(kFieldThreads) k_finish_amj(GridDev G, double* cu, double* amu, double* acu) {
+  op_finish_amj(G, blockIdx.x, cu, amu, acu);
+}
+
+// convergence_tester (simulation_class.f03:522-606) on component `comp` of b:
+// op 0 records s_re/s_im; op 1 compares against the record, writes rel/abs/converged
+// into res and records the new sums for the next iteration.
+__global__ void __launch_bounds__(1024) k_conv(GridDev G, const double* __restrict__ b, int comp, int op,
+                                               double* __restrict__ st, double reltol, double abstol) {
+  __shared__ double red[33];
+  const int nr = G.nr, M = G.M;
+  double* s_re = st;
+  double* s_im = st + nr;
+  double* res = st + 2 * nr;
+  double mx_old = 0.0, mx_new = 0.0;
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    double nre = 0.0, nim = 0.0;   // record of the current field
+    double ore = s_re[i - 1], oim = s_im[i - 1];
+    if (op == 1) {
+      const double v = ore * ore + oim * oim;
+      mx_old = fmax(mx_old, v);
+    }
+    for (int m = 0; m <= M; ++m) {
+      const double vr = fabs(FLD(b, 3, part_re(m), comp, i));
+      nre = nre + vr;
+      if (op == 1) ore = ore - vr;
+      if (m == 0) continue;
+      const double vi = fabs(FLD(b, 3, part_im(m), comp, i));
+      nim = nim + vi;
+      if (op == 1) oim = oim - vi;
+    }
+    if (op == 1) mx_new = fmax(mx_new, ore * ore + oim * oim);
+    s_re[i - 1] = nre;
+    s_im[i - 1] = nim;
+  }
+  if (op == 0) return;
+  // max-reductions (order independent, exact)
+  for (int off = 16; off > 0; off >>= 1) {
+    mx_old = fmax(mx_old, __shfl_down_sync(FULLMASK, mx_old, off));
+    mx_new = fmax(mx_new, __shfl_down_sync(FULLMASK, mx_new, off));
+  }
+  __shared__ double red2[33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { red[warp] = mx_old; red2[warp] = mx_new; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, c = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a = fmax(a, red[w]); c = fmax(c, red2[w]); }
+    const double old_norm = sqrt(a), abs_res = sqrt(c);
+    const double rel = old_norm > 2.220446049250313e-16 ? abs_res / old_norm : 1.7976931348623157e308;
+    res[0] = rel;
+    res[1] = abs_res;
+    res[2] = (rel < reltol || abs_res < abstol) ? 1.0 : 0.0;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Host launchers
+// ------------------------------------------------------------------------------------
+static size_t field_smem(const qpad_ctx* ctx) { return (size_t)4 * (ctx->g.nr + 2) * sizeof(double); }
+
+static int ensure_smem_attr(qpad_ctx* ctx) {
+  if (ctx->field_attr_done) return 0;
+  const size_t need = field_smem(ctx);
+  const void* ks[] = {(const void*)k_field_op, (const void*)k_slice_begin, (const void*)k_iter_e,
+                      (const void*)k_iter_b, (const void*)k_slice_end};
+  for (const void* k : ks) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "cudaFuncSetAttribute(smem)");
+  }
+  ctx->field_attr_done = true;
+  return 0;
+}
+
+int launch_field_op(qpad_ctx* ctx, int op, FieldArgs a) {
+  if (int r = ensure_smem_attr(ctx)) return r;
+  k_field_op<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, op, ctx->fac, a);
+  return check_launch(ctx, "k_field_op");
+}
+
+int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op) {
+  k_conv<<<1, 1024, 0, ctx->stream>>>(ctx->g, b, comp, op, ctx->conv, ctx->reltol, ctx->abstol);
+  return check_launch(ctx, "k_conv");
+}
+
+int launch_slice_begin(qpad_ctx* ctx, int j, int use_qn) {
+  if (int r = ensure_smem_attr(ctx)) return r;
+  k_slice_begin<<<3 * (ctx->g.M + 1), kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac,
+                                                                                     slice_fields(ctx), j, use_qn);
+  return check_launch(ctx, "k_slice_begin");
+}
+
+int launch_iter_e(qpad_ctx* ctx) {
+  if (int r = ensure_smem_attr(ctx)) return r;
+  k_iter_e<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac, slice_fields(ctx));
+  return check_launch(ctx, "k_iter_e");
+}
+
+int launch_iter_b(qpad_ctx* ctx) {
+  if (int r = ensure_smem_attr(ctx)) return r;
+  k_iter_b<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac, slice_fields(ctx));
+  return check_launch(ctx, "k_iter_b");
+}
+
+int launch_slice_end(qpad_ctx* ctx, int j) {
+  if (int r = ensure_smem_attr(ctx)) return r;
+  k_slice_end<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac, slice_fields(ctx), j);
+  return check_launch(ctx, "k_slice_end");
+}
+
+int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn) {
+  k_finish_q<<<ctx->g.M + 1, kFieldThreads, 0, ctx->stream>>>(ctx->g, raw, add_qn ? ctx->qn : nullptr, out);
+  return check_launch(ctx, "k_finish_q");
+}
+
+int launch_finish_amj(qpad_ctx* ctx, double* cu, double* amu, double* acu) {
+  k_finish_amj<<<ctx->g.M + 1, kFieldThreads, 0, ctx->stream>>>(ctx->g, cu, amu, acu);
+  return check_launch(ctx, "k_finish_amj");
+}
+
+}  // namespace qpad

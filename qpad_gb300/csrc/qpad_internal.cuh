@@ -1,0 +1,167 @@
+// qpad_internal.cuh -- shared device/host declarations of the GB300 quasi-static slice loop.
+//
+// Device data layout (all FP64 in the reference-arithmetic path):
+//   slice field f1    f[(p*nc + c)*ld + i]          p = mode part (0: m=0, 2m-1: Re m, 2m: Im m)
+//                                                   c = component, i = node 0..nr+1 (ld = nr+2)
+//   3D store f2       f[(((s-1)*P + p)*nc + c)*ld + i]   s = xi slice 1..nz+1
+//   particles         structure of arrays, one float64 array per coordinate
+// The layouts are the reference's f1(dim, 0:nr+1) per mode part with the component
+// index moved outward, so that each radial line is contiguous for the tridiagonal
+// solves and coalesced for the source builders.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/qpad_gpu.h"
+
+#define QPAD_MAX_MODE 8
+#define QPAD_MAX_PARTS (2 * QPAD_MAX_MODE + 1)
+
+namespace qpad {
+
+// Kinds of tridiagonal operator with distinct matrices (field_solver_class.f03:256-561).
+// psi, Ez and Bz share one matrix per mode (their interior rows and boundary rows are
+// identical), the beam B-perp potential differs only in its m = 0 outer row.
+enum OpKind { OK_GEN = 0, OK_BT = 1, OK_BPLUS = 2, OK_BMINUS = 3, OK_NKINDS = 4 };
+
+struct GridDev {
+  int nr, nz, M, P, ld, bnd;
+  double dr, dxi, idr, relax_fac;
+};
+
+__host__ __device__ inline int part_re(int m) { return m == 0 ? 0 : 2 * m - 1; }
+__host__ __device__ inline int part_im(int m) { return 2 * m; }
+
+__host__ __device__ inline size_t fidx(int ld, int nc, int p, int c, int i) {
+  return ((size_t)p * nc + c) * (size_t)ld + (size_t)i;
+}
+
+// Factor tables for one (kind, mode): forward multipliers w, reciprocal pivots ib and
+// back-substitution multipliers g of the Thomas factorisation, each of length nr.
+__host__ __device__ inline size_t fac_off(int nr, int M, int kind, int m) {
+  return ((size_t)kind * (M + 1) + m) * 3 * (size_t)nr;
+}
+
+int field_ncomp(int field);
+
+struct Species;
+struct Beam;
+
+}  // namespace qpad
+
+struct qpad_ctx {
+  qpad::GridDev g;
+  int iter_max;
+  double reltol, abstol, dt;
+  int precision;
+  int device;
+  cudaStream_t stream = nullptr;
+  double* fac = nullptr;                       // device factor tables
+  double* f[QPAD_NFIELDS] = {};                // slice fields
+  double* f2[QPAD_NFIELDS] = {};               // 3D stores (only some fields have one)
+  double* qn = nullptr;                        // neutralising background (sum over species)
+  double* qraw = nullptr;                      // raw charge deposit scratch
+  double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
+  double* scratch = nullptr;                   // per-call deposit scratch (cu, amu, acu)
+  double* beam_scratch = nullptr;              // per-beam charge store scratch
+  double* h_res = nullptr;                     // pinned mirror of res
+  int* d_err = nullptr;                        // device error word
+  std::vector<qpad_species*> species;
+  std::vector<qpad_beam*> beams;
+  std::string err;
+  int slice_counter = 0;
+  bool field_attr_done = false;
+  int64_t launches = 0;                        // kernels launched on this context
+  // per-kernel-family CUDA-event timing (qpad_profile_enable / qpad_profile_read)
+  bool prof_on = false;
+  struct Prof { std::vector<cudaEvent_t> pending; double ms = 0.0; int64_t n = 0; };
+  std::map<std::string, Prof> prof;
+  std::vector<cudaEvent_t> ev_pool;
+};
+
+struct qpad_species {
+  qpad_ctx* ctx;
+  double qbm;
+  int push_type, neutralized, sort_freq;
+  int64_t np, npmax;
+  // SoA particle state; [0] active, [1] scratch for compaction / sorting
+  double *x[2], *y[2], *px[2], *py[2], *pz[2], *gamma[2], *psi[2], *q[2];
+  int32_t* key = nullptr;       // cell keys / flags
+  int32_t* aux = nullptr;       // per-particle rank / index scratch
+  int32_t* blk = nullptr;       // per-block counts / histograms
+  int64_t blk_cap = 0;
+  int64_t* d_count = nullptr;   // device particle count
+  int64_t* d_total = nullptr;   // scan total scratch
+  int64_t* h_count = nullptr;   // pinned mirror
+  double* pristine = nullptr;   // device copy of the last uploaded particles (8 x npmax)
+  int64_t np_pristine = 0;
+  double* qf = nullptr;         // this species' charge density (finished deposit)
+  double* qn = nullptr;         // this species' neutralising background
+};
+
+struct qpad_beam {
+  qpad_ctx* ctx;
+  double qbm;
+  int push_type, evolution;
+  int64_t nb, npmax;
+  double *x[2], *y[2], *z[2], *px[2], *py[2], *pz[2], *q[2];
+  int32_t* key = nullptr;
+  int32_t* blk = nullptr;
+  int64_t blk_cap = 0;
+  int64_t* d_count = nullptr;
+  int64_t* d_total = nullptr;
+  int32_t* aux = nullptr;
+  int64_t* h_count = nullptr;
+};
+
+namespace qpad {
+
+// ---- status helpers (capi.cu) -----------------------------------------------------------
+int set_err(qpad_ctx* ctx, int code, const std::string& msg);
+int cuda_check(qpad_ctx* ctx, cudaError_t e, const char* what);
+int check_launch(qpad_ctx* ctx, const char* what, int nlaunch = 1);
+// CUDA-event bracket of one launch family on ctx->stream (no-ops unless profiling is on)
+void prof_begin(qpad_ctx* ctx, const char* name);
+void prof_end(qpad_ctx* ctx, const char* name);
+void prof_collect(qpad_ctx* ctx);   // folds completed pairs into the totals (stream idle)
+
+// ---- field kernels (fields.cu) ----------------------------------------------------------
+int build_factors(qpad_ctx* ctx);
+enum FieldOp {
+  FOP_PSI = 0, FOP_BZ, FOP_BT_BEAM, FOP_BT_ITER, FOP_EZ, FOP_ET, FOP_DJDXI
+};
+struct FieldArgs {
+  double* out;        // destination field
+  const double* in0;  // first source
+  const double* in1;  // second source (psi for ET, cu for BT_ITER, amu for DJDXI)
+};
+int launch_field_op(qpad_ctx* ctx, int op, FieldArgs a);
+int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op);
+// fused phases of one slice
+int launch_slice_begin(qpad_ctx* ctx, int j, int neutralized_any);
+int launch_iter_e(qpad_ctx* ctx);
+int launch_iter_b(qpad_ctx* ctx);
+int launch_slice_end(qpad_ctx* ctx, int j);
+int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn);
+int launch_finish_amj(qpad_ctx* ctx, double* cu, double* amu, double* acu);
+
+// ---- particle kernels (plasma.cu, beam.cu) ---------------------------------------------
+int species_qdeposit_raw(qpad_species* sp, double* qraw);
+int species_amjdp_raw(qpad_species* sp, const double* ef, const double* bf, double* cu, double* amu,
+                      double* acu, double dt);
+int species_push_u(qpad_species* sp, const double* ef, const double* bf, double dt, int fuse_x);
+int species_push_x(qpad_species* sp, double dt);
+int species_compact(qpad_species* sp);
+int species_sort(qpad_species* sp);
+int species_interp_psi(qpad_species* sp, const double* psif);
+int species_sync_count(qpad_species* sp);
+int beam_qdeposit(qpad_beam* bm, double* q2);
+int beam_finish_q(qpad_ctx* ctx, double* q2);
+int beam_push(qpad_beam* bm, const double* e2, const double* b2);
+
+}  // namespace qpad
