@@ -171,8 +171,9 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("gloo")
         torch.cuda.set_device(local)
+    from qpad_gb300.replicas import reduce_timing, replica_seed
     deck = _deck(args)
-    deck.seed = deck.seed + 17 * rank          # independent replica per GPU
+    deck.seed = replica_seed(deck.seed, rank)   # independent replica per GPU
     prec = K.PREC_FP64 if args.precision == "fp64" else K.PREC_MIXED
     inputs = Q.deck_inputs(deck)
     sim = Q.build_simulation(deck, precision=prec, device=local, inputs=inputs)
@@ -207,13 +208,9 @@ def run_ours(args):
     sim.profile(False)
     dev_s = step_ms / 1e3 if nstep else wall
     barrier()
-    if dist is not None:
-        import torch
-        tt = torch.tensor([dev_s], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_s = float(tt.item())
     pushes_step = npl * deck.nz
-    value = world * pushes_step * args.steps / dev_s
+    dev_s, total_pushes = reduce_timing(dev_s, float(pushes_step * args.steps), dist)
+    value = total_pushes / dev_s
     iters_per_slice = iters_tot / (args.steps * deck.nz)
 
     # end to end through the C ABI with host buffers: renew from host arrays every step

@@ -83,6 +83,12 @@ int qpad_field_layout(const qpad_ctx* ctx, int field, int* ncomp, int64_t* ld);
 int qpad_device_count(int* count);
 /* Kernel launches issued on this context so far (all kernels of this library). */
 int qpad_launch_count(const qpad_ctx* ctx, int64_t* count);
+/* qpad_3d_step runs its slice loop as one CUDA graph (a WHILE node over slices holding a
+ * WHILE node over predictor-corrector iterations, both conditions set on the device) when
+ * on != 0 (the default); off, the host drives slices and iterations. */
+int qpad_set_graph(qpad_ctx* ctx, int on);
+/* 1 if the last 3D step ran as a graph. */
+int qpad_graph_active(const qpad_ctx* ctx, int* active);
 /* Per-kernel CUDA-event timing on the context's stream: enable/disable, then read the
  * accumulated device time (ms) and launch count of one kernel family by name
  * ("amjdp", "qdeposit", "push", "field", "beam_push", "beam_qdeposit"). */

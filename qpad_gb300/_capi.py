@@ -67,6 +67,8 @@ _SIGS = {
     "qpad_field_layout": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), I64P]),
     "qpad_device_count": (C.c_int, [C.POINTER(C.c_int)]),
     "qpad_launch_count": (C.c_int, [C.c_void_p, I64P]),
+    "qpad_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "qpad_graph_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "qpad_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
     "qpad_profile_read": (C.c_int, [C.c_void_p, C.c_char_p, D, I64P]),
     "qpad_species_reset": (C.c_int, [C.c_void_p]),

@@ -1,5 +1,6 @@
 // capi.cu -- the C ABI (include/qpad_gpu.h): contexts, fields, species, beams and the
 // fused slice / 3D-step drivers of run_simulation (simulation_class.f03:294-512).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -233,10 +234,22 @@ int species_load(qpad_species* sp, const double* x, const double* p, const doubl
   if (cudaMemcpyAsync(sp->d_count, sp->h_count, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
     return check_launch(ctx, "count upload");
   if (int r = save_pristine(sp)) return r;
+  // the neutralising background is deposited in FP64 from the FP64 particles in both paths
   if (int r = species_set_background(sp)) return r;
   if (int r = rebuild_total_background(ctx)) return r;
+  if (ctx->precision == QPAD_PREC_MIXED) {
+    if (int r = mixed_from_fp64(sp)) return r;           // convert + sort by cell
+    if (int r = species_sync_count(sp)) return r;
+    sp->np_pristine = sp->np;
+    if (int r = mixed_save_pristine(sp)) return r;
+  }
   return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "species load");
 }
+
+bool is_mixed(const qpad_species* sp) { return sp->ctx->precision == QPAD_PREC_MIXED; }
+
+// FP64 buffers [0] mirror the mixed state before any read of particle data
+int sync_fp64_view(qpad_species* sp) { return is_mixed(sp) ? mixed_to_fp64(sp) : 0; }
 
 int beam_load(qpad_beam* bm, const double* x, const double* p, const double* q, int64_t nb) {
   qpad_ctx* ctx = bm->ctx;
@@ -293,6 +306,12 @@ extern "C" int qpad_ctx_create(const qpad_grid_desc* d, qpad_ctx** out) {
   if (!r) r = dmalloc(ctx, (void**)&ctx->qn, f1_elems(ctx, QPAD_F_Q_SPE) * sizeof(double), "qn");
   if (!r) r = dmalloc(ctx, (void**)&ctx->qraw, f1_elems(ctx, QPAD_F_Q_SPE) * sizeof(double), "qraw");
   if (!r) r = dmalloc(ctx, (void**)&ctx->conv, (2 * (size_t)g.nr + 8) * sizeof(double), "conv");
+  if (!r && ctx->precision == QPAD_PREC_MIXED)
+    r = dmalloc(ctx, (void**)&ctx->gtab, (size_t)g.ld * g.P * 6 * sizeof(float), "gather table");
+  if (!r) r = dmalloc(ctx, (void**)&ctx->d_j, 2 * sizeof(int), "slice index");
+  if (!r) r = dmalloc(ctx, (void**)&ctx->d_iter, 2 * sizeof(int), "iteration counter");
+  if (!r) r = dmalloc(ctx, (void**)&ctx->d_stats, (size_t)g.nz * sizeof(qpad_slice_stats), "slice stats");
+  if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->h_j, 2 * sizeof(int)), "pinned slice index");
   if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->h_res, 8 * sizeof(double)), "pinned");
   if (!r) r = build_factors(ctx);
   if (!r) r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "create sync");
@@ -321,6 +340,13 @@ extern "C" int qpad_ctx_destroy(qpad_ctx* ctx) {
   if (ctx->qraw) cudaFree(ctx->qraw);
   if (ctx->conv) cudaFree(ctx->conv);
   if (ctx->scratch) cudaFree(ctx->scratch);
+  if (ctx->gtab) cudaFree(ctx->gtab);
+  if (ctx->beam_scratch) cudaFree(ctx->beam_scratch);
+  if (ctx->d_j) cudaFree(ctx->d_j);
+  if (ctx->d_iter) cudaFree(ctx->d_iter);
+  if (ctx->d_stats) cudaFree(ctx->d_stats);
+  if (ctx->h_j) cudaFreeHost(ctx->h_j);
+  if (ctx->step_exec) cudaGraphExecDestroy(ctx->step_exec);
   if (ctx->h_res) cudaFreeHost(ctx->h_res);
   prof_collect(ctx);
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
@@ -353,6 +379,19 @@ extern "C" int qpad_device_count(int* count) {
     n = 0;
   }
   if (count) *count = n;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_set_graph(qpad_ctx* ctx, int on) {
+  if (!ctx) return QPAD_E_ARG;
+  ctx->use_graph = on != 0;
+  if (on) ctx->graph_status.clear();
+  return QPAD_OK;
+}
+
+extern "C" int qpad_graph_active(const qpad_ctx* ctx, int* active) {
+  if (!ctx || !active) return QPAD_E_ARG;
+  *active = (ctx->use_graph && ctx->step_exec != nullptr) ? 1 : 0;
   return QPAD_OK;
 }
 
@@ -568,6 +607,7 @@ extern "C" int qpad_species_create(qpad_ctx* ctx, const qpad_species_desc* d, co
   if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&sp->h_count, sizeof(int64_t)), "pinned count");
   if (!r) r = dmalloc(ctx, (void**)&sp->qf, f1_elems(ctx, QPAD_F_Q_SPE) * sizeof(double), "species q");
   if (!r) r = dmalloc(ctx, (void**)&sp->qn, f1_elems(ctx, QPAD_F_Q_SPE) * sizeof(double), "species qn");
+  if (!r && ctx->precision == QPAD_PREC_MIXED) r = mixed_alloc(sp);
   if (!r) {
     ctx->species.push_back(sp);
     r = species_load(sp, x, p, gamma, psi, q, np);
@@ -594,6 +634,7 @@ extern "C" int qpad_species_destroy(qpad_species* sp) {
   if (sp->qf) cudaFree(sp->qf);
   if (sp->qn) cudaFree(sp->qn);
   if (sp->pristine) cudaFree(sp->pristine);
+  mixed_free(sp);
   for (size_t i = 0; i < ctx->species.size(); ++i)
     if (ctx->species[i] == sp) { ctx->species.erase(ctx->species.begin() + i); break; }
   delete sp;
@@ -611,11 +652,15 @@ extern "C" int qpad_species_reset(qpad_species* sp) {
   if (!sp) return QPAD_E_ARG;
   qpad_ctx* ctx = sp->ctx;
   sp->np = sp->np_pristine;
-  double* dst[8] = {sp->x[0], sp->y[0], sp->px[0], sp->py[0], sp->pz[0], sp->gamma[0], sp->psi[0], sp->q[0]};
-  for (int a = 0; a < 8; ++a)
-    if (sp->np > 0 && cudaMemcpyAsync(dst[a], sp->pristine + (size_t)a * sp->npmax, sizeof(double) * sp->np,
-                                      cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
-      return check_launch(ctx, "reset copy");
+  if (is_mixed(sp)) {
+    if (int r = mixed_restore_pristine(sp)) return r;
+  } else {
+    double* dst[8] = {sp->x[0], sp->y[0], sp->px[0], sp->py[0], sp->pz[0], sp->gamma[0], sp->psi[0], sp->q[0]};
+    for (int a = 0; a < 8; ++a)
+      if (sp->np > 0 && cudaMemcpyAsync(dst[a], sp->pristine + (size_t)a * sp->npmax, sizeof(double) * sp->np,
+                                        cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+        return check_launch(ctx, "reset copy");
+  }
   *sp->h_count = sp->np;
   return cuda_check(ctx, cudaMemcpyAsync(sp->d_count, sp->h_count, sizeof(int64_t), cudaMemcpyHostToDevice,
                                          ctx->stream), "reset count");
@@ -633,6 +678,7 @@ extern "C" int qpad_species_download(qpad_species* sp, double* x, double* p, dou
   if (!sp) return QPAD_E_ARG;
   qpad_ctx* ctx = sp->ctx;
   if (int r = species_sync_count(sp)) return r;
+  if (int r = sync_fp64_view(sp)) return r;
   const int64_t n = sp->np;
   if (np) *np = n;
   double* staging = sp->x[1];
@@ -649,7 +695,7 @@ extern "C" int qpad_species_qdp(qpad_species* sp, int q) {
   qpad_ctx* ctx = sp->ctx;
   const size_t n1 = f1_elems(ctx, QPAD_F_Q_SPE);
   if (cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess) return check_launch(ctx, "memset");
-  if (int r = species_qdeposit_raw(sp, ctx->qraw)) return r;
+  if (int r = is_mixed(sp) ? mixed_qdeposit_raw(sp, ctx->qraw) : species_qdeposit_raw(sp, ctx->qraw)) return r;
   if (int r = launch_finish_q(ctx, ctx->qraw, sp->qf, 0)) return r;
   k_add2<<<elem_grid(n1), 256, 0, ctx->stream>>>(ctx->f[q], sp->qf, sp->neutralized ? sp->qn : nullptr, n1);
   return check_launch(ctx, "qdp add");
@@ -676,7 +722,12 @@ extern "C" int qpad_species_amjdp(qpad_species* sp, int ef, int bf, int cu, int 
   double* sacu = samu + n3;
   if (cudaMemsetAsync(scu, 0, (2 * n3 + n2) * sizeof(double), ctx->stream) != cudaSuccess)
     return check_launch(ctx, "memset");
-  if (int r = species_amjdp_raw(sp, ctx->f[ef], ctx->f[bf], scu, samu, sacu, dt)) return r;
+  if (is_mixed(sp)) {
+    if (int r = launch_gtab(ctx, ctx->f[ef], ctx->f[bf])) return r;
+    if (int r = mixed_amjdp_raw(sp, ctx->gtab, scu, samu, sacu, dt)) return r;
+  } else {
+    if (int r = species_amjdp_raw(sp, ctx->f[ef], ctx->f[bf], scu, samu, sacu, dt)) return r;
+  }
   if (int r = launch_finish_amj(ctx, scu, samu, sacu)) return r;
   k_add<<<elem_grid(n3), 256, 0, ctx->stream>>>(ctx->f[cu], scu, ctx->f[cu], n3);
   k_add<<<elem_grid(n3), 256, 0, ctx->stream>>>(ctx->f[amu], samu, ctx->f[amu], n3);
@@ -687,21 +738,29 @@ extern "C" int qpad_species_amjdp(qpad_species* sp, int ef, int bf, int cu, int 
 extern "C" int qpad_species_push_u(qpad_species* sp, int ef, int bf, double dt) {
   if (!sp || !valid_field(ef) || !valid_field(bf) || field_ncomp(ef) != 3 || field_ncomp(bf) != 3)
     return sp ? set_err(sp->ctx, QPAD_E_ARG, "push_u: bad args") : QPAD_E_ARG;
+  if (is_mixed(sp)) {
+    if (int r = launch_gtab(sp->ctx, sp->ctx->f[ef], sp->ctx->f[bf])) return r;
+    return mixed_push(sp, sp->ctx->gtab, dt, 1, 0);
+  }
   return species_push_u(sp, sp->ctx->f[ef], sp->ctx->f[bf], dt, 0);
 }
 
 extern "C" int qpad_species_push_x(qpad_species* sp, double dt) {
   if (!sp) return QPAD_E_ARG;
+  if (is_mixed(sp)) return mixed_push(sp, sp->ctx->gtab, dt, 0, 1);
   return species_push_x(sp, dt);
 }
 
 extern "C" int qpad_species_interp_psi(qpad_species* sp, int psi) {
   if (!sp || !valid_field(psi) || field_ncomp(psi) != 1) return sp ? set_err(sp->ctx, QPAD_E_ARG, "interp_psi") : QPAD_E_ARG;
+  if (is_mixed(sp)) return mixed_interp_psi(sp, sp->ctx->f[psi]);
   return species_interp_psi(sp, sp->ctx->f[psi]);
 }
 
 extern "C" int qpad_species_sort(qpad_species* sp) {
   if (!sp) return QPAD_E_ARG;
+  // the mixed path keeps its particles sorted by cell (order inside a cell not kept)
+  if (is_mixed(sp)) return mixed_sort_public(sp);
   return species_sort(sp);
 }
 
@@ -813,31 +872,156 @@ extern "C" int qpad_beam_push(qpad_beam* bm, int ef, int bf) {
 // =====================================================================================
 namespace {
 
+// ---- the three phases of one slice, shared by the host-driven and the graph drivers ----
+// Prologue (simulation_class.f03:344-364): charge deposit, beam B-perp, psi, Bz, record.
+int enqueue_slice_prologue(qpad_ctx* ctx, cudaGraphConditionalHandle hi, int use_h) {
+  const size_t n1 = f1_elems(ctx, QPAD_F_Q_SPE);
+  int any_ntd = 0;
+  for (auto* s : ctx->species) any_ntd |= s->neutralized;
+  const bool mixed = ctx->precision == QPAD_PREC_MIXED;
+  if (cudaMemsetAsync(ctx->d_iter, 0, sizeof(int), ctx->stream) != cudaSuccess ||
+      cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "slice prologue memsets", 0);
+  for (auto* s : ctx->species)
+    if (int r = mixed ? mixed_qdeposit_raw(s, ctx->qraw) : species_qdeposit_raw(s, ctx->qraw)) return r;
+  if (int r = launch_slice_begin(ctx, any_ntd)) return r;
+  for (auto* s : ctx->species)
+    if (s->push_type == QPAD_PUSH2_STD)
+      if (int r = mixed ? mixed_interp_psi(s, ctx->f[QPAD_F_PSI]) : species_interp_psi(s, ctx->f[QPAD_F_PSI]))
+        return r;
+  return launch_conv(ctx, ctx->f[QPAD_F_B_SPE], 1, 0, use_h, hi, use_h);
+}
+
+// One predictor-corrector iteration (simulation_class.f03:372-396).
+int enqueue_iteration(qpad_ctx* ctx, cudaGraphConditionalHandle h, int use_h) {
+  const bool mixed = ctx->precision == QPAD_PREC_MIXED;
+  if (int r = launch_iter_e(ctx)) return r;
+  for (auto* s : ctx->species) {
+    const int r = mixed ? mixed_amjdp_raw(s, ctx->gtab, ctx->f[QPAD_F_CU], ctx->f[QPAD_F_AMU], ctx->f[QPAD_F_ACU],
+                                          ctx->g.dxi)
+                        : species_amjdp_raw(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], ctx->f[QPAD_F_CU],
+                                            ctx->f[QPAD_F_AMU], ctx->f[QPAD_F_ACU], ctx->g.dxi);
+    if (r) return r;
+  }
+  if (int r = launch_iter_b(ctx)) return r;
+  return launch_conv(ctx, ctx->f[QPAD_F_B_SPE], 1, 1, 1, h, use_h);
+}
+
+// Epilogue (simulation_class.f03:403-456): stores, final fields, J-perp predictor, push.
+int enqueue_slice_epilogue(qpad_ctx* ctx, int sort_now) {
+  const bool mixed = ctx->precision == QPAD_PREC_MIXED;
+  if (int r = launch_slice_end(ctx)) return r;
+  for (auto* s : ctx->species) {
+    if (mixed) {
+      if (int r = mixed_push(s, ctx->gtab, ctx->g.dxi, 1, 1)) return r;   // sorts by cell every slice
+      continue;
+    }
+    if (int r = species_push_u(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], ctx->g.dxi, 1)) return r;
+    if (sort_now && s->sort_freq > 0)
+      if (int r = species_sort(s)) return r;
+  }
+  return 0;
+}
+
+// Graph of the whole slice loop: WHILE(j <= nz) { prologue; WHILE(not converged) { iteration }; epilogue; ++j }.
+// The iteration condition is set by the convergence kernel, the slice condition by k_advance.
+int build_step_graph(qpad_ctx* ctx) {
+  cudaGraph_t top = nullptr;
+  cudaGraphConditionalHandle hs = 0, hi = 0;
+  cudaGraphNode_t nslice = nullptr, niter = nullptr;
+  cudaGraph_t sbody = nullptr, ibody = nullptr;
+  const bool prof = ctx->prof_on;
+  ctx->prof_on = false;                          // event nodes are not allowed in conditional bodies
+  int r = cuda_check(ctx, cudaGraphCreate(&top, 0), "graph create");
+  if (!r) r = cuda_check(ctx, cudaGraphConditionalHandleCreate(&hs, top, 1, cudaGraphCondAssignDefault), "slice handle");
+  if (!r) {
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = hs;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    r = cuda_check(ctx, cudaGraphAddNode(&nslice, top, nullptr, nullptr, 0, &p), "slice while node");
+    if (!r) sbody = p.conditional.phGraph_out[0];
+  }
+  if (!r) r = cuda_check(ctx, cudaGraphConditionalHandleCreate(&hi, sbody, 1, cudaGraphCondAssignDefault), "iter handle");
+  if (!r) r = cuda_check(ctx, cudaStreamBeginCaptureToGraph(ctx->stream, sbody, nullptr, nullptr, 0,
+                                                            cudaStreamCaptureModeThreadLocal), "capture slice");
+  const int64_t l0 = ctx->launches;
+  int64_t l1 = l0, l2 = l0, l3 = l0;
+  if (!r) {
+    r = enqueue_slice_prologue(ctx, hi, 1);
+    l1 = ctx->launches;
+    if (!r) {
+      cudaStreamCaptureStatus cs;
+      cudaGraph_t cg = nullptr;
+      const cudaGraphNode_t* deps = nullptr;
+      size_t nd = 0;
+      r = cuda_check(ctx, cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &cg, &deps, nullptr, &nd), "capture info");
+      if (!r) {
+        cudaGraphNodeParams p = {};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = hi;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        r = cuda_check(ctx, cudaGraphAddNode(&niter, cg, deps, nullptr, nd, &p), "iteration while node");
+        if (!r) ibody = p.conditional.phGraph_out[0];
+        if (!r)
+          r = cuda_check(ctx, cudaStreamUpdateCaptureDependencies(ctx->stream, &niter, nullptr, 1,
+                                                                  cudaStreamSetCaptureDependencies), "capture deps");
+      }
+    }
+    if (!r) r = enqueue_slice_epilogue(ctx, 1);
+    if (!r) r = launch_advance(ctx, hs);
+    l2 = ctx->launches;
+    cudaGraph_t out = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &out);
+    if (!r) r = cuda_check(ctx, e, "end capture slice");
+  }
+  if (!r) r = cuda_check(ctx, cudaStreamBeginCaptureToGraph(ctx->stream, ibody, nullptr, nullptr, 0,
+                                                            cudaStreamCaptureModeThreadLocal), "capture iteration");
+  if (!r) {
+    const int64_t l2b = ctx->launches;
+    r = enqueue_iteration(ctx, hi, 1);
+    l3 = l2 + (ctx->launches - l2b);
+    cudaGraph_t out = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &out);
+    if (!r) r = cuda_check(ctx, e, "end capture iteration");
+  }
+  // captured launches are not executions: keep the per-phase counts, undo the increments
+  ctx->g_pro = l1 - l0;
+  ctx->g_epi = l2 - l1;
+  ctx->g_it = l3 - l2;
+  ctx->launches = l0;
+  cudaGraphExec_t exec = nullptr;
+  if (!r) r = cuda_check(ctx, cudaGraphInstantiate(&exec, top, 0), "graph instantiate");
+  if (top) cudaGraphDestroy(top);
+  ctx->prof_on = prof;
+  cudaGetLastError();
+  if (r) return r;
+  if (ctx->step_exec) cudaGraphExecDestroy(ctx->step_exec);
+  ctx->step_exec = exec;
+  return 0;
+}
+
+std::string step_key(const qpad_ctx* ctx) {
+  std::string k = std::to_string(ctx->precision);
+  for (auto* s : ctx->species)
+    k += "|" + std::to_string((long long)s->np) + ":" + std::to_string(s->push_type) + ":" +
+         std::to_string(s->neutralized) + ":" + std::to_string(s->sort_freq);
+  return k;
+}
+
 int slice_step(qpad_ctx* ctx, int j, qpad_slice_stats* st) {
   const GridDev& g = ctx->g;
-  const size_t n1 = f1_elems(ctx, QPAD_F_Q_SPE);
-  int any_ntd = 0, any_std = 0;
-  for (auto* s : ctx->species) { any_ntd |= s->neutralized; any_std |= (s->push_type == QPAD_PUSH2_STD); }
-  // q_spe = 0; spe%qdp(q_spe)  -> raw deposit, finished in k_slice_begin
-  if (cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess) return check_launch(ctx, "qraw");
-  for (auto* s : ctx->species)
-    if (int r = species_qdeposit_raw(s, ctx->qraw)) return r;
-  if (int r = launch_slice_begin(ctx, j, any_ntd)) return r;
-  if (any_std)
-    for (auto* s : ctx->species)
-      if (s->push_type == QPAD_PUSH2_STD)
-        if (int r = species_interp_psi(s, ctx->f[QPAD_F_PSI])) return r;
-  if (int r = launch_conv(ctx, ctx->f[QPAD_F_B_SPE], 1, 0)) return r;
+  // slice index lives on the device (the graph driver advances it there)
+  *ctx->h_j = j;
+  if (cudaMemcpyAsync(ctx->d_j, ctx->h_j, sizeof(int), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "slice index", 0);
+  if (int r = enqueue_slice_prologue(ctx, 0, 0)) return r;
   int l;
   double rel = 0.0, ab = 0.0;
   for (l = 1; l <= ctx->iter_max; ++l) {
-    if (int r = launch_iter_e(ctx)) return r;
-    for (auto* s : ctx->species)
-      if (int r = species_amjdp_raw(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], ctx->f[QPAD_F_CU], ctx->f[QPAD_F_AMU],
-                                    ctx->f[QPAD_F_ACU], g.dxi))
-        return r;
-    if (int r = launch_iter_b(ctx)) return r;
-    if (int r = launch_conv(ctx, ctx->f[QPAD_F_B_SPE], 1, 1)) return r;
+    if (int r = enqueue_iteration(ctx, 0, 0)) return r;
     if (int r = d2h(ctx, ctx->h_res, ctx->conv + 2 * g.nr, 3)) return r;
     if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "iteration sync")) return r;
     if (ctx->prof_on) prof_collect(ctx);
@@ -850,13 +1034,9 @@ int slice_step(qpad_ctx* ctx, int j, qpad_slice_stats* st) {
     st->rel_res = rel;
     st->abs_res = ab;
   }
-  if (int r = launch_slice_end(ctx, j)) return r;
-  for (auto* s : ctx->species) {
-    if (int r = species_push_u(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], g.dxi, 1)) return r;
-    if (s->sort_freq > 0 && (j % s->sort_freq) == 0)
-      if (int r = species_sort(s)) return r;
-  }
-  return 0;
+  int sort_now = 0;
+  for (auto* s : ctx->species) sort_now |= (s->sort_freq > 0 && (j % s->sort_freq) == 0);
+  return enqueue_slice_epilogue(ctx, sort_now);
 }
 
 }  // namespace
@@ -881,8 +1061,43 @@ extern "C" int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* sta
   for (int f : zero_fields)
     if (cudaMemsetAsync(ctx->f[f], 0, f1_elems(ctx, f) * sizeof(double), ctx->stream) != cudaSuccess)
       return check_launch(ctx, "zero fields");
-  for (int j = 1; j <= ctx->g.nz; ++j)
-    if (int r = slice_step(ctx, j, stats ? stats + (j - 1) : nullptr)) return r;
+  // the slice loop runs as one CUDA graph when the configuration allows it (sorting every
+  // few slices is host-driven); otherwise the host drives it slice by slice
+  bool use_graph = ctx->use_graph;
+  for (auto* s : ctx->species) use_graph &= (s->sort_freq == 0);
+  if (use_graph) {
+    const std::string key = step_key(ctx);
+    if (!ctx->step_exec || ctx->step_key != key) {
+      if (int r = build_step_graph(ctx)) {
+        ctx->graph_status = "graph build failed: " + ctx->err;
+        ctx->use_graph = false;
+        use_graph = false;
+        cudaGetLastError();
+      } else {
+        ctx->step_key = key;
+      }
+    }
+  }
+  if (use_graph) {
+    *ctx->h_j = 1;
+    if (cudaMemcpyAsync(ctx->d_j, ctx->h_j, sizeof(int), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+      return check_launch(ctx, "slice index", 0);
+    if (int r = cuda_check(ctx, cudaGraphLaunch(ctx->step_exec, ctx->stream), "graph launch")) return r;
+    ctx->h_stats.resize(ctx->g.nz);
+    if (int r = cuda_check(ctx, cudaMemcpyAsync(ctx->h_stats.data(), ctx->d_stats,
+                                                sizeof(qpad_slice_stats) * ctx->g.nz, cudaMemcpyDeviceToHost,
+                                                ctx->stream), "stats"))
+      return r;
+    if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "graph step")) return r;
+    // kernels the graph ran: per slice the prologue and epilogue, per iteration the body
+    int64_t iters = 0;
+    for (const auto& s : ctx->h_stats) iters += s.iters;
+    ctx->launches += (int64_t)ctx->g.nz * (ctx->g_pro + ctx->g_epi) + iters * ctx->g_it;
+    if (stats) std::copy(ctx->h_stats.begin(), ctx->h_stats.end(), stats);
+  } else {
+    for (int j = 1; j <= ctx->g.nz; ++j)
+      if (int r = slice_step(ctx, j, stats ? stats + (j - 1) : nullptr)) return r;
+  }
   if (push_beams)
     for (auto* b : ctx->beams)
       if (int r = beam_push(b, ctx->f2[QPAD_F_E], ctx->f2[QPAD_F_B])) return r;

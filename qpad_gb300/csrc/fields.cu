@@ -750,6 +750,22 @@ __device__ void op_finish_amj(const GridDev& G, int m, double* __restrict__ cu, 
   __syncthreads();
 }
 
+// FP32 gather table of the mixed-precision particle path: T[(node*P + part)*6 + c],
+// c = 0..2 the E components, 3..5 the B components, nodes 0..nr+1.
+__device__ void op_write_gtab(const GridDev& G, int m, const double* __restrict__ e, const double* __restrict__ b,
+                              float* __restrict__ T) {
+  const int np_ = m == 0 ? 1 : 2;
+  for (int h = 0; h < np_; ++h) {
+    const int p = h == 0 ? part_re(m) : part_im(m);
+    for (int k = threadIdx.x; k < 6 * G.ld; k += blockDim.x) {
+      const int i = k / 6, c = k % 6;
+      const double v = c < 3 ? FLD(e, 3, p, c, i) : FLD(b, 3, p, c - 3, i);
+      T[((size_t)i * G.P + p) * 6 + c] = (float)v;
+    }
+  }
+  __syncthreads();
+}
+
 // c = a + b over all components and nodes of mode m (add_f1_binary)
 __device__ void op_add(const GridDev& G, int m, int nc, const double* a, const double* b, double* c) {
   const int np_ = m == 0 ? 1 : 2;
@@ -808,6 +824,7 @@ struct SliceFields {
   double* f2[QPAD_NFIELDS];
   const double* qraw;
   const double* qn;
+  float* gtab;   // FP32 gather table, written when the mixed path is active
 };
 
 static SliceFields slice_fields(qpad_ctx* ctx) {
@@ -815,7 +832,17 @@ static SliceFields slice_fields(qpad_ctx* ctx) {
   for (int k = 0; k < QPAD_NFIELDS; ++k) { s.f[k] = ctx->f[k]; s.f2[k] = ctx->f2[k]; }
   s.qraw = ctx->qraw;
   s.qn = ctx->qn;
+  s.gtab = ctx->precision == QPAD_PREC_MIXED ? ctx->gtab : nullptr;
   return s;
+}
+
+__global__ void __launch_bounds__(kFieldThreads) k_gtab(GridDev G, const double* e, const double* b, float* T) {
+  op_write_gtab(G, blockIdx.x, e, b, T);
+}
+
+int launch_gtab(qpad_ctx* ctx, const double* e, const double* b) {
+  k_gtab<<<ctx->g.M + 1, kFieldThreads, 0, ctx->stream>>>(ctx->g, e, b, ctx->gtab);
+  return check_launch(ctx, "k_gtab");
 }
 
 __device__ __forceinline__ double* store_slice(const GridDev& G, double* f2, int nc, int j) {
@@ -825,9 +852,11 @@ __device__ __forceinline__ double* store_slice(const GridDev& G, double* f2, int
 // Start of slice j (simulation_class.f03:344-360): beam B-perp from the stored beam
 // charge; species charge (+ background) and psi; Bz from the carried current.
 __global__ void __launch_bounds__(kFieldThreads) k_slice_begin(GridDev G, const double* __restrict__ fac,
-                                                               SliceFields F, int j, int use_qn) {
+                                                               SliceFields F, const int* __restrict__ jp,
+                                                               int use_qn) {
   extern __shared__ double sm[];
   __shared__ double sc[6 * 32 + 8];
+  const int j = *jp;
   const int job = blockIdx.x / (G.M + 1), m = blockIdx.x % (G.M + 1);
   if (job == 0) {
     const double* qs = store_slice(G, F.f2[QPAD_F_Q_BEAM], 1, j);
@@ -850,6 +879,7 @@ __global__ void __launch_bounds__(kFieldThreads) k_iter_e(GridDev G, const doubl
   op_add(G, m, 3, F.f[QPAD_F_B_SPE], F.f[QPAD_F_B_BEAM], F.f[QPAD_F_B]);
   op_ez(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_E]);
   op_et(G, m, F.f[QPAD_F_B], F.f[QPAD_F_PSI], F.f[QPAD_F_E]);
+  if (F.gtab) op_write_gtab(G, m, F.f[QPAD_F_E], F.f[QPAD_F_B], F.gtab);
   op_fill(G, m, 3, F.f[QPAD_F_CU], 0.0);
   op_fill(G, m, 2, F.f[QPAD_F_ACU], 0.0);
   op_fill(G, m, 3, F.f[QPAD_F_AMU], 0.0);
@@ -870,9 +900,10 @@ __global__ void __launch_bounds__(kFieldThreads) k_iter_b(GridDev G, const doubl
 // End of slice j (simulation_class.f03:403-456 without the particle push): cbq and the
 // stores of cu and rho, total and species fields, the J-perp predictor for slice j+1.
 __global__ void __launch_bounds__(kFieldThreads) k_slice_end(GridDev G, const double* __restrict__ fac,
-                                                             SliceFields F, int j) {
+                                                             SliceFields F, const int* __restrict__ jp) {
   extern __shared__ double sm[];
   __shared__ double sc[6 * 32 + 8];
+  const int j = *jp;
   const int m = blockIdx.x;
   const int npart = m == 0 ? 1 : 2;
   double* cu = F.f[QPAD_F_CU];
@@ -901,6 +932,7 @@ __global__ void __launch_bounds__(kFieldThreads) k_slice_end(GridDev G, const do
       }
   }
   __syncthreads();
+  if (F.gtab) op_write_gtab(G, m, F.f[QPAD_F_E], F.f[QPAD_F_B], F.gtab);
   op_copy(G, m, 3, F.f[QPAD_F_E], store_slice(G, F.f2[QPAD_F_E], 3, j));
   op_copy(G, m, 3, F.f[QPAD_F_B], store_slice(G, F.f2[QPAD_F_B], 3, j));
   op_copy(G, m, 1, F.f[QPAD_F_PSI], store_slice(G, F.f2[QPAD_F_PSI], 1, j));
@@ -919,9 +951,21 @@ __global__ void __launch_bounds__(kFieldThreads) k_finish_amj(GridDev G, double*
 
 // convergence_tester (simulation_class.f03:522-606) on component `comp` of b:
 // op 0 records s_re/s_im; op 1 compares against the record, writes rel/abs/converged
-// into res and records the new sums for the next iteration.
+// into res and records the new sums for the next iteration.  With a loop state, op 1 also
+// counts the iteration, stores the slice's statistics and, inside a CUDA graph, sets the
+// condition of the predictor-corrector WHILE node (continue while not converged and
+// below iter_max, simulation_class.f03:370-398).
+struct ConvLoop {
+  int* iter_ctr;                 // iterations taken in the current slice
+  qpad_slice_stats* stats;       // per-slice statistics [nz]
+  const int* jp;                 // current slice (1-based)
+  int iter_max;
+  cudaGraphConditionalHandle h;  // WHILE-node handle
+  int use_h;
+};
+
 __global__ void __launch_bounds__(1024) k_conv(GridDev G, const double* __restrict__ b, int comp, int op,
-                                               double* __restrict__ st, double reltol, double abstol) {
+                                               double* __restrict__ st, double reltol, double abstol, ConvLoop L) {
   __shared__ double red[33];
   const int nr = G.nr, M = G.M;
   double* s_re = st;
@@ -948,7 +992,12 @@ __global__ void __launch_bounds__(1024) k_conv(GridDev G, const double* __restri
     s_re[i - 1] = nre;
     s_im[i - 1] = nim;
   }
-  if (op == 0) return;
+  if (op == 0) {
+    // 'record' opens the iteration loop of a new slice: re-arm its WHILE condition (a
+    // nested conditional keeps its last value between entries within one graph launch)
+    if (L.use_h && threadIdx.x == 0) cudaGraphSetConditional(L.h, 1u);
+    return;
+  }
   // max-reductions (order independent, exact)
   for (int off = 16; off > 0; off >>= 1) {
     mx_old = fmax(mx_old, __shfl_down_sync(FULLMASK, mx_old, off));
@@ -963,10 +1012,30 @@ __global__ void __launch_bounds__(1024) k_conv(GridDev G, const double* __restri
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a = fmax(a, red[w]); c = fmax(c, red2[w]); }
     const double old_norm = sqrt(a), abs_res = sqrt(c);
     const double rel = old_norm > 2.220446049250313e-16 ? abs_res / old_norm : 1.7976931348623157e308;
+    const bool converged = rel < reltol || abs_res < abstol;
     res[0] = rel;
     res[1] = abs_res;
-    res[2] = (rel < reltol || abs_res < abstol) ? 1.0 : 0.0;
+    res[2] = converged ? 1.0 : 0.0;
+    if (L.iter_ctr) {
+      const int it = *L.iter_ctr + 1;
+      *L.iter_ctr = it;
+      if (L.stats && L.jp) {
+        qpad_slice_stats s;
+        s.iters = it;
+        s.rel_res = rel;
+        s.abs_res = abs_res;
+        L.stats[*L.jp - 1] = s;
+      }
+      if (L.use_h) cudaGraphSetConditional(L.h, (!converged && it < L.iter_max) ? 1u : 0u);
+    }
   }
+}
+
+// Advances the slice counter and sets the condition of the slice WHILE node.
+__global__ void k_advance(int* __restrict__ jp, int nz, cudaGraphConditionalHandle h) {
+  const int j = *jp + 1;
+  *jp = j;
+  cudaGraphSetConditional(h, j <= nz ? 1u : 0u);
 }
 
 // ------------------------------------------------------------------------------------
@@ -993,15 +1062,30 @@ int launch_field_op(qpad_ctx* ctx, int op, FieldArgs a) {
   return check_launch(ctx, "k_field_op");
 }
 
-int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op) {
-  k_conv<<<1, 1024, 0, ctx->stream>>>(ctx->g, b, comp, op, ctx->conv, ctx->reltol, ctx->abstol);
+int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op, int loop_state, cudaGraphConditionalHandle h,
+                int use_h) {
+  ConvLoop L{};
+  if (loop_state) {
+    L.iter_ctr = ctx->d_iter;
+    L.stats = ctx->d_stats;
+    L.jp = ctx->d_j;
+    L.iter_max = ctx->iter_max;
+    L.h = h;
+    L.use_h = use_h;
+  }
+  k_conv<<<1, 1024, 0, ctx->stream>>>(ctx->g, b, comp, op, ctx->conv, ctx->reltol, ctx->abstol, L);
   return check_launch(ctx, "k_conv");
 }
 
-int launch_slice_begin(qpad_ctx* ctx, int j, int use_qn) {
+int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle h) {
+  k_advance<<<1, 1, 0, ctx->stream>>>(ctx->d_j, ctx->g.nz, h);
+  return check_launch(ctx, "k_advance");
+}
+
+int launch_slice_begin(qpad_ctx* ctx, int use_qn) {
   if (int r = ensure_smem_attr(ctx)) return r;
   k_slice_begin<<<3 * (ctx->g.M + 1), kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac,
-                                                                                     slice_fields(ctx), j, use_qn);
+                                                                                     slice_fields(ctx), ctx->d_j, use_qn);
   return check_launch(ctx, "k_slice_begin");
 }
 
@@ -1017,9 +1101,10 @@ int launch_iter_b(qpad_ctx* ctx) {
   return check_launch(ctx, "k_iter_b");
 }
 
-int launch_slice_end(qpad_ctx* ctx, int j) {
+int launch_slice_end(qpad_ctx* ctx) {
   if (int r = ensure_smem_attr(ctx)) return r;
-  k_slice_end<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac, slice_fields(ctx), j);
+  k_slice_end<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac, slice_fields(ctx),
+                                                                              ctx->d_j);
   return check_launch(ctx, "k_slice_end");
 }
 

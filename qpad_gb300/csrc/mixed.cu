@@ -1,0 +1,708 @@
+// mixed.cu -- mixed-precision plasma particle path (QPAD_PREC_MIXED).
+//
+// Particles: each Cartesian coordinate is an integer cell plus an FP32 offset in [0,1)
+// (x = (cell + offset) * dr), so positions do not lose precision as they are advanced
+// slice after slice; momenta, charge, gamma and psi are FP32.  The particles are kept
+// sorted by radial cell (counting sort after every push).
+//
+// Gather: E and B are read from an FP32 table [node][part][E0,E1,E2,B0,B1,B2] written by
+// the field kernels after every FP64 solve, so one particle reads two contiguous records.
+//
+// Deposit: each CTA takes a chunk of consecutive (sorted) particles, whose cells span a
+// narrow radial window.  Contributions are reduced across the warp when all 32 lanes sit
+// in the same cell (the common case for sorted particles), accumulated in an FP32
+// shared-memory tile of that window, and the tile is folded into the FP64 global mode
+// arrays with one atomic per entry.  Windows wider than the tile fall back to direct FP64
+// atomics.  The field solves that follow stay FP64.
+//
+// Reference routines: part2d::qdeposit (part2d_class.f03:231-359), amjdeposit_robust /
+// _std (:746-1010, 478-744), push_u_robust / _std (:1879-1965, 1790-1877), push_x
+// (:2221-2262), update_bound (:2307-2353), sort (:2498-2579), interp_psi (:2264-2305).
+#include <algorithm>
+
+#include "particles.cuh"
+
+namespace qpad {
+
+static constexpr int kMixThreads = 256;
+static constexpr int kMixRounds = 2;
+static constexpr int kChunk = kMixThreads * kMixRounds;   // particles per CTA in the deposits
+static constexpr int kTileNodes = 64;                     // radial window of the FP32 tile
+#define FULL 0xffffffffu
+
+struct MArr {
+  int32_t* cxy;
+  float *fx, *fy, *px, *py, *pz, *q, *gam, *psi;
+  int32_t* key;
+};
+
+static MArr marr(qpad_species* sp, int b) {
+  return MArr{sp->cxy[b], sp->fx[b], sp->fy[b], sp->mpx[b], sp->mpy[b], sp->mpz[b],
+              sp->mq[b],  sp->mgam[b], sp->mpsi[b], sp->mkey[b]};
+}
+
+static int mgrid(int64_t n, int per) {
+  int64_t b = (n + per - 1) / per;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 1 << 30));
+}
+
+__device__ __forceinline__ void unpack_cell(int32_t c, int& ix, int& iy) {
+  ix = (int)(int16_t)(uint16_t)((uint32_t)c & 0xffffu);
+  iy = (int)(int16_t)(uint16_t)((uint32_t)c >> 16);
+}
+
+__device__ __forceinline__ int32_t pack_cell(int ix, int iy) {
+  return (int32_t)(((uint32_t)(uint16_t)(int16_t)ix) | ((uint32_t)(uint16_t)(int16_t)iy << 16));
+}
+
+// Radial interpolation data in cell units (FP32).
+struct MInterp {
+  float w0, w1, pcos, psin;
+  int idx;
+  bool ok;
+};
+
+__device__ __forceinline__ MInterp minterp(int32_t c, float fx, float fy, int nr) {
+  int ix, iy;
+  unpack_cell(c, ix, iy);
+  const float X = (float)ix + fx, Y = (float)iy + fy;
+  const float r = sqrtf(X * X + Y * Y);
+  MInterp m;
+  m.pcos = X / r;
+  m.psin = Y / r;
+  m.ok = r >= 0.0f && r < (float)nr;
+  const int ip = m.ok ? (int)r : 0;
+  m.idx = ip + 1;
+  m.w1 = m.ok ? r - (float)ip : 0.0f;
+  m.w0 = m.ok ? 1.0f - m.w1 : 0.0f;
+  return m;
+}
+
+// E and B gathered from the FP32 table (interp_field, interp_part2d.f03:67-109)
+__device__ __forceinline__ void mgather(const float* __restrict__ T, int P, int M, const MInterp& ii, float ep[3],
+                                        float bp[3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { ep[c] = 0.0f; bp[c] = 0.0f; }
+  if (!ii.ok) return;
+  const float* t0 = T + (size_t)ii.idx * P * 6;
+  const float* t1 = t0 + (size_t)P * 6;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    ep[c] = __ldg(t0 + c) * ii.w0 + __ldg(t1 + c) * ii.w1;
+    bp[c] = __ldg(t0 + 3 + c) * ii.w0 + __ldg(t1 + 3 + c) * ii.w1;
+  }
+  float phr = 1.0f, phi = 0.0f;
+  for (int m = 1; m <= M; ++m) {
+    const float t = phr * ii.pcos - phi * ii.psin;
+    phi = phr * ii.psin + phi * ii.pcos;
+    phr = t;
+    const float pre = 2.0f * phr, pim = 2.0f * phi;
+    const float* r0 = t0 + (2 * m - 1) * 6;
+    const float* i0 = t0 + (2 * m) * 6;
+    const float* r1 = t1 + (2 * m - 1) * 6;
+    const float* i1 = t1 + (2 * m) * 6;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      ep[c] += (__ldg(r0 + c) * pre - __ldg(i0 + c) * pim) * ii.w0 + (__ldg(r1 + c) * pre - __ldg(i1 + c) * pim) * ii.w1;
+      bp[c] += (__ldg(r0 + 3 + c) * pre - __ldg(i0 + 3 + c) * pim) * ii.w0 +
+               (__ldg(r1 + 3 + c) * pre - __ldg(i1 + 3 + c) * pim) * ii.w1;
+    }
+  }
+}
+
+// Adds NV values of this lane into tile[base .. base+NV) -- one reduced atomic per value
+// when the whole warp shares the destination, else one atomic per lane.
+template <int NV>
+__device__ __forceinline__ void warp_tile_add(float* tile, int base, const float (&v)[NV], bool full, bool valid,
+                                              int lane) {
+  if (full) {
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+      float s = v[c];
+      s += __shfl_xor_sync(FULL, s, 16);
+      s += __shfl_xor_sync(FULL, s, 8);
+      s += __shfl_xor_sync(FULL, s, 4);
+      s += __shfl_xor_sync(FULL, s, 2);
+      s += __shfl_xor_sync(FULL, s, 1);
+      if (lane == 0) atomicAdd(tile + base + c, s);
+    }
+  } else if (valid) {
+#pragma unroll
+    for (int c = 0; c < NV; ++c) atomicAdd(tile + base + c, v[c]);
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// charge deposit (ρ - Jz): tile entries [node][part]
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMixThreads) k_mqdeposit(GridDev G, const int64_t* __restrict__ n_ptr, MArr A,
+                                                           double* __restrict__ qraw) {
+  __shared__ float tile[kTileNodes * QPAD_MAX_PARTS];
+  const int64_t n = *n_ptr;
+  const int64_t c0 = (int64_t)blockIdx.x * kChunk;
+  if (c0 >= n) return;
+  const int64_t c1 = min(c0 + kChunk, n);
+  const int k0 = A.key[c0], k1 = A.key[c1 - 1];
+  const int W = k1 - k0 + 2;
+  const bool use_tile = W <= kTileNodes && k0 >= 1;
+  const int P = G.P, ld = G.ld;
+  if (use_tile)
+    for (int k = threadIdx.x; k < W * P; k += blockDim.x) tile[k] = 0.0f;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = 0; r < kMixRounds; ++r) {
+    const int64_t i = c0 + (int64_t)warp * 32 * kMixRounds + r * 32 + lane;
+    const bool valid = i < c1;
+    MInterp ii;
+    float q = 0.0f;
+    if (valid) {
+      ii = minterp(A.cxy[i], A.fx[i], A.fy[i], G.nr);
+      q = A.q[i];
+    } else {
+      ii.ok = false; ii.idx = 1; ii.w0 = ii.w1 = 0.0f; ii.pcos = 1.0f; ii.psin = 0.0f;
+    }
+    const bool live = valid && ii.ok;
+    const unsigned grp = __match_any_sync(FULL, live ? ii.idx : -1 - lane);
+    const bool inwin = use_tile && ii.idx >= k0 && ii.idx <= k1;
+    const bool full = grp == FULL && inwin;                      // warp-uniform
+    const bool tile_lane = full || (inwin && live);
+    const float wj[2] = {ii.w0, ii.w1};
+    if (tile_lane) {
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const float v[1] = {wj[j] * q};
+        warp_tile_add<1>(tile, (ii.idx + j - k0) * P, v, full, live, lane);
+      }
+    } else if (live) {
+#pragma unroll
+      for (int j = 0; j < 2; ++j) atomicAdd(qraw + ii.idx + j, (double)(wj[j] * q));
+    }
+    float phr = q, phi = 0.0f;
+    const float ph0r = ii.pcos, ph0i = -ii.psin;
+    for (int m = 1; m <= G.M; ++m) {
+      const float t = phr * ph0r - phi * ph0i;
+      phi = phr * ph0i + phi * ph0r;
+      phr = t;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        if (tile_lane) {
+          const int base = (ii.idx + j - k0) * P + 2 * m - 1;
+          const float v[2] = {wj[j] * phr, wj[j] * phi};
+          warp_tile_add<2>(tile, base, v, full, live, lane);
+        } else if (live) {
+          atomicAdd(qraw + (size_t)(2 * m - 1) * ld + ii.idx + j, (double)(wj[j] * phr));
+          atomicAdd(qraw + (size_t)(2 * m) * ld + ii.idx + j, (double)(wj[j] * phi));
+        }
+      }
+    }
+  }
+  if (!use_tile) return;
+  __syncthreads();
+  for (int k = threadIdx.x; k < W * P; k += blockDim.x) {
+    const float v = tile[k];
+    if (v != 0.0f) {
+      const int nl = k / P, p = k % P;
+      atomicAdd(qraw + (size_t)p * ld + k0 + nl, (double)v);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// current / acceleration / momentum-flux deposit with the predictor push
+// tile entries [node][part][8]: cu 0..2, acu 3..4, amu 5..7
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMixThreads) k_mamjdp(GridDev G, int push_type, float qbm, float dt,
+                                                        const int64_t* __restrict__ n_ptr, MArr A,
+                                                        const float* __restrict__ T, double* __restrict__ cu,
+                                                        double* __restrict__ amu, double* __restrict__ acu,
+                                                        int write_back) {
+  __shared__ float tile[kTileNodes * QPAD_MAX_PARTS * 8];
+  const int64_t n = *n_ptr;
+  const int64_t c0 = (int64_t)blockIdx.x * kChunk;
+  if (c0 >= n) return;
+  const int64_t c1 = min(c0 + kChunk, n);
+  const int k0 = A.key[c0], k1 = A.key[c1 - 1];
+  const int W = k1 - k0 + 2;
+  const bool use_tile = W <= kTileNodes && k0 >= 1;
+  const int P = G.P, ld = G.ld, M = G.M;
+  if (use_tile)
+    for (int k = threadIdx.x; k < W * P * 8; k += blockDim.x) tile[k] = 0.0f;
+  __syncthreads();
+  const float idt = 1.0f / dt, qtmh = 0.5f * qbm * dt;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = 0; r < kMixRounds; ++r) {
+    const int64_t i = c0 + (int64_t)warp * 32 * kMixRounds + r * 32 + lane;
+    const bool valid = i < c1;
+    float v[8];
+    MInterp ii;
+    float qq = 0.0f;
+    if (valid) {
+      ii = minterp(A.cxy[i], A.fx[i], A.fy[i], G.nr);
+      float ep[3], bp[3], wp[3], u0[3], u[3], ut[3];
+      mgather(T, P, M, ii, ep, bp);
+      wp[0] = ep[0] - bp[1];
+      wp[1] = ep[1] + bp[0];
+      wp[2] = ep[2];
+      const float p1 = A.px[i], p2 = A.py[i];
+      u0[0] = p1 * ii.pcos + p2 * ii.psin;
+      u0[1] = p2 * ii.pcos - p1 * ii.psin;
+      u0[2] = A.pz[i];
+      const float psi_in = A.psi[i];
+      if (push_type == QPAD_PUSH2_ROBUST) {
+        float gam = sqrtf(1.0f + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
+        const float qtmh1 = qtmh * gam / (gam - u0[2]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { ep[c] *= qtmh1; ut[c] = u0[c] + ep[c]; }
+        gam = sqrtf(1.0f + ut[0] * ut[0] + ut[1] * ut[1] + ut[2] * ut[2]);
+        const float qtmh2 = qtmh / (gam - ut[2]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) bp[c] *= qtmh2;
+      } else {
+        const float gam = sqrtf(1.0f + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
+        const float qtmh2 = qtmh / (1.0f - qbm * psi_in);
+        const float qtmh1 = qtmh2 * gam;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { bp[c] *= qtmh2; ut[c] = u0[c] + ep[c] * qtmh1; }
+      }
+      u[0] = ut[0] + ut[1] * bp[2] - ut[2] * bp[1];
+      u[1] = ut[1] + ut[2] * bp[0] - ut[0] * bp[2];
+      u[2] = ut[2] + ut[0] * bp[1] - ut[1] * bp[0];
+      const float ostq = 2.0f / (1.0f + bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) bp[c] *= ostq;
+      {
+        const float t0 = ut[0] + u[1] * bp[2] - u[2] * bp[1];
+        const float t1 = ut[1] + u[2] * bp[0] - u[0] * bp[2];
+        const float t2 = ut[2] + u[0] * bp[1] - u[1] * bp[0];
+        ut[0] = t0; ut[1] = t1; ut[2] = t2;
+      }
+      if (push_type == QPAD_PUSH2_ROBUST) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) u[c] = ut[c] + ep[c];
+      } else {
+        const float gam = sqrtf(1.0f + ut[0] * ut[0] + ut[1] * ut[1] + ut[2] * ut[2]);
+        const float qtmh1 = qtmh / (1.0f - qbm * psi_in) * gam;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) u[c] = ut[c] + ep[c] * qtmh1;
+      }
+      float du0 = idt * (u[0] - u0[0]);
+      float du1 = idt * (u[1] - u0[1]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) u[c] = 0.5f * (u[c] + u0[c]);
+      const float g = sqrtf(1.0f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+      float ipsi;
+      if (push_type == QPAD_PUSH2_ROBUST) {
+        ipsi = 1.0f / (g - u[2]);
+        if (write_back) { A.gam[i] = g; A.psi[i] = (1.0f - 1.0f / ipsi) / qbm; }
+      } else {
+        ipsi = 1.0f / (1.0f - qbm * psi_in);
+        A.gam[i] = g;
+      }
+      const float dpsi = qbm * (wp[2] - (wp[0] * u[0] + wp[1] * u[1]) * ipsi);
+      du0 += u[0] * dpsi * ipsi;
+      du1 += u[1] * dpsi * ipsi;
+      v[0] = u[0]; v[1] = u[1]; v[2] = u[2]; v[3] = du0; v[4] = du1;
+      v[5] = u[0] * u[0] * ipsi; v[6] = u[0] * u[1] * ipsi; v[7] = u[1] * u[1] * ipsi;
+      qq = A.q[i] * ipsi;
+    } else {
+      ii.ok = false; ii.idx = 1; ii.w0 = ii.w1 = 0.0f; ii.pcos = 1.0f; ii.psin = 0.0f;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) v[c] = 0.0f;
+    }
+    const bool live = valid && ii.ok;
+    const unsigned grp = __match_any_sync(FULL, live ? ii.idx : -1 - lane);
+    const bool inwin = use_tile && ii.idx >= k0 && ii.idx <= k1;
+    const bool full = grp == FULL && inwin;                      // warp-uniform
+    const bool tile_lane = full || (inwin && live);
+    const float wj[2] = {ii.w0, ii.w1};
+    float phr = qq, phi = 0.0f;
+    const float ph0r = ii.pcos, ph0i = -ii.psin;
+    for (int m = 0; m <= M; ++m) {
+      if (m > 0) {
+        const float t = phr * ph0r - phi * ph0i;
+        phi = phr * ph0i + phi * ph0r;
+        phr = t;
+      }
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int node = ii.idx + j;
+        const int ph = m == 0 ? 1 : 2;
+        for (int h = 0; h < ph; ++h) {
+          const int p = m == 0 ? 0 : 2 * m - 1 + h;
+          const float w = wj[j] * (h == 0 ? phr : phi);
+          float vv[8];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) vv[c] = w * v[c];
+          if (tile_lane) {
+            warp_tile_add<8>(tile, ((node - k0) * P + p) * 8, vv, full, live, lane);
+          } else if (live) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) atomicAdd(cu + ((size_t)p * 3 + c) * ld + node, (double)vv[c]);
+#pragma unroll
+            for (int c = 0; c < 2; ++c) atomicAdd(acu + ((size_t)p * 2 + c) * ld + node, (double)vv[3 + c]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) atomicAdd(amu + ((size_t)p * 3 + c) * ld + node, (double)vv[5 + c]);
+          }
+        }
+      }
+    }
+  }
+  if (!use_tile) return;
+  __syncthreads();
+  for (int k = threadIdx.x; k < W * P * 8; k += blockDim.x) {
+    const float val = tile[k];
+    if (val == 0.0f) continue;
+    const int c = k & 7, pnode = k >> 3;
+    const int nl = pnode / P, p = pnode % P, node = k0 + nl;
+    double* dst = c < 3 ? cu + ((size_t)p * 3 + c) * ld : (c < 5 ? acu + ((size_t)p * 2 + (c - 3)) * ld
+                                                                 : amu + ((size_t)p * 3 + (c - 5)) * ld);
+    atomicAdd(dst + node, (double)val);
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// push_u + push_x + edge test + new cell key
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMixThreads) k_mpush(GridDev G, int push_type, float qbm, float dt,
+                                                       const int64_t* __restrict__ n_ptr, MArr A,
+                                                       const float* __restrict__ T, int do_u, int do_x) {
+  const int64_t n = *n_ptr;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float qtmh = qbm * dt * 0.5f;
+  int ix, iy;
+  unpack_cell(A.cxy[i], ix, iy);
+  float fx = A.fx[i], fy = A.fy[i];
+  float p[3] = {A.px[i], A.py[i], A.pz[i]};
+  float g = A.gam[i];
+  if (do_u) {
+  const MInterp ii = minterp(A.cxy[i], fx, fy, G.nr);
+  float ep[3], bp[3], ut[3];
+  mgather(T, G.P, G.M, ii, ep, bp);
+  float t = ep[0] * ii.pcos - ep[1] * ii.psin;
+  ep[1] = ep[0] * ii.psin + ep[1] * ii.pcos;
+  ep[0] = t;
+  t = bp[0] * ii.pcos - bp[1] * ii.psin;
+  bp[1] = bp[0] * ii.psin + bp[1] * ii.pcos;
+  bp[0] = t;
+  float qtmh1, qtmh2;
+  if (push_type == QPAD_PUSH2_ROBUST) {
+    const float gam = sqrtf(1.0f + p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    qtmh1 = qtmh / (gam - p[2]);
+    qtmh2 = qtmh1 * gam;
+  } else {
+    qtmh1 = qtmh / (1.0f - qbm * A.psi[i]);
+    qtmh2 = qtmh1 * g;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { ep[c] *= qtmh2; bp[c] *= qtmh1; ut[c] = p[c] + ep[c]; }
+  p[0] = ut[0] + ut[1] * bp[2] - ut[2] * bp[1];
+  p[1] = ut[1] + ut[2] * bp[0] - ut[0] * bp[2];
+  p[2] = ut[2] + ut[0] * bp[1] - ut[1] * bp[0];
+  const float ostq = 2.0f / (1.0f + bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) bp[c] *= ostq;
+  {
+    const float t0 = ut[0] + p[1] * bp[2] - p[2] * bp[1];
+    const float t1 = ut[1] + p[2] * bp[0] - p[0] * bp[2];
+    const float t2 = ut[2] + p[0] * bp[1] - p[1] * bp[0];
+    p[0] = t0 + ep[0]; p[1] = t1 + ep[1]; p[2] = t2 + ep[2];
+  }
+  g = sqrtf(1.0f + p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+  A.px[i] = p[0]; A.py[i] = p[1]; A.pz[i] = p[2];
+  A.gam[i] = g;
+  }
+  if (!do_x) return;
+  // x += p dt / (gamma - pz), in cell units, renormalising the offset into [0,1)
+  const float dtc = dt / (g - p[2]) * (float)G.idr;
+  fx += p[0] * dtc;
+  fy += p[1] * dtc;
+  const float sx = floorf(fx), sy = floorf(fy);
+  ix += (int)sx; fx -= sx;
+  iy += (int)sy; fy -= sy;
+  if (fx >= 1.0f) { fx -= 1.0f; ix += 1; }
+  if (fy >= 1.0f) { fy -= 1.0f; iy += 1; }
+  const float X = (float)ix + fx, Y = (float)iy + fy;
+  const float r = sqrtf(X * X + Y * Y);
+  const bool alive = r < (float)G.nr && ix > -32000 && ix < 32000 && iy > -32000 && iy < 32000;
+  A.cxy[i] = pack_cell(alive ? ix : 0, alive ? iy : 0);
+  A.fx[i] = fx;
+  A.fy[i] = fy;
+  A.key[i] = alive ? (int)r + 1 : G.nr + 1;
+}
+
+// ------------------------------------------------------------------------------------
+// counting sort by key (1..nr, nr+1 = removed); order inside a cell is not kept
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMixThreads) k_mhist(const int64_t* __restrict__ n_ptr, const int32_t* __restrict__ key,
+                                                       int32_t* __restrict__ hist) {
+  const int64_t n = *n_ptr;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  const int k = valid ? key[i] : -1;
+  const unsigned grp = __match_any_sync(FULL, k);
+  const int lane = threadIdx.x & 31;
+  if (valid && (grp & ((1u << lane) - 1u)) == 0) atomicAdd(hist + k, __popc(grp));
+}
+
+__global__ void __launch_bounds__(1024) k_mscan(int nk, const int32_t* __restrict__ hist, int32_t* __restrict__ cursor,
+                                                int64_t* __restrict__ n_ptr, int dead_key) {
+  __shared__ int sh[64];
+  int carry = 0;
+  for (int base = 0; base < nk; base += blockDim.x) {
+    const int k = base + threadIdx.x;
+    const int v = k < nk ? hist[k] : 0;
+    int x = v;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int o = __shfl_up_sync(FULL, x, off);
+      if (lane >= off) x += o;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = lane < nw ? sh[lane] : 0;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int o = __shfl_up_sync(FULL, w, off);
+        if (lane >= off) w += o;
+      }
+      sh[32 + lane] = w;
+    }
+    __syncthreads();
+    const int before = warp > 0 ? sh[32 + warp - 1] : 0;
+    const int tot = sh[32 + nw - 1];
+    if (k < nk) cursor[k] = carry + before + x - v;
+    if (k == dead_key) *n_ptr = carry + before + x - v;    // particles before the removed bucket
+    carry += tot;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kMixThreads) k_mscatter(const int64_t* __restrict__ n_old, MArr S, MArr D,
+                                                          int32_t* __restrict__ cursor) {
+  const int64_t n = *n_old;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  const int k = valid ? S.key[i] : -1;
+  const unsigned grp = __match_any_sync(FULL, k);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(grp) - 1;
+  int base = 0;
+  if (valid && lane == leader) base = atomicAdd(cursor + k, __popc(grp));
+  base = __shfl_sync(FULL, base, leader);
+  if (!valid) return;
+  const int d = base + __popc(grp & ((1u << lane) - 1u));
+  D.cxy[d] = S.cxy[i]; D.fx[d] = S.fx[i]; D.fy[d] = S.fy[i];
+  D.px[d] = S.px[i]; D.py[d] = S.py[i]; D.pz[d] = S.pz[i];
+  D.q[d] = S.q[i]; D.gam[d] = S.gam[i]; D.psi[d] = S.psi[i];
+  D.key[d] = k;
+}
+
+__global__ void k_copy_count(const int64_t* __restrict__ a, int64_t* __restrict__ b) { *b = *a; }
+
+// ------------------------------------------------------------------------------------
+// conversions
+// ------------------------------------------------------------------------------------
+__global__ void k_to_mixed(GridDev G, const int64_t* __restrict__ n_ptr, const double* __restrict__ x,
+                           const double* __restrict__ y, const double* __restrict__ px, const double* __restrict__ py,
+                           const double* __restrict__ pz, const double* __restrict__ gam,
+                           const double* __restrict__ psi, const double* __restrict__ q, MArr A) {
+  const int64_t n = *n_ptr;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double tx = x[i] * G.idr, ty = y[i] * G.idr;
+  const double sx = floor(tx), sy = floor(ty);
+  float fx = (float)(tx - sx), fy = (float)(ty - sy);
+  int ix = (int)sx, iy = (int)sy;
+  if (fx >= 1.0f) { fx -= 1.0f; ix += 1; }
+  if (fy >= 1.0f) { fy -= 1.0f; iy += 1; }
+  A.cxy[i] = pack_cell(ix, iy);
+  A.fx[i] = fx;
+  A.fy[i] = fy;
+  A.px[i] = (float)px[i]; A.py[i] = (float)py[i]; A.pz[i] = (float)pz[i];
+  A.gam[i] = (float)gam[i]; A.psi[i] = (float)psi[i]; A.q[i] = (float)q[i];
+  const float X = (float)ix + fx, Y = (float)iy + fy;
+  const float r = sqrtf(X * X + Y * Y);
+  A.key[i] = r < (float)G.nr ? (int)r + 1 : G.nr + 1;
+}
+
+__global__ void k_to_fp64(GridDev G, const int64_t* __restrict__ n_ptr, MArr A, double* __restrict__ x,
+                          double* __restrict__ y, double* __restrict__ px, double* __restrict__ py,
+                          double* __restrict__ pz, double* __restrict__ gam, double* __restrict__ psi,
+                          double* __restrict__ q) {
+  const int64_t n = *n_ptr;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int ix, iy;
+  unpack_cell(A.cxy[i], ix, iy);
+  x[i] = ((double)ix + (double)A.fx[i]) * G.dr;
+  y[i] = ((double)iy + (double)A.fy[i]) * G.dr;
+  px[i] = A.px[i]; py[i] = A.py[i]; pz[i] = A.pz[i];
+  gam[i] = A.gam[i]; psi[i] = A.psi[i]; q[i] = A.q[i];
+}
+
+__global__ void __launch_bounds__(kMixThreads) k_minterp_psi(GridDev G, const int64_t* __restrict__ n_ptr, MArr A,
+                                                             const double* __restrict__ psif) {
+  const int64_t n = *n_ptr;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const MInterp ii = minterp(A.cxy[i], A.fx[i], A.fy[i], G.nr);
+  if (!ii.ok) { A.psi[i] = 0.0f; return; }
+  const int i0 = ii.idx;
+  float v = (float)psif[i0] * ii.w0 + (float)psif[i0 + 1] * ii.w1;
+  float phr = 1.0f, phi = 0.0f;
+  for (int m = 1; m <= G.M; ++m) {
+    const float t = phr * ii.pcos - phi * ii.psin;
+    phi = phr * ii.psin + phi * ii.pcos;
+    phr = t;
+    const double* fr = psif + (size_t)(2 * m - 1) * G.ld + i0;
+    const double* fi = psif + (size_t)(2 * m) * G.ld + i0;
+    v += ((float)fr[0] * 2.0f * phr - (float)fi[0] * 2.0f * phi) * ii.w0 +
+         ((float)fr[1] * 2.0f * phr - (float)fi[1] * 2.0f * phi) * ii.w1;
+  }
+  A.psi[i] = v;
+}
+
+// ------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------
+int mixed_alloc(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  const size_t cap = (size_t)sp->npmax;
+  const size_t per = cap * (sizeof(int32_t) * 2 + sizeof(float) * 8);   // cxy, key, 8 floats
+  void* blk = nullptr;
+  cudaError_t e = cudaMalloc(&blk, 2 * per + 256);
+  if (e != cudaSuccess) { cudaGetLastError(); return set_err(ctx, QPAD_E_NOMEM, "cudaMalloc(mixed particles)"); }
+  sp->mixed_block = blk;
+  char* p = (char*)blk;
+  for (int b = 0; b < 2; ++b) {
+    sp->cxy[b] = (int32_t*)p; p += cap * sizeof(int32_t);
+    sp->mkey[b] = (int32_t*)p; p += cap * sizeof(int32_t);
+    float** fs[8] = {&sp->fx[b], &sp->fy[b], &sp->mpx[b], &sp->mpy[b], &sp->mpz[b], &sp->mq[b], &sp->mgam[b],
+                     &sp->mpsi[b]};
+    for (int a = 0; a < 8; ++a) { *fs[a] = (float*)p; p += cap * sizeof(float); }
+  }
+  e = cudaMalloc(&sp->mixed_pristine, per + 256);
+  if (e != cudaSuccess) { cudaGetLastError(); return set_err(ctx, QPAD_E_NOMEM, "cudaMalloc(mixed pristine)"); }
+  e = cudaMalloc(&sp->hist, sizeof(int32_t) * (ctx->g.nr + 4));
+  if (e == cudaSuccess) e = cudaMalloc(&sp->cursor, sizeof(int32_t) * (ctx->g.nr + 4));
+  if (e != cudaSuccess) { cudaGetLastError(); return set_err(ctx, QPAD_E_NOMEM, "cudaMalloc(mixed sort)"); }
+  return 0;
+}
+
+void mixed_free(qpad_species* sp) {
+  if (sp->mixed_block) cudaFree(sp->mixed_block);
+  if (sp->mixed_pristine) cudaFree(sp->mixed_pristine);
+  if (sp->hist) cudaFree(sp->hist);
+  if (sp->cursor) cudaFree(sp->cursor);
+  sp->mixed_block = sp->mixed_pristine = nullptr;
+  sp->hist = sp->cursor = nullptr;
+}
+
+
+// sorts the mixed state by key; the new count (without removed particles) lands in d_count
+static int mixed_sort(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  const int64_t n = sp->np;
+  if (n == 0) return 0;
+  const int nk = ctx->g.nr + 2;
+  if (cudaMemsetAsync(sp->hist, 0, sizeof(int32_t) * nk, ctx->stream) != cudaSuccess) return check_launch(ctx, "hist0", 0);
+  k_mhist<<<mgrid(n, kMixThreads), kMixThreads, 0, ctx->stream>>>(sp->d_count, sp->mkey[0], sp->hist);
+  k_copy_count<<<1, 1, 0, ctx->stream>>>(sp->d_count, sp->d_total);      // old count for the scatter
+  k_mscan<<<1, 1024, 0, ctx->stream>>>(nk, sp->hist, sp->cursor, sp->d_count, ctx->g.nr + 1);
+  k_mscatter<<<mgrid(n, kMixThreads), kMixThreads, 0, ctx->stream>>>(sp->d_total, marr(sp, 0), marr(sp, 1),
+                                                                      sp->cursor);
+  if (int r = check_launch(ctx, "mixed sort", 4)) return r;
+  // copy the sorted half back into place (the two halves are contiguous blocks of 10
+  // arrays), so that kernels captured in a CUDA graph keep valid arguments
+  return cuda_check(ctx, cudaMemcpyAsync(sp->cxy[0], sp->cxy[1], (size_t)sp->npmax * 40, cudaMemcpyDeviceToDevice,
+                                         ctx->stream), "mixed copy back");
+}
+
+int mixed_from_fp64(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  if (sp->np == 0) return 0;
+  k_to_mixed<<<mgrid(sp->np, kMixThreads), kMixThreads, 0, ctx->stream>>>(
+      ctx->g, sp->d_count, sp->x[0], sp->y[0], sp->px[0], sp->py[0], sp->pz[0], sp->gamma[0], sp->psi[0], sp->q[0],
+      marr(sp, 0));
+  if (int r = check_launch(ctx, "to mixed")) return r;
+  return mixed_sort(sp);
+}
+
+int mixed_to_fp64(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  if (sp->np == 0) return 0;
+  k_to_fp64<<<mgrid(sp->np, kMixThreads), kMixThreads, 0, ctx->stream>>>(
+      ctx->g, sp->d_count, marr(sp, 0), sp->x[0], sp->y[0], sp->px[0], sp->py[0], sp->pz[0], sp->gamma[0],
+      sp->psi[0], sp->q[0]);
+  return check_launch(ctx, "to fp64");
+}
+
+int mixed_save_pristine(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  const size_t cap = (size_t)sp->npmax;
+  char* p = (char*)sp->mixed_pristine;
+  const void* src[10] = {sp->cxy[0], sp->mkey[0], sp->fx[0], sp->fy[0], sp->mpx[0], sp->mpy[0],
+                         sp->mpz[0], sp->mq[0],   sp->mgam[0], sp->mpsi[0]};
+  for (int a = 0; a < 10; ++a) {
+    if (cudaMemcpyAsync(p + a * cap * 4, src[a], cap * 4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+      return check_launch(ctx, "mixed pristine", 0);
+  }
+  return 0;
+}
+
+int mixed_restore_pristine(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  const size_t cap = (size_t)sp->npmax;
+  const char* p = (const char*)sp->mixed_pristine;
+  void* dst[10] = {sp->cxy[0], sp->mkey[0], sp->fx[0], sp->fy[0], sp->mpx[0], sp->mpy[0],
+                   sp->mpz[0], sp->mq[0],   sp->mgam[0], sp->mpsi[0]};
+  for (int a = 0; a < 10; ++a) {
+    if (cudaMemcpyAsync(dst[a], p + a * cap * 4, cap * 4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+      return check_launch(ctx, "mixed restore", 0);
+  }
+  return 0;
+}
+
+int mixed_qdeposit_raw(qpad_species* sp, double* qraw) {
+  qpad_ctx* ctx = sp->ctx;
+  if (sp->np == 0) return 0;
+  prof_begin(ctx, "qdeposit");
+  k_mqdeposit<<<mgrid(sp->np, kChunk), kMixThreads, 0, ctx->stream>>>(ctx->g, sp->d_count, marr(sp, 0), qraw);
+  prof_end(ctx, "qdeposit");
+  return check_launch(ctx, "k_mqdeposit");
+}
+
+int mixed_amjdp_raw(qpad_species* sp, const float* gtab, double* cu, double* amu, double* acu, double dt) {
+  qpad_ctx* ctx = sp->ctx;
+  if (sp->np == 0) return 0;
+  prof_begin(ctx, "amjdp");
+  k_mamjdp<<<mgrid(sp->np, kChunk), kMixThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
+                                                                    sp->d_count, marr(sp, 0), gtab, cu, amu, acu, 0);
+  prof_end(ctx, "amjdp");
+  return check_launch(ctx, "k_mamjdp");
+}
+
+int mixed_push(qpad_species* sp, const float* gtab, double dt, int do_u, int do_x) {
+  qpad_ctx* ctx = sp->ctx;
+  if (sp->np == 0) return 0;
+  prof_begin(ctx, "push");
+  k_mpush<<<mgrid(sp->np, kMixThreads), kMixThreads, 0, ctx->stream>>>(
+      ctx->g, sp->push_type, (float)sp->qbm, (float)dt, sp->d_count, marr(sp, 0), gtab, do_u, do_x);
+  prof_end(ctx, "push");
+  if (int r = check_launch(ctx, "k_mpush")) return r;
+  return do_x ? mixed_sort(sp) : 0;
+}
+
+int mixed_sort_public(qpad_species* sp) { return mixed_sort(sp); }
+
+int mixed_interp_psi(qpad_species* sp, const double* psif) {
+  qpad_ctx* ctx = sp->ctx;
+  if (sp->np == 0) return 0;
+  k_minterp_psi<<<mgrid(sp->np, kMixThreads), kMixThreads, 0, ctx->stream>>>(ctx->g, sp->d_count, marr(sp, 0), psif);
+  return check_launch(ctx, "k_minterp_psi");
+}
+
+}  // namespace qpad

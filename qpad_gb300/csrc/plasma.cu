@@ -376,11 +376,13 @@ static PArrays arrays_of(qpad_species* sp, int b) {
   return a;
 }
 
-static void swap_buffers(qpad_species* sp) {
-  std::swap(sp->x[0], sp->x[1]); std::swap(sp->y[0], sp->y[1]);
-  std::swap(sp->px[0], sp->px[1]); std::swap(sp->py[0], sp->py[1]);
-  std::swap(sp->pz[0], sp->pz[1]); std::swap(sp->gamma[0], sp->gamma[1]);
-  std::swap(sp->psi[0], sp->psi[1]); std::swap(sp->q[0], sp->q[1]);
+// The scatter target [1] is copied back into [0] (one contiguous block of 8 x npmax
+// doubles) instead of swapping pointers, so that kernels captured in a CUDA graph keep
+// valid arguments from slice to slice.
+static int copy_back(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  return cuda_check(ctx, cudaMemcpyAsync(sp->x[0], sp->x[1], sizeof(double) * 8 * (size_t)sp->npmax,
+                                         cudaMemcpyDeviceToDevice, ctx->stream), "copy back");
 }
 
 int species_qdeposit_raw(qpad_species* sp, double* qraw) {
@@ -440,8 +442,8 @@ int species_compact(qpad_species* sp) {
   k_compact_scatter<<<grid_for(n, kPartThreads), kPartThreads, 0, ctx->stream>>>(sp->d_count, sp->key, pos,
                                                                                  arrays_of(sp, 0), arrays_of(sp, 1), 8);
   k_set_count<<<1, 1, 0, ctx->stream>>>(sp->d_count, sp->d_total);
-  swap_buffers(sp);
-  return check_launch(ctx, "compact", 3);
+  if (int r = check_launch(ctx, "compact", 3)) return r;
+  return copy_back(sp);
 }
 
 int species_sort(qpad_species* sp) {
@@ -461,8 +463,8 @@ int species_sort(qpad_species* sp) {
   if (int r = scan_i32(ctx, hist, excl, nh, tmp, nullptr)) return r;
   k_sort_scatter<<<grid_for(n, kPartThreads), kPartThreads, 0, ctx->stream>>>(
       ctx->g, sp->d_count, sp->key, sp->aux, excl, ntiles, arrays_of(sp, 0), arrays_of(sp, 1), nullptr);
-  swap_buffers(sp);
-  return check_launch(ctx, "sort", 3);
+  if (int r = check_launch(ctx, "sort", 3)) return r;
+  return copy_back(sp);
 }
 
 int species_interp_psi(qpad_species* sp, const double* psif) {

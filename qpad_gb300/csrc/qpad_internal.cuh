@@ -67,6 +67,7 @@ struct qpad_ctx {
   double* qn = nullptr;                        // neutralising background (sum over species)
   double* qraw = nullptr;                      // raw charge deposit scratch
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
+  float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
   double* scratch = nullptr;                   // per-call deposit scratch (cu, amu, acu)
   double* beam_scratch = nullptr;              // per-beam charge store scratch
   double* h_res = nullptr;                     // pinned mirror of res
@@ -76,6 +77,18 @@ struct qpad_ctx {
   std::string err;
   int slice_counter = 0;
   bool field_attr_done = false;
+  // device-side loop state of the slice driver
+  int* d_j = nullptr;                          // current slice (1-based)
+  int* d_iter = nullptr;                       // predictor-corrector iterations in this slice
+  qpad_slice_stats* d_stats = nullptr;         // per-slice statistics [nz]
+  int* h_j = nullptr;                          // pinned staging of the slice index
+  // CUDA graph of the whole slice loop (WHILE over slices, WHILE over iterations)
+  cudaGraphExec_t step_exec = nullptr;
+  std::string step_key;                        // configuration the graph was built for
+  std::string graph_status;                    // why the graph path is off, if it is
+  bool use_graph = true;
+  int64_t g_pro = 0, g_it = 0, g_epi = 0;      // kernels per slice prologue / iteration / epilogue
+  std::vector<qpad_slice_stats> h_stats;       // per-slice statistics read back after a graph step
   int64_t launches = 0;                        // kernels launched on this context
   // per-kernel-family CUDA-event timing (qpad_profile_enable / qpad_profile_read)
   bool prof_on = false;
@@ -100,6 +113,16 @@ struct qpad_species {
   int64_t* h_count = nullptr;   // pinned mirror
   double* pristine = nullptr;   // device copy of the last uploaded particles (8 x npmax)
   int64_t np_pristine = 0;
+  // mixed-precision state (QPAD_PREC_MIXED): position = (cell + offset) * dr per axis,
+  // cell packed as two int16 in cxy, offsets in [0,1); FP32 momenta, charge, gamma, psi.
+  int32_t* cxy[2] = {};
+  float *fx[2] = {}, *fy[2] = {}, *mpx[2] = {}, *mpy[2] = {}, *mpz[2] = {}, *mq[2] = {}, *mgam[2] = {},
+        *mpsi[2] = {};
+  int32_t* mkey[2] = {};        // radial cell key 1..nr (nr+1: left the box), sorted ascending
+  int32_t* hist = nullptr;      // nr+2 counters
+  int32_t* cursor = nullptr;    // nr+2 scatter cursors
+  void* mixed_block = nullptr;
+  void* mixed_pristine = nullptr;
   double* qf = nullptr;         // this species' charge density (finished deposit)
   double* qn = nullptr;         // this species' neutralising background
 };
@@ -141,12 +164,15 @@ struct FieldArgs {
   const double* in1;  // second source (psi for ET, cu for BT_ITER, amu for DJDXI)
 };
 int launch_field_op(qpad_ctx* ctx, int op, FieldArgs a);
-int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op);
+// loop_state: count iterations, store per-slice stats, and (use_h) drive the WHILE node h
+int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op, int loop_state = 0,
+                cudaGraphConditionalHandle h = 0, int use_h = 0);
+int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle h);   // ++slice, set slice WHILE condition
 // fused phases of one slice
-int launch_slice_begin(qpad_ctx* ctx, int j, int neutralized_any);
+int launch_slice_begin(qpad_ctx* ctx, int neutralized_any);   // slice index read from ctx->d_j
 int launch_iter_e(qpad_ctx* ctx);
 int launch_iter_b(qpad_ctx* ctx);
-int launch_slice_end(qpad_ctx* ctx, int j);
+int launch_slice_end(qpad_ctx* ctx);
 int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn);
 int launch_finish_amj(qpad_ctx* ctx, double* cu, double* amu, double* acu);
 
@@ -160,6 +186,21 @@ int species_compact(qpad_species* sp);
 int species_sort(qpad_species* sp);
 int species_interp_psi(qpad_species* sp, const double* psif);
 int species_sync_count(qpad_species* sp);
+// ---- mixed-precision particle path (mixed.cu) ------------------------------------------
+int mixed_alloc(qpad_species* sp);
+void mixed_free(qpad_species* sp);
+int mixed_from_fp64(qpad_species* sp);      // FP64 buffers [0] -> mixed state, sorted
+int mixed_to_fp64(qpad_species* sp);        // mixed state -> FP64 buffers [0]
+int mixed_save_pristine(qpad_species* sp);
+int mixed_restore_pristine(qpad_species* sp);
+int mixed_qdeposit_raw(qpad_species* sp, double* qraw);
+int mixed_amjdp_raw(qpad_species* sp, const float* gtab, double* cu, double* amu, double* acu, double dt);
+// push_u (do_u) and/or push_x + update_bound + sort (do_x)
+int mixed_push(qpad_species* sp, const float* gtab, double dt, int do_u, int do_x);
+int mixed_sort_public(qpad_species* sp);
+int mixed_interp_psi(qpad_species* sp, const double* psif);
+int launch_gtab(qpad_ctx* ctx, const double* e, const double* b);   // FP32 gather table of (e, b)
+
 int beam_qdeposit(qpad_beam* bm, double* q2);
 int beam_finish_q(qpad_ctx* ctx, double* q2);
 int beam_push(qpad_beam* bm, const double* e2, const double* b2);

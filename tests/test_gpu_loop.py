@@ -73,6 +73,37 @@ def test_3d_step_matches_oracle(M, push_type):
     sim.close()
 
 
+@pytest.mark.parametrize("precision", [Q._capi.PREC_FP64, Q._capi.PREC_MIXED])
+def test_graph_and_host_driven_loops_agree(precision):
+    """The CUDA-graph slice loop (device-side WHILE conditions) equals the host-driven one."""
+    deck = _deck(2)
+    pl, beams = Q.deck_inputs(deck)
+    runs = []
+    for graph in (True, False):
+        s = Q.Simulation(deck.nr, deck.nz, 2, deck.dr, deck.dxi, iter_max=deck.iter_max, dt=deck.dt,
+                         precision=precision)
+        s.lib.qpad_set_graph(s.h, int(graph))
+        s.add_species(*pl)
+        s.add_beam(*beams[0])
+        it, _ = s.run_3d_step()
+        import ctypes
+        a = ctypes.c_int()
+        s.lib.qpad_graph_active(s.h, ctypes.byref(a))
+        assert a.value == int(graph)
+        runs.append((it, [s.e.store(j) for j in (1, deck.nz // 2, deck.nz)], s))
+    (ia, ea, sa), (ib, eb, sb) = runs
+    if precision == Q._capi.PREC_FP64:
+        assert np.array_equal(ia, ib)
+        for x, y in zip(ea, eb):
+            assert field_errors(x, y).max() < 1e-12
+    else:
+        assert abs(float(ia.mean()) - float(ib.mean())) < 0.5
+        for x, y in zip(ea, eb):
+            assert field_errors(x, y).max() < 1e-4
+    sa.close()
+    sb.close()
+
+
 def test_slice_by_slice_api_matches_fused_step():
     """qpad_slice_step driven from the host equals the fused 3D step."""
     deck = _deck(1)

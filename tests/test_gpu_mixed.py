@@ -1,0 +1,122 @@
+"""Mixed-precision path (FP32 particles and deposits, FP64 solves) against the FP64 oracle.
+
+The target is every per-mode field within 1e-4 relative L2 of the FP64 oracle; single
+deposits are checked against the FP32 rounding level.
+"""
+import numpy as np
+import pytest
+
+import qpad_gb300 as Q
+from oracle import oracle as O
+from qpad_gb300 import _capi as K
+from tests.helpers import field_errors, plasma_to_oracle, smooth_field
+
+pytestmark = pytest.mark.gpu
+
+
+def _plasma(nr, dr, seed, uth=0.05):
+    x, p, g, ps, q = Q.load_plasma(nr, dr, seed, 2, 2, 8, uth=(uth, uth, uth))
+    rng = np.random.default_rng(seed)
+    x = np.ascontiguousarray(x + rng.uniform(-0.45, 0.45, x.shape) * dr)
+    return x, p, g, ps, q
+
+
+@pytest.mark.parametrize("nr,M", [(64, 1), (128, 2), (96, 4)])
+def test_mixed_qdeposit(nr, M):
+    dr = 0.04
+    g = O.grid(nr, 4, M, dr, 0.04)
+    sim = Q.Simulation(nr, 4, M, dr, 0.04, precision=K.PREC_MIXED)
+    x, p, gam, ps, q = _plasma(nr, dr, nr + M)
+    sp = sim.add_species(x, p, gam, ps, q, neutralized=False)
+    sim.q_spe.fill(0.0)
+    sp.qdp(sim.q_spe)
+    ref = O.qdeposit(g, plasma_to_oracle(x, p, gam, ps, q))
+    err = field_errors(sim.q_spe.download(), ref, nodes=slice(0, None))
+    assert err.max() < 2e-6, err
+    sim.close()
+
+
+@pytest.mark.parametrize("nr,M", [(64, 1), (128, 2), (96, 4)])
+def test_mixed_amjdp(nr, M):
+    dr, dt = 0.04, 0.04
+    g = O.grid(nr, 4, M, dr, dt)
+    rng = np.random.default_rng(100 + nr + M)
+    ef = smooth_field(rng, g, 3, scale=0.5)
+    bf = smooth_field(rng, g, 3, scale=0.5)
+    sim = Q.Simulation(nr, 4, M, dr, dt, precision=K.PREC_MIXED)
+    x, p, gam, ps, q = _plasma(nr, dr, 7 + nr)
+    sp = sim.add_species(x, p, gam, ps, q)
+    sim.e.upload(ef)
+    sim.b.upload(bf)
+    for f in (sim.cu, sim.amu, sim.acu):
+        f.fill(0.0)
+    sp.amjdp(sim.e, sim.b, sim.cu, sim.amu, sim.acu, dt)
+    cu, amu, dcu = O.amjdeposit(g, O.PUSH_ROBUST, -1.0, dt, plasma_to_oracle(x, p, gam, ps, q), ef, bf)
+    for got, ref in ((sim.cu.download(), cu), (sim.amu.download(), amu), (sim.acu.download(), dcu)):
+        err = field_errors(got, ref, nodes=slice(0, None))
+        assert err.max() < 2e-4, err
+    sim.close()
+
+
+def test_mixed_push_keeps_particles_and_positions():
+    nr, M, dr, dt = 64, 2, 0.04, 0.2
+    g = O.grid(nr, 4, M, dr, dt)
+    rng = np.random.default_rng(7)
+    ef = smooth_field(rng, g, 3, scale=2.0)
+    bf = smooth_field(rng, g, 3, scale=2.0)
+    sim = Q.Simulation(nr, 4, M, dr, dt, precision=K.PREC_MIXED)
+    x, p, gam, ps, q = _plasma(nr, dr, 9, uth=0.3)
+    sp = sim.add_species(x, p, gam, ps, q)
+    sim.e.upload(ef)
+    sim.b.upload(bf)
+    sp.push_u(sim.e, sim.b, dt)
+    sp.push_x(dt)
+    pl = plasma_to_oracle(x, p, gam, ps, q)
+    O.push_u(g, O.PUSH_ROBUST, -1.0, dt, pl, ef, bf)
+    O.push_x(pl, dt)
+    n = O.update_bound(g, pl)
+    x2, p2, g2, ps2, q2 = sp.download()
+    # removal can differ only for particles within FP32 rounding of the edge
+    assert abs(len(q2) - n) <= 2
+    r_gpu = np.sort(np.hypot(x2[:, 0], x2[:, 1]))
+    r_ref = np.sort(np.hypot(pl.x[:n], pl.y[:n]))
+    m = min(len(r_gpu), len(r_ref))
+    assert np.max(np.abs(r_gpu[:m] - r_ref[:m])) < 1e-5
+    # the path keeps particles sorted by radial cell
+    assert np.all(np.diff(np.floor(np.hypot(x2[:, 0], x2[:, 1]) / dr)) >= -1)
+    sim.close()
+
+
+@pytest.mark.parametrize("M", [1, 2])
+def test_mixed_3d_step_within_1e4_of_fp64_oracle(M):
+    deck = Q.decks.Deck("mixed_loop", nr=64, nz=40, max_mode=M, dr=0.04, dxi=0.04, ppc=(2, 1), num_theta=8,
+                        uth=2e-3, seed=3, beams=[Q.decks.BeamSpec(2.0, 0.4, 0.3, 0.6, 20000, x0=0.04)],
+                        iter_max=30, iter_reltol=1e-6)
+    pl, beams = Q.deck_inputs(deck)
+    g = O.grid(deck.nr, deck.nz, M, deck.dr, deck.dxi)
+    osim = O.Sim(g, iter_max=deck.iter_max, iter_reltol=deck.iter_reltol, dt3d=deck.dt, sp_npmax=len(pl[4]),
+                 beams=[(-1.0, O.PUSH3_REDUCED, len(beams[0][2]))])
+    osim.set_plasma(plasma_to_oracle(*pl))
+    from tests.helpers import beam_to_oracle
+    osim.set_beam(0, beam_to_oracle(*beams[0]))
+    oiters, _ = osim.run_3dstep()
+    sim = Q.Simulation(deck.nr, deck.nz, M, deck.dr, deck.dxi, iter_max=deck.iter_max,
+                       iter_reltol=deck.iter_reltol, dt=deck.dt, precision=K.PREC_MIXED)
+    sim.add_species(*pl)
+    sim.add_beam(*beams[0])
+    iters, _ = sim.run_3d_step()
+    worst = {}
+    for name in ("e", "b", "psi"):
+        ref = osim.store(name)[:deck.nz]
+        got = np.stack([sim.fields[name].store(s) for s in range(1, deck.nz + 1)])
+        # relative L2 per (mode part, component) over all slices and nodes
+        errs = []
+        for p in range(2 * M + 1):
+            for c in range(ref.shape[2]):
+                nrm = np.linalg.norm(ref[:, p, c, 1:])
+                if nrm > 1e-8 * np.linalg.norm(ref[:, :, c, 1:]):
+                    errs.append(np.linalg.norm(got[:, p, c, 1:] - ref[:, p, c, 1:]) / nrm)
+        worst[name] = max(errs)
+    assert max(worst.values()) < 1e-4, worst
+    assert abs(float(np.mean(iters)) - float(np.mean(oiters))) < 1.0
+    sim.close()
