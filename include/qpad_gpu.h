@@ -89,6 +89,8 @@ int qpad_launch_count(const qpad_ctx* ctx, int64_t* count);
 int qpad_set_graph(qpad_ctx* ctx, int on);
 /* 1 if the last 3D step ran as a graph. */
 int qpad_graph_active(const qpad_ctx* ctx, int* active);
+/* Why the graph path was switched off ("" while it is on). */
+const char* qpad_graph_status(const qpad_ctx* ctx);
 /* Per-kernel CUDA-event timing on the context's stream: enable/disable, then read the
  * accumulated device time (ms) and launch count of one kernel family by name
  * ("amjdp", "qdeposit", "push", "field", "beam_push", "beam_qdeposit"). */

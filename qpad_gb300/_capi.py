@@ -69,6 +69,7 @@ _SIGS = {
     "qpad_launch_count": (C.c_int, [C.c_void_p, I64P]),
     "qpad_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
     "qpad_graph_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "qpad_graph_status": (C.c_char_p, [C.c_void_p]),
     "qpad_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
     "qpad_profile_read": (C.c_int, [C.c_void_p, C.c_char_p, D, I64P]),
     "qpad_species_reset": (C.c_int, [C.c_void_p]),

@@ -194,6 +194,16 @@ class Simulation:
         self._check(self.lib.qpad_conv_test(self.h, b.id, dim, 0 if op == "record" else 1, C.byref(rel), C.byref(ab)))
         return rel.value, ab.value
 
+    def use_graph(self, on: bool):
+        """Run 3D steps as one CUDA graph (default) or drive slices/iterations from the host."""
+        self._check(self.lib.qpad_set_graph(self.h, int(on)))
+
+    def graph_active(self):
+        """(whether the last 3D step ran as a graph, reason when it did not)."""
+        a = C.c_int()
+        self._check(self.lib.qpad_graph_active(self.h, C.byref(a)))
+        return bool(a.value), self.lib.qpad_graph_status(self.h).decode()
+
     def launch_count(self) -> int:
         n = C.c_int64()
         self._check(self.lib.qpad_launch_count(self.h, C.byref(n)))

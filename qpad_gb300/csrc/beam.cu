@@ -69,7 +69,7 @@ __global__ void k_beam_finish_q(GridDev G, double* __restrict__ q2) {
     double o;
     if (i == 0) o = 0.0;
     else if (i == 1) o = (p == 0) ? 8.0 * v : 0.0;
-    else o = v * (1.0 / (double)(i - 1));
+    else o = v * G.inv[i];
     row[i] = o;
   }
 }

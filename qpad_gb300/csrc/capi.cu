@@ -336,6 +336,7 @@ extern "C" int qpad_ctx_destroy(qpad_ctx* ctx) {
     if (ctx->f2[f]) cudaFree(ctx->f2[f]);
   }
   if (ctx->fac) cudaFree(ctx->fac);
+  if (ctx->rtab) cudaFree(ctx->rtab);
   if (ctx->qn) cudaFree(ctx->qn);
   if (ctx->qraw) cudaFree(ctx->qraw);
   if (ctx->conv) cudaFree(ctx->conv);
@@ -394,6 +395,8 @@ extern "C" int qpad_graph_active(const qpad_ctx* ctx, int* active) {
   *active = (ctx->use_graph && ctx->step_exec != nullptr) ? 1 : 0;
   return QPAD_OK;
 }
+
+extern "C" const char* qpad_graph_status(const qpad_ctx* ctx) { return ctx ? ctx->graph_status.c_str() : ""; }
 
 extern "C" int qpad_launch_count(const qpad_ctx* ctx, int64_t* count) {
   if (!ctx || !count) return QPAD_E_ARG;

@@ -103,7 +103,19 @@ int build_factors(qpad_ctx* ctx) {
         if (!std::isfinite(ib[k]) || !std::isfinite(w[k]))
           return set_err(ctx, QPAD_E_ARG, "singular tridiagonal operator (check nr, dr, relax_fac)");
     }
-  cudaError_t e = cudaMalloc(&ctx->fac, h.size() * sizeof(double));
+  // node tables of the finite-difference factors (same FP64 expressions as the reference)
+  std::vector<double> rt(2 * (size_t)g.ld, 0.0);
+  for (int i = 2; i < g.ld; ++i) {
+    rt[i] = g.idr / (double)(i - 1);
+    rt[g.ld + i] = 1.0 / (double)(i - 1);
+  }
+  cudaError_t e = cudaMalloc(&ctx->rtab, rt.size() * sizeof(double));
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(node tables)");
+  e = cudaMemcpy(ctx->rtab, rt.data(), rt.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "upload node tables");
+  ctx->g.ir = ctx->rtab;
+  ctx->g.inv = ctx->rtab + g.ld;
+  e = cudaMalloc(&ctx->fac, h.size() * sizeof(double));
   if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(factors)");
   return cuda_check(ctx, cudaMemcpy(ctx->fac, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice),
                     "upload factors");
@@ -263,11 +275,11 @@ __device__ __forceinline__ void src_bz_row(const GridDev& G, int m, int i, const
     if (i == 1) {
       re = -2.0 * idr * FLD(cu, 3, 0, 1, 2);
     } else if (i == nr) {
-      const double ir = idr / (double)(nr - 1);
+      const double ir = G.ir[nr];
       re = -idrh * (3.0 * FLD(cu, 3, 0, 1, nr) - 4.0 * FLD(cu, 3, 0, 1, nr - 1) + FLD(cu, 3, 0, 1, nr - 2)) -
            ir * FLD(cu, 3, 0, 1, nr);
     } else {
-      const double ir = idr / (double)(i - 1);
+      const double ir = G.ir[i];
       re = -idrh * (FLD(cu, 3, 0, 1, i + 1) - FLD(cu, 3, 0, 1, i - 1)) - ir * FLD(cu, 3, 0, 1, i);
     }
     im = 0.0;
@@ -276,7 +288,7 @@ __device__ __forceinline__ void src_bz_row(const GridDev& G, int m, int i, const
   const int pr = part_re(m), pi = part_im(m);
   const double dm = (double)m;
   if (i == nr) {
-    const double ir = idr / (double)(nr - 1);
+    const double ir = G.ir[nr];
     re = -idrh * (3.0 * FLD(cu, 3, pr, 1, nr) - 4.0 * FLD(cu, 3, pr, 1, nr - 1) + FLD(cu, 3, pr, 1, nr - 2)) -
          ir * FLD(cu, 3, pr, 1, nr) - dm * ir * FLD(cu, 3, pi, 0, nr);
     im = -idrh * (3.0 * FLD(cu, 3, pi, 1, nr) - 4.0 * FLD(cu, 3, pi, 1, nr - 1) + FLD(cu, 3, pi, 1, nr - 2)) -
@@ -296,7 +308,7 @@ __device__ __forceinline__ void src_bz_row(const GridDev& G, int m, int i, const
     im = -idr * (FLD(cu, 3, pi, 1, 3) - FLD(cu, 3, pi, 1, 2)) - ir * FLD(cu, 3, pi, 1, 2) +
          dm * ir * FLD(cu, 3, pr, 0, 2);
   } else {
-    const double ir = idr / (double)(i - 1);
+    const double ir = G.ir[i];
     re = -idrh * (FLD(cu, 3, pr, 1, i + 1) - FLD(cu, 3, pr, 1, i - 1)) - ir * FLD(cu, 3, pr, 1, i) -
          dm * ir * FLD(cu, 3, pi, 0, i);
     im = -idrh * (FLD(cu, 3, pi, 1, i + 1) - FLD(cu, 3, pi, 1, i - 1)) - ir * FLD(cu, 3, pi, 1, i) +
@@ -359,13 +371,13 @@ __device__ void op_bt_beam(const GridDev& G, int m, const double* fac, double* s
           rr = ri = pr_ = pi_ = 0.0;
         }
       } else if (i == nr) {
-        const double ir = idr / (double)(nr - 1);
+        const double ir = G.ir[nr];
         rr = -ir * dm * d1[nr];
         ri = ir * dm * d0[nr];
         pr_ = -idrh * (3.0 * d0[nr] - 4.0 * d0[nr - 1] + d0[nr - 2]);
         pi_ = -idrh * (3.0 * d1[nr] - 4.0 * d1[nr - 1] + d1[nr - 2]);
       } else {
-        const double ir = idr / (double)(i - 1);
+        const double ir = G.ir[i];
         rr = -ir * dm * d1[i];
         ri = ir * dm * d0[i];
         pr_ = -idrh * (d0[i + 1] - d0[i - 1]);
@@ -442,7 +454,7 @@ __device__ void op_bt_iter(const GridDev& G, int m, const double* fac, double* s
         s2im = idr * FLD(cu, 3, pi, 2, 2);
       }
     } else if (i == nr) {
-      const double ir = idr / (double)(nr - 1);
+      const double ir = G.ir[nr];
       s1re = -FLD(dcu, 2, pr, 1, nr) + dm * FLD(cu, 3, pi, 2, nr) * ir;
       s1im = -FLD(dcu, 2, pi, 1, nr) - dm * FLD(cu, 3, pr, 2, nr) * ir;
       s2re = FLD(dcu, 2, pr, 0, nr) +
@@ -450,7 +462,7 @@ __device__ void op_bt_iter(const GridDev& G, int m, const double* fac, double* s
       s2im = FLD(dcu, 2, pi, 0, nr) +
              idrh * (3.0 * FLD(cu, 3, pi, 2, nr) - 4.0 * FLD(cu, 3, pi, 2, nr - 1) + FLD(cu, 3, pi, 2, nr - 2));
     } else {
-      const double ir = idr / (double)(i - 1);
+      const double ir = G.ir[i];
       s1re = -FLD(dcu, 2, pr, 1, i) + dm * FLD(cu, 3, pi, 2, i) * ir;
       s1im = -FLD(dcu, 2, pi, 1, i) - dm * FLD(cu, 3, pr, 2, i) * ir;
       s2re = FLD(dcu, 2, pr, 0, i) + idrh * (FLD(cu, 3, pr, 2, i + 1) - FLD(cu, 3, pr, 2, i - 1));
@@ -509,13 +521,13 @@ __device__ void op_ez(const GridDev& G, int m, const double* fac, double* sm, do
       if (i == 1) {
         v = 0.0;   // set after the reduction
       } else if (i == nr - 1) {
-        const double ir = idr / (double)(nr - 2);
+        const double ir = G.ir[nr - 1];
         v = idrh * (FLD(cu, 3, 0, 0, nr) - FLD(cu, 3, 0, 0, nr - 2)) + ir * FLD(cu, 3, 0, 0, nr - 1);
       } else if (i == nr) {
-        const double ir = idr / (double)(nr - 1);
+        const double ir = G.ir[nr];
         v = idr * (FLD(cu, 3, 0, 0, nr) - FLD(cu, 3, 0, 0, nr - 1)) + ir * FLD(cu, 3, 0, 0, nr);
       } else {
-        const double ir = idr / (double)(i - 1);
+        const double ir = G.ir[i];
         v = idrh * (FLD(cu, 3, 0, 0, i + 1) - FLD(cu, 3, 0, 0, i - 1)) + ir * FLD(cu, 3, 0, 0, i);
         div += v * (double)(i - 1);
       }
@@ -530,7 +542,7 @@ __device__ void op_ez(const GridDev& G, int m, const double* fac, double* sm, do
     for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
       double re, im;
       if (i == nr) {
-        const double ir = idr / (double)(nr - 1);
+        const double ir = G.ir[nr];
         re = idrh * (3.0 * FLD(cu, 3, pr, 0, nr) - 4.0 * FLD(cu, 3, pr, 0, nr - 1) + FLD(cu, 3, pr, 0, nr - 2)) +
              ir * FLD(cu, 3, pr, 0, nr) - dm * ir * FLD(cu, 3, pi, 1, nr);
         im = idrh * (3.0 * FLD(cu, 3, pi, 0, nr) - 4.0 * FLD(cu, 3, pi, 0, nr - 1) + FLD(cu, 3, pi, 0, nr - 2)) +
@@ -550,7 +562,7 @@ __device__ void op_ez(const GridDev& G, int m, const double* fac, double* sm, do
         im = idr * (FLD(cu, 3, pi, 0, 3) - FLD(cu, 3, pi, 0, 2)) + ir * FLD(cu, 3, pi, 0, 2) +
              dm * ir * FLD(cu, 3, pr, 1, 2);
       } else {
-        const double ir = idr / (double)(i - 1);
+        const double ir = G.ir[i];
         re = idrh * (FLD(cu, 3, pr, 0, i + 1) - FLD(cu, 3, pr, 0, i - 1)) + ir * FLD(cu, 3, pr, 0, i) -
              dm * ir * FLD(cu, 3, pi, 1, i);
         im = idrh * (FLD(cu, 3, pi, 0, i + 1) - FLD(cu, 3, pi, 0, i - 1)) + ir * FLD(cu, 3, pi, 0, i) +
@@ -605,7 +617,7 @@ __device__ void op_et(const GridDev& G, int m, const double* __restrict__ b, con
           r0 = i0 = r1 = i1 = 0.0;
         }
       } else {
-        const double ir = idr / (double)(i - 1);
+        const double ir = G.ir[i];
         if (i == nr) {
           r0 = FLD(b, 3, pr, 1, nr) + idrh * (4.0 * FLD(psi, 1, pr, 0, nr - 1) - FLD(psi, 1, pr, 0, nr - 2) -
                                               3.0 * FLD(psi, 1, pr, 0, nr));
@@ -641,11 +653,11 @@ __device__ void op_djdxi(const GridDev& G, int m, const double* __restrict__ acu
         v0 = 0.0;
         v1 = 0.0;
       } else if (i == nr) {
-        const double ir = idr / (double)(nr - 1);
+        const double ir = G.ir[nr];
         v0 = A_(0, 0, nr) + idrh * (4.0 * U_(0, 0, nr - 1) - U_(0, 0, nr - 2) - 3.0 * U_(0, 0, nr)) - ir * U_(0, 0, nr);
         v1 = A_(0, 1, nr) + idrh * (4.0 * U_(0, 1, nr - 1) - U_(0, 1, nr - 2) - 3.0 * U_(0, 1, nr)) - ir * U_(0, 1, nr);
       } else {
-        const double ir = idr / (double)(i - 1);
+        const double ir = G.ir[i];
         v0 = A_(0, 0, i) - idrh * (U_(0, 0, i + 1) - U_(0, 0, i - 1)) - ir * U_(0, 0, i);
         v1 = A_(0, 1, i) - idrh * (U_(0, 1, i + 1) - U_(0, 1, i - 1)) - ir * U_(0, 1, i);
       }
@@ -666,7 +678,7 @@ __device__ void op_djdxi(const GridDev& G, int m, const double* __restrict__ acu
           a0 = a1 = b0 = b1 = 0.0;
         }
       } else if (i == nr) {
-        const double ir = idr / (double)(nr - 1);
+        const double ir = G.ir[nr];
         a0 = A_(r, 0, nr) + idrh * (4.0 * U_(r, 0, nr - 1) - U_(r, 0, nr - 2) - 3.0 * U_(r, 0, nr)) - ir * U_(r, 0, nr) + dm * ir * U_(s, 1, nr);
         a1 = A_(r, 1, nr) + idrh * (4.0 * U_(r, 1, nr - 1) - U_(r, 1, nr - 2) - 3.0 * U_(r, 1, nr)) - ir * U_(r, 1, nr) + dm * ir * U_(s, 2, nr);
         b0 = A_(s, 0, nr) + idrh * (4.0 * U_(s, 0, nr - 1) - U_(s, 0, nr - 2) - 3.0 * U_(s, 0, nr)) - ir * U_(s, 0, nr) - dm * ir * U_(r, 1, nr);
@@ -678,7 +690,7 @@ __device__ void op_djdxi(const GridDev& G, int m, const double* __restrict__ acu
         b0 = A_(s, 0, 2) - idr * (U_(s, 0, 3) - U_(s, 0, 2)) - ir * U_(s, 0, 2) - dm * ir * U_(r, 1, 2);
         b1 = A_(s, 1, 2) - idr * (U_(s, 1, 3) - U_(s, 1, 2)) - ir * U_(s, 1, 2) - dm * ir * U_(r, 2, 2);
       } else {
-        const double ir = idr / (double)(i - 1);
+        const double ir = G.ir[i];
         a0 = A_(r, 0, i) - idrh * (U_(r, 0, i + 1) - U_(r, 0, i - 1)) - ir * U_(r, 0, i) + dm * ir * U_(s, 1, i);
         a1 = A_(r, 1, i) - idrh * (U_(r, 1, i + 1) - U_(r, 1, i - 1)) - ir * U_(r, 1, i) + dm * ir * U_(s, 2, i);
         b0 = A_(s, 0, i) - idrh * (U_(s, 0, i + 1) - U_(s, 0, i - 1)) - ir * U_(s, 0, i) - dm * ir * U_(r, 1, i);
@@ -708,7 +720,7 @@ __device__ void op_finish_q(const GridDev& G, int m, const double* __restrict__ 
       double v;
       if (i == 0) v = 0.0;
       else if (i == 1) v = (m == 0) ? 8.0 * r : 0.0;
-      else v = r * (1.0 / (double)(i - 1));
+      else v = r * G.inv[i];
       if (qn) v = (0.0 + v) + FLD(qn, 1, p, 0, i);
       FLD(out, 1, p, 0, i) = v;
     }
@@ -738,7 +750,7 @@ __device__ void op_finish_amj(const GridDev& G, int m, double* __restrict__ cu, 
         for (int c = 0; c < 2; ++c) FLD(acu, 2, p, c, 1) = fac_ == 0.0 ? 0.0 : fac_ * FLD(acu, 2, p, c, 1);
         for (int c = 0; c < 3; ++c) FLD(amu, 3, p, c, 1) = fam == 0.0 ? 0.0 : fam * FLD(amu, 3, p, c, 1);
       } else {
-        const double ir = 1.0 / (double)(i - 1);
+        const double ir = G.inv[i];
         for (int c = 0; c < 3; ++c) {
           FLD(cu, 3, p, c, i) = FLD(cu, 3, p, c, i) * ir;
           FLD(amu, 3, p, c, i) = FLD(amu, 3, p, c, i) * ir;

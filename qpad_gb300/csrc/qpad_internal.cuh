@@ -32,6 +32,10 @@ enum OpKind { OK_GEN = 0, OK_BT = 1, OK_BPLUS = 2, OK_BMINUS = 3, OK_NKINDS = 4 
 struct GridDev {
   int nr, nz, M, P, ld, bnd;
   double dr, dxi, idr, relax_fac;
+  // per-node factors of the reference's finite differences and deposit scaling, computed
+  // once with the same FP64 expressions: ir[i] = idr / (i-1), inv[i] = 1 / (i-1) (i >= 2)
+  const double* ir;
+  const double* inv;
 };
 
 __host__ __device__ inline int part_re(int m) { return m == 0 ? 0 : 2 * m - 1; }
@@ -62,6 +66,7 @@ struct qpad_ctx {
   int device;
   cudaStream_t stream = nullptr;
   double* fac = nullptr;                       // device factor tables
+  double* rtab = nullptr;                      // ir / inv node tables (2 x ld)
   double* f[QPAD_NFIELDS] = {};                // slice fields
   double* f2[QPAD_NFIELDS] = {};               // 3D stores (only some fields have one)
   double* qn = nullptr;                        // neutralising background (sum over species)
