@@ -156,6 +156,17 @@ int qpad_species_count(qpad_species* sp, int64_t* np);
 int qpad_species_qdp(qpad_species* sp, int q);
 /* species2d::amjdp (species2d_class.f03:233-280): cu, amu, dcu += deposits */
 int qpad_species_amjdp(qpad_species* sp, int ef, int bf, int cu, int amu, int dcu, double dt);
+/* No counterpart in the reference.  Same arguments and result as qpad_species_amjdp, but
+ * the call allocates no device memory (no cudaMalloc, cudaFree or allocating library
+ * routine), for callers whose device memory is fixed by their own pool or that must not
+ * allocate once the run has started.  Its deposit scratch is one static device array of
+ * 1 MiB (131072 doubles) in the library image, held on every GPU that loads the library
+ * until the process exits; grids with 8 * (2*max_mode+1) * (nr+2) > 131072 are rejected
+ * with QPAD_E_CAPACITY.  The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  All calls in
+ * the process share the one array, so calls that overlap on the GPU (other streams, other
+ * contexts on the same device) race; calls on one stream are ordered and safe. */
+int qpad_species_amjdp_noalloc(qpad_species* sp, int ef, int bf, int cu, int amu, int dcu, double dt);
 /* species2d::push_u (species2d_class.f03:282-309) */
 int qpad_species_push_u(qpad_species* sp, int ef, int bf, double dt);
 /* species2d::push_x (species2d_class.f03:311-327): push_x + update_bound */

@@ -99,6 +99,8 @@ _SIGS = {
     "qpad_species_count": (C.c_int, [C.c_void_p, I64P]),
     "qpad_species_qdp": (C.c_int, [C.c_void_p, C.c_int]),
     "qpad_species_amjdp": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]),
+    "qpad_species_amjdp_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                             C.c_double]),
     "qpad_species_push_u": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double]),
     "qpad_species_push_x": (C.c_int, [C.c_void_p, C.c_double]),
     "qpad_species_interp_psi": (C.c_int, [C.c_void_p, C.c_int]),

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -736,6 +737,77 @@ extern "C" int qpad_species_amjdp(qpad_species* sp, int ef, int bf, int cu, int 
   k_add<<<elem_grid(n3), 256, 0, ctx->stream>>>(ctx->f[amu], samu, ctx->f[amu], n3);
   k_add<<<elem_grid(n2), 256, 0, ctx->stream>>>(ctx->f[dcu], sacu, ctx->f[dcu], n2);
   return check_launch(ctx, "amjdp add", 3);
+}
+
+// ---- current deposit without any device allocation ---------------------------------
+// qpad_species_amjdp allocates its deposit scratch with cudaMalloc on its first call.
+// Some callers cannot allow that: a host code whose device memory is handed out by its
+// own pool and capped at start-up, a caller that runs under a tool or a stream-ordered
+// allocator where a stray cudaMalloc fails or stalls the device, or a caller that wants
+// every allocation of the run to happen before its first slice.  For them the deposit
+// scratch below is a fixed device array in this library's module image: the CUDA driver
+// reserves it when the module loads, on every GPU that loads the library, and it stays
+// reserved until the process exits.  Its size is fixed at kNoAllocScratchDoubles doubles
+// (1 MiB); a grid needing more is rejected with QPAD_E_CAPACITY.
+namespace {
+constexpr size_t kNoAllocScratchDoubles = (size_t)1 << 17;
+constexpr int kNoAllocMaxDevices = 64;
+__device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// In host code g_noalloc_scratch names a host-side shadow, not device memory: the device
+// address comes from cudaGetSymbolAddress, taken once per device with that device current.
+int noalloc_scratch(qpad_ctx* ctx, double** out) {
+  const int dev = ctx->device;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return set_err(ctx, QPAD_E_ARG, "no-alloc amjdp: device ordinal");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    int cur = -1;
+    if (int r = cuda_check(ctx, cudaGetDevice(&cur), "cudaGetDevice")) return r;
+    if (cur != dev)
+      if (int r = cuda_check(ctx, cudaSetDevice(dev), "cudaSetDevice")) return r;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (cur != dev) cudaSetDevice(cur);
+    if (int r = cuda_check(ctx, e, "cudaGetSymbolAddress")) return r;
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return QPAD_OK;
+}
+}  // namespace
+
+extern "C" int qpad_species_amjdp_noalloc(qpad_species* sp, int ef, int bf, int cu, int amu, int dcu, double dt) {
+  if (!sp || !valid_field(ef) || !valid_field(bf) || !valid_field(cu) || !valid_field(amu) || !valid_field(dcu) ||
+      field_ncomp(ef) != 3 || field_ncomp(bf) != 3 || field_ncomp(cu) != 3 || field_ncomp(amu) != 3 ||
+      field_ncomp(dcu) != 2 || !(dt > 0))
+    return sp ? set_err(sp->ctx, QPAD_E_ARG, "amjdp_noalloc: bad args") : QPAD_E_ARG;
+  qpad_ctx* ctx = sp->ctx;
+  const size_t n3 = f1_elems(ctx, QPAD_F_CU), n2 = f1_elems(ctx, QPAD_F_ACU);
+  if (2 * n3 + n2 > kNoAllocScratchDoubles)
+    return set_err(ctx, QPAD_E_CAPACITY,
+                   "amjdp_noalloc: grid needs " + std::to_string(2 * n3 + n2) + " scratch doubles, limit is " +
+                       std::to_string(kNoAllocScratchDoubles) + " (8 * (2*max_mode+1) * (nr+2) must fit)");
+  double* scu = nullptr;
+  if (int r = noalloc_scratch(ctx, &scu)) return r;
+  double* samu = scu + n3;
+  double* sacu = samu + n3;
+  // the array keeps whatever the previous call left in it
+  if (cudaMemsetAsync(scu, 0, (2 * n3 + n2) * sizeof(double), ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "memset");
+  if (is_mixed(sp)) {
+    if (int r = launch_gtab(ctx, ctx->f[ef], ctx->f[bf])) return r;
+    if (int r = mixed_amjdp_raw(sp, ctx->gtab, scu, samu, sacu, dt)) return r;
+  } else {
+    if (int r = species_amjdp_raw(sp, ctx->f[ef], ctx->f[bf], scu, samu, sacu, dt)) return r;
+  }
+  if (int r = launch_finish_amj(ctx, scu, samu, sacu)) return r;
+  k_add<<<elem_grid(n3), 256, 0, ctx->stream>>>(ctx->f[cu], scu, ctx->f[cu], n3);
+  k_add<<<elem_grid(n3), 256, 0, ctx->stream>>>(ctx->f[amu], samu, ctx->f[amu], n3);
+  k_add<<<elem_grid(n2), 256, 0, ctx->stream>>>(ctx->f[dcu], sacu, ctx->f[dcu], n2);
+  return check_launch(ctx, "amjdp_noalloc add", 3);
 }
 
 extern "C" int qpad_species_push_u(qpad_species* sp, int ef, int bf, double dt) {
