@@ -91,7 +91,12 @@ class ClockSampler:
 
 def _deck(args):
     from qpad_gb300 import decks
-    return decks.DECKS[args.deck]()
+    d = decks.DECKS[args.deck]()
+    if args.slices:
+        # profiling runs: the same slice workload over fewer slices
+        d.nz = args.slices
+        d.name = f"{d.name}_nz{args.slices}"
+    return d
 
 
 def cpu_sample(deck, nslices, steps=1, nthreads=None):
@@ -177,6 +182,7 @@ def run_ours(args):
     prec = K.PREC_FP64 if args.precision == "fp64" else K.PREC_MIXED
     inputs = Q.deck_inputs(deck)
     sim = Q.build_simulation(deck, precision=prec, device=local, inputs=inputs)
+    sim.use_graph(args.graph == "on")
     sp = sim.species[0]
     npl = len(inputs[0][4])
     nbeam = sum(len(b[2]) for b in inputs[1])
@@ -213,9 +219,10 @@ def run_ours(args):
     sim.profile(True)
     sp.reset()
     sim.run_3d_step()
-    kern = {k: sim.profile_read(k) for k in ("amjdp", "push", "qdeposit", "beam_push", "beam_qdeposit", "step")}
+    kern = {k: sim.profile_read(k) for k in ("amjdp", "iterate", "push", "qdeposit", "slice_begin", "iter_e",
+                                             "slice_end", "conv", "beam_push", "beam_qdeposit", "step")}
     sim.profile(False)
-    sim.use_graph(True)
+    sim.use_graph(args.graph == "on")
     amj_ms, namj = kern["amjdp"]
     barrier()
     pushes_step = npl * deck.nz
@@ -295,6 +302,9 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--cpu-slices", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--slices", type=int, default=0, help="override the deck's slice count (profiling runs)")
+    ap.add_argument("--graph", default="on", choices=["on", "off"],
+                    help="off: host-driven slice loop (one launch per kernel, visible to per-kernel profilers)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -1213,6 +1213,9 @@ int64_t orc_load_beam(const orc_grid* g, orc_rng* r, const orc_beam_desc* d, dou
   const double er = (double)g->nr * dr, ez = (double)g->nz * dz;
   const double q_per_part = (d->qm >= 0.0 ? 1.0 : -1.0) * d->tot_charge /
                             (2.0 * ORC_PI * (double)d->tot_num * (dr * dr) * dz);
+  /* an empty sampling range would make the rejection loop below endless */
+  for (int k = 0; k < 3; ++k)
+    if (!(d->range_lo[k] < d->range_hi[k]) || !(d->sigma[k] > 0.0)) return -1;
   int64_t n = 0;
   for (int64_t i = 0; i < d->tot_num; ++i) {
     double xt[3];

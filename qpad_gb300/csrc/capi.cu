@@ -314,7 +314,14 @@ extern "C" int qpad_ctx_create(const qpad_grid_desc* d, qpad_ctx** out) {
   if (!r) r = dmalloc(ctx, (void**)&ctx->d_stats, (size_t)g.nz * sizeof(qpad_slice_stats), "slice stats");
   if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->h_j, 2 * sizeof(int)), "pinned slice index");
   if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->h_res, 8 * sizeof(double)), "pinned");
+  if (!r) r = dmalloc(ctx, (void**)&ctx->raw, 8 * (size_t)g.P * g.ld * sizeof(double), "raw deposits");
+  if (!r) r = dmalloc(ctx, (void**)&ctx->iter_tickets, 64 * sizeof(unsigned int), "iteration tickets");
+  if (!r) r = cuda_check(ctx, cudaMemsetAsync(ctx->raw, 0, 8 * (size_t)g.P * g.ld * sizeof(double), ctx->stream),
+                         "raw deposits");
+  if (!r) r = cuda_check(ctx, cudaMemsetAsync(ctx->iter_tickets, 0, 64 * sizeof(unsigned int), ctx->stream),
+                         "iteration tickets");
   if (!r) r = build_factors(ctx);
+  if (!r) r = iterate_setup(ctx);
   if (!r) r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "create sync");
   if (r) {
     g_create_err = ctx->err;
@@ -340,6 +347,8 @@ extern "C" int qpad_ctx_destroy(qpad_ctx* ctx) {
   if (ctx->rtab) cudaFree(ctx->rtab);
   if (ctx->qn) cudaFree(ctx->qn);
   if (ctx->qraw) cudaFree(ctx->qraw);
+  if (ctx->raw) cudaFree(ctx->raw);
+  if (ctx->iter_tickets) cudaFree(ctx->iter_tickets);
   if (ctx->conv) cudaFree(ctx->conv);
   if (ctx->scratch) cudaFree(ctx->scratch);
   if (ctx->gtab) cudaFree(ctx->gtab);
@@ -960,6 +969,8 @@ int enqueue_slice_prologue(qpad_ctx* ctx, cudaGraphConditionalHandle hi, int use
   for (auto* s : ctx->species)
     if (int r = mixed ? mixed_qdeposit_raw(s, ctx->qraw) : species_qdeposit_raw(s, ctx->qraw)) return r;
   if (int r = launch_slice_begin(ctx, any_ntd)) return r;
+  // E of the first iteration (later iterations get theirs from k_iterate)
+  if (int r = launch_iter_e(ctx)) return r;
   for (auto* s : ctx->species)
     if (s->push_type == QPAD_PUSH2_STD)
       if (int r = mixed ? mixed_interp_psi(s, ctx->f[QPAD_F_PSI]) : species_interp_psi(s, ctx->f[QPAD_F_PSI]))
@@ -968,18 +979,20 @@ int enqueue_slice_prologue(qpad_ctx* ctx, cudaGraphConditionalHandle hi, int use
 }
 
 // One predictor-corrector iteration (simulation_class.f03:372-396).
+// The deposit goes to the raw buffers; k_iterate finishes it, solves B-perp, Bz and the
+// next iteration's E, and runs the convergence test.
 int enqueue_iteration(qpad_ctx* ctx, cudaGraphConditionalHandle h, int use_h) {
   const bool mixed = ctx->precision == QPAD_PREC_MIXED;
-  if (int r = launch_iter_e(ctx)) return r;
+  const size_t P1 = (size_t)ctx->g.P * ctx->g.ld;
+  double* rcu = ctx->raw;
+  double* ramu = ctx->raw + 3 * P1;
+  double* racu = ctx->raw + 6 * P1;
   for (auto* s : ctx->species) {
-    const int r = mixed ? mixed_amjdp_raw(s, ctx->gtab, ctx->f[QPAD_F_CU], ctx->f[QPAD_F_AMU], ctx->f[QPAD_F_ACU],
-                                          ctx->g.dxi)
-                        : species_amjdp_raw(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], ctx->f[QPAD_F_CU],
-                                            ctx->f[QPAD_F_AMU], ctx->f[QPAD_F_ACU], ctx->g.dxi);
+    const int r = mixed ? mixed_amjdp_raw(s, ctx->gtab, rcu, ramu, racu, ctx->g.dxi)
+                        : species_amjdp_raw(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], rcu, ramu, racu, ctx->g.dxi);
     if (r) return r;
   }
-  if (int r = launch_iter_b(ctx)) return r;
-  return launch_conv(ctx, ctx->f[QPAD_F_B_SPE], 1, 1, 1, h, use_h);
+  return launch_iterate(ctx, 1, h, use_h);
 }
 
 // Epilogue (simulation_class.f03:403-456): stores, final fields, J-perp predictor, push.

@@ -15,7 +15,7 @@
 #include <cstdio>
 #include <vector>
 
-#include "qpad_internal.cuh"
+#include "stencils.cuh"
 
 namespace qpad {
 
@@ -266,56 +266,6 @@ __device__ void op_psi(const GridDev& G, int m, const double* fac, double* sm, d
   __syncthreads();
 }
 
-// Bz source: field_b_class.f03:205-307
-__device__ __forceinline__ void src_bz_row(const GridDev& G, int m, int i, const double* __restrict__ cu,
-                                           double& re, double& im) {
-  const int nr = G.nr;
-  const double idr = G.idr, idrh = 0.5 * idr;
-  if (m == 0) {
-    if (i == 1) {
-      re = -2.0 * idr * FLD(cu, 3, 0, 1, 2);
-    } else if (i == nr) {
-      const double ir = G.ir[nr];
-      re = -idrh * (3.0 * FLD(cu, 3, 0, 1, nr) - 4.0 * FLD(cu, 3, 0, 1, nr - 1) + FLD(cu, 3, 0, 1, nr - 2)) -
-           ir * FLD(cu, 3, 0, 1, nr);
-    } else {
-      const double ir = G.ir[i];
-      re = -idrh * (FLD(cu, 3, 0, 1, i + 1) - FLD(cu, 3, 0, 1, i - 1)) - ir * FLD(cu, 3, 0, 1, i);
-    }
-    im = 0.0;
-    return;
-  }
-  const int pr = part_re(m), pi = part_im(m);
-  const double dm = (double)m;
-  if (i == nr) {
-    const double ir = G.ir[nr];
-    re = -idrh * (3.0 * FLD(cu, 3, pr, 1, nr) - 4.0 * FLD(cu, 3, pr, 1, nr - 1) + FLD(cu, 3, pr, 1, nr - 2)) -
-         ir * FLD(cu, 3, pr, 1, nr) - dm * ir * FLD(cu, 3, pi, 0, nr);
-    im = -idrh * (3.0 * FLD(cu, 3, pi, 1, nr) - 4.0 * FLD(cu, 3, pi, 1, nr - 1) + FLD(cu, 3, pi, 1, nr - 2)) -
-         ir * FLD(cu, 3, pi, 1, nr) + dm * ir * FLD(cu, 3, pr, 0, nr);
-  } else if (i == 1) {
-    if (m % 2 == 0) {
-      re = -2.0 * idr * FLD(cu, 3, pr, 1, 2) - dm * idr * FLD(cu, 3, pi, 0, 2);
-      im = -2.0 * idr * FLD(cu, 3, pi, 1, 2) + dm * idr * FLD(cu, 3, pr, 0, 2);
-    } else {
-      re = 0.0;
-      im = 0.0;
-    }
-  } else if (i == 2 && m == 1) {
-    const double ir = idr;
-    re = -idr * (FLD(cu, 3, pr, 1, 3) - FLD(cu, 3, pr, 1, 2)) - ir * FLD(cu, 3, pr, 1, 2) -
-         dm * ir * FLD(cu, 3, pi, 0, 2);
-    im = -idr * (FLD(cu, 3, pi, 1, 3) - FLD(cu, 3, pi, 1, 2)) - ir * FLD(cu, 3, pi, 1, 2) +
-         dm * ir * FLD(cu, 3, pr, 0, 2);
-  } else {
-    const double ir = G.ir[i];
-    re = -idrh * (FLD(cu, 3, pr, 1, i + 1) - FLD(cu, 3, pr, 1, i - 1)) - ir * FLD(cu, 3, pr, 1, i) -
-         dm * ir * FLD(cu, 3, pi, 0, i);
-    im = -idrh * (FLD(cu, 3, pi, 1, i + 1) - FLD(cu, 3, pi, 1, i - 1)) - ir * FLD(cu, 3, pi, 1, i) +
-         dm * ir * FLD(cu, 3, pr, 0, i);
-  }
-}
-
 // Bz: field_b_class.f03:508-543, 760-796
 __device__ void op_bz(const GridDev& G, int m, const double* fac, double* sm, double* sc,
                       const double* __restrict__ cu, double* __restrict__ b) {
@@ -324,7 +274,7 @@ __device__ void op_bz(const GridDev& G, int m, const double* fac, double* sm, do
   double* d1 = sm + (nr + 2);
   for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
     double re, im;
-    src_bz_row(G, m, i, cu, re, im);
+    row_bz_src(G, m, i, GlobalF{cu, G.ld, 3}, re, im);
     d0[i] = re;
     d1[i] = im;
   }
@@ -397,34 +347,26 @@ __device__ void op_bt_beam(const GridDev& G, int m, const double* fac, double* s
 __device__ void op_bt_iter(const GridDev& G, int m, const double* fac, double* sm, double* sc,
                            const double* __restrict__ dcu, const double* __restrict__ cu, double* __restrict__ b) {
   const int nr = G.nr;
-  const double idr = G.idr, idrh = 0.5 * idr, rix = G.relax_fac * (idr * idr), dm = (double)m;
   double* b1re = sm;
   double* b1im = sm + (nr + 2);
   double* b2re = sm + 2 * (nr + 2);
   double* b2im = sm + 3 * (nr + 2);
-  if (m == 0) {
-    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
-      double v1, v2;
-      if (i == 1) {
-        v1 = 0.0;
-        v2 = 0.0;
-      } else if (i == nr) {
-        v1 = -FLD(dcu, 2, 0, 1, nr) - FLD(b, 3, 0, 0, nr) * rix;
-        v2 = FLD(dcu, 2, 0, 0, nr) +
-             idrh * (3.0 * FLD(cu, 3, 0, 2, nr) - 4.0 * FLD(cu, 3, 0, 2, nr - 1) + FLD(cu, 3, 0, 2, nr - 2)) -
-             FLD(b, 3, 0, 1, nr) * rix;
-      } else if (i == 2) {
-        v1 = -FLD(dcu, 2, 0, 1, 2) - FLD(b, 3, 0, 0, 2) * rix;
-        v2 = FLD(dcu, 2, 0, 0, 2) + idr * (FLD(cu, 3, 0, 2, 3) - FLD(cu, 3, 0, 2, 2)) - FLD(b, 3, 0, 1, 2) * rix;
-      } else {
-        v1 = -FLD(dcu, 2, 0, 1, i) - FLD(b, 3, 0, 0, i) * rix;
-        v2 = FLD(dcu, 2, 0, 0, i) + idrh * (FLD(cu, 3, 0, 2, i + 1) - FLD(cu, 3, 0, 2, i - 1)) -
-             FLD(b, 3, 0, 1, i) * rix;
-      }
-      b1re[i] = v1;
-      b2re[i] = v2;
+  const GlobalF DC{dcu, G.ld, 2}, CU{cu, G.ld, 3}, BO{b, G.ld, 3};
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    double o[4];
+    row_btiter_src(G, m, i, DC, CU, BO, o);
+    if (m == 0) {
+      b1re[i] = o[0];
+      b2re[i] = o[1];
+    } else {
+      b1re[i] = o[0];
+      b1im[i] = o[1];
+      b2re[i] = o[2];
+      b2im[i] = o[3];
     }
-    __syncthreads();
+  }
+  __syncthreads();
+  if (m == 0) {
     const double* w = fac + fac_off(nr, G.M, OK_BPLUS, 0);
     tri_solve<1>(nr, w, w + nr, w + 2 * nr, b1re + 1, b1re + 1, sc);
     w = fac + fac_off(nr, G.M, OK_BMINUS, 0);
@@ -437,45 +379,6 @@ __device__ void op_bt_iter(const GridDev& G, int m, const double* fac, double* s
     return;
   }
   const int pr = part_re(m), pi = part_im(m);
-  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
-    double s1re, s1im, s2re, s2im;
-    if (i == 1) {
-      if (m == 1) {
-        s1re = -FLD(dcu, 2, pr, 1, 1) + idr * dm * FLD(cu, 3, pi, 2, 2);
-        s1im = -FLD(dcu, 2, pi, 1, 1) - idr * dm * FLD(cu, 3, pr, 2, 2);
-        s2re = FLD(dcu, 2, pr, 0, 1) + idr * FLD(cu, 3, pr, 2, 2);
-        s2im = FLD(dcu, 2, pi, 0, 1) + idr * FLD(cu, 3, pi, 2, 2);
-      } else if (m % 2 == 0) {
-        s1re = s1im = s2re = s2im = 0.0;
-      } else {
-        s1re = idr * dm * FLD(cu, 3, pi, 2, 2);
-        s1im = idr * dm * FLD(cu, 3, pr, 2, 2);
-        s2re = idr * FLD(cu, 3, pr, 2, 2);
-        s2im = idr * FLD(cu, 3, pi, 2, 2);
-      }
-    } else if (i == nr) {
-      const double ir = G.ir[nr];
-      s1re = -FLD(dcu, 2, pr, 1, nr) + dm * FLD(cu, 3, pi, 2, nr) * ir;
-      s1im = -FLD(dcu, 2, pi, 1, nr) - dm * FLD(cu, 3, pr, 2, nr) * ir;
-      s2re = FLD(dcu, 2, pr, 0, nr) +
-             idrh * (3.0 * FLD(cu, 3, pr, 2, nr) - 4.0 * FLD(cu, 3, pr, 2, nr - 1) + FLD(cu, 3, pr, 2, nr - 2));
-      s2im = FLD(dcu, 2, pi, 0, nr) +
-             idrh * (3.0 * FLD(cu, 3, pi, 2, nr) - 4.0 * FLD(cu, 3, pi, 2, nr - 1) + FLD(cu, 3, pi, 2, nr - 2));
-    } else {
-      const double ir = G.ir[i];
-      s1re = -FLD(dcu, 2, pr, 1, i) + dm * FLD(cu, 3, pi, 2, i) * ir;
-      s1im = -FLD(dcu, 2, pi, 1, i) - dm * FLD(cu, 3, pr, 2, i) * ir;
-      s2re = FLD(dcu, 2, pr, 0, i) + idrh * (FLD(cu, 3, pr, 2, i + 1) - FLD(cu, 3, pr, 2, i - 1));
-      s2im = FLD(dcu, 2, pi, 0, i) + idrh * (FLD(cu, 3, pi, 2, i + 1) - FLD(cu, 3, pi, 2, i - 1));
-    }
-    const double br0 = FLD(b, 3, pr, 0, i), bi0 = FLD(b, 3, pi, 0, i);
-    const double br1 = FLD(b, 3, pr, 1, i), bi1 = FLD(b, 3, pi, 1, i);
-    b1re[i] = s1re - s2im - (br0 - bi1) * rix;
-    b1im[i] = s1im + s2re - (bi0 + br1) * rix;
-    b2re[i] = s1re + s2im - (br0 + bi1) * rix;
-    b2im[i] = s1im - s2re - (bi0 - br1) * rix;
-  }
-  __syncthreads();
   const double* w = fac + fac_off(nr, G.M, OK_BPLUS, m);
   tri_solve<2>(nr, w, w + nr, w + 2 * nr, b1re + 1, b1im + 1, sc);
   w = fac + fac_off(nr, G.M, OK_BMINUS, m);
@@ -511,66 +414,21 @@ __device__ double block_sum(double v, double* sc) {
 __device__ void op_ez(const GridDev& G, int m, const double* fac, double* sm, double* sc,
                       const double* __restrict__ cu, double* __restrict__ e) {
   const int nr = G.nr, pr = part_re(m), pi = part_im(m);
-  const double idr = G.idr, idrh = 0.5 * idr, dm = (double)m;
   double* d0 = sm;
   double* d1 = sm + (nr + 2);
+  const GlobalF CU{cu, G.ld, 3};
+  double div = 0.0;
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
+    double re, im;
+    bool in_div;
+    row_ez_src(G, m, i, CU, re, im, in_div);
+    if (in_div) div += re * (double)(i - 1);
+    d0[i] = re;
+    if (m > 0) d1[i] = im;
+  }
   if (m == 0) {
-    double div = 0.0;
-    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
-      double v;
-      if (i == 1) {
-        v = 0.0;   // set after the reduction
-      } else if (i == nr - 1) {
-        const double ir = G.ir[nr - 1];
-        v = idrh * (FLD(cu, 3, 0, 0, nr) - FLD(cu, 3, 0, 0, nr - 2)) + ir * FLD(cu, 3, 0, 0, nr - 1);
-      } else if (i == nr) {
-        const double ir = G.ir[nr];
-        v = idr * (FLD(cu, 3, 0, 0, nr) - FLD(cu, 3, 0, 0, nr - 1)) + ir * FLD(cu, 3, 0, 0, nr);
-      } else {
-        const double ir = G.ir[i];
-        v = idrh * (FLD(cu, 3, 0, 0, i + 1) - FLD(cu, 3, 0, 0, i - 1)) + ir * FLD(cu, 3, 0, 0, i);
-        div += v * (double)(i - 1);
-      }
-      d0[i] = v;
-    }
     div = block_sum(div, sc);
-    if (threadIdx.x == 0) {
-      div = div - idrh * (FLD(cu, 3, 0, 0, nr - 2) + FLD(cu, 3, 0, 0, nr - 1)) * ((double)nr - 2.5);
-      d0[1] = -8.0 * div;
-    }
-  } else {
-    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
-      double re, im;
-      if (i == nr) {
-        const double ir = G.ir[nr];
-        re = idrh * (3.0 * FLD(cu, 3, pr, 0, nr) - 4.0 * FLD(cu, 3, pr, 0, nr - 1) + FLD(cu, 3, pr, 0, nr - 2)) +
-             ir * FLD(cu, 3, pr, 0, nr) - dm * ir * FLD(cu, 3, pi, 1, nr);
-        im = idrh * (3.0 * FLD(cu, 3, pi, 0, nr) - 4.0 * FLD(cu, 3, pi, 0, nr - 1) + FLD(cu, 3, pi, 0, nr - 2)) +
-             ir * FLD(cu, 3, pi, 0, nr) + dm * ir * FLD(cu, 3, pr, 1, nr);
-      } else if (i == 1) {
-        if (m % 2 == 0) {
-          re = 2.0 * idr * FLD(cu, 3, pr, 0, 2) - dm * idr * FLD(cu, 3, pi, 1, 2);
-          im = 2.0 * idr * FLD(cu, 3, pi, 0, 2) + dm * idr * FLD(cu, 3, pr, 1, 2);
-        } else {
-          re = 0.0;
-          im = 0.0;
-        }
-      } else if (i == 2 && m == 1) {
-        const double ir = idr;
-        re = idr * (FLD(cu, 3, pr, 0, 3) - FLD(cu, 3, pr, 0, 2)) + ir * FLD(cu, 3, pr, 0, 2) -
-             dm * ir * FLD(cu, 3, pi, 1, 2);
-        im = idr * (FLD(cu, 3, pi, 0, 3) - FLD(cu, 3, pi, 0, 2)) + ir * FLD(cu, 3, pi, 0, 2) +
-             dm * ir * FLD(cu, 3, pr, 1, 2);
-      } else {
-        const double ir = G.ir[i];
-        re = idrh * (FLD(cu, 3, pr, 0, i + 1) - FLD(cu, 3, pr, 0, i - 1)) + ir * FLD(cu, 3, pr, 0, i) -
-             dm * ir * FLD(cu, 3, pi, 1, i);
-        im = idrh * (FLD(cu, 3, pi, 0, i + 1) - FLD(cu, 3, pi, 0, i - 1)) + ir * FLD(cu, 3, pi, 0, i) +
-             dm * ir * FLD(cu, 3, pr, 1, i);
-      }
-      d0[i] = re;
-      d1[i] = im;
-    }
+    if (threadIdx.x == 0) d0[1] = ez_axis_row(G, div, CU);
   }
   __syncthreads();
   solve_mode(G, fac, OK_GEN, m, d0 + 1, m > 0 ? d1 + 1 : nullptr, sc);
@@ -584,56 +442,19 @@ __device__ void op_ez(const GridDev& G, int m, const double* fac, double* sm, do
 // E-perp from B and psi: field_e_class.f03:412-514 (no solve)
 __device__ void op_et(const GridDev& G, int m, const double* __restrict__ b, const double* __restrict__ psi,
                       double* __restrict__ e) {
-  const int nr = G.nr;
-  const double idr = G.idr, idrh = idr * 0.5, dm = (double)m;
-  if (m == 0) {
-    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
-      double e0, e1;
-      if (i == 1) {
-        e0 = 0.0;
-        e1 = 0.0;
-      } else if (i == nr) {
-        e0 = FLD(b, 3, 0, 1, nr) + idrh * (4.0 * FLD(psi, 1, 0, 0, nr - 1) - FLD(psi, 1, 0, 0, nr - 2) -
-                                           3.0 * FLD(psi, 1, 0, 0, nr));
-        e1 = -FLD(b, 3, 0, 0, nr);
-      } else {
-        e0 = FLD(b, 3, 0, 1, i) - idrh * (FLD(psi, 1, 0, 0, i + 1) - FLD(psi, 1, 0, 0, i - 1));
-        e1 = -FLD(b, 3, 0, 0, i);
-      }
-      FLD(e, 3, 0, 0, i) = e0;
-      FLD(e, 3, 0, 1, i) = e1;
-    }
-  } else {
-    const int pr = part_re(m), pi = part_im(m);
-    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
-      double r0, i0, r1, i1;
-      if (i == 1) {
-        if (m == 1) {
-          r0 = FLD(b, 3, pr, 1, 1) - idr * FLD(psi, 1, pr, 0, 2);
-          i0 = FLD(b, 3, pi, 1, 1) - idr * FLD(psi, 1, pi, 0, 2);
-          r1 = -FLD(b, 3, pr, 0, 1) + idr * FLD(psi, 1, pi, 0, 2);
-          i1 = -FLD(b, 3, pi, 0, 1) - idr * FLD(psi, 1, pr, 0, 2);
-        } else {
-          r0 = i0 = r1 = i1 = 0.0;
-        }
-      } else {
-        const double ir = G.ir[i];
-        if (i == nr) {
-          r0 = FLD(b, 3, pr, 1, nr) + idrh * (4.0 * FLD(psi, 1, pr, 0, nr - 1) - FLD(psi, 1, pr, 0, nr - 2) -
-                                              3.0 * FLD(psi, 1, pr, 0, nr));
-          i0 = FLD(b, 3, pi, 1, nr) + idrh * (4.0 * FLD(psi, 1, pi, 0, nr - 1) - FLD(psi, 1, pi, 0, nr - 2) -
-                                              3.0 * FLD(psi, 1, pi, 0, nr));
-        } else {
-          r0 = FLD(b, 3, pr, 1, i) - idrh * (FLD(psi, 1, pr, 0, i + 1) - FLD(psi, 1, pr, 0, i - 1));
-          i0 = FLD(b, 3, pi, 1, i) - idrh * (FLD(psi, 1, pi, 0, i + 1) - FLD(psi, 1, pi, 0, i - 1));
-        }
-        r1 = -FLD(b, 3, pr, 0, i) + ir * dm * FLD(psi, 1, pi, 0, i);
-        i1 = -FLD(b, 3, pi, 0, i) - ir * dm * FLD(psi, 1, pr, 0, i);
-      }
-      FLD(e, 3, pr, 0, i) = r0;
-      FLD(e, 3, pi, 0, i) = i0;
-      FLD(e, 3, pr, 1, i) = r1;
-      FLD(e, 3, pi, 1, i) = i1;
+  const GlobalF B{b, G.ld, 3}, PS{psi, G.ld, 1};
+  const int pr = part_re(m), pi = part_im(m);
+  for (int i = 1 + threadIdx.x; i <= G.nr; i += blockDim.x) {
+    double o[4];
+    row_et(G, m, i, B, PS, o);
+    if (m == 0) {
+      FLD(e, 3, 0, 0, i) = o[0];
+      FLD(e, 3, 0, 1, i) = o[1];
+    } else {
+      FLD(e, 3, pr, 0, i) = o[0];
+      FLD(e, 3, pi, 0, i) = o[1];
+      FLD(e, 3, pr, 1, i) = o[2];
+      FLD(e, 3, pi, 1, i) = o[3];
     }
   }
   __syncthreads();
@@ -642,68 +463,18 @@ __device__ void op_et(const GridDev& G, int m, const double* __restrict__ b, con
 // dJ_perp/dxi: field_src_class.f03:273-405 (no solve)
 __device__ void op_djdxi(const GridDev& G, int m, const double* __restrict__ acu, const double* __restrict__ amu,
                          double* __restrict__ dcu) {
-  const int nr = G.nr;
-  const double idr = G.idr, idrh = idr * 0.5, dm = (double)m;
-#define A_(p, c, i) FLD(acu, 2, p, c, i)
-#define U_(p, c, i) FLD(amu, 3, p, c, i)
-  if (m == 0) {
-    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
-      double v0, v1;
-      if (i == 1) {
-        v0 = 0.0;
-        v1 = 0.0;
-      } else if (i == nr) {
-        const double ir = G.ir[nr];
-        v0 = A_(0, 0, nr) + idrh * (4.0 * U_(0, 0, nr - 1) - U_(0, 0, nr - 2) - 3.0 * U_(0, 0, nr)) - ir * U_(0, 0, nr);
-        v1 = A_(0, 1, nr) + idrh * (4.0 * U_(0, 1, nr - 1) - U_(0, 1, nr - 2) - 3.0 * U_(0, 1, nr)) - ir * U_(0, 1, nr);
-      } else {
-        const double ir = G.ir[i];
-        v0 = A_(0, 0, i) - idrh * (U_(0, 0, i + 1) - U_(0, 0, i - 1)) - ir * U_(0, 0, i);
-        v1 = A_(0, 1, i) - idrh * (U_(0, 1, i + 1) - U_(0, 1, i - 1)) - ir * U_(0, 1, i);
-      }
-      FLD(dcu, 2, 0, 0, i) = v0;
-      FLD(dcu, 2, 0, 1, i) = v1;
-    }
-  } else {
-    const int r = part_re(m), s = part_im(m);
-    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
-      double a0, a1, b0, b1;
-      if (i == 1) {
-        if (m == 1) {
-          a0 = A_(r, 0, 1) - 2.0 * idr * U_(r, 0, 2) + dm * idr * U_(s, 1, 2);
-          a1 = A_(r, 1, 1) - 2.0 * idr * U_(r, 1, 2) + dm * idr * U_(s, 2, 2);
-          b0 = A_(s, 0, 1) - 2.0 * idr * U_(s, 0, 2) - dm * idr * U_(r, 1, 2);
-          b1 = A_(s, 1, 1) - 2.0 * idr * U_(s, 1, 2) - dm * idr * U_(r, 2, 2);
-        } else {
-          a0 = a1 = b0 = b1 = 0.0;
-        }
-      } else if (i == nr) {
-        const double ir = G.ir[nr];
-        a0 = A_(r, 0, nr) + idrh * (4.0 * U_(r, 0, nr - 1) - U_(r, 0, nr - 2) - 3.0 * U_(r, 0, nr)) - ir * U_(r, 0, nr) + dm * ir * U_(s, 1, nr);
-        a1 = A_(r, 1, nr) + idrh * (4.0 * U_(r, 1, nr - 1) - U_(r, 1, nr - 2) - 3.0 * U_(r, 1, nr)) - ir * U_(r, 1, nr) + dm * ir * U_(s, 2, nr);
-        b0 = A_(s, 0, nr) + idrh * (4.0 * U_(s, 0, nr - 1) - U_(s, 0, nr - 2) - 3.0 * U_(s, 0, nr)) - ir * U_(s, 0, nr) - dm * ir * U_(r, 1, nr);
-        b1 = A_(s, 1, nr) + idrh * (4.0 * U_(s, 1, nr - 1) - U_(s, 1, nr - 2) - 3.0 * U_(s, 1, nr)) - ir * U_(s, 1, nr) - dm * ir * U_(r, 2, nr);
-      } else if (i == 2 && m == 2) {
-        const double ir = idr;
-        a0 = A_(r, 0, 2) - idr * (U_(r, 0, 3) - U_(r, 0, 2)) - ir * U_(r, 0, 2) + dm * ir * U_(s, 1, 2);
-        a1 = A_(r, 1, 2) - idr * (U_(r, 1, 3) - U_(r, 1, 2)) - ir * U_(r, 1, 2) + dm * ir * U_(s, 2, 2);
-        b0 = A_(s, 0, 2) - idr * (U_(s, 0, 3) - U_(s, 0, 2)) - ir * U_(s, 0, 2) - dm * ir * U_(r, 1, 2);
-        b1 = A_(s, 1, 2) - idr * (U_(s, 1, 3) - U_(s, 1, 2)) - ir * U_(s, 1, 2) - dm * ir * U_(r, 2, 2);
-      } else {
-        const double ir = G.ir[i];
-        a0 = A_(r, 0, i) - idrh * (U_(r, 0, i + 1) - U_(r, 0, i - 1)) - ir * U_(r, 0, i) + dm * ir * U_(s, 1, i);
-        a1 = A_(r, 1, i) - idrh * (U_(r, 1, i + 1) - U_(r, 1, i - 1)) - ir * U_(r, 1, i) + dm * ir * U_(s, 2, i);
-        b0 = A_(s, 0, i) - idrh * (U_(s, 0, i + 1) - U_(s, 0, i - 1)) - ir * U_(s, 0, i) - dm * ir * U_(r, 1, i);
-        b1 = A_(s, 1, i) - idrh * (U_(s, 1, i + 1) - U_(s, 1, i - 1)) - ir * U_(s, 1, i) - dm * ir * U_(r, 2, i);
-      }
-      FLD(dcu, 2, r, 0, i) = a0;
-      FLD(dcu, 2, r, 1, i) = a1;
-      FLD(dcu, 2, s, 0, i) = b0;
-      FLD(dcu, 2, s, 1, i) = b1;
+  const GlobalF A{acu, G.ld, 2}, U{amu, G.ld, 3};
+  const int pr = part_re(m), pi = part_im(m);
+  for (int i = 1 + threadIdx.x; i <= G.nr; i += blockDim.x) {
+    double o[4];
+    row_djdxi(G, m, i, A, U, o);
+    FLD(dcu, 2, pr, 0, i) = o[0];
+    FLD(dcu, 2, pr, 1, i) = o[1];
+    if (m > 0) {
+      FLD(dcu, 2, pi, 0, i) = o[2];
+      FLD(dcu, 2, pi, 1, i) = o[3];
     }
   }
-#undef A_
-#undef U_
   __syncthreads();
 }
 
@@ -736,27 +507,11 @@ __device__ void op_finish_amj(const GridDev& G, int m, double* __restrict__ cu, 
   for (int h = 0; h < np_; ++h) {
     const int p = h == 0 ? part_re(m) : part_im(m);
     for (int i = threadIdx.x; i <= G.nr + 1; i += blockDim.x) {
-      if (i == 0) {
-        for (int c = 0; c < 3; ++c) { FLD(cu, 3, p, c, 0) = 0.0; FLD(amu, 3, p, c, 0) = 0.0; }
-        for (int c = 0; c < 2; ++c) FLD(acu, 2, p, c, 0) = 0.0;
-      } else if (i == 1) {
-        const double fcu0 = (m == 1) ? 8.0 : 0.0;   // J_r, J_phi
-        const double fcu2 = (m == 0) ? 8.0 : 0.0;   // J_z
-        const double fac_ = (m == 1) ? 8.0 : 0.0;   // acu
-        const double fam = (m == 2) ? 8.0 : 0.0;    // amu
-        FLD(cu, 3, p, 0, 1) = fcu0 == 0.0 ? 0.0 : fcu0 * FLD(cu, 3, p, 0, 1);
-        FLD(cu, 3, p, 1, 1) = fcu0 == 0.0 ? 0.0 : fcu0 * FLD(cu, 3, p, 1, 1);
-        FLD(cu, 3, p, 2, 1) = fcu2 == 0.0 ? 0.0 : fcu2 * FLD(cu, 3, p, 2, 1);
-        for (int c = 0; c < 2; ++c) FLD(acu, 2, p, c, 1) = fac_ == 0.0 ? 0.0 : fac_ * FLD(acu, 2, p, c, 1);
-        for (int c = 0; c < 3; ++c) FLD(amu, 3, p, c, 1) = fam == 0.0 ? 0.0 : fam * FLD(amu, 3, p, c, 1);
-      } else {
-        const double ir = G.inv[i];
-        for (int c = 0; c < 3; ++c) {
-          FLD(cu, 3, p, c, i) = FLD(cu, 3, p, c, i) * ir;
-          FLD(amu, 3, p, c, i) = FLD(amu, 3, p, c, i) * ir;
-        }
-        for (int c = 0; c < 2; ++c) FLD(acu, 2, p, c, i) = FLD(acu, 2, p, c, i) * ir;
+      for (int c = 0; c < 3; ++c) {
+        FLD(cu, 3, p, c, i) = finish_amj(G, m, 0, c, i, FLD(cu, 3, p, c, i));
+        FLD(amu, 3, p, c, i) = finish_amj(G, m, 1, c, i, FLD(amu, 3, p, c, i));
       }
+      for (int c = 0; c < 2; ++c) FLD(acu, 2, p, c, i) = finish_amj(G, m, 2, c, i, FLD(acu, 2, p, c, i));
     }
   }
   __syncthreads();
@@ -967,43 +722,17 @@ __global__ void __launch_bounds__(kFieldThreads) k_finish_amj(GridDev G, double*
 // counts the iteration, stores the slice's statistics and, inside a CUDA graph, sets the
 // condition of the predictor-corrector WHILE node (continue while not converged and
 // below iter_max, simulation_class.f03:370-398).
-struct ConvLoop {
-  int* iter_ctr;                 // iterations taken in the current slice
-  qpad_slice_stats* stats;       // per-slice statistics [nz]
-  const int* jp;                 // current slice (1-based)
-  int iter_max;
-  cudaGraphConditionalHandle h;  // WHILE-node handle
-  int use_h;
-};
-
 __global__ void __launch_bounds__(1024) k_conv(GridDev G, const double* __restrict__ b, int comp, int op,
                                                double* __restrict__ st, double reltol, double abstol, ConvLoop L) {
   __shared__ double red[33];
-  const int nr = G.nr, M = G.M;
+  __shared__ double red2[33];
+  const int nr = G.nr;
   double* s_re = st;
   double* s_im = st + nr;
   double* res = st + 2 * nr;
+  const GlobalF B{b, G.ld, 3};
   double mx_old = 0.0, mx_new = 0.0;
-  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) {
-    double nre = 0.0, nim = 0.0;   // record of the current field
-    double ore = s_re[i - 1], oim = s_im[i - 1];
-    if (op == 1) {
-      const double v = ore * ore + oim * oim;
-      mx_old = fmax(mx_old, v);
-    }
-    for (int m = 0; m <= M; ++m) {
-      const double vr = fabs(FLD(b, 3, part_re(m), comp, i));
-      nre = nre + vr;
-      if (op == 1) ore = ore - vr;
-      if (m == 0) continue;
-      const double vi = fabs(FLD(b, 3, part_im(m), comp, i));
-      nim = nim + vi;
-      if (op == 1) oim = oim - vi;
-    }
-    if (op == 1) mx_new = fmax(mx_new, ore * ore + oim * oim);
-    s_re[i - 1] = nre;
-    s_im[i - 1] = nim;
-  }
+  for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) conv_node(G, B, comp, i, s_re, s_im, op == 1, mx_old, mx_new);
   if (op == 0) {
     // 'record' opens the iteration loop of a new slice: re-arm its WHILE condition (a
     // nested conditional keeps its last value between entries within one graph launch)
@@ -1015,31 +744,13 @@ __global__ void __launch_bounds__(1024) k_conv(GridDev G, const double* __restri
     mx_old = fmax(mx_old, __shfl_down_sync(FULLMASK, mx_old, off));
     mx_new = fmax(mx_new, __shfl_down_sync(FULLMASK, mx_new, off));
   }
-  __shared__ double red2[33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) { red[warp] = mx_old; red2[warp] = mx_new; }
   __syncthreads();
   if (threadIdx.x == 0) {
     double a = 0.0, c = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a = fmax(a, red[w]); c = fmax(c, red2[w]); }
-    const double old_norm = sqrt(a), abs_res = sqrt(c);
-    const double rel = old_norm > 2.220446049250313e-16 ? abs_res / old_norm : 1.7976931348623157e308;
-    const bool converged = rel < reltol || abs_res < abstol;
-    res[0] = rel;
-    res[1] = abs_res;
-    res[2] = converged ? 1.0 : 0.0;
-    if (L.iter_ctr) {
-      const int it = *L.iter_ctr + 1;
-      *L.iter_ctr = it;
-      if (L.stats && L.jp) {
-        qpad_slice_stats s;
-        s.iters = it;
-        s.rel_res = rel;
-        s.abs_res = abs_res;
-        L.stats[*L.jp - 1] = s;
-      }
-      if (L.use_h) cudaGraphSetConditional(L.h, (!converged && it < L.iter_max) ? 1u : 0u);
-    }
+    conv_decide(a, c, reltol, abstol, res, L);
   }
 }
 
@@ -1085,7 +796,9 @@ int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op, int loop_state
     L.h = h;
     L.use_h = use_h;
   }
+  prof_begin(ctx, "conv");
   k_conv<<<1, 1024, 0, ctx->stream>>>(ctx->g, b, comp, op, ctx->conv, ctx->reltol, ctx->abstol, L);
+  prof_end(ctx, "conv");
   return check_launch(ctx, "k_conv");
 }
 
@@ -1096,14 +809,18 @@ int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle h) {
 
 int launch_slice_begin(qpad_ctx* ctx, int use_qn) {
   if (int r = ensure_smem_attr(ctx)) return r;
+  prof_begin(ctx, "slice_begin");
   k_slice_begin<<<3 * (ctx->g.M + 1), kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac,
                                                                                      slice_fields(ctx), ctx->d_j, use_qn);
+  prof_end(ctx, "slice_begin");
   return check_launch(ctx, "k_slice_begin");
 }
 
 int launch_iter_e(qpad_ctx* ctx) {
   if (int r = ensure_smem_attr(ctx)) return r;
+  prof_begin(ctx, "iter_e");
   k_iter_e<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac, slice_fields(ctx));
+  prof_end(ctx, "iter_e");
   return check_launch(ctx, "k_iter_e");
 }
 
@@ -1115,8 +832,10 @@ int launch_iter_b(qpad_ctx* ctx) {
 
 int launch_slice_end(qpad_ctx* ctx) {
   if (int r = ensure_smem_attr(ctx)) return r;
+  prof_begin(ctx, "slice_end");
   k_slice_end<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac, slice_fields(ctx),
                                                                               ctx->d_j);
+  prof_end(ctx, "slice_end");
   return check_launch(ctx, "k_slice_end");
 }
 

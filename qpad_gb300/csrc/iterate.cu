@@ -1,0 +1,500 @@
+// iterate.cu -- one predictor-corrector iteration of a slice as one cluster kernel.
+//
+// GB300 executes FP64 at 1/64 of its FP32 rate, so the FP64 field work of an iteration
+// has to be spread over many SMs instead of one CTA per mode.  Here each azimuthal mode m
+// is one thread-block cluster of CL CTAs; CTA `rank` of the cluster owns the radial rows
+// [rank*R, (rank+1)*R) of that mode (row k = node k+1).  After the plasma deposit the
+// kernel does, per node it owns:
+//
+//   finish the raw deposits (axis rule, 1/(i-1)), dJ/dxi, and the right-hand sides of
+//   B+ / B- (the B-perp predictor-corrector), Bz and Ez (simulation_class.f03:386-392,
+//   and the Ez of the next iteration, :375-378, which depends only on the same current);
+//   the tridiagonal solves of all of them at once, split across the cluster;
+//   B-perp, Bz, Ez, b = b_spe + b_beam, E-perp, the FP32 gather table; and the
+//   convergence test (:394-396, simulation_class.f03:522-606).
+//
+// Solves.  Both substitutions of a factored tridiagonal system are first-order affine
+// recurrences.  Within a CTA, each right-hand side is taken by a group of kLanes lanes,
+// each composing a contiguous run of rows, combined by a shuffle scan inside the group;
+// the CTA's composite map is published in shared memory, and after a cluster barrier
+// every CTA composes the maps of the CTAs before it (after it, for the back
+// substitution) through distributed shared memory and replays its rows.
+//
+// Convergence.  The record is a per-node sum over all modes, so it cannot be formed
+// inside one cluster.  Each CTA counts in on a per-node-range ticket after writing its
+// B-perp; the last of the M+1 CTAs of a node range evaluates the record there and folds
+// its maxima into two global words (atomicMax on the bit patterns of non-negative
+// doubles, which is exact and order independent); the last node range to finish takes
+// the verdict, drives the loop state and resets the tickets.  No CTA waits on another.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
+#include "stencils.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace qpad {
+
+static constexpr int kIterThreads = 256;
+static constexpr int kLanes = 4;           // lanes per right-hand side in the solves
+static constexpr int kMaxRhs = 8;          // B+ (re, im), B- (re, im), Bz (re, im), Ez (re, im)
+static constexpr int kCompConv = 1;        // convergence on B_phi
+
+struct IterArgs {
+  GridDev G;
+  const double* fac;
+  double* raw;            // raw deposits [cu 3 | amu 3 | acu 2] x P x ld, zeroed after use
+  double *cu, *amu, *acu, *dcu;
+  double* b_spe;
+  const double* b_beam;
+  double *b, *e;
+  const double* psi;
+  float* gtab;            // FP32 gather table (mixed path) or null
+  double* conv;           // s_re[nr], s_im[nr], res[..]
+  unsigned int* tickets;  // [0, CL): node-range tickets; [CL]: range counter
+  unsigned long long* maxima;
+  ConvLoop L;
+  double reltol, abstol;
+  int R;                  // rows per CTA
+};
+
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release;\n" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory"); }
+
+// Raw deposit of component c of `which` (0 cu, 1 amu, 2 acu), finished on the fly.
+struct RawFin {
+  const GridDev* G;
+  const double* raw;
+  int m, which, nc;
+  __device__ __forceinline__ double operator()(int p, int c, int i) const {
+    return finish_amj(*G, m, which, c, i, raw[fidx(G->ld, nc, p, c, i)]);
+  }
+};
+
+__global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
+  extern __shared__ double dsm[];                // d[kMaxRhs][R]
+  __shared__ double fwd[kMaxRhs][2], bwd[kMaxRhs][2];
+  __shared__ double wpart[kIterThreads / 32];
+  __shared__ double divp;
+  __shared__ unsigned int s_ticket;
+  cg::cluster_group cluster = cg::this_cluster();
+  const GridDev& G = a.G;
+  const int CL = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int m = blockIdx.x / CL;
+  const int nr = G.nr, ld = G.ld, P = G.P;
+  const int pr = part_re(m), pi = part_im(m);
+  const int nrhs = m == 0 ? 4 : 8;
+  const int r0 = min(rank * a.R, nr), r1 = min(r0 + a.R, nr);
+  const int Rc = r1 - r0;
+  const int t = threadIdx.x;
+  const size_t P1 = (size_t)P * ld;
+  double* raw_cu = a.raw;
+  double* raw_amu = a.raw + 3 * P1;
+  double* raw_acu = a.raw + 6 * P1;
+  const RawFin CU{&G, raw_cu, m, 0, 3}, AMU{&G, raw_amu, m, 1, 3}, ACU{&G, raw_acu, m, 2, 2};
+  const GlobalF BO{a.b_spe, ld, 3};
+
+  // ---- sources, one thread per owned node ---------------------------------------------
+  double div = 0.0;
+  for (int k = t; k < Rc; k += blockDim.x) {
+    const int i = r0 + k + 1;
+    double dj[4];
+    row_djdxi(G, m, i, ACU, AMU, dj);
+    const auto DC = [&](int p, int c, int) { return p == pr ? dj[c] : dj[2 + c]; };
+    double bt[4];
+    row_btiter_src(G, m, i, DC, CU, BO, bt);
+    double zr, zi, er, ei;
+    bool in_div;
+    row_bz_src(G, m, i, CU, zr, zi);
+    row_ez_src(G, m, i, CU, er, ei, in_div);
+    if (in_div) div += er * (double)(i - 1);
+    if (m == 0) {
+      dsm[0 * a.R + k] = bt[0];
+      dsm[1 * a.R + k] = bt[1];
+      dsm[2 * a.R + k] = zr;
+      dsm[3 * a.R + k] = er;
+    } else {
+      dsm[0 * a.R + k] = bt[0];
+      dsm[1 * a.R + k] = bt[2];
+      dsm[2 * a.R + k] = zr;
+      dsm[3 * a.R + k] = er;
+      dsm[4 * a.R + k] = bt[1];
+      dsm[5 * a.R + k] = bt[3];
+      dsm[6 * a.R + k] = zi;
+      dsm[7 * a.R + k] = ei;
+    }
+    // finished deposits and dJ/dxi of this node
+    for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
+      const int p = h == 0 ? pr : pi;
+      for (int c = 0; c < 3; ++c) {
+        a.cu[fidx(ld, 3, p, c, i)] = CU(p, c, i);
+        a.amu[fidx(ld, 3, p, c, i)] = AMU(p, c, i);
+      }
+      for (int c = 0; c < 2; ++c) {
+        a.acu[fidx(ld, 2, p, c, i)] = ACU(p, c, i);
+        a.dcu[fidx(ld, 2, p, c, i)] = dj[2 * h + c];
+      }
+    }
+  }
+  // guard nodes 0 and nr+1 of the finished deposits
+  if (t < 2 && ((t == 0 && rank == 0) || (t == 1 && rank == CL - 1))) {
+    const int i = t == 0 ? 0 : nr + 1;
+    for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
+      const int p = h == 0 ? pr : pi;
+      for (int c = 0; c < 3; ++c) {
+        a.cu[fidx(ld, 3, p, c, i)] = CU(p, c, i);
+        a.amu[fidx(ld, 3, p, c, i)] = AMU(p, c, i);
+      }
+      for (int c = 0; c < 2; ++c) a.acu[fidx(ld, 2, p, c, i)] = ACU(p, c, i);
+    }
+  }
+  // the m = 0 axis row of Ez needs the weighted sum over the whole line
+  if (m == 0) {
+    for (int off = 16; off > 0; off >>= 1) div += __shfl_down_sync(0xffffffffu, div, off);
+    if ((t & 31) == 0) wpart[t >> 5] = div;
+    __syncthreads();
+    if (t == 0) {
+      double s = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += wpart[w];
+      divp = s;
+    }
+    cluster.sync();
+    if (rank == 0 && t == 0) {
+      double s = 0.0;
+      for (int q = 0; q < CL; ++q) s += *cluster.map_shared_rank(&divp, q);
+      dsm[3 * a.R + 0] = ez_axis_row(G, s, CU);
+    }
+  }
+  __syncthreads();
+
+  // ---- forward substitution y_k = d_k - w_k y_{k-1} ------------------------------------
+  const int rhs = t / kLanes, l = t % kLanes;
+  const bool solver = t < 32 * ((kMaxRhs * kLanes + 31) / 32);   // whole warps take part in the shuffles
+  const bool act = rhs < nrhs;
+  const int RL = (Rc + kLanes - 1) / kLanes;
+  const int k0 = min(l * RL, Rc), k1 = min(k0 + RL, Rc);
+  const int kind = (rhs & 3) == 0 ? OK_BPLUS : (rhs & 3) == 1 ? OK_BMINUS : OK_GEN;
+  const double* fw = a.fac + fac_off(nr, G.M, kind, m);
+  const double* fib = fw + nr;
+  const double* fg = fib + nr;
+  double* d = dsm + (size_t)(act ? rhs : 0) * a.R;
+  double Aex = 0.0, Bex = 1.0;
+  if (solver) {
+    double A = 0.0, B = 1.0;
+    if (act)
+      for (int k = k0; k < k1; ++k) {
+        const double w = fw[r0 + k];
+        A = d[k] - w * A;
+        B = -w * B;
+      }
+#pragma unroll
+    for (int off = 1; off < kLanes; off <<= 1) {
+      const double Ao = __shfl_up_sync(0xffffffffu, A, off, kLanes);
+      const double Bo = __shfl_up_sync(0xffffffffu, B, off, kLanes);
+      if (l >= off) {
+        A = A + B * Ao;
+        B = B * Bo;
+      }
+    }
+    Aex = __shfl_up_sync(0xffffffffu, A, 1, kLanes);
+    Bex = __shfl_up_sync(0xffffffffu, B, 1, kLanes);
+    if (l == 0) {
+      Aex = 0.0;
+      Bex = 1.0;
+    }
+    if (act && l == kLanes - 1) {
+      fwd[rhs][0] = B;
+      fwd[rhs][1] = A;
+    }
+  }
+  cluster.sync();
+  if (solver && act) {
+    double y = 0.0;                                   // y at the row before this CTA
+    for (int q = 0; q < rank; ++q) {
+      const double* mq = cluster.map_shared_rank(&fwd[rhs][0], q);
+      y = mq[1] + mq[0] * y;
+    }
+    y = Aex + Bex * y;
+    for (int k = k0; k < k1; ++k) {
+      y = d[k] - fw[r0 + k] * y;
+      d[k] = y;
+    }
+  }
+  // every CTA of the cluster has read its sources: clear the raw deposits it owns
+  for (int k = t; k < Rc + 2; k += blockDim.x) {
+    int i = r0 + k + 1;
+    if (k == Rc) {
+      if (rank != 0) continue;
+      i = 0;
+    } else if (k == Rc + 1) {
+      if (rank != CL - 1) continue;
+      i = nr + 1;
+    }
+    for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
+      const int p = h == 0 ? pr : pi;
+      for (int c = 0; c < 3; ++c) {
+        raw_cu[fidx(ld, 3, p, c, i)] = 0.0;
+        raw_amu[fidx(ld, 3, p, c, i)] = 0.0;
+      }
+      for (int c = 0; c < 2; ++c) raw_acu[fidx(ld, 2, p, c, i)] = 0.0;
+    }
+  }
+  __syncthreads();
+
+  // ---- back substitution x_k = y_k ib_k - g_k x_{k+1} -----------------------------------
+  if (solver) {
+    double A = 0.0, B = 1.0;
+    if (act)
+      for (int k = k1 - 1; k >= k0; --k) {
+        const double g = fg[r0 + k];
+        A = d[k] * fib[r0 + k] - g * A;
+        B = -g * B;
+      }
+#pragma unroll
+    for (int off = 1; off < kLanes; off <<= 1) {
+      const double Ao = __shfl_down_sync(0xffffffffu, A, off, kLanes);
+      const double Bo = __shfl_down_sync(0xffffffffu, B, off, kLanes);
+      if (l + off < kLanes) {
+        A = A + B * Ao;
+        B = B * Bo;
+      }
+    }
+    Aex = __shfl_down_sync(0xffffffffu, A, 1, kLanes);
+    Bex = __shfl_down_sync(0xffffffffu, B, 1, kLanes);
+    if (l == kLanes - 1) {
+      Aex = 0.0;
+      Bex = 1.0;
+    }
+    if (act && l == 0) {
+      bwd[rhs][0] = B;
+      bwd[rhs][1] = A;
+    }
+  }
+  cluster.sync();
+  if (solver && act) {
+    double x = 0.0;                                   // x at the row after this CTA
+    for (int q = CL - 1; q > rank; --q) {
+      const double* mq = cluster.map_shared_rank(&bwd[rhs][0], q);
+      x = mq[1] + mq[0] * x;
+    }
+    x = Aex + Bex * x;
+    for (int k = k1 - 1; k >= k0; --k) {
+      x = d[k] * fib[r0 + k] - fg[r0 + k] * x;
+      d[k] = x;
+    }
+  }
+  // last access to another CTA's shared memory is done; the matching wait sits at the end
+  cluster_arrive();
+  __syncthreads();
+
+  // ---- fields of the owned nodes -------------------------------------------------------
+  for (int k = t; k < Rc; k += blockDim.x) {
+    const int i = r0 + k + 1;
+    double bs[2][3], bb[2][3];
+    if (m == 0) {
+      bs[0][0] = (i == 1) ? 0.0 : dsm[0 * a.R + k];
+      bs[0][1] = (i == 1) ? 0.0 : dsm[1 * a.R + k];
+      bs[0][2] = dsm[2 * a.R + k];
+      a.e[fidx(ld, 3, 0, 2, i)] = dsm[3 * a.R + k];
+    } else {
+      const bool zero = (i == 1 && m != 1);
+      const double b1re = dsm[0 * a.R + k], b2re = dsm[1 * a.R + k];
+      const double b1im = dsm[4 * a.R + k], b2im = dsm[5 * a.R + k];
+      bs[0][0] = zero ? 0.0 : 0.5 * (b1re + b2re);
+      bs[1][0] = zero ? 0.0 : 0.5 * (b1im + b2im);
+      bs[0][1] = zero ? 0.0 : 0.5 * (b1im - b2im);
+      bs[1][1] = zero ? 0.0 : 0.5 * (-b1re + b2re);
+      bs[0][2] = (i == 1) ? 0.0 : dsm[2 * a.R + k];
+      bs[1][2] = (i == 1) ? 0.0 : dsm[6 * a.R + k];
+      a.e[fidx(ld, 3, pr, 2, i)] = (i == 1) ? 0.0 : dsm[3 * a.R + k];
+      a.e[fidx(ld, 3, pi, 2, i)] = (i == 1) ? 0.0 : dsm[7 * a.R + k];
+    }
+    const int nh = m == 0 ? 1 : 2;
+    for (int h = 0; h < nh; ++h) {
+      const int p = h == 0 ? pr : pi;
+      for (int c = 0; c < 3; ++c) {
+        a.b_spe[fidx(ld, 3, p, c, i)] = bs[h][c];
+        bb[h][c] = bs[h][c] + a.b_beam[fidx(ld, 3, p, c, i)];
+        a.b[fidx(ld, 3, p, c, i)] = bb[h][c];
+      }
+    }
+    const auto Bn = [&](int p, int c, int) { return p == pr ? bb[0][c] : bb[1][c]; };
+    double et[4];
+    row_et(G, m, i, Bn, GlobalF{a.psi, ld, 1}, et);
+    if (m == 0) {
+      a.e[fidx(ld, 3, 0, 0, i)] = et[0];
+      a.e[fidx(ld, 3, 0, 1, i)] = et[1];
+    } else {
+      a.e[fidx(ld, 3, pr, 0, i)] = et[0];
+      a.e[fidx(ld, 3, pi, 0, i)] = et[1];
+      a.e[fidx(ld, 3, pr, 1, i)] = et[2];
+      a.e[fidx(ld, 3, pi, 1, i)] = et[3];
+    }
+  }
+  // guard nodes of b = b_spe + b_beam
+  if (t < 2 && ((t == 0 && rank == 0) || (t == 1 && rank == CL - 1))) {
+    const int i = t == 0 ? 0 : nr + 1;
+    for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
+      const int p = h == 0 ? pr : pi;
+      for (int c = 0; c < 3; ++c)
+        a.b[fidx(ld, 3, p, c, i)] = a.b_spe[fidx(ld, 3, p, c, i)] + a.b_beam[fidx(ld, 3, p, c, i)];
+    }
+  }
+  __syncthreads();
+  if (a.gtab) {
+    const int i0 = rank == 0 ? 0 : r0 + 1;
+    const int i1 = rank == CL - 1 ? nr + 1 : r1;
+    const int nh = m == 0 ? 1 : 2;
+    const int n = (i1 - i0 + 1) * nh * 6;
+    for (int q = t; q < n; q += blockDim.x) {
+      const int c = q % 6, h = (q / 6) % nh, i = i0 + q / (6 * nh);
+      const int p = h == 0 ? pr : pi;
+      const double v = c < 3 ? a.e[fidx(ld, 3, p, c, i)] : a.b[fidx(ld, 3, p, c - 3, i)];
+      a.gtab[((size_t)i * P + p) * 6 + c] = (float)v;
+    }
+  }
+
+  // ---- convergence test -----------------------------------------------------------------
+  __threadfence();                                    // this CTA's B-perp, visible device-wide
+  __syncthreads();
+  if (t == 0) s_ticket = atomicAdd(&a.tickets[rank], 1u);
+  __syncthreads();
+  if (s_ticket == (unsigned)G.M) {                    // the last mode of this node range
+    __threadfence();
+    struct LdcgF {
+      const double* f;
+      int ld;
+      __device__ __forceinline__ double operator()(int p, int c, int i) const { return __ldcg(f + fidx(ld, 3, p, c, i)); }
+    } Bc{a.b_spe, ld};
+    double* s_re = a.conv;
+    double* s_im = a.conv + nr;
+    double mx_old = 0.0, mx_new = 0.0;
+    for (int k = t; k < Rc; k += blockDim.x) conv_node(G, Bc, kCompConv, r0 + k + 1, s_re, s_im, true, mx_old, mx_new);
+    for (int off = 16; off > 0; off >>= 1) {
+      mx_old = fmax(mx_old, __shfl_down_sync(0xffffffffu, mx_old, off));
+      mx_new = fmax(mx_new, __shfl_down_sync(0xffffffffu, mx_new, off));
+    }
+    __shared__ double rmo[kIterThreads / 32], rmn[kIterThreads / 32];
+    if ((t & 31) == 0) {
+      rmo[t >> 5] = mx_old;
+      rmn[t >> 5] = mx_new;
+    }
+    __syncthreads();
+    if (t == 0) {
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+        mx_old = fmax(mx_old, rmo[w]);
+        mx_new = fmax(mx_new, rmn[w]);
+      }
+      atomicMax(&a.maxima[0], (unsigned long long)__double_as_longlong(mx_old));
+      atomicMax(&a.maxima[1], (unsigned long long)__double_as_longlong(mx_new));
+      a.tickets[rank] = 0u;
+      __threadfence();
+      const unsigned int done = atomicAdd(&a.tickets[CL], 1u);
+      if (done == (unsigned)(CL - 1)) {               // the last node range: the verdict
+        __threadfence();
+        const double vo = __longlong_as_double((long long)atomicAdd(&a.maxima[0], 0ull));
+        const double vn = __longlong_as_double((long long)atomicAdd(&a.maxima[1], 0ull));
+        conv_decide(vo, vn, a.reltol, a.abstol, a.conv + 2 * nr, a.L);
+        a.maxima[0] = 0ull;
+        a.maxima[1] = 0ull;
+        a.tickets[CL] = 0u;
+        __threadfence();
+      }
+    }
+  }
+  cluster_wait();
+}
+
+// ------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------
+static int cluster_for(int nr) { return std::max(1, std::min(16, nr / 32)); }
+
+int iterate_setup(qpad_ctx* ctx) {
+  if (ctx->iter_cl > 0) return 0;
+  cudaError_t e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cluster attribute");
+  for (int cl = cluster_for(ctx->g.nr); cl >= 1; cl /= 2) {
+    const int R = (ctx->g.nr + cl - 1) / cl;
+    const size_t smem = (size_t)kMaxRhs * R * sizeof(double);
+    if (smem > 48 * 1024) {
+      e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return cuda_check(ctx, e, "iterate smem");
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cl * (ctx->g.M + 1));
+    cfg.blockDim = dim3(kIterThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    e = cudaOccupancyMaxActiveClusters(&ncl, k_iterate, &cfg);
+    if (e == cudaSuccess && ncl >= 1) {
+      ctx->iter_cl = cl;
+      ctx->iter_rows = R;
+      return 0;
+    }
+    cudaGetLastError();
+  }
+  return set_err(ctx, QPAD_E_CUDA, "no cluster shape of the iteration kernel fits this GPU");
+}
+
+int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h) {
+  if (int r = iterate_setup(ctx)) return r;
+  IterArgs a;
+  a.G = ctx->g;
+  a.fac = ctx->fac;
+  a.raw = ctx->raw;
+  a.cu = ctx->f[QPAD_F_CU];
+  a.amu = ctx->f[QPAD_F_AMU];
+  a.acu = ctx->f[QPAD_F_ACU];
+  a.dcu = ctx->f[QPAD_F_DCU];
+  a.b_spe = ctx->f[QPAD_F_B_SPE];
+  a.b_beam = ctx->f[QPAD_F_B_BEAM];
+  a.b = ctx->f[QPAD_F_B];
+  a.e = ctx->f[QPAD_F_E];
+  a.psi = ctx->f[QPAD_F_PSI];
+  a.gtab = ctx->precision == QPAD_PREC_MIXED ? ctx->gtab : nullptr;
+  a.conv = ctx->conv;
+  a.tickets = ctx->iter_tickets;
+  a.maxima = reinterpret_cast<unsigned long long*>(ctx->iter_tickets + 32);
+  a.L = ConvLoop{};
+  if (loop_state) {
+    a.L.iter_ctr = ctx->d_iter;
+    a.L.stats = ctx->d_stats;
+    a.L.jp = ctx->d_j;
+    a.L.iter_max = ctx->iter_max;
+    a.L.h = h;
+    a.L.use_h = use_h;
+  }
+  a.reltol = ctx->reltol;
+  a.abstol = ctx->abstol;
+  a.R = ctx->iter_rows;
+  const int cl = ctx->iter_cl;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cl * (ctx->g.M + 1));
+  cfg.blockDim = dim3(kIterThreads);
+  cfg.dynamicSmemBytes = (size_t)kMaxRhs * a.R * sizeof(double);
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cl;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  prof_begin(ctx, "iterate");
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k_iterate, a);
+  prof_end(ctx, "iterate");
+  if (e != cudaSuccess) return cuda_check(ctx, e, "k_iterate launch");
+  return check_launch(ctx, "k_iterate");
+}
+
+}  // namespace qpad

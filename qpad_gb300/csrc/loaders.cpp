@@ -87,6 +87,9 @@ extern "C" int64_t qpad_load_plasma(int nr, double dr, qpad_rng* r, int ppc1, in
 extern "C" int64_t qpad_load_beam(int nr, int nz, double dr, double dxi, qpad_rng* r, const qpad_beam_load_desc* d,
                                   double* x, double* p, double* q, int64_t cap) {
   if (!r || !d || !x || !p || !q || d->tot_num < 0 || nr < 1 || nz < 1) return -1;
+  // the rejection sampling below needs a non-empty range in every direction
+  for (int k = 0; k < 3; ++k)
+    if (!(d->range_lo[k] < d->range_hi[k]) || !(d->sigma[k] > 0.0)) return -1;
   const double er = (double)nr * dr, ez = (double)nz * dxi;
   const double q_per_part =
       (d->qm >= 0.0 ? 1.0 : -1.0) * d->tot_charge / (2.0 * kPi * (double)d->tot_num * (dr * dr) * dxi);

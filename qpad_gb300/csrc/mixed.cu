@@ -525,7 +525,9 @@ __global__ void k_to_mixed(GridDev G, const int64_t* __restrict__ n_ptr, const d
   A.gam[i] = (float)gam[i]; A.psi[i] = (float)psi[i]; A.q[i] = (float)q[i];
   const float X = (float)ix + fx, Y = (float)iy + fy;
   const float r = sqrtf(X * X + Y * Y);
-  A.key[i] = r < (float)G.nr ? (int)r + 1 : G.nr + 1;
+  // a particle handed in beyond the edge is kept (the reference removes particles only in
+  // update_bound after a push); it sorts into the last cell and deposits nothing
+  A.key[i] = r < (float)G.nr ? (int)r + 1 : G.nr;
 }
 
 __global__ void k_to_fp64(GridDev G, const int64_t* __restrict__ n_ptr, MArr A, double* __restrict__ x,

@@ -53,6 +53,18 @@ __host__ __device__ inline size_t fac_off(int nr, int M, int kind, int m) {
 
 int field_ncomp(int field);
 
+// Loop state of the predictor-corrector iteration, updated by the convergence test:
+// iterations taken, per-slice statistics and, inside a CUDA graph, the WHILE-node
+// condition (continue while not converged and below iter_max, simulation_class.f03:370-398).
+struct ConvLoop {
+  int* iter_ctr;                 // iterations taken in the current slice
+  qpad_slice_stats* stats;       // per-slice statistics [nz]
+  const int* jp;                 // current slice (1-based)
+  int iter_max;
+  cudaGraphConditionalHandle h;  // WHILE-node handle
+  int use_h;
+};
+
 struct Species;
 struct Beam;
 
@@ -71,6 +83,9 @@ struct qpad_ctx {
   double* f2[QPAD_NFIELDS] = {};               // 3D stores (only some fields have one)
   double* qn = nullptr;                        // neutralising background (sum over species)
   double* qraw = nullptr;                      // raw charge deposit scratch
+  double* raw = nullptr;                       // raw current deposits of the loop [cu 3|amu 3|acu 2] x P x ld
+  unsigned int* iter_tickets = nullptr;        // convergence tickets and maxima of k_iterate
+  int iter_cl = 0, iter_rows = 0;              // cluster size and rows per CTA of k_iterate
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
   float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
   double* scratch = nullptr;                   // per-call deposit scratch (cu, amu, acu)
@@ -180,6 +195,9 @@ int launch_iter_b(qpad_ctx* ctx);
 int launch_slice_end(qpad_ctx* ctx);
 int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn);
 int launch_finish_amj(qpad_ctx* ctx, double* cu, double* amu, double* acu);
+// one predictor-corrector iteration after the deposit, as a cluster kernel (iterate.cu)
+int iterate_setup(qpad_ctx* ctx);
+int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h);
 
 // ---- particle kernels (plasma.cu, beam.cu) ---------------------------------------------
 int species_qdeposit_raw(qpad_species* sp, double* qraw);

@@ -1,6 +1,8 @@
 """Builds a Simulation from a synthetic deck (simulation::new for the benchmark shapes)."""
 from __future__ import annotations
 
+import numpy as np
+
 from . import _capi as K
 from .api import Simulation, load_beam, load_plasma
 from .decks import Deck
@@ -14,8 +16,13 @@ def deck_inputs(deck: Deck, step: int = 0):
     """
     pl = load_plasma(deck.nr, deck.dr, deck.seed * 1000 + step, deck.ppc[0], deck.ppc[1], deck.num_theta,
                      uth=(deck.uth, deck.uth, deck.uth))
-    beams = [load_beam(deck.nr, deck.nz, deck.dr, deck.dxi, deck.seed * 1000 + 999 + k,
-                       **b.load_args(deck.nz, deck.dxi)) for k, b in enumerate(deck.beams)]
+    beams = []
+    for k, b in enumerate(deck.beams):
+        args = b.load_args(deck.nz, deck.dxi)
+        if args["range_lo"][2] >= args["range_hi"][2]:       # beam entirely behind a shortened box
+            beams.append((np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0)))
+            continue
+        beams.append(load_beam(deck.nr, deck.nz, deck.dr, deck.dxi, deck.seed * 1000 + 999 + k, **args))
     return pl, beams
 
 

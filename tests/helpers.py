@@ -15,15 +15,33 @@ def rel_l2(a: np.ndarray, b: np.ndarray, floor: float = 0.0) -> float:
     return d / n
 
 
-def field_errors(gpu: np.ndarray, ref: np.ndarray, nodes=slice(1, None)):
-    """Per (part, component) relative L2 over nodes 1..nr (+guard); parts/components
-    whose reference is identically zero are compared against the field's global norm."""
+def field_errors(gpu: np.ndarray, ref: np.ndarray, nodes=slice(1, None), floor_rel=1e-12):
+    """Per (part, component) relative L2 over nodes 1..nr (+guard) of one slice field;
+    parts/components whose reference norm is below floor_rel of the whole field's norm
+    are compared against that floor instead of themselves."""
     P, nc = ref.shape[0], ref.shape[1]
     glob = float(np.linalg.norm(ref[:, :, nodes])) or 1.0
     errs = np.zeros((P, nc))
     for p in range(P):
         for c in range(nc):
-            errs[p, c] = rel_l2(gpu[p, c, nodes], ref[p, c, nodes], floor=1e-12 * glob)
+            errs[p, c] = rel_l2(gpu[p, c, nodes], ref[p, c, nodes], floor=floor_rel * glob)
+    return errs
+
+
+def store_errors(gpu: np.ndarray, ref: np.ndarray, nodes=slice(1, None), floor_rel=1e-6):
+    """Per (part, component) relative L2 of a whole 3D store, shape (nz, P, ncomp, nr+2),
+    over all slices and nodes 1..nr (+guard).
+
+    The norm is taken over the step, not slice by slice: ahead of the beam the plasma is
+    neutral and psi holds round-off only, which summation order alone changes completely.
+    Parts below floor_rel of the store's norm (round-off parts, e.g. the m>=1 parts of a
+    ring loaded at evenly spaced angles) are compared against that floor."""
+    P, nc = ref.shape[1], ref.shape[2]
+    glob = float(np.linalg.norm(ref[:, :, :, nodes])) or 1.0
+    errs = np.zeros((P, nc))
+    for p in range(P):
+        for c in range(nc):
+            errs[p, c] = rel_l2(gpu[:, p, c, nodes], ref[:, p, c, nodes], floor=floor_rel * glob)
     return errs
 
 

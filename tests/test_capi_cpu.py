@@ -5,6 +5,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from tests.conftest import ROOT
 
@@ -73,3 +74,18 @@ def test_beam_loader_matches_oracle(olib):
     assert len(qq) == 2 * n
     np.testing.assert_array_equal(xq[n:, :2], -xq[:n, :2])
     np.testing.assert_array_equal(qq[:n], 0.5 * q)
+
+
+def test_beam_loader_rejects_empty_range():
+    """An empty sampling range is an error, not an endless rejection loop."""
+    import qpad_gb300 as Q
+    with pytest.raises(Q.QpadError):
+        Q.load_beam(32, 16, 0.1, 0.1, 5, 100, 1.0, -1.0, 1000.0, (0.0, 0.0, 3.0), (0.1, 0.1, 0.2),
+                    (-0.5, -0.5, 3.0), (0.5, 0.5, 1.6))
+
+
+def test_deck_inputs_skip_beam_behind_short_box():
+    import qpad_gb300 as Q
+    deck = Q.decks.c2().scaled(nz=48)
+    pl, beams = Q.deck_inputs(deck)
+    assert len(beams) == 2 and len(beams[1][2]) == 0 and len(beams[0][2]) > 0

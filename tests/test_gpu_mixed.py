@@ -83,10 +83,23 @@ def test_mixed_push_keeps_particles_and_positions():
     edge = nr * dr
     r_gpu = np.sort(np.hypot(x2[:, 0], x2[:, 1]))
     r_ref = np.sort(np.hypot(pl.x[:n], pl.y[:n]))
-    r_gpu = r_gpu[r_gpu < edge - 1e-3]
-    r_ref = r_ref[r_ref < edge - 1e-3]
-    assert len(r_gpu) == len(r_ref)
-    assert np.max(np.abs(r_gpu - r_ref)) < 1e-5
+    # pair the sorted radii within 1e-5; what stays unpaired must sit at the edge
+    only_gpu, only_ref = [], []
+    i = j = 0
+    while i < len(r_ref) and j < len(r_gpu):
+        if abs(r_ref[i] - r_gpu[j]) < 1e-5:
+            i += 1
+            j += 1
+        elif r_ref[i] < r_gpu[j]:
+            only_ref.append(r_ref[i])
+            i += 1
+        else:
+            only_gpu.append(r_gpu[j])
+            j += 1
+    only_ref += list(r_ref[i:])
+    only_gpu += list(r_gpu[j:])
+    assert len(only_ref) <= 2 and len(only_gpu) <= 2, (only_ref, only_gpu)
+    assert all(r > edge - 1e-3 for r in only_ref + only_gpu), (edge, only_ref, only_gpu)
     # the path keeps particles sorted by radial cell
     assert np.all(np.diff(np.floor(np.hypot(x2[:, 0], x2[:, 1]) / dr)) >= -1)
     sim.close()
