@@ -675,8 +675,10 @@ extern "C" int qpad_species_reset(qpad_species* sp) {
         return check_launch(ctx, "reset copy");
   }
   *sp->h_count = sp->np;
-  return cuda_check(ctx, cudaMemcpyAsync(sp->d_count, sp->h_count, sizeof(int64_t), cudaMemcpyHostToDevice,
-                                         ctx->stream), "reset count");
+  if (int r = cuda_check(ctx, cudaMemcpyAsync(sp->d_count, sp->h_count, sizeof(int64_t), cudaMemcpyHostToDevice,
+                                              ctx->stream), "reset count"))
+    return r;
+  return is_mixed(sp) ? mixed_index(sp) : 0;
 }
 
 extern "C" int qpad_species_count(qpad_species* sp, int64_t* np) {

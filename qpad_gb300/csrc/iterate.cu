@@ -72,8 +72,58 @@ struct RawFin {
   }
 };
 
+// Composite of the per-CTA maps (B, A) published in maps[rhs] by the other CTAs of the
+// cluster, applied to 0: forward, the CTAs before `rank` in increasing order; backward,
+// the CTAs after it in decreasing order.  Lane l of the right-hand side's group composes
+// a block of up to kQB consecutive maps (their remote loads all in flight together) and a
+// shuffle scan over the group joins the blocks.  Every lane of the warp must call it.
+static constexpr int kQB = (16 + kLanes - 1) / kLanes;
+__device__ __forceinline__ double compose_maps(const cg::cluster_group& cluster, double* maps, int rhs, bool act,
+                                               int l, int rank, int CL, bool forward) {
+  double cA = 0.0, cB = 1.0;
+#pragma unroll
+  for (int j = 0; j < kQB; ++j) {
+    const int n = l * kQB + j;                       // position in the composition order
+    const int q = forward ? n : CL - 1 - n;
+    if (act && (forward ? q < rank : q > rank)) {
+      const double* mq = cluster.map_shared_rank(maps + 2 * rhs, q);
+      const double Bq = mq[0], Aq = mq[1];
+      cA = Aq + Bq * cA;
+      cB = Bq * cB;
+    }
+  }
+#pragma unroll
+  for (int off = 1; off < kLanes; off <<= 1) {
+    const double Ao = __shfl_up_sync(0xffffffffu, cA, off, kLanes);
+    const double Bo = __shfl_up_sync(0xffffffffu, cB, off, kLanes);
+    if (l >= off) {
+      cA = cA + cB * Ao;
+      cB = cB * Bo;
+    }
+  }
+  return __shfl_sync(0xffffffffu, cA, kLanes - 1, kLanes);
+}
+
+// Shared-memory view of a staged node window: component `c0 + c` of part p (the Re or
+// the Im part of this CTA's mode) at node i.
+struct WinF {
+  const double* w;
+  int W, wb, pr, c0;
+  __device__ __forceinline__ double operator()(int p, int c, int i) const {
+    return w[((c0 + c) * 2 + (p == pr ? 0 : 1)) * W + (i - wb)];
+  }
+};
+
+// Shared-memory staging of one CTA (doubles): the finished deposits on the node window
+// [r0-1, r1+2] (cu 0..2, amu 3..5, acu 6..7), b_spe components 0..1 and b_beam on the owned
+// nodes, psi on the window, the factor rows of the three matrices, the right-hand sides.
+__host__ __device__ inline size_t iterate_smem_doubles(int R) {
+  const size_t W = (size_t)R + 4;
+  return 16 * W + 4 * (size_t)R + 6 * (size_t)R + 2 * W + 9 * (size_t)R + (size_t)kMaxRhs * R;
+}
+
 __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
-  extern __shared__ double dsm[];                // d[kMaxRhs][R]
+  extern __shared__ double smem[];
   __shared__ double fwd[kMaxRhs][2], bwd[kMaxRhs][2];
   __shared__ double wpart[kIterThreads / 32];
   __shared__ double divp;
@@ -85,16 +135,57 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   const int m = blockIdx.x / CL;
   const int nr = G.nr, ld = G.ld, P = G.P;
   const int pr = part_re(m), pi = part_im(m);
+  const int nh = m == 0 ? 1 : 2;                 // parts of this mode
   const int nrhs = m == 0 ? 4 : 8;
-  const int r0 = min(rank * a.R, nr), r1 = min(r0 + a.R, nr);
+  const int R = a.R;
+  const int r0 = min(rank * R, nr), r1 = min(r0 + R, nr);
   const int Rc = r1 - r0;
   const int t = threadIdx.x;
+  const int W = R + 4, wb = r0 - 1;
   const size_t P1 = (size_t)P * ld;
   double* raw_cu = a.raw;
   double* raw_amu = a.raw + 3 * P1;
   double* raw_acu = a.raw + 6 * P1;
-  const RawFin CU{&G, raw_cu, m, 0, 3}, AMU{&G, raw_amu, m, 1, 3}, ACU{&G, raw_acu, m, 2, 2};
-  const GlobalF BO{a.b_spe, ld, 3};
+  double* win = smem;                            // [8][2][W]
+  double* bo = win + 16 * W;                     // [2][2][R]
+  double* bbm = bo + 4 * R;                      // [3][2][R]
+  double* psw = bbm + 6 * R;                     // [2][W]
+  double* facs = psw + 2 * W;                    // [3 kinds][w, ib, g][R]
+  double* dsm = facs + 9 * R;                    // [kMaxRhs][R]
+
+  // ---- staging: every load of the iteration's inputs in flight at once ------------------
+  for (int q = t; q < 8 * nh * W; q += blockDim.x) {
+    const int c8 = q / (nh * W), h = (q / W) % nh, node = wb + q % W;
+    const int p = h == 0 ? pr : pi;
+    double v = 0.0;
+    if (node >= 0 && node <= nr + 1) {
+      if (c8 < 3) v = finish_amj(G, m, 0, c8, node, raw_cu[fidx(ld, 3, p, c8, node)]);
+      else if (c8 < 6) v = finish_amj(G, m, 1, c8 - 3, node, raw_amu[fidx(ld, 3, p, c8 - 3, node)]);
+      else v = finish_amj(G, m, 2, c8 - 6, node, raw_acu[fidx(ld, 2, p, c8 - 6, node)]);
+    }
+    win[(c8 * 2 + h) * W + q % W] = v;
+  }
+  for (int q = t; q < nh * W; q += blockDim.x) {
+    const int h = q / W, node = wb + q % W;
+    psw[h * W + q % W] = (node >= 0 && node <= nr + 1) ? a.psi[fidx(ld, 1, h == 0 ? pr : pi, 0, node)] : 0.0;
+  }
+  for (int q = t; q < 5 * nh * R; q += blockDim.x) {
+    const int c5 = q / (nh * R), h = (q / R) % nh, k = q % R;
+    if (k >= Rc) continue;
+    const int p = h == 0 ? pr : pi, i = r0 + 1 + k;
+    if (c5 < 2) bo[(c5 * 2 + h) * R + k] = a.b_spe[fidx(ld, 3, p, c5, i)];
+    else bbm[((c5 - 2) * 2 + h) * R + k] = a.b_beam[fidx(ld, 3, p, c5 - 2, i)];
+  }
+  for (int q = t; q < 9 * R; q += blockDim.x) {
+    const int ka = q / (3 * R), arr = (q / R) % 3, k = q % R;
+    if (k >= Rc) continue;
+    const int kind = ka == 0 ? OK_BPLUS : ka == 1 ? OK_BMINUS : OK_GEN;
+    facs[q] = a.fac[fac_off(nr, G.M, kind, m) + (size_t)arr * nr + r0 + k];
+  }
+  __syncthreads();
+  const WinF CU{win, W, wb, pr, 0}, AMU{win, W, wb, pr, 3}, ACU{win, W, wb, pr, 6};
+  const WinF PS{psw, W, wb, pr, 0};
+  const auto BO = [&](int p, int c, int i) { return bo[(c * 2 + (p == pr ? 0 : 1)) * R + (i - r0 - 1)]; };
 
   // ---- sources, one thread per owned node ---------------------------------------------
   double div = 0.0;
@@ -111,43 +202,34 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     row_ez_src(G, m, i, CU, er, ei, in_div);
     if (in_div) div += er * (double)(i - 1);
     if (m == 0) {
-      dsm[0 * a.R + k] = bt[0];
-      dsm[1 * a.R + k] = bt[1];
-      dsm[2 * a.R + k] = zr;
-      dsm[3 * a.R + k] = er;
+      dsm[0 * R + k] = bt[0];
+      dsm[1 * R + k] = bt[1];
+      dsm[2 * R + k] = zr;
+      dsm[3 * R + k] = er;
     } else {
-      dsm[0 * a.R + k] = bt[0];
-      dsm[1 * a.R + k] = bt[2];
-      dsm[2 * a.R + k] = zr;
-      dsm[3 * a.R + k] = er;
-      dsm[4 * a.R + k] = bt[1];
-      dsm[5 * a.R + k] = bt[3];
-      dsm[6 * a.R + k] = zi;
-      dsm[7 * a.R + k] = ei;
+      dsm[0 * R + k] = bt[0];
+      dsm[1 * R + k] = bt[2];
+      dsm[2 * R + k] = zr;
+      dsm[3 * R + k] = er;
+      dsm[4 * R + k] = bt[1];
+      dsm[5 * R + k] = bt[3];
+      dsm[6 * R + k] = zi;
+      dsm[7 * R + k] = ei;
     }
-    // finished deposits and dJ/dxi of this node
-    for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
-      const int p = h == 0 ? pr : pi;
-      for (int c = 0; c < 3; ++c) {
-        a.cu[fidx(ld, 3, p, c, i)] = CU(p, c, i);
-        a.amu[fidx(ld, 3, p, c, i)] = AMU(p, c, i);
-      }
-      for (int c = 0; c < 2; ++c) {
-        a.acu[fidx(ld, 2, p, c, i)] = ACU(p, c, i);
-        a.dcu[fidx(ld, 2, p, c, i)] = dj[2 * h + c];
-      }
-    }
+    for (int h = 0; h < nh; ++h)
+      for (int c = 0; c < 2; ++c) a.dcu[fidx(ld, 2, h == 0 ? pr : pi, c, i)] = dj[2 * h + c];
   }
-  // guard nodes 0 and nr+1 of the finished deposits
-  if (t < 2 && ((t == 0 && rank == 0) || (t == 1 && rank == CL - 1))) {
-    const int i = t == 0 ? 0 : nr + 1;
-    for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
+  // finished deposits of the owned nodes (and of the guard nodes at the two ends)
+  {
+    const int i0 = rank == 0 ? 0 : r0 + 1, i1 = rank == CL - 1 ? nr + 1 : r1;
+    const int nn = i1 - i0 + 1;
+    for (int q = t; q < 8 * nh * nn; q += blockDim.x) {
+      const int c8 = q / (nh * nn), h = (q / nn) % nh, i = i0 + q % nn;
       const int p = h == 0 ? pr : pi;
-      for (int c = 0; c < 3; ++c) {
-        a.cu[fidx(ld, 3, p, c, i)] = CU(p, c, i);
-        a.amu[fidx(ld, 3, p, c, i)] = AMU(p, c, i);
-      }
-      for (int c = 0; c < 2; ++c) a.acu[fidx(ld, 2, p, c, i)] = ACU(p, c, i);
+      const double v = win[(c8 * 2 + h) * W + (i - wb)];
+      if (c8 < 3) a.cu[fidx(ld, 3, p, c8, i)] = v;
+      else if (c8 < 6) a.amu[fidx(ld, 3, p, c8 - 3, i)] = v;
+      else a.acu[fidx(ld, 2, p, c8 - 6, i)] = v;
     }
   }
   // the m = 0 axis row of Ez needs the weighted sum over the whole line
@@ -164,7 +246,8 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     if (rank == 0 && t == 0) {
       double s = 0.0;
       for (int q = 0; q < CL; ++q) s += *cluster.map_shared_rank(&divp, q);
-      dsm[3 * a.R + 0] = ez_axis_row(G, s, CU);
+      const RawFin CUg{&G, raw_cu, 0, 0, 3};      // nodes nr-2, nr-1 lie outside this window
+      dsm[3 * R + 0] = ez_axis_row(G, s, CUg);
     }
   }
   __syncthreads();
@@ -175,17 +258,17 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   const bool act = rhs < nrhs;
   const int RL = (Rc + kLanes - 1) / kLanes;
   const int k0 = min(l * RL, Rc), k1 = min(k0 + RL, Rc);
-  const int kind = (rhs & 3) == 0 ? OK_BPLUS : (rhs & 3) == 1 ? OK_BMINUS : OK_GEN;
-  const double* fw = a.fac + fac_off(nr, G.M, kind, m);
-  const double* fib = fw + nr;
-  const double* fg = fib + nr;
-  double* d = dsm + (size_t)(act ? rhs : 0) * a.R;
+  const int ka = (rhs & 3) < 2 ? (rhs & 3) : 2;          // B+, B-, then the shared Bz / Ez matrix
+  const double* fw = facs + ka * 3 * R;
+  const double* fib = fw + R;
+  const double* fg = fib + R;
+  double* d = dsm + (size_t)(act ? rhs : 0) * R;
   double Aex = 0.0, Bex = 1.0;
   if (solver) {
     double A = 0.0, B = 1.0;
     if (act)
       for (int k = k0; k < k1; ++k) {
-        const double w = fw[r0 + k];
+        const double w = fw[k];
         A = d[k] - w * A;
         B = -w * B;
       }
@@ -210,15 +293,12 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     }
   }
   cluster.sync();
+  double carry = 0.0;                                 // y at the row before this CTA
+  if (solver) carry = compose_maps(cluster, &fwd[0][0], rhs, act, l, rank, CL, true);
   if (solver && act) {
-    double y = 0.0;                                   // y at the row before this CTA
-    for (int q = 0; q < rank; ++q) {
-      const double* mq = cluster.map_shared_rank(&fwd[rhs][0], q);
-      y = mq[1] + mq[0] * y;
-    }
-    y = Aex + Bex * y;
+    double y = Aex + Bex * carry;
     for (int k = k0; k < k1; ++k) {
-      y = d[k] - fw[r0 + k] * y;
+      y = d[k] - fw[k] * y;
       d[k] = y;
     }
   }
@@ -248,8 +328,8 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     double A = 0.0, B = 1.0;
     if (act)
       for (int k = k1 - 1; k >= k0; --k) {
-        const double g = fg[r0 + k];
-        A = d[k] * fib[r0 + k] - g * A;
+        const double g = fg[k];
+        A = d[k] * fib[k] - g * A;
         B = -g * B;
       }
 #pragma unroll
@@ -273,15 +353,12 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     }
   }
   cluster.sync();
+  carry = 0.0;                                        // x at the row after this CTA
+  if (solver) carry = compose_maps(cluster, &bwd[0][0], rhs, act, l, rank, CL, false);
   if (solver && act) {
-    double x = 0.0;                                   // x at the row after this CTA
-    for (int q = CL - 1; q > rank; --q) {
-      const double* mq = cluster.map_shared_rank(&bwd[rhs][0], q);
-      x = mq[1] + mq[0] * x;
-    }
-    x = Aex + Bex * x;
+    double x = Aex + Bex * carry;
     for (int k = k1 - 1; k >= k0; --k) {
-      x = d[k] * fib[r0 + k] - fg[r0 + k] * x;
+      x = d[k] * fib[k] - fg[k] * x;
       d[k] = x;
     }
   }
@@ -292,67 +369,68 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   // ---- fields of the owned nodes -------------------------------------------------------
   for (int k = t; k < Rc; k += blockDim.x) {
     const int i = r0 + k + 1;
-    double bs[2][3], bb[2][3];
+    double bs[2][3], bb[2][3], ee[2][3];
     if (m == 0) {
-      bs[0][0] = (i == 1) ? 0.0 : dsm[0 * a.R + k];
-      bs[0][1] = (i == 1) ? 0.0 : dsm[1 * a.R + k];
-      bs[0][2] = dsm[2 * a.R + k];
-      a.e[fidx(ld, 3, 0, 2, i)] = dsm[3 * a.R + k];
+      bs[0][0] = (i == 1) ? 0.0 : dsm[0 * R + k];
+      bs[0][1] = (i == 1) ? 0.0 : dsm[1 * R + k];
+      bs[0][2] = dsm[2 * R + k];
+      ee[0][2] = dsm[3 * R + k];
     } else {
       const bool zero = (i == 1 && m != 1);
-      const double b1re = dsm[0 * a.R + k], b2re = dsm[1 * a.R + k];
-      const double b1im = dsm[4 * a.R + k], b2im = dsm[5 * a.R + k];
+      const double b1re = dsm[0 * R + k], b2re = dsm[1 * R + k];
+      const double b1im = dsm[4 * R + k], b2im = dsm[5 * R + k];
       bs[0][0] = zero ? 0.0 : 0.5 * (b1re + b2re);
       bs[1][0] = zero ? 0.0 : 0.5 * (b1im + b2im);
       bs[0][1] = zero ? 0.0 : 0.5 * (b1im - b2im);
       bs[1][1] = zero ? 0.0 : 0.5 * (-b1re + b2re);
-      bs[0][2] = (i == 1) ? 0.0 : dsm[2 * a.R + k];
-      bs[1][2] = (i == 1) ? 0.0 : dsm[6 * a.R + k];
-      a.e[fidx(ld, 3, pr, 2, i)] = (i == 1) ? 0.0 : dsm[3 * a.R + k];
-      a.e[fidx(ld, 3, pi, 2, i)] = (i == 1) ? 0.0 : dsm[7 * a.R + k];
+      bs[0][2] = (i == 1) ? 0.0 : dsm[2 * R + k];
+      bs[1][2] = (i == 1) ? 0.0 : dsm[6 * R + k];
+      ee[0][2] = (i == 1) ? 0.0 : dsm[3 * R + k];
+      ee[1][2] = (i == 1) ? 0.0 : dsm[7 * R + k];
     }
-    const int nh = m == 0 ? 1 : 2;
+    for (int h = 0; h < nh; ++h)
+      for (int c = 0; c < 3; ++c) bb[h][c] = bs[h][c] + bbm[(c * 2 + h) * R + k];
+    const auto Bn = [&](int p, int c, int) { return p == pr ? bb[0][c] : bb[1][c]; };
+    double et[4];
+    row_et(G, m, i, Bn, PS, et);
+    if (m == 0) {
+      ee[0][0] = et[0];
+      ee[0][1] = et[1];
+    } else {
+      ee[0][0] = et[0];
+      ee[1][0] = et[1];
+      ee[0][1] = et[2];
+      ee[1][1] = et[3];
+    }
     for (int h = 0; h < nh; ++h) {
       const int p = h == 0 ? pr : pi;
       for (int c = 0; c < 3; ++c) {
         a.b_spe[fidx(ld, 3, p, c, i)] = bs[h][c];
-        bb[h][c] = bs[h][c] + a.b_beam[fidx(ld, 3, p, c, i)];
         a.b[fidx(ld, 3, p, c, i)] = bb[h][c];
+        a.e[fidx(ld, 3, p, c, i)] = ee[h][c];
+      }
+      if (a.gtab) {
+        float* T = a.gtab + ((size_t)i * P + p) * 6;
+        for (int c = 0; c < 3; ++c) {
+          T[c] = (float)ee[h][c];
+          T[3 + c] = (float)bb[h][c];
+        }
       }
     }
-    const auto Bn = [&](int p, int c, int) { return p == pr ? bb[0][c] : bb[1][c]; };
-    double et[4];
-    row_et(G, m, i, Bn, GlobalF{a.psi, ld, 1}, et);
-    if (m == 0) {
-      a.e[fidx(ld, 3, 0, 0, i)] = et[0];
-      a.e[fidx(ld, 3, 0, 1, i)] = et[1];
-    } else {
-      a.e[fidx(ld, 3, pr, 0, i)] = et[0];
-      a.e[fidx(ld, 3, pi, 0, i)] = et[1];
-      a.e[fidx(ld, 3, pr, 1, i)] = et[2];
-      a.e[fidx(ld, 3, pi, 1, i)] = et[3];
-    }
   }
-  // guard nodes of b = b_spe + b_beam
+  // guard nodes: b = b_spe + b_beam there too, and their gather-table records
   if (t < 2 && ((t == 0 && rank == 0) || (t == 1 && rank == CL - 1))) {
     const int i = t == 0 ? 0 : nr + 1;
-    for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
+    for (int h = 0; h < nh; ++h) {
       const int p = h == 0 ? pr : pi;
-      for (int c = 0; c < 3; ++c)
-        a.b[fidx(ld, 3, p, c, i)] = a.b_spe[fidx(ld, 3, p, c, i)] + a.b_beam[fidx(ld, 3, p, c, i)];
-    }
-  }
-  __syncthreads();
-  if (a.gtab) {
-    const int i0 = rank == 0 ? 0 : r0 + 1;
-    const int i1 = rank == CL - 1 ? nr + 1 : r1;
-    const int nh = m == 0 ? 1 : 2;
-    const int n = (i1 - i0 + 1) * nh * 6;
-    for (int q = t; q < n; q += blockDim.x) {
-      const int c = q % 6, h = (q / 6) % nh, i = i0 + q / (6 * nh);
-      const int p = h == 0 ? pr : pi;
-      const double v = c < 3 ? a.e[fidx(ld, 3, p, c, i)] : a.b[fidx(ld, 3, p, c - 3, i)];
-      a.gtab[((size_t)i * P + p) * 6 + c] = (float)v;
+      for (int c = 0; c < 3; ++c) {
+        const double v = a.b_spe[fidx(ld, 3, p, c, i)] + a.b_beam[fidx(ld, 3, p, c, i)];
+        a.b[fidx(ld, 3, p, c, i)] = v;
+        if (a.gtab) {
+          a.gtab[((size_t)i * P + p) * 6 + 3 + c] = (float)v;
+          a.gtab[((size_t)i * P + p) * 6 + c] = (float)a.e[fidx(ld, 3, p, c, i)];
+        }
+      }
     }
   }
 
@@ -418,7 +496,7 @@ int iterate_setup(qpad_ctx* ctx) {
   if (e != cudaSuccess) return cuda_check(ctx, e, "cluster attribute");
   for (int cl = cluster_for(ctx->g.nr); cl >= 1; cl /= 2) {
     const int R = (ctx->g.nr + cl - 1) / cl;
-    const size_t smem = (size_t)kMaxRhs * R * sizeof(double);
+    const size_t smem = iterate_smem_doubles(R) * sizeof(double);
     if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return cuda_check(ctx, e, "iterate smem");
@@ -481,7 +559,7 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cl * (ctx->g.M + 1));
   cfg.blockDim = dim3(kIterThreads);
-  cfg.dynamicSmemBytes = (size_t)kMaxRhs * a.R * sizeof(double);
+  cfg.dynamicSmemBytes = iterate_smem_doubles(a.R) * sizeof(double);
   cfg.stream = ctx->stream;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;

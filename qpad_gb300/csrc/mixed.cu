@@ -25,9 +25,9 @@
 namespace qpad {
 
 static constexpr int kMixThreads = 256;
-static constexpr int kMixRounds = 2;
-static constexpr int kChunk = kMixThreads * kMixRounds;   // particles per CTA in the deposits
-static constexpr int kTileNodes = 64;                     // radial window of the FP32 tile
+static constexpr int kItem = 128;                         // particles per deposit work item (one warp)
+static constexpr int kPPL = kItem / 32;                   // particles per lane in a work item
+static constexpr int kItemThreads = 128;                  // four work items per CTA
 #define FULL 0xffffffffu
 
 struct MArr {
@@ -110,253 +110,233 @@ __device__ __forceinline__ void mgather(const float* __restrict__ T, int P, int 
   }
 }
 
-// Adds NV values of this lane into tile[base .. base+NV) -- one reduced atomic per value
-// when the whole warp shares the destination, else one atomic per lane.
-template <int NV>
-__device__ __forceinline__ void warp_tile_add(float* tile, int base, const float (&v)[NV], bool full, bool valid,
-                                              int lane) {
-  if (full) {
+// Sum over the 32 lanes of each of 32 values: after the exchange, lane l holds in a[0]
+// the total of value l (a transposing butterfly, 31 shuffles for 32 sums).
+__device__ __forceinline__ void butterfly32(float (&a)[32], int lane) {
 #pragma unroll
-    for (int c = 0; c < NV; ++c) {
-      float s = v[c];
-      s += __shfl_xor_sync(FULL, s, 16);
-      s += __shfl_xor_sync(FULL, s, 8);
-      s += __shfl_xor_sync(FULL, s, 4);
-      s += __shfl_xor_sync(FULL, s, 2);
-      s += __shfl_xor_sync(FULL, s, 1);
-      if (lane == 0) atomicAdd(tile + base + c, s);
-    }
-  } else if (valid) {
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool up = (lane & s) != 0;
 #pragma unroll
-    for (int c = 0; c < NV; ++c) atomicAdd(tile + base + c, v[c]);
-  }
-}
-
-// ------------------------------------------------------------------------------------
-// charge deposit (ρ - Jz): tile entries [node][part]
-// ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kMixThreads) k_mqdeposit(GridDev G, const int64_t* __restrict__ n_ptr, MArr A,
-                                                           double* __restrict__ qraw) {
-  __shared__ float tile[kTileNodes * QPAD_MAX_PARTS];
-  const int64_t n = *n_ptr;
-  const int64_t c0 = (int64_t)blockIdx.x * kChunk;
-  if (c0 >= n) return;
-  const int64_t c1 = min(c0 + kChunk, n);
-  const int k0 = A.key[c0], k1 = A.key[c1 - 1];
-  const int W = k1 - k0 + 2;
-  const bool use_tile = W <= kTileNodes && k0 >= 1;
-  const int P = G.P, ld = G.ld;
-  if (use_tile)
-    for (int k = threadIdx.x; k < W * P; k += blockDim.x) tile[k] = 0.0f;
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int r = 0; r < kMixRounds; ++r) {
-    const int64_t i = c0 + (int64_t)warp * 32 * kMixRounds + r * 32 + lane;
-    const bool valid = i < c1;
-    MInterp ii;
-    float q = 0.0f;
-    if (valid) {
-      ii = minterp(A.cxy[i], A.fx[i], A.fy[i], G.nr);
-      q = A.q[i];
-    } else {
-      ii.ok = false; ii.idx = 1; ii.w0 = ii.w1 = 0.0f; ii.pcos = 1.0f; ii.psin = 0.0f;
-    }
-    const bool live = valid && ii.ok;
-    const unsigned grp = __match_any_sync(FULL, live ? ii.idx : -1 - lane);
-    const bool inwin = use_tile && ii.idx >= k0 && ii.idx <= k1;
-    const bool full = grp == FULL && inwin;                      // warp-uniform
-    const bool tile_lane = full || (inwin && live);
-    const float wj[2] = {ii.w0, ii.w1};
-    if (tile_lane) {
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const float v[1] = {wj[j] * q};
-        warp_tile_add<1>(tile, (ii.idx + j - k0) * P, v, full, live, lane);
-      }
-    } else if (live) {
-#pragma unroll
-      for (int j = 0; j < 2; ++j) atomicAdd(qraw + ii.idx + j, (double)(wj[j] * q));
-    }
-    float phr = q, phi = 0.0f;
-    const float ph0r = ii.pcos, ph0i = -ii.psin;
-    for (int m = 1; m <= G.M; ++m) {
-      const float t = phr * ph0r - phi * ph0i;
-      phi = phr * ph0i + phi * ph0r;
-      phr = t;
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        if (tile_lane) {
-          const int base = (ii.idx + j - k0) * P + 2 * m - 1;
-          const float v[2] = {wj[j] * phr, wj[j] * phi};
-          warp_tile_add<2>(tile, base, v, full, live, lane);
-        } else if (live) {
-          atomicAdd(qraw + (size_t)(2 * m - 1) * ld + ii.idx + j, (double)(wj[j] * phr));
-          atomicAdd(qraw + (size_t)(2 * m) * ld + ii.idx + j, (double)(wj[j] * phi));
-        }
-      }
-    }
-  }
-  if (!use_tile) return;
-  __syncthreads();
-  for (int k = threadIdx.x; k < W * P; k += blockDim.x) {
-    const float v = tile[k];
-    if (v != 0.0f) {
-      const int nl = k / P, p = k % P;
-      atomicAdd(qraw + (size_t)p * ld + k0 + nl, (double)v);
+    for (int k = 0; k < s; ++k) {
+      const float send = up ? a[k] : a[k + s];
+      const float keep = up ? a[k + s] : a[k];
+      a[k] = keep + __shfl_xor_sync(FULL, send, s);
     }
   }
 }
 
 // ------------------------------------------------------------------------------------
-// current / acceleration / momentum-flux deposit with the predictor push
-// tile entries [node][part][8]: cu 0..2, acu 3..4, amu 5..7
+// charge deposit (rho - Jz), one warp per work item (kItem particles of one cell)
 // ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kMixThreads) k_mamjdp(GridDev G, int push_type, float qbm, float dt,
-                                                        const int64_t* __restrict__ n_ptr, MArr A,
-                                                        const float* __restrict__ T, double* __restrict__ cu,
-                                                        double* __restrict__ amu, double* __restrict__ acu,
-                                                        int write_back) {
-  __shared__ float tile[kTileNodes * QPAD_MAX_PARTS * 8];
-  const int64_t n = *n_ptr;
-  const int64_t c0 = (int64_t)blockIdx.x * kChunk;
-  if (c0 >= n) return;
-  const int64_t c1 = min(c0 + kChunk, n);
-  const int k0 = A.key[c0], k1 = A.key[c1 - 1];
-  const int W = k1 - k0 + 2;
-  const bool use_tile = W <= kTileNodes && k0 >= 1;
-  const int P = G.P, ld = G.ld, M = G.M;
-  if (use_tile)
-    for (int k = threadIdx.x; k < W * P * 8; k += blockDim.x) tile[k] = 0.0f;
-  __syncthreads();
-  const float idt = 1.0f / dt, qtmh = 0.5f * qbm * dt;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int r = 0; r < kMixRounds; ++r) {
-    const int64_t i = c0 + (int64_t)warp * 32 * kMixRounds + r * 32 + lane;
-    const bool valid = i < c1;
-    float v[8];
-    MInterp ii;
-    float qq = 0.0f;
-    if (valid) {
-      ii = minterp(A.cxy[i], A.fx[i], A.fy[i], G.nr);
-      float ep[3], bp[3], wp[3], u0[3], u[3], ut[3];
-      mgather(T, P, M, ii, ep, bp);
-      wp[0] = ep[0] - bp[1];
-      wp[1] = ep[1] + bp[0];
-      wp[2] = ep[2];
-      const float p1 = A.px[i], p2 = A.py[i];
-      u0[0] = p1 * ii.pcos + p2 * ii.psin;
-      u0[1] = p2 * ii.pcos - p1 * ii.psin;
-      u0[2] = A.pz[i];
-      const float psi_in = A.psi[i];
-      if (push_type == QPAD_PUSH2_ROBUST) {
-        float gam = sqrtf(1.0f + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
-        const float qtmh1 = qtmh * gam / (gam - u0[2]);
+__global__ void __launch_bounds__(kItemThreads) k_mqdeposit(GridDev G, const int4* __restrict__ items,
+                                                            const int* __restrict__ n_items, MArr A,
+                                                            double* __restrict__ qraw) {
+  const int lane = threadIdx.x & 31;
+  const int it = blockIdx.x * (kItemThreads / 32) + (threadIdx.x >> 5);
+  if (it >= *n_items) return;                          // warp-uniform
+  const int4 item = items[it];
+  const int key = item.x, start = item.y, cnt = item.z;
+  float wq[kPPL][2], pc[kPPL][2];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) { ep[c] *= qtmh1; ut[c] = u0[c] + ep[c]; }
-        gam = sqrtf(1.0f + ut[0] * ut[0] + ut[1] * ut[1] + ut[2] * ut[2]);
-        const float qtmh2 = qtmh / (gam - ut[2]);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) bp[c] *= qtmh2;
-      } else {
-        const float gam = sqrtf(1.0f + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
-        const float qtmh2 = qtmh / (1.0f - qbm * psi_in);
-        const float qtmh1 = qtmh2 * gam;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) { bp[c] *= qtmh2; ut[c] = u0[c] + ep[c] * qtmh1; }
+  for (int j = 0; j < kPPL; ++j) {
+    const int o = j * 32 + lane;
+    wq[j][0] = wq[j][1] = 0.0f;
+    pc[j][0] = 1.0f;
+    pc[j][1] = 0.0f;
+    if (o < cnt) {
+      const int i = start + o;
+      const MInterp ii = minterp(A.cxy[i], A.fx[i], A.fy[i], G.nr);
+      if (ii.ok) {
+        const float q = A.q[i];
+        wq[j][0] = q * ii.w0;
+        wq[j][1] = q * ii.w1;
+        pc[j][0] = ii.pcos;
+        pc[j][1] = -ii.psin;
       }
-      u[0] = ut[0] + ut[1] * bp[2] - ut[2] * bp[1];
-      u[1] = ut[1] + ut[2] * bp[0] - ut[0] * bp[2];
-      u[2] = ut[2] + ut[0] * bp[1] - ut[1] * bp[0];
-      const float ostq = 2.0f / (1.0f + bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2]);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) bp[c] *= ostq;
-      {
-        const float t0 = ut[0] + u[1] * bp[2] - u[2] * bp[1];
-        const float t1 = ut[1] + u[2] * bp[0] - u[0] * bp[2];
-        const float t2 = ut[2] + u[0] * bp[1] - u[1] * bp[0];
-        ut[0] = t0; ut[1] = t1; ut[2] = t2;
-      }
-      if (push_type == QPAD_PUSH2_ROBUST) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) u[c] = ut[c] + ep[c];
-      } else {
-        const float gam = sqrtf(1.0f + ut[0] * ut[0] + ut[1] * ut[1] + ut[2] * ut[2]);
-        const float qtmh1 = qtmh / (1.0f - qbm * psi_in) * gam;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) u[c] = ut[c] + ep[c] * qtmh1;
-      }
-      float du0 = idt * (u[0] - u0[0]);
-      float du1 = idt * (u[1] - u0[1]);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) u[c] = 0.5f * (u[c] + u0[c]);
-      const float g = sqrtf(1.0f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
-      float ipsi;
-      if (push_type == QPAD_PUSH2_ROBUST) {
-        ipsi = 1.0f / (g - u[2]);
-        if (write_back) { A.gam[i] = g; A.psi[i] = (1.0f - 1.0f / ipsi) / qbm; }
-      } else {
-        ipsi = 1.0f / (1.0f - qbm * psi_in);
-        A.gam[i] = g;
-      }
-      const float dpsi = qbm * (wp[2] - (wp[0] * u[0] + wp[1] * u[1]) * ipsi);
-      du0 += u[0] * dpsi * ipsi;
-      du1 += u[1] * dpsi * ipsi;
-      v[0] = u[0]; v[1] = u[1]; v[2] = u[2]; v[3] = du0; v[4] = du1;
-      v[5] = u[0] * u[0] * ipsi; v[6] = u[0] * u[1] * ipsi; v[7] = u[1] * u[1] * ipsi;
-      qq = A.q[i] * ipsi;
-    } else {
-      ii.ok = false; ii.idx = 1; ii.w0 = ii.w1 = 0.0f; ii.pcos = 1.0f; ii.psin = 0.0f;
-#pragma unroll
-      for (int c = 0; c < 8; ++c) v[c] = 0.0f;
     }
-    const bool live = valid && ii.ok;
-    const unsigned grp = __match_any_sync(FULL, live ? ii.idx : -1 - lane);
-    const bool inwin = use_tile && ii.idx >= k0 && ii.idx <= k1;
-    const bool full = grp == FULL && inwin;                      // warp-uniform
-    const bool tile_lane = full || (inwin && live);
-    const float wj[2] = {ii.w0, ii.w1};
-    float phr = qq, phi = 0.0f;
-    const float ph0r = ii.pcos, ph0i = -ii.psin;
-    for (int m = 0; m <= M; ++m) {
+  }
+  float ph[kPPL][2];
+#pragma unroll
+  for (int j = 0; j < kPPL; ++j) { ph[j][0] = 1.0f; ph[j][1] = 0.0f; }
+  for (int m = 0; m <= G.M; ++m) {
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};          // [node 0/1][re, im]
+#pragma unroll
+    for (int j = 0; j < kPPL; ++j) {
       if (m > 0) {
-        const float t = phr * ph0r - phi * ph0i;
-        phi = phr * ph0i + phi * ph0r;
-        phr = t;
+        const float t = ph[j][0] * pc[j][0] - ph[j][1] * pc[j][1];
+        ph[j][1] = ph[j][0] * pc[j][1] + ph[j][1] * pc[j][0];
+        ph[j][0] = t;
       }
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const int node = ii.idx + j;
-        const int ph = m == 0 ? 1 : 2;
-        for (int h = 0; h < ph; ++h) {
-          const int p = m == 0 ? 0 : 2 * m - 1 + h;
-          const float w = wj[j] * (h == 0 ? phr : phi);
-          float vv[8];
+      for (int jn = 0; jn < 2; ++jn) {
+        acc[2 * jn] += wq[j][jn] * ph[j][0];
+        acc[2 * jn + 1] += wq[j][jn] * ph[j][1];
+      }
+    }
 #pragma unroll
-          for (int c = 0; c < 8; ++c) vv[c] = w * v[c];
-          if (tile_lane) {
-            warp_tile_add<8>(tile, ((node - k0) * P + p) * 8, vv, full, live, lane);
-          } else if (live) {
+    for (int k = 0; k < 4; ++k)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) atomicAdd(cu + ((size_t)p * 3 + c) * ld + node, (double)vv[c]);
+      for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(FULL, acc[k], off);
+    if (lane < 4) {
+      const int jn = lane >> 1, h = lane & 1;
+      float v = acc[0];
 #pragma unroll
-            for (int c = 0; c < 2; ++c) atomicAdd(acu + ((size_t)p * 2 + c) * ld + node, (double)vv[3 + c]);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) atomicAdd(amu + ((size_t)p * 3 + c) * ld + node, (double)vv[5 + c]);
-          }
-        }
+      for (int k = 1; k < 4; ++k)
+        if (lane == k) v = acc[k];
+      if (!(m == 0 && h == 1) && v != 0.0f) {
+        const int p = m == 0 ? 0 : 2 * m - 1 + h;
+        atomicAdd(qraw + (size_t)p * G.ld + key + jn, (double)v);
       }
     }
   }
-  if (!use_tile) return;
-  __syncthreads();
-  for (int k = threadIdx.x; k < W * P * 8; k += blockDim.x) {
-    const float val = tile[k];
-    if (val == 0.0f) continue;
-    const int c = k & 7, pnode = k >> 3;
-    const int nl = pnode / P, p = pnode % P, node = k0 + nl;
-    double* dst = c < 3 ? cu + ((size_t)p * 3 + c) * ld : (c < 5 ? acu + ((size_t)p * 2 + (c - 3)) * ld
-                                                                 : amu + ((size_t)p * 3 + (c - 5)) * ld);
-    atomicAdd(dst + node, (double)val);
+}
+
+// Predictor push of one particle (amjdeposit_robust / _std): the deposit values
+// v = {u0, u1, u2, du0, du1, u0 u0 / (g - u2) .. } and the charge factor qq = q / (g - u2).
+__device__ __forceinline__ void mpredict(const GridDev& G, int push_type, float qbm, float dt, const MArr& A,
+                                         const float* __restrict__ T, int64_t i, int write_back, const MInterp& ii,
+                                         float v[8], float& qq) {
+  const float idt = 1.0f / dt, qtmh = 0.5f * qbm * dt;
+  float ep[3], bp[3], wp[3], u0[3], u[3], ut[3];
+  mgather(T, G.P, G.M, ii, ep, bp);
+  wp[0] = ep[0] - bp[1];
+  wp[1] = ep[1] + bp[0];
+  wp[2] = ep[2];
+  const float p1 = A.px[i], p2 = A.py[i];
+  u0[0] = p1 * ii.pcos + p2 * ii.psin;
+  u0[1] = p2 * ii.pcos - p1 * ii.psin;
+  u0[2] = A.pz[i];
+  const float psi_in = A.psi[i];
+  if (push_type == QPAD_PUSH2_ROBUST) {
+    float gam = sqrtf(1.0f + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
+    const float qtmh1 = qtmh * gam / (gam - u0[2]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { ep[c] *= qtmh1; ut[c] = u0[c] + ep[c]; }
+    gam = sqrtf(1.0f + ut[0] * ut[0] + ut[1] * ut[1] + ut[2] * ut[2]);
+    const float qtmh2 = qtmh / (gam - ut[2]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) bp[c] *= qtmh2;
+  } else {
+    const float gam = sqrtf(1.0f + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
+    const float qtmh2 = qtmh / (1.0f - qbm * psi_in);
+    const float qtmh1 = qtmh2 * gam;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { bp[c] *= qtmh2; ut[c] = u0[c] + ep[c] * qtmh1; }
+  }
+  u[0] = ut[0] + ut[1] * bp[2] - ut[2] * bp[1];
+  u[1] = ut[1] + ut[2] * bp[0] - ut[0] * bp[2];
+  u[2] = ut[2] + ut[0] * bp[1] - ut[1] * bp[0];
+  const float ostq = 2.0f / (1.0f + bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) bp[c] *= ostq;
+  {
+    const float t0 = ut[0] + u[1] * bp[2] - u[2] * bp[1];
+    const float t1 = ut[1] + u[2] * bp[0] - u[0] * bp[2];
+    const float t2 = ut[2] + u[0] * bp[1] - u[1] * bp[0];
+    ut[0] = t0; ut[1] = t1; ut[2] = t2;
+  }
+  if (push_type == QPAD_PUSH2_ROBUST) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) u[c] = ut[c] + ep[c];
+  } else {
+    const float gam = sqrtf(1.0f + ut[0] * ut[0] + ut[1] * ut[1] + ut[2] * ut[2]);
+    const float qtmh1 = qtmh / (1.0f - qbm * psi_in) * gam;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) u[c] = ut[c] + ep[c] * qtmh1;
+  }
+  float du0 = idt * (u[0] - u0[0]);
+  float du1 = idt * (u[1] - u0[1]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) u[c] = 0.5f * (u[c] + u0[c]);
+  const float g = sqrtf(1.0f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  float ipsi;
+  if (push_type == QPAD_PUSH2_ROBUST) {
+    ipsi = 1.0f / (g - u[2]);
+    if (write_back) { A.gam[i] = g; A.psi[i] = (1.0f - 1.0f / ipsi) / qbm; }
+  } else {
+    ipsi = 1.0f / (1.0f - qbm * psi_in);
+    A.gam[i] = g;
+  }
+  const float dpsi = qbm * (wp[2] - (wp[0] * u[0] + wp[1] * u[1]) * ipsi);
+  du0 += u[0] * dpsi * ipsi;
+  du1 += u[1] * dpsi * ipsi;
+  v[0] = u[0]; v[1] = u[1]; v[2] = u[2]; v[3] = du0; v[4] = du1;
+  v[5] = u[0] * u[0] * ipsi; v[6] = u[0] * u[1] * ipsi; v[7] = u[1] * u[1] * ipsi;
+  qq = A.q[i] * ipsi;
+}
+
+// ------------------------------------------------------------------------------------
+// current / acceleration / momentum-flux deposit with the predictor push, one warp per
+// work item.  Every particle of an item sits in the same cell, so all of them deposit to
+// the same two nodes: per mode, each lane accumulates its particles' 32 values
+// [node 0/1][Re/Im][cu 0..2, acu 3..4, amu 5..7] in registers, one butterfly sums them
+// over the warp, and each lane adds one total into the FP64 arrays.
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_type, float qbm, float dt,
+                                                         const int4* __restrict__ items, const int* __restrict__ n_items,
+                                                         MArr A, const float* __restrict__ T, double* __restrict__ cu,
+                                                         double* __restrict__ amu, double* __restrict__ acu,
+                                                         int write_back) {
+  const int lane = threadIdx.x & 31;
+  const int it = blockIdx.x * (kItemThreads / 32) + (threadIdx.x >> 5);
+  if (it >= *n_items) return;                          // warp-uniform
+  const int4 item = items[it];
+  const int key = item.x, start = item.y, cnt = item.z;
+  const int ld = G.ld;
+  float v[kPPL][8], wq[kPPL][2], pc[kPPL][2];
+#pragma unroll
+  for (int j = 0; j < kPPL; ++j) {
+    const int o = j * 32 + lane;
+    wq[j][0] = wq[j][1] = 0.0f;
+    pc[j][0] = 1.0f;
+    pc[j][1] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[j][c] = 0.0f;
+    if (o < cnt) {
+      const int i = start + o;
+      const MInterp ii = minterp(A.cxy[i], A.fx[i], A.fy[i], G.nr);
+      if (ii.ok) {
+        float qq;
+        mpredict(G, push_type, qbm, dt, A, T, i, write_back, ii, v[j], qq);
+        wq[j][0] = qq * ii.w0;
+        wq[j][1] = qq * ii.w1;
+        pc[j][0] = ii.pcos;
+        pc[j][1] = -ii.psin;
+      }
+    }
+  }
+  float ph[kPPL][2];
+#pragma unroll
+  for (int j = 0; j < kPPL; ++j) { ph[j][0] = 1.0f; ph[j][1] = 0.0f; }
+  const int jn = lane >> 4, h = (lane >> 3) & 1, c = lane & 7;
+  double* dst = c < 3 ? cu + (size_t)c * ld : (c < 5 ? acu + (size_t)(c - 3) * ld : amu + (size_t)(c - 5) * ld);
+  const int ncomp = c < 3 ? 3 : (c < 5 ? 2 : 3);
+  for (int m = 0; m <= G.M; ++m) {
+    float acc[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) acc[k] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kPPL; ++j) {
+      if (m > 0) {
+        const float t = ph[j][0] * pc[j][0] - ph[j][1] * pc[j][1];
+        ph[j][1] = ph[j][0] * pc[j][1] + ph[j][1] * pc[j][0];
+        ph[j][0] = t;
+      }
+#pragma unroll
+      for (int n = 0; n < 2; ++n) {
+        const float cre = wq[j][n] * ph[j][0], cim = wq[j][n] * ph[j][1];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          acc[n * 16 + k] += cre * v[j][k];
+          acc[n * 16 + 8 + k] += cim * v[j][k];
+        }
+      }
+    }
+    butterfly32(acc, lane);
+    if (!(m == 0 && h == 1) && acc[0] != 0.0f) {
+      const int p = m == 0 ? 0 : 2 * m - 1 + h;
+      atomicAdd(dst + (size_t)p * ncomp * ld + key + jn, (double)acc[0]);
+    }
   }
 }
 
@@ -445,39 +425,49 @@ __global__ void __launch_bounds__(kMixThreads) k_mhist(const int64_t* __restrict
   if (valid && (grp & ((1u << lane) - 1u)) == 0) atomicAdd(hist + k, __popc(grp));
 }
 
-__global__ void __launch_bounds__(1024) k_mscan(int nk, const int32_t* __restrict__ hist, int32_t* __restrict__ cursor,
-                                                int64_t* __restrict__ n_ptr, int dead_key) {
-  __shared__ int sh[64];
-  int carry = 0;
+// Exclusive scan of the cell histogram into the scatter cursors and the cell starts, and
+// the deposit work items: cell k (1..nr) of n_k particles becomes ceil(n_k / kItem) items
+// {k, first particle, count}.  One CTA.
+__global__ void __launch_bounds__(1024) k_mscan(int nk, int nr, const int32_t* __restrict__ hist,
+                                                int32_t* __restrict__ cursor, int64_t* __restrict__ n_ptr,
+                                                int dead_key, int4* __restrict__ items, int* __restrict__ n_items) {
+  __shared__ int sh[64], shi[64];
+  int carry = 0, carry_i = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int base = 0; base < nk; base += blockDim.x) {
     const int k = base + threadIdx.x;
     const int v = k < nk ? hist[k] : 0;
-    int x = v;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int ni = (k >= 1 && k <= nr) ? (v + kItem - 1) / kItem : 0;
+    int x = v, xi = ni;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-      const int o = __shfl_up_sync(FULL, x, off);
-      if (lane >= off) x += o;
+      const int o = __shfl_up_sync(FULL, x, off), oi = __shfl_up_sync(FULL, xi, off);
+      if (lane >= off) { x += o; xi += oi; }
     }
-    if (lane == 31) sh[warp] = x;
+    if (lane == 31) { sh[warp] = x; shi[warp] = xi; }
     __syncthreads();
     if (warp == 0) {
-      int w = lane < nw ? sh[lane] : 0;
+      int w = lane < nw ? sh[lane] : 0, wi = lane < nw ? shi[lane] : 0;
 #pragma unroll
       for (int off = 1; off < 32; off <<= 1) {
-        const int o = __shfl_up_sync(FULL, w, off);
-        if (lane >= off) w += o;
+        const int o = __shfl_up_sync(FULL, w, off), oi = __shfl_up_sync(FULL, wi, off);
+        if (lane >= off) { w += o; wi += oi; }
       }
       sh[32 + lane] = w;
+      shi[32 + lane] = wi;
     }
     __syncthreads();
-    const int before = warp > 0 ? sh[32 + warp - 1] : 0;
-    const int tot = sh[32 + nw - 1];
-    if (k < nk) cursor[k] = carry + before + x - v;
-    if (k == dead_key) *n_ptr = carry + before + x - v;    // particles before the removed bucket
+    const int before = warp > 0 ? sh[32 + warp - 1] : 0, before_i = warp > 0 ? shi[32 + warp - 1] : 0;
+    const int tot = sh[32 + nw - 1], tot_i = shi[32 + nw - 1];
+    const int ex = carry + before + x - v, exi = carry_i + before_i + xi - ni;
+    if (k < nk) cursor[k] = ex;
+    if (k == dead_key) *n_ptr = ex;                   // particles before the removed bucket
+    for (int j = 0; j < ni; ++j) items[exi + j] = make_int4(k, ex + j * kItem, min(kItem, v - j * kItem), 0);
     carry += tot;
+    carry_i += tot_i;
     __syncthreads();
   }
+  if (threadIdx.x == 0) *n_items = carry_i;
 }
 
 __global__ void __launch_bounds__(kMixThreads) k_mscatter(const int64_t* __restrict__ n_old, MArr S, MArr D,
@@ -590,6 +580,10 @@ int mixed_alloc(qpad_species* sp) {
   if (e != cudaSuccess) { cudaGetLastError(); return set_err(ctx, QPAD_E_NOMEM, "cudaMalloc(mixed pristine)"); }
   e = cudaMalloc(&sp->hist, sizeof(int32_t) * (ctx->g.nr + 4));
   if (e == cudaSuccess) e = cudaMalloc(&sp->cursor, sizeof(int32_t) * (ctx->g.nr + 4));
+  sp->items_cap = (int64_t)(cap / kItem) + ctx->g.nr + 2;
+  if (e == cudaSuccess) e = cudaMalloc(&sp->items, sizeof(int4) * (size_t)sp->items_cap);
+  if (e == cudaSuccess) e = cudaMalloc(&sp->d_nitems, sizeof(int) * 2);
+  if (e == cudaSuccess) e = cudaMemset(sp->d_nitems, 0, sizeof(int) * 2);
   if (e != cudaSuccess) { cudaGetLastError(); return set_err(ctx, QPAD_E_NOMEM, "cudaMalloc(mixed sort)"); }
   return 0;
 }
@@ -599,8 +593,12 @@ void mixed_free(qpad_species* sp) {
   if (sp->mixed_pristine) cudaFree(sp->mixed_pristine);
   if (sp->hist) cudaFree(sp->hist);
   if (sp->cursor) cudaFree(sp->cursor);
+  if (sp->items) cudaFree(sp->items);
+  if (sp->d_nitems) cudaFree(sp->d_nitems);
   sp->mixed_block = sp->mixed_pristine = nullptr;
   sp->hist = sp->cursor = nullptr;
+  sp->items = nullptr;
+  sp->d_nitems = nullptr;
 }
 
 
@@ -613,7 +611,8 @@ static int mixed_sort(qpad_species* sp) {
   if (cudaMemsetAsync(sp->hist, 0, sizeof(int32_t) * nk, ctx->stream) != cudaSuccess) return check_launch(ctx, "hist0", 0);
   k_mhist<<<mgrid(n, kMixThreads), kMixThreads, 0, ctx->stream>>>(sp->d_count, sp->mkey[0], sp->hist);
   k_copy_count<<<1, 1, 0, ctx->stream>>>(sp->d_count, sp->d_total);      // old count for the scatter
-  k_mscan<<<1, 1024, 0, ctx->stream>>>(nk, sp->hist, sp->cursor, sp->d_count, ctx->g.nr + 1);
+  k_mscan<<<1, 1024, 0, ctx->stream>>>(nk, ctx->g.nr, sp->hist, sp->cursor, sp->d_count, ctx->g.nr + 1, sp->items,
+                                       sp->d_nitems);
   k_mscatter<<<mgrid(n, kMixThreads), kMixThreads, 0, ctx->stream>>>(sp->d_total, marr(sp, 0), marr(sp, 1),
                                                                       sp->cursor);
   if (int r = check_launch(ctx, "mixed sort", 4)) return r;
@@ -621,6 +620,24 @@ static int mixed_sort(qpad_species* sp) {
   // arrays), so that kernels captured in a CUDA graph keep valid arguments
   return cuda_check(ctx, cudaMemcpyAsync(sp->cxy[0], sp->cxy[1], (size_t)sp->npmax * 40, cudaMemcpyDeviceToDevice,
                                          ctx->stream), "mixed copy back");
+}
+
+// Rebuilds the deposit work items of a state that is already sorted by cell.
+int mixed_index(qpad_species* sp) {
+  qpad_ctx* ctx = sp->ctx;
+  const int64_t n = sp->np;
+  if (n == 0) return 0;
+  const int nk = ctx->g.nr + 2;
+  if (cudaMemsetAsync(sp->hist, 0, sizeof(int32_t) * nk, ctx->stream) != cudaSuccess) return check_launch(ctx, "hist0", 0);
+  k_mhist<<<mgrid(n, kMixThreads), kMixThreads, 0, ctx->stream>>>(sp->d_count, sp->mkey[0], sp->hist);
+  k_mscan<<<1, 1024, 0, ctx->stream>>>(nk, ctx->g.nr, sp->hist, sp->cursor, sp->d_count, ctx->g.nr + 1, sp->items,
+                                       sp->d_nitems);
+  return check_launch(ctx, "mixed index", 2);
+}
+
+static int item_blocks(const qpad_species* sp) {
+  const int64_t bound = sp->np / kItem + sp->ctx->g.nr + 2;     // >= sum over cells of ceil(n_k / kItem)
+  return (int)((std::min<int64_t>(bound, sp->items_cap) + kItemThreads / 32 - 1) / (kItemThreads / 32));
 }
 
 int mixed_from_fp64(qpad_species* sp) {
@@ -672,7 +689,7 @@ int mixed_qdeposit_raw(qpad_species* sp, double* qraw) {
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
   prof_begin(ctx, "qdeposit");
-  k_mqdeposit<<<mgrid(sp->np, kChunk), kMixThreads, 0, ctx->stream>>>(ctx->g, sp->d_count, marr(sp, 0), qraw);
+  k_mqdeposit<<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
   prof_end(ctx, "qdeposit");
   return check_launch(ctx, "k_mqdeposit");
 }
@@ -681,8 +698,9 @@ int mixed_amjdp_raw(qpad_species* sp, const float* gtab, double* cu, double* amu
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
   prof_begin(ctx, "amjdp");
-  k_mamjdp<<<mgrid(sp->np, kChunk), kMixThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
-                                                                    sp->d_count, marr(sp, 0), gtab, cu, amu, acu, 0);
+  k_mamjdp<<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
+                                                              sp->items, sp->d_nitems, marr(sp, 0), gtab, cu, amu,
+                                                              acu, 0);
   prof_end(ctx, "amjdp");
   return check_launch(ctx, "k_mamjdp");
 }

@@ -141,6 +141,9 @@ struct qpad_species {
   int32_t* mkey[2] = {};        // radial cell key 1..nr (nr+1: left the box), sorted ascending
   int32_t* hist = nullptr;      // nr+2 counters
   int32_t* cursor = nullptr;    // nr+2 scatter cursors
+  int4* items = nullptr;        // deposit work items {cell, first, count} of the sorted state
+  int* d_nitems = nullptr;      // number of work items
+  int64_t items_cap = 0;
   void* mixed_block = nullptr;
   void* mixed_pristine = nullptr;
   double* qf = nullptr;         // this species' charge density (finished deposit)
@@ -221,6 +224,7 @@ int mixed_amjdp_raw(qpad_species* sp, const float* gtab, double* cu, double* amu
 // push_u (do_u) and/or push_x + update_bound + sort (do_x)
 int mixed_push(qpad_species* sp, const float* gtab, double dt, int do_u, int do_x);
 int mixed_sort_public(qpad_species* sp);
+int mixed_index(qpad_species* sp);          // deposit work items of an already sorted state
 int mixed_interp_psi(qpad_species* sp, const double* psif);
 int launch_gtab(qpad_ctx* ctx, const double* e, const double* b);   // FP32 gather table of (e, b)
 
