@@ -5,10 +5,12 @@ B-perp predictor-corrector (iter_reltol 1e-6), beam push, and the plasma renewal
 the reference performs after every 3D step.  The metric's first half, plasma
 particle-pushes/s, is the headline value (one plasma particle advanced through one
 slice, all of its predictor-corrector deposits included); B-perp iterations per slice
-are reported beside it.
+are reported beside it.  The headline path is the mixed-precision one (FP32 particles,
+FP64 solves); the plain FP64 path runs on the same deck and inputs as the comparison arm
+("compare", "speedup_vs_fp64", "iters_change_vs_fp64").
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--deck c2] [--precision fp64|mixed]
+                  [--deck c2] [--precision mixed|fp64] [--no-compare]
 
 --impl reference times the reference algorithm's CPU implementation (the project's C
 restatement of it, OpenMP over particles, every host core) on a bounded sample of the
@@ -162,36 +164,21 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
-    import numpy as np
-
+def _measure(args, deck, inputs, prec, local, dist, full=True):
+    """Times args.steps 3D steps of one simulation (after args.warmup untimed ones) on the
+    library's stream with CUDA events; with `full`, also the end-to-end pass with host
+    buffers and one host-driven step with per-kernel event timing."""
     import qpad_gb300 as Q
-    from qpad_gb300 import _capi as K
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-        torch.cuda.set_device(local)
-    from qpad_gb300.replicas import reduce_timing, replica_seed
-    deck = _deck(args)
-    deck.seed = replica_seed(deck.seed, rank)   # independent replica per GPU
-    prec = K.PREC_FP64 if args.precision == "fp64" else K.PREC_MIXED
-    inputs = Q.deck_inputs(deck)
+    from qpad_gb300.replicas import reduce_timing
     sim = Q.build_simulation(deck, precision=prec, device=local, inputs=inputs)
     sim.use_graph(args.graph == "on")
     sp = sim.species[0]
     npl = len(inputs[0][4])
-    nbeam = sum(len(b[2]) for b in inputs[1])
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    # warm-up (also fills the caches of the allocator and the factor tables)
     for _ in range(args.warmup):
         sp.reset()
         sim.run_3d_step()
@@ -213,38 +200,77 @@ def run_ours(args):
     sim.profile(False)
     graph_on, graph_why = sim.graph_active()
     dev_s = step_ms / 1e3 if nstep else wall
-    # kernel timing pass (outside the timed region): one host-driven step with CUDA events
-    # bracketing every launch of the particle kernels on the library's stream
-    sim.use_graph(False)
-    sim.profile(True)
-    sp.reset()
-    sim.run_3d_step()
-    kern = {k: sim.profile_read(k) for k in ("amjdp", "iterate", "push", "qdeposit", "slice_begin", "iter_e",
-                                             "slice_end", "conv", "beam_push", "beam_qdeposit", "step")}
-    sim.profile(False)
-    sim.use_graph(args.graph == "on")
-    amj_ms, namj = kern["amjdp"]
     barrier()
     pushes_step = npl * deck.nz
     dev_s, total_pushes = reduce_timing(dev_s, float(pushes_step * args.steps), dist)
-    value = total_pushes / dev_s
-    iters_per_slice = iters_tot / (args.steps * deck.nz)
+    out = {"value": total_pushes / dev_s, "ms_per_step": dev_s * 1e3 / args.steps,
+           "iters_per_slice": iters_tot / (args.steps * deck.nz), "wall_s": wall, "launches": launches,
+           "graph": {"active": graph_on, "status": graph_why}, "clocks": clk.summary(), "dev_s": dev_s,
+           "pushes_step": pushes_step}
+    if full:
+        # kernel timing pass (outside the timed region): one host-driven step with CUDA events
+        # bracketing every launch of each kernel family on the library's stream
+        sim.use_graph(False)
+        sim.profile(True)
+        sp.reset()
+        sim.run_3d_step()
+        out["kern"] = {k: sim.profile_read(k) for k in ("amjdp", "iterate", "push", "qdeposit", "slice_begin",
+                                                         "iter_e", "slice_end", "conv", "beam_push",
+                                                         "beam_qdeposit", "step")}
+        sim.profile(False)
+        sim.use_graph(args.graph == "on")
+        # end to end through the C ABI with host buffers: renew from host arrays every step
+        x, p, g, ps, q = inputs[0]
+        h2d = sum(a.nbytes for a in (x, p, g, ps, q))
+        d2h = 0
+        e2e_t0 = time.perf_counter()
+        for _ in range(max(1, args.steps)):
+            sp.renew(x, p, g, ps, q)
+            it, _ = sim.run_3d_step()
+            d2h += int(it.sum()) * 24 + 8
+        e2e_s = time.perf_counter() - e2e_t0
+        e2e_steps = max(1, args.steps)
+        world = dist.get_world_size() if dist is not None else 1
+        out["e2e"] = {"value": world * pushes_step * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                      "d2h_bytes_per_step": d2h // e2e_steps}
+    sim.close()
+    return out
 
-    # end to end through the C ABI with host buffers: renew from host arrays every step
-    x, p, g, ps, q = inputs[0]
-    h2d = sum(a.nbytes for a in (x, p, g, ps, q))
-    e2e_t0 = time.perf_counter()
-    d2h = 0
-    for _ in range(max(1, args.steps)):
-        sp.renew(x, p, g, ps, q)
-        it, _ = sim.run_3d_step()
-        d2h += int(it.sum()) * 24 + 8
-    e2e_s = time.perf_counter() - e2e_t0
-    e2e_steps = max(1, args.steps)
-    e2e = world * pushes_step * e2e_steps / e2e_s
 
+def run_ours(args):
+    import qpad_gb300 as Q
+    from qpad_gb300 import _capi as K
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        torch.cuda.set_device(local)
+    from qpad_gb300.replicas import replica_seed
+    deck = _deck(args)
+    deck.seed = replica_seed(deck.seed, rank)   # independent replica per GPU
+    prec = K.PREC_FP64 if args.precision == "fp64" else K.PREC_MIXED
+    inputs = Q.deck_inputs(deck)
+    npl = len(inputs[0][4])
+    nbeam = sum(len(b[2]) for b in inputs[1])
+    r = _measure(args, deck, inputs, prec, local, dist, full=True)
+    # the other arm of the metric: the plain FP64 path on the same deck and inputs
+    cmp = None
+    if not args.no_compare:
+        other = K.PREC_FP64 if prec == K.PREC_MIXED else K.PREC_MIXED
+        c = _measure(args, deck, inputs, other, local, dist, full=False)
+        cmp = {"path": "fp64" if other == K.PREC_FP64 else "mixed", "value": c["value"],
+               "ms_per_step": c["ms_per_step"], "iters_per_slice": c["iters_per_slice"],
+               "graph": c["graph"]["active"]}
+    kern = r["kern"]
+    amj_ms, namj = kern["amjdp"]
     peak, peak_kind = _peaks()
-    bytes_per_particle = 64   # FP64 amjdp: reads x, y, px, py, pz, q; writes gamma, psi
+    # algorithmic bytes per particle of one amjdp pass: FP64 reads x, y, px, py, pz, q and
+    # writes gamma, psi (64 B); mixed reads the cell word, two offsets, three momenta and q (28 B)
+    bytes_per_particle = 64 if prec == K.PREC_FP64 else 28
     amj_avg_s = (amj_ms / 1e3) / max(namj, 1)
     achieved = bytes_per_particle * npl / amj_avg_s / 1e9 if namj else None
     traffic = None
@@ -254,31 +280,36 @@ def run_ours(args):
             traffic = json.load(open(tf)).get(args.precision)
         except Exception:
             traffic = None
+    dev_s = r["dev_s"]
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32/f64",
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if prec == K.PREC_FP64 else "f32 particles / f64 solves",
         "data": "synthetic (seeded deck, no dataset)",
         "config": {"workload": deck.name, "nr": deck.nr, "nz": deck.nz, "max_mode": deck.max_mode,
                    "plasma_particles_per_slice": npl, "beam_particles": nbeam, "path": args.precision,
                    "iter_reltol": deck.iter_reltol, "iter_max": deck.iter_max,
                    "l2": "step working set above L2 (beam arrays and 3D field stores); per-slice data L2-resident",
                    "parallelism": f"replicas x{world}"},
-        "iters_per_slice": iters_per_slice,
+        "iters_per_slice": r["iters_per_slice"],
         "slices_per_s": world * deck.nz * args.steps / dev_s,
         "beam_pushes_per_s": world * nbeam * args.steps / dev_s,
-        "wall_s": wall,
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h // e2e_steps},
-        "gpu_launches": launches,
+        "wall_s": r["wall_s"],
+        "e2e": r["e2e"],
+        "gpu_launches": r["launches"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "k_amjdp", "peak_kind": peak_kind,
+                     "kernel": "k_amjdp" if prec == K.PREC_FP64 else "k_mamjdp", "peak_kind": peak_kind,
                      "bytes_per_launch": bytes_per_particle * npl, "avg_launch_us": amj_avg_s * 1e6},
-        "clocks": clk.summary(),
-        "graph": {"active": graph_on, "status": graph_why},
+        "clocks": r["clocks"],
+        "graph": r["graph"],
         "kernel_ms_per_step": {k: round(v[0], 3) for k, v in kern.items()},
         "kernel_launches_per_step": {k: v[1] for k, v in kern.items()},
     }
+    if cmp is not None:
+        line["compare"] = cmp
+        line["speedup_vs_" + cmp["path"]] = r["value"] / cmp["value"]
+        line["iters_change_vs_" + cmp["path"]] = r["iters_per_slice"] / cmp["iters_per_slice"] - 1.0
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_sample(deck, args.cpu_slices)
         line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": "port",
@@ -286,7 +317,6 @@ def run_ours(args):
                                           f"{cb['particles_per_slice']} plasma particles, OpenMP oracle"}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    sim.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
@@ -299,7 +329,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--deck", default="c2")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP64 (or mixed) comparison arm")
     ap.add_argument("--cpu-slices", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slices", type=int, default=0, help="override the deck's slice count (profiling runs)")

@@ -294,7 +294,7 @@ extern "C" int qpad_ctx_create(const qpad_grid_desc* d, qpad_ctx** out) {
   if (!ctx) return QPAD_E_NOMEM;
   GridDev& g = ctx->g;
   g.nr = d->nr; g.nz = d->nz; g.M = d->max_mode; g.P = 2 * d->max_mode + 1; g.ld = d->nr + 2; g.bnd = d->bnd;
-  g.dr = d->dr; g.dxi = d->dxi; g.idr = 1.0 / d->dr;
+  g.dr = d->dr; g.dxi = d->dxi; g.idr = 1.0 / d->dr; g.toff = 0;
   g.relax_fac = d->relax_fac >= 0.0 ? d->relax_fac : 1.0e-3 * ((d->dr / 0.02) * (d->dr / 0.02));
   ctx->iter_max = d->iter_max; ctx->reltol = d->iter_reltol; ctx->abstol = d->iter_abstol; ctx->dt = d->dt;
   ctx->precision = d->precision; ctx->device = d->device;
@@ -315,10 +315,10 @@ extern "C" int qpad_ctx_create(const qpad_grid_desc* d, qpad_ctx** out) {
   if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->h_j, 2 * sizeof(int)), "pinned slice index");
   if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->h_res, 8 * sizeof(double)), "pinned");
   if (!r) r = dmalloc(ctx, (void**)&ctx->raw, 8 * (size_t)g.P * g.ld * sizeof(double), "raw deposits");
-  if (!r) r = dmalloc(ctx, (void**)&ctx->iter_tickets, 64 * sizeof(unsigned int), "iteration tickets");
+  if (!r) r = dmalloc(ctx, (void**)&ctx->iter_tickets, 128 * sizeof(unsigned int), "iteration tickets");
   if (!r) r = cuda_check(ctx, cudaMemsetAsync(ctx->raw, 0, 8 * (size_t)g.P * g.ld * sizeof(double), ctx->stream),
                          "raw deposits");
-  if (!r) r = cuda_check(ctx, cudaMemsetAsync(ctx->iter_tickets, 0, 64 * sizeof(unsigned int), ctx->stream),
+  if (!r) r = cuda_check(ctx, cudaMemsetAsync(ctx->iter_tickets, 0, 128 * sizeof(unsigned int), ctx->stream),
                          "iteration tickets");
   if (!r) r = build_factors(ctx);
   if (!r) r = iterate_setup(ctx);

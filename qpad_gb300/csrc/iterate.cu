@@ -53,7 +53,7 @@ struct IterArgs {
   float* gtab;            // FP32 gather table (mixed path) or null
   double* conv;           // s_re[nr], s_im[nr], res[..]
   unsigned int* tickets;  // [0, CL): node-range tickets; [CL]: range counter
-  unsigned long long* maxima;
+  double* slots;           // per node range: the two maxima of the convergence test
   ConvLoop L;
   double reltol, abstol;
   int R;                  // rows per CTA
@@ -117,9 +117,19 @@ struct WinF {
 // Shared-memory staging of one CTA (doubles): the finished deposits on the node window
 // [r0-1, r1+2] (cu 0..2, amu 3..5, acu 6..7), b_spe components 0..1 and b_beam on the owned
 // nodes, psi on the window, the factor rows of the three matrices, the right-hand sides.
-__host__ __device__ inline size_t iterate_smem_doubles(int R) {
+__host__ __device__ inline size_t iterate_smem_doubles(int R, int ld) {
   const size_t W = (size_t)R + 4;
-  return 16 * W + 4 * (size_t)R + 6 * (size_t)R + 2 * W + 9 * (size_t)R + (size_t)kMaxRhs * R;
+  (void)ld;
+  return 16 * W + 4 * (size_t)R + 6 * (size_t)R + 2 * W + 9 * (size_t)R + (size_t)kMaxRhs * R + 2 * W + 4 * (size_t)R;
+}
+
+// 8-byte asynchronous copy global -> shared (cp.async), and the wait for all of them
+__device__ __forceinline__ void cp_async8(double* dst, const double* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
 __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
@@ -129,11 +139,10 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   __shared__ double divp;
   __shared__ unsigned int s_ticket;
   cg::cluster_group cluster = cg::this_cluster();
-  const GridDev& G = a.G;
   const int CL = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
   const int m = blockIdx.x / CL;
-  const int nr = G.nr, ld = G.ld, P = G.P;
+  const int nr = a.G.nr, ld = a.G.ld, P = a.G.P;
   const int pr = part_re(m), pi = part_im(m);
   const int nh = m == 0 ? 1 : 2;                 // parts of this mode
   const int nrhs = m == 0 ? 4 : 8;
@@ -152,84 +161,102 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   double* psw = bbm + 6 * R;                     // [2][W]
   double* facs = psw + 2 * W;                    // [3 kinds][w, ib, g][R]
   double* dsm = facs + 9 * R;                    // [kMaxRhs][R]
+  double* tab = dsm + kMaxRhs * R;               // node tables ir, inv on the window
+  double* djs = tab + 2 * W;                     // dJ/dxi of the owned nodes [4][R]
+  GridDev G = a.G;                               // the node tables read from shared memory
+  G.ir = tab;
+  G.inv = tab + W;
+  G.toff = wb;
 
-  // ---- staging: every load of the iteration's inputs in flight at once ------------------
-  for (int q = t; q < 8 * nh * W; q += blockDim.x) {
-    const int c8 = q / (nh * W), h = (q / W) % nh, node = wb + q % W;
-    const int p = h == 0 ? pr : pi;
-    double v = 0.0;
+  // ---- staging: every copy of the iteration's inputs in flight at once (cp.async) -------
+  for (int k = t; k < W; k += blockDim.x) {
+    const int node = wb + k;
     if (node >= 0 && node <= nr + 1) {
-      if (c8 < 3) v = finish_amj(G, m, 0, c8, node, raw_cu[fidx(ld, 3, p, c8, node)]);
-      else if (c8 < 6) v = finish_amj(G, m, 1, c8 - 3, node, raw_amu[fidx(ld, 3, p, c8 - 3, node)]);
-      else v = finish_amj(G, m, 2, c8 - 6, node, raw_acu[fidx(ld, 2, p, c8 - 6, node)]);
+      cp_async8(tab + k, a.G.ir + node);
+      cp_async8(tab + W + k, a.G.inv + node);
+    } else {
+      tab[k] = 0.0;
+      tab[W + k] = 0.0;
     }
-    win[(c8 * 2 + h) * W + q % W] = v;
   }
-  for (int q = t; q < nh * W; q += blockDim.x) {
-    const int h = q / W, node = wb + q % W;
-    psw[h * W + q % W] = (node >= 0 && node <= nr + 1) ? a.psi[fidx(ld, 1, h == 0 ? pr : pi, 0, node)] : 0.0;
+  for (int row = 0; row < 8 * nh; ++row) {       // raw deposits on the window
+    const int c8 = row / nh, h = row % nh, p = h == 0 ? pr : pi;
+    const double* src = c8 < 3 ? raw_cu + fidx(ld, 3, p, c8, 0)
+                               : (c8 < 6 ? raw_amu + fidx(ld, 3, p, c8 - 3, 0) : raw_acu + fidx(ld, 2, p, c8 - 6, 0));
+    double* dst = win + (c8 * 2 + h) * W;
+    for (int k = t; k < W; k += blockDim.x) {
+      const int node = wb + k;
+      if (node >= 0 && node <= nr + 1) cp_async8(dst + k, src + node);
+      else dst[k] = 0.0;
+    }
   }
-  for (int q = t; q < 5 * nh * R; q += blockDim.x) {
-    const int c5 = q / (nh * R), h = (q / R) % nh, k = q % R;
-    if (k >= Rc) continue;
-    const int p = h == 0 ? pr : pi, i = r0 + 1 + k;
-    if (c5 < 2) bo[(c5 * 2 + h) * R + k] = a.b_spe[fidx(ld, 3, p, c5, i)];
-    else bbm[((c5 - 2) * 2 + h) * R + k] = a.b_beam[fidx(ld, 3, p, c5 - 2, i)];
+  for (int h = 0; h < nh; ++h) {                 // psi on the window
+    const double* src = a.psi + fidx(ld, 1, h == 0 ? pr : pi, 0, 0);
+    for (int k = t; k < W; k += blockDim.x) {
+      const int node = wb + k;
+      if (node >= 0 && node <= nr + 1) cp_async8(psw + h * W + k, src + node);
+      else psw[h * W + k] = 0.0;
+    }
   }
-  for (int q = t; q < 9 * R; q += blockDim.x) {
-    const int ka = q / (3 * R), arr = (q / R) % 3, k = q % R;
-    if (k >= Rc) continue;
+  for (int row = 0; row < 5 * nh; ++row) {       // b_spe (B_old) and b_beam on the owned nodes
+    const int c5 = row / nh, h = row % nh, p = h == 0 ? pr : pi;
+    const double* src = c5 < 2 ? a.b_spe + fidx(ld, 3, p, c5, r0 + 1) : a.b_beam + fidx(ld, 3, p, c5 - 2, r0 + 1);
+    double* dst = c5 < 2 ? bo + (c5 * 2 + h) * R : bbm + ((c5 - 2) * 2 + h) * R;
+    for (int k = t; k < Rc; k += blockDim.x) cp_async8(dst + k, src + k);
+  }
+  for (int row = 0; row < 9; ++row) {            // factor rows
+    const int ka = row / 3, arr = row % 3;
     const int kind = ka == 0 ? OK_BPLUS : ka == 1 ? OK_BMINUS : OK_GEN;
-    facs[q] = a.fac[fac_off(nr, G.M, kind, m) + (size_t)arr * nr + r0 + k];
+    const double* src = a.fac + fac_off(nr, G.M, kind, m) + (size_t)arr * nr + r0;
+    for (int k = t; k < Rc; k += blockDim.x) cp_async8(facs + row * R + k, src + k);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  for (int q = t; q < 8 * nh * W; q += blockDim.x) {   // finish the deposits in place
+    const int row = q / W, k = q % W, c8 = row / nh, node = wb + k;
+    if (node < 0 || node > nr + 1) continue;
+    double& v = win[(c8 * 2 + row % nh) * W + k];
+    v = c8 < 3 ? finish_amj(G, m, 0, c8, node, v) : (c8 < 6 ? finish_amj(G, m, 1, c8 - 3, node, v)
+                                                                : finish_amj(G, m, 2, c8 - 6, node, v));
   }
   __syncthreads();
   const WinF CU{win, W, wb, pr, 0}, AMU{win, W, wb, pr, 3}, ACU{win, W, wb, pr, 6};
   const WinF PS{psw, W, wb, pr, 0};
   const auto BO = [&](int p, int c, int i) { return bo[(c * 2 + (p == pr ? 0 : 1)) * R + (i - r0 - 1)]; };
 
-  // ---- sources, one thread per owned node ---------------------------------------------
+  // ---- sources: (node, equation group) per thread ---------------------------------------
+  // group 0: dJ/dxi and the B+ / B- right-hand sides; group 1: Bz; group 2: Ez
   double div = 0.0;
-  for (int k = t; k < Rc; k += blockDim.x) {
-    const int i = r0 + k + 1;
-    double dj[4];
-    row_djdxi(G, m, i, ACU, AMU, dj);
-    const auto DC = [&](int p, int c, int) { return p == pr ? dj[c] : dj[2 + c]; };
-    double bt[4];
-    row_btiter_src(G, m, i, DC, CU, BO, bt);
-    double zr, zi, er, ei;
-    bool in_div;
-    row_bz_src(G, m, i, CU, zr, zi);
-    row_ez_src(G, m, i, CU, er, ei, in_div);
-    if (in_div) div += er * (double)(i - 1);
-    if (m == 0) {
-      dsm[0 * R + k] = bt[0];
-      dsm[1 * R + k] = bt[1];
+  for (int q = t; q < 3 * Rc; q += blockDim.x) {
+    const int job = q / Rc, k = q % Rc, i = r0 + k + 1;
+    if (job == 0) {
+      double dj[4];
+      row_djdxi(G, m, i, ACU, AMU, dj);
+      const auto DC = [&](int p, int c, int) { return p == pr ? dj[c] : dj[2 + c]; };
+      double bt[4];
+      row_btiter_src(G, m, i, DC, CU, BO, bt);
+      if (m == 0) {
+        dsm[0 * R + k] = bt[0];
+        dsm[1 * R + k] = bt[1];
+      } else {
+        dsm[0 * R + k] = bt[0];
+        dsm[1 * R + k] = bt[2];
+        dsm[4 * R + k] = bt[1];
+        dsm[5 * R + k] = bt[3];
+      }
+      for (int c = 0; c < 4; ++c) djs[c * R + k] = dj[c];
+    } else if (job == 1) {
+      double zr, zi;
+      row_bz_src(G, m, i, CU, zr, zi);
       dsm[2 * R + k] = zr;
-      dsm[3 * R + k] = er;
+      if (m > 0) dsm[6 * R + k] = zi;
     } else {
-      dsm[0 * R + k] = bt[0];
-      dsm[1 * R + k] = bt[2];
-      dsm[2 * R + k] = zr;
+      double er, ei;
+      bool in_div;
+      row_ez_src(G, m, i, CU, er, ei, in_div);
+      if (in_div) div += er * (double)(i - 1);
       dsm[3 * R + k] = er;
-      dsm[4 * R + k] = bt[1];
-      dsm[5 * R + k] = bt[3];
-      dsm[6 * R + k] = zi;
-      dsm[7 * R + k] = ei;
-    }
-    for (int h = 0; h < nh; ++h)
-      for (int c = 0; c < 2; ++c) a.dcu[fidx(ld, 2, h == 0 ? pr : pi, c, i)] = dj[2 * h + c];
-  }
-  // finished deposits of the owned nodes (and of the guard nodes at the two ends)
-  {
-    const int i0 = rank == 0 ? 0 : r0 + 1, i1 = rank == CL - 1 ? nr + 1 : r1;
-    const int nn = i1 - i0 + 1;
-    for (int q = t; q < 8 * nh * nn; q += blockDim.x) {
-      const int c8 = q / (nh * nn), h = (q / nn) % nh, i = i0 + q % nn;
-      const int p = h == 0 ? pr : pi;
-      const double v = win[(c8 * 2 + h) * W + (i - wb)];
-      if (c8 < 3) a.cu[fidx(ld, 3, p, c8, i)] = v;
-      else if (c8 < 6) a.amu[fidx(ld, 3, p, c8 - 3, i)] = v;
-      else a.acu[fidx(ld, 2, p, c8 - 6, i)] = v;
+      if (m > 0) dsm[7 * R + k] = ei;
     }
   }
   // the m = 0 axis row of Ez needs the weighted sum over the whole line
@@ -246,8 +273,8 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     if (rank == 0 && t == 0) {
       double s = 0.0;
       for (int q = 0; q < CL; ++q) s += *cluster.map_shared_rank(&divp, q);
-      const RawFin CUg{&G, raw_cu, 0, 0, 3};      // nodes nr-2, nr-1 lie outside this window
-      dsm[3 * R + 0] = ez_axis_row(G, s, CUg);
+      const RawFin CUg{&a.G, raw_cu, 0, 0, 3};    // nodes nr-2, nr-1 lie outside this window
+      dsm[3 * R + 0] = ez_axis_row(a.G, s, CUg);
     }
   }
   __syncthreads();
@@ -302,25 +329,6 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
       d[k] = y;
     }
   }
-  // every CTA of the cluster has read its sources: clear the raw deposits it owns
-  for (int k = t; k < Rc + 2; k += blockDim.x) {
-    int i = r0 + k + 1;
-    if (k == Rc) {
-      if (rank != 0) continue;
-      i = 0;
-    } else if (k == Rc + 1) {
-      if (rank != CL - 1) continue;
-      i = nr + 1;
-    }
-    for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
-      const int p = h == 0 ? pr : pi;
-      for (int c = 0; c < 3; ++c) {
-        raw_cu[fidx(ld, 3, p, c, i)] = 0.0;
-        raw_amu[fidx(ld, 3, p, c, i)] = 0.0;
-      }
-      for (int c = 0; c < 2; ++c) raw_acu[fidx(ld, 2, p, c, i)] = 0.0;
-    }
-  }
   __syncthreads();
 
   // ---- back substitution x_k = y_k ib_k - g_k x_{k+1} -----------------------------------
@@ -366,54 +374,75 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   cluster_arrive();
   __syncthreads();
 
-  // ---- fields of the owned nodes -------------------------------------------------------
-  for (int k = t; k < Rc; k += blockDim.x) {
-    const int i = r0 + k + 1;
-    double bs[2][3], bb[2][3], ee[2][3];
-    if (m == 0) {
-      bs[0][0] = (i == 1) ? 0.0 : dsm[0 * R + k];
-      bs[0][1] = (i == 1) ? 0.0 : dsm[1 * R + k];
-      bs[0][2] = dsm[2 * R + k];
-      ee[0][2] = dsm[3 * R + k];
-    } else {
-      const bool zero = (i == 1 && m != 1);
-      const double b1re = dsm[0 * R + k], b2re = dsm[1 * R + k];
-      const double b1im = dsm[4 * R + k], b2im = dsm[5 * R + k];
-      bs[0][0] = zero ? 0.0 : 0.5 * (b1re + b2re);
-      bs[1][0] = zero ? 0.0 : 0.5 * (b1im + b2im);
-      bs[0][1] = zero ? 0.0 : 0.5 * (b1im - b2im);
-      bs[1][1] = zero ? 0.0 : 0.5 * (-b1re + b2re);
-      bs[0][2] = (i == 1) ? 0.0 : dsm[2 * R + k];
-      bs[1][2] = (i == 1) ? 0.0 : dsm[6 * R + k];
-      ee[0][2] = (i == 1) ? 0.0 : dsm[3 * R + k];
-      ee[1][2] = (i == 1) ? 0.0 : dsm[7 * R + k];
-    }
-    for (int h = 0; h < nh; ++h)
-      for (int c = 0; c < 3; ++c) bb[h][c] = bs[h][c] + bbm[(c * 2 + h) * R + k];
-    const auto Bn = [&](int p, int c, int) { return p == pr ? bb[0][c] : bb[1][c]; };
-    double et[4];
-    row_et(G, m, i, Bn, PS, et);
-    if (m == 0) {
-      ee[0][0] = et[0];
-      ee[0][1] = et[1];
-    } else {
-      ee[0][0] = et[0];
-      ee[1][0] = et[1];
-      ee[0][1] = et[2];
-      ee[1][1] = et[3];
-    }
-    for (int h = 0; h < nh; ++h) {
-      const int p = h == 0 ? pr : pi;
-      for (int c = 0; c < 3; ++c) {
-        a.b_spe[fidx(ld, 3, p, c, i)] = bs[h][c];
-        a.b[fidx(ld, 3, p, c, i)] = bb[h][c];
-        a.e[fidx(ld, 3, p, c, i)] = ee[h][c];
+  // ---- fields of the owned nodes: (node, group) per thread ------------------------------
+  // group 0: B-perp from B+ / B-, b = b_spe + b_beam and E-perp; group 1: Bz and Ez
+  for (int q = t; q < 2 * Rc; q += blockDim.x) {
+    const int job = q / Rc, k = q % Rc, i = r0 + k + 1;
+    if (job == 0) {
+      double bs[2][2], bb[2][2];
+      if (m == 0) {
+        bs[0][0] = (i == 1) ? 0.0 : dsm[0 * R + k];
+        bs[0][1] = (i == 1) ? 0.0 : dsm[1 * R + k];
+      } else {
+        const bool zero = (i == 1 && m != 1);
+        const double b1re = dsm[0 * R + k], b2re = dsm[1 * R + k];
+        const double b1im = dsm[4 * R + k], b2im = dsm[5 * R + k];
+        bs[0][0] = zero ? 0.0 : 0.5 * (b1re + b2re);
+        bs[1][0] = zero ? 0.0 : 0.5 * (b1im + b2im);
+        bs[0][1] = zero ? 0.0 : 0.5 * (b1im - b2im);
+        bs[1][1] = zero ? 0.0 : 0.5 * (-b1re + b2re);
       }
-      if (a.gtab) {
-        float* T = a.gtab + ((size_t)i * P + p) * 6;
-        for (int c = 0; c < 3; ++c) {
-          T[c] = (float)ee[h][c];
-          T[3 + c] = (float)bb[h][c];
+      for (int h = 0; h < nh; ++h)
+        for (int c = 0; c < 2; ++c) bb[h][c] = bs[h][c] + bbm[(c * 2 + h) * R + k];
+      const auto Bn = [&](int p, int c, int) { return p == pr ? bb[0][c] : bb[1][c]; };
+      double et[4];
+      row_et(G, m, i, Bn, PS, et);
+      double ee[2][2];
+      if (m == 0) {
+        ee[0][0] = et[0];
+        ee[0][1] = et[1];
+      } else {
+        ee[0][0] = et[0];
+        ee[1][0] = et[1];
+        ee[0][1] = et[2];
+        ee[1][1] = et[3];
+      }
+      for (int h = 0; h < nh; ++h) {
+        const int p = h == 0 ? pr : pi;
+        for (int c = 0; c < 2; ++c) {
+          a.b_spe[fidx(ld, 3, p, c, i)] = bs[h][c];
+          a.b[fidx(ld, 3, p, c, i)] = bb[h][c];
+          a.e[fidx(ld, 3, p, c, i)] = ee[h][c];
+        }
+        if (a.gtab) {
+          float* T = a.gtab + ((size_t)i * P + p) * 6;
+          T[0] = (float)ee[h][0];
+          T[1] = (float)ee[h][1];
+          T[3] = (float)bb[h][0];
+          T[4] = (float)bb[h][1];
+        }
+      }
+    } else {
+      double bz[2], ez[2];
+      if (m == 0) {
+        bz[0] = dsm[2 * R + k];
+        ez[0] = dsm[3 * R + k];
+      } else {
+        bz[0] = (i == 1) ? 0.0 : dsm[2 * R + k];
+        bz[1] = (i == 1) ? 0.0 : dsm[6 * R + k];
+        ez[0] = (i == 1) ? 0.0 : dsm[3 * R + k];
+        ez[1] = (i == 1) ? 0.0 : dsm[7 * R + k];
+      }
+      for (int h = 0; h < nh; ++h) {
+        const int p = h == 0 ? pr : pi;
+        const double bzt = bz[h] + bbm[(2 * 2 + h) * R + k];
+        a.b_spe[fidx(ld, 3, p, 2, i)] = bz[h];
+        a.b[fidx(ld, 3, p, 2, i)] = bzt;
+        a.e[fidx(ld, 3, p, 2, i)] = ez[h];
+        if (a.gtab) {
+          float* T = a.gtab + ((size_t)i * P + p) * 6;
+          T[2] = (float)ez[h];
+          T[5] = (float)bzt;
         }
       }
     }
@@ -441,15 +470,23 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   __syncthreads();
   if (s_ticket == (unsigned)G.M) {                    // the last mode of this node range
     __threadfence();
-    struct LdcgF {
-      const double* f;
-      int ld;
-      __device__ __forceinline__ double operator()(int p, int c, int i) const { return __ldcg(f + fidx(ld, 3, p, c, i)); }
-    } Bc{a.b_spe, ld};
     double* s_re = a.conv;
     double* s_im = a.conv + nr;
     double mx_old = 0.0, mx_new = 0.0;
-    for (int k = t; k < Rc; k += blockDim.x) conv_node(G, Bc, kCompConv, r0 + k + 1, s_re, s_im, true, mx_old, mx_new);
+    for (int k = t; k < Rc; k += blockDim.x) {
+      const int i = r0 + k + 1;
+      double bv[QPAD_MAX_PARTS];                     // every mode's B_phi here, loads in flight together
+#pragma unroll
+      for (int p = 0; p < QPAD_MAX_PARTS; ++p) bv[p] = p < P ? __ldcg(a.b_spe + fidx(ld, 3, p, kCompConv, i)) : 0.0;
+      const auto Bc = [&](int p, int, int) {
+        double v = 0.0;
+#pragma unroll
+        for (int q = 0; q < QPAD_MAX_PARTS; ++q)
+          if (q == p) v = bv[q];
+        return v;
+      };
+      conv_node(G, Bc, kCompConv, i, s_re, s_im, true, mx_old, mx_new);
+    }
     for (int off = 16; off > 0; off >>= 1) {
       mx_old = fmax(mx_old, __shfl_down_sync(0xffffffffu, mx_old, off));
       mx_new = fmax(mx_new, __shfl_down_sync(0xffffffffu, mx_new, off));
@@ -465,21 +502,48 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
         mx_old = fmax(mx_old, rmo[w]);
         mx_new = fmax(mx_new, rmn[w]);
       }
-      atomicMax(&a.maxima[0], (unsigned long long)__double_as_longlong(mx_old));
-      atomicMax(&a.maxima[1], (unsigned long long)__double_as_longlong(mx_new));
+      a.slots[2 * rank] = mx_old;
+      a.slots[2 * rank + 1] = mx_new;
       a.tickets[rank] = 0u;
       __threadfence();
       const unsigned int done = atomicAdd(&a.tickets[CL], 1u);
       if (done == (unsigned)(CL - 1)) {               // the last node range: the verdict
         __threadfence();
-        const double vo = __longlong_as_double((long long)atomicAdd(&a.maxima[0], 0ull));
-        const double vn = __longlong_as_double((long long)atomicAdd(&a.maxima[1], 0ull));
+        double vo = 0.0, vn = 0.0;                      // max over the ranges (exact, any order)
+        for (int q = 0; q < CL; ++q) {
+          vo = fmax(vo, __ldcg(a.slots + 2 * q));
+          vn = fmax(vn, __ldcg(a.slots + 2 * q + 1));
+        }
         conv_decide(vo, vn, a.reltol, a.abstol, a.conv + 2 * nr, a.L);
-        a.maxima[0] = 0ull;
-        a.maxima[1] = 0ull;
         a.tickets[CL] = 0u;
         __threadfence();
       }
+    }
+  }
+  // ---- stores nothing in this kernel waits for: the finished deposits, dJ/dxi, and the
+  // cleared raw deposits (every CTA of the cluster staged its window before the forward
+  // barrier)
+  {
+    const int i0 = rank == 0 ? 0 : r0 + 1, i1 = rank == CL - 1 ? nr + 1 : r1;
+    const int nn = i1 - i0 + 1;
+    for (int q = t; q < 8 * nh * nn; q += blockDim.x) {
+      const int c8 = q / (nh * nn), h = (q / nn) % nh, i = i0 + q % nn;
+      const int p = h == 0 ? pr : pi;
+      const double v = win[(c8 * 2 + h) * W + (i - wb)];
+      if (c8 < 3) {
+        a.cu[fidx(ld, 3, p, c8, i)] = v;
+        raw_cu[fidx(ld, 3, p, c8, i)] = 0.0;
+      } else if (c8 < 6) {
+        a.amu[fidx(ld, 3, p, c8 - 3, i)] = v;
+        raw_amu[fidx(ld, 3, p, c8 - 3, i)] = 0.0;
+      } else {
+        a.acu[fidx(ld, 2, p, c8 - 6, i)] = v;
+        raw_acu[fidx(ld, 2, p, c8 - 6, i)] = 0.0;
+      }
+    }
+    for (int q = t; q < 2 * nh * Rc; q += blockDim.x) {
+      const int c = q / (nh * Rc), h = (q / Rc) % nh, k = q % Rc;
+      a.dcu[fidx(ld, 2, h == 0 ? pr : pi, c, r0 + k + 1)] = djs[(2 * h + c) * R + k];
     }
   }
   cluster_wait();
@@ -496,7 +560,7 @@ int iterate_setup(qpad_ctx* ctx) {
   if (e != cudaSuccess) return cuda_check(ctx, e, "cluster attribute");
   for (int cl = cluster_for(ctx->g.nr); cl >= 1; cl /= 2) {
     const int R = (ctx->g.nr + cl - 1) / cl;
-    const size_t smem = iterate_smem_doubles(R) * sizeof(double);
+    const size_t smem = iterate_smem_doubles(R, ctx->g.ld) * sizeof(double);
     if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return cuda_check(ctx, e, "iterate smem");
@@ -542,7 +606,7 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   a.gtab = ctx->precision == QPAD_PREC_MIXED ? ctx->gtab : nullptr;
   a.conv = ctx->conv;
   a.tickets = ctx->iter_tickets;
-  a.maxima = reinterpret_cast<unsigned long long*>(ctx->iter_tickets + 32);
+  a.slots = reinterpret_cast<double*>(ctx->iter_tickets + 32);
   a.L = ConvLoop{};
   if (loop_state) {
     a.L.iter_ctr = ctx->d_iter;
@@ -559,7 +623,7 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cl * (ctx->g.M + 1));
   cfg.blockDim = dim3(kIterThreads);
-  cfg.dynamicSmemBytes = iterate_smem_doubles(a.R) * sizeof(double);
+  cfg.dynamicSmemBytes = iterate_smem_doubles(a.R, ctx->g.ld) * sizeof(double);
   cfg.stream = ctx->stream;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;

@@ -33,9 +33,12 @@ struct GridDev {
   int nr, nz, M, P, ld, bnd;
   double dr, dxi, idr, relax_fac;
   // per-node factors of the reference's finite differences and deposit scaling, computed
-  // once with the same FP64 expressions: ir[i] = idr / (i-1), inv[i] = 1 / (i-1) (i >= 2)
+  // once with the same FP64 expressions: ir[i] = idr / (i-1), inv[i] = 1 / (i-1) (i >= 2);
+  // entry i sits at ir[i - toff] (toff = 0 for the full tables, the window start for a
+  // window of them staged in shared memory)
   const double* ir;
   const double* inv;
+  int toff;
 };
 
 __host__ __device__ inline int part_re(int m) { return m == 0 ? 0 : 2 * m - 1; }

@@ -32,7 +32,7 @@ __device__ __forceinline__ double finish_amj(const GridDev& G, int m, int which,
     else f = m == 1 ? 8.0 : 0.0;
     return f == 0.0 ? 0.0 : f * raw;
   }
-  return raw * G.inv[i];
+  return raw * G.inv[(i) - G.toff];
 }
 
 // dJ_perp/dxi (field_src_class.f03:273-405).  m = 0: o[0..1] = dcu(0, 0..1, i);
@@ -46,11 +46,11 @@ __device__ __forceinline__ void row_djdxi(const GridDev& G, int m, int i, const 
       o[0] = 0.0;
       o[1] = 0.0;
     } else if (i == nr) {
-      const double ir = G.ir[nr];
+      const double ir = G.ir[(nr) - G.toff];
       o[0] = A_(0, 0, nr) + idrh * (4.0 * U_(0, 0, nr - 1) - U_(0, 0, nr - 2) - 3.0 * U_(0, 0, nr)) - ir * U_(0, 0, nr);
       o[1] = A_(0, 1, nr) + idrh * (4.0 * U_(0, 1, nr - 1) - U_(0, 1, nr - 2) - 3.0 * U_(0, 1, nr)) - ir * U_(0, 1, nr);
     } else {
-      const double ir = G.ir[i];
+      const double ir = G.ir[(i) - G.toff];
       o[0] = A_(0, 0, i) - idrh * (U_(0, 0, i + 1) - U_(0, 0, i - 1)) - ir * U_(0, 0, i);
       o[1] = A_(0, 1, i) - idrh * (U_(0, 1, i + 1) - U_(0, 1, i - 1)) - ir * U_(0, 1, i);
     }
@@ -67,7 +67,7 @@ __device__ __forceinline__ void row_djdxi(const GridDev& G, int m, int i, const 
       o[0] = o[1] = o[2] = o[3] = 0.0;
     }
   } else if (i == nr) {
-    const double ir = G.ir[nr];
+    const double ir = G.ir[(nr) - G.toff];
     o[0] = A_(r, 0, nr) + idrh * (4.0 * U_(r, 0, nr - 1) - U_(r, 0, nr - 2) - 3.0 * U_(r, 0, nr)) - ir * U_(r, 0, nr) +
            dm * ir * U_(s, 1, nr);
     o[1] = A_(r, 1, nr) + idrh * (4.0 * U_(r, 1, nr - 1) - U_(r, 1, nr - 2) - 3.0 * U_(r, 1, nr)) - ir * U_(r, 1, nr) +
@@ -83,7 +83,7 @@ __device__ __forceinline__ void row_djdxi(const GridDev& G, int m, int i, const 
     o[2] = A_(s, 0, 2) - idr * (U_(s, 0, 3) - U_(s, 0, 2)) - ir * U_(s, 0, 2) - dm * ir * U_(r, 1, 2);
     o[3] = A_(s, 1, 2) - idr * (U_(s, 1, 3) - U_(s, 1, 2)) - ir * U_(s, 1, 2) - dm * ir * U_(r, 2, 2);
   } else {
-    const double ir = G.ir[i];
+    const double ir = G.ir[(i) - G.toff];
     o[0] = A_(r, 0, i) - idrh * (U_(r, 0, i + 1) - U_(r, 0, i - 1)) - ir * U_(r, 0, i) + dm * ir * U_(s, 1, i);
     o[1] = A_(r, 1, i) - idrh * (U_(r, 1, i + 1) - U_(r, 1, i - 1)) - ir * U_(r, 1, i) + dm * ir * U_(s, 2, i);
     o[2] = A_(s, 0, i) - idrh * (U_(s, 0, i + 1) - U_(s, 0, i - 1)) - ir * U_(s, 0, i) - dm * ir * U_(r, 1, i);
@@ -132,13 +132,13 @@ __device__ __forceinline__ void row_btiter_src(const GridDev& G, int m, int i, c
       s2im = idr * CU(pi, 2, 2);
     }
   } else if (i == nr) {
-    const double ir = G.ir[nr];
+    const double ir = G.ir[(nr) - G.toff];
     s1re = -DC(pr, 1, nr) + dm * CU(pi, 2, nr) * ir;
     s1im = -DC(pi, 1, nr) - dm * CU(pr, 2, nr) * ir;
     s2re = DC(pr, 0, nr) + idrh * (3.0 * CU(pr, 2, nr) - 4.0 * CU(pr, 2, nr - 1) + CU(pr, 2, nr - 2));
     s2im = DC(pi, 0, nr) + idrh * (3.0 * CU(pi, 2, nr) - 4.0 * CU(pi, 2, nr - 1) + CU(pi, 2, nr - 2));
   } else {
-    const double ir = G.ir[i];
+    const double ir = G.ir[(i) - G.toff];
     s1re = -DC(pr, 1, i) + dm * CU(pi, 2, i) * ir;
     s1im = -DC(pi, 1, i) - dm * CU(pr, 2, i) * ir;
     s2re = DC(pr, 0, i) + idrh * (CU(pr, 2, i + 1) - CU(pr, 2, i - 1));
@@ -161,10 +161,10 @@ __device__ __forceinline__ void row_bz_src(const GridDev& G, int m, int i, const
     if (i == 1) {
       re = -2.0 * idr * CU(0, 1, 2);
     } else if (i == nr) {
-      const double ir = G.ir[nr];
+      const double ir = G.ir[(nr) - G.toff];
       re = -idrh * (3.0 * CU(0, 1, nr) - 4.0 * CU(0, 1, nr - 1) + CU(0, 1, nr - 2)) - ir * CU(0, 1, nr);
     } else {
-      const double ir = G.ir[i];
+      const double ir = G.ir[(i) - G.toff];
       re = -idrh * (CU(0, 1, i + 1) - CU(0, 1, i - 1)) - ir * CU(0, 1, i);
     }
     im = 0.0;
@@ -173,7 +173,7 @@ __device__ __forceinline__ void row_bz_src(const GridDev& G, int m, int i, const
   const int pr = part_re(m), pi = part_im(m);
   const double dm = (double)m;
   if (i == nr) {
-    const double ir = G.ir[nr];
+    const double ir = G.ir[(nr) - G.toff];
     re = -idrh * (3.0 * CU(pr, 1, nr) - 4.0 * CU(pr, 1, nr - 1) + CU(pr, 1, nr - 2)) - ir * CU(pr, 1, nr) -
          dm * ir * CU(pi, 0, nr);
     im = -idrh * (3.0 * CU(pi, 1, nr) - 4.0 * CU(pi, 1, nr - 1) + CU(pi, 1, nr - 2)) - ir * CU(pi, 1, nr) +
@@ -191,7 +191,7 @@ __device__ __forceinline__ void row_bz_src(const GridDev& G, int m, int i, const
     re = -idr * (CU(pr, 1, 3) - CU(pr, 1, 2)) - ir * CU(pr, 1, 2) - dm * ir * CU(pi, 0, 2);
     im = -idr * (CU(pi, 1, 3) - CU(pi, 1, 2)) - ir * CU(pi, 1, 2) + dm * ir * CU(pr, 0, 2);
   } else {
-    const double ir = G.ir[i];
+    const double ir = G.ir[(i) - G.toff];
     re = -idrh * (CU(pr, 1, i + 1) - CU(pr, 1, i - 1)) - ir * CU(pr, 1, i) - dm * ir * CU(pi, 0, i);
     im = -idrh * (CU(pi, 1, i + 1) - CU(pi, 1, i - 1)) - ir * CU(pi, 1, i) + dm * ir * CU(pr, 0, i);
   }
@@ -211,13 +211,13 @@ __device__ __forceinline__ void row_ez_src(const GridDev& G, int m, int i, const
     if (i == 1) {
       re = 0.0;
     } else if (i == nr - 1) {
-      const double ir = G.ir[nr - 1];
+      const double ir = G.ir[(nr - 1) - G.toff];
       re = idrh * (CU(0, 0, nr) - CU(0, 0, nr - 2)) + ir * CU(0, 0, nr - 1);
     } else if (i == nr) {
-      const double ir = G.ir[nr];
+      const double ir = G.ir[(nr) - G.toff];
       re = idr * (CU(0, 0, nr) - CU(0, 0, nr - 1)) + ir * CU(0, 0, nr);
     } else {
-      const double ir = G.ir[i];
+      const double ir = G.ir[(i) - G.toff];
       re = idrh * (CU(0, 0, i + 1) - CU(0, 0, i - 1)) + ir * CU(0, 0, i);
       in_div = true;
     }
@@ -225,7 +225,7 @@ __device__ __forceinline__ void row_ez_src(const GridDev& G, int m, int i, const
   }
   const int pr = part_re(m), pi = part_im(m);
   if (i == nr) {
-    const double ir = G.ir[nr];
+    const double ir = G.ir[(nr) - G.toff];
     re = idrh * (3.0 * CU(pr, 0, nr) - 4.0 * CU(pr, 0, nr - 1) + CU(pr, 0, nr - 2)) + ir * CU(pr, 0, nr) -
          dm * ir * CU(pi, 1, nr);
     im = idrh * (3.0 * CU(pi, 0, nr) - 4.0 * CU(pi, 0, nr - 1) + CU(pi, 0, nr - 2)) + ir * CU(pi, 0, nr) +
@@ -243,7 +243,7 @@ __device__ __forceinline__ void row_ez_src(const GridDev& G, int m, int i, const
     re = idr * (CU(pr, 0, 3) - CU(pr, 0, 2)) + ir * CU(pr, 0, 2) - dm * ir * CU(pi, 1, 2);
     im = idr * (CU(pi, 0, 3) - CU(pi, 0, 2)) + ir * CU(pi, 0, 2) + dm * ir * CU(pr, 1, 2);
   } else {
-    const double ir = G.ir[i];
+    const double ir = G.ir[(i) - G.toff];
     re = idrh * (CU(pr, 0, i + 1) - CU(pr, 0, i - 1)) + ir * CU(pr, 0, i) - dm * ir * CU(pi, 1, i);
     im = idrh * (CU(pi, 0, i + 1) - CU(pi, 0, i - 1)) + ir * CU(pi, 0, i) + dm * ir * CU(pr, 1, i);
   }
@@ -288,7 +288,7 @@ __device__ __forceinline__ void row_et(const GridDev& G, int m, int i, const BF&
     }
     return;
   }
-  const double ir = G.ir[i];
+  const double ir = G.ir[(i) - G.toff];
   if (i == nr) {
     o[0] = B(pr, 1, nr) + idrh * (4.0 * PS(pr, 0, nr - 1) - PS(pr, 0, nr - 2) - 3.0 * PS(pr, 0, nr));
     o[1] = B(pi, 1, nr) + idrh * (4.0 * PS(pi, 0, nr - 1) - PS(pi, 0, nr - 2) - 3.0 * PS(pi, 0, nr));
