@@ -164,7 +164,7 @@ def run_reference(args):
     return 0
 
 
-def _measure(args, deck, inputs, prec, local, dist, full=True):
+def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
     """Times args.steps 3D steps of one simulation (after args.warmup untimed ones) on the
     library's stream with CUDA events; with `full`, also the end-to-end pass with host
     buffers and one host-driven step with per-kernel event timing."""
@@ -172,6 +172,11 @@ def _measure(args, deck, inputs, prec, local, dist, full=True):
     from qpad_gb300.replicas import reduce_timing
     sim = Q.build_simulation(deck, precision=prec, device=local, inputs=inputs)
     sim.use_graph(args.graph == "on")
+    if guess:
+        from qpad_gb300 import learned as LR
+        from qpad_gb300.train_guess import DEFAULT_OUT
+        nets = LR.load(DEFAULT_OUT, deck.max_mode, device=local)
+        LR.attach(sim, *nets)
     sp = sim.species[0]
     npl = len(inputs[0][4])
 
@@ -265,6 +270,15 @@ def run_ours(args):
         cmp = {"path": "fp64" if other == K.PREC_FP64 else "mixed", "value": c["value"],
                "ms_per_step": c["ms_per_step"], "iters_per_slice": c["iters_per_slice"],
                "graph": c["graph"]["active"]}
+    # the learned guess (trained nets for the c2 shape), measured as its own arm
+    learned = None
+    if not args.no_compare and deck.name.startswith("c2") and deck.max_mode == 2:
+        from qpad_gb300.train_guess import DEFAULT_OUT
+        if os.path.exists(DEFAULT_OUT):
+            g = _measure(args, deck, inputs, prec, local, dist, full=False, guess=True)
+            learned = {"value": g["value"], "ms_per_step": g["ms_per_step"], "iters_per_slice": g["iters_per_slice"],
+                       "iters_change": g["iters_per_slice"] / r["iters_per_slice"] - 1.0,
+                       "weights": os.path.relpath(DEFAULT_OUT, ROOT)}
     kern = r["kern"]
     amj_ms, namj = kern["amjdp"]
     peak, peak_kind = _peaks()
@@ -306,6 +320,8 @@ def run_ours(args):
         "kernel_ms_per_step": {k: round(v[0], 3) for k, v in kern.items()},
         "kernel_launches_per_step": {k: v[1] for k, v in kern.items()},
     }
+    if learned is not None:
+        line["learned_guess"] = learned
     if cmp is not None:
         line["compare"] = cmp
         line["speedup_vs_" + cmp["path"]] = r["value"] / cmp["value"]

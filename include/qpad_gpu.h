@@ -223,6 +223,37 @@ typedef struct qpad_beam_load_desc {
 int64_t qpad_load_beam(int nr, int nz, double dr, double dxi, qpad_rng* r,
                        const qpad_beam_load_desc* d, double* x, double* p, double* q, int64_t cap);
 
+/* ---- learned predictor-corrector guess (no counterpart in the reference) ------------
+ * A radial 1D conv net (layers x conv1d(ksize), width channels, GELU between layers),
+ * trained and evaluated by this library's own BF16 tensor-core kernels with FP32
+ * accumulation.  Host arrays are sample-major [sample][channel][nr]. */
+typedef struct qpad_learn qpad_learn;
+int qpad_learn_create(int cin, int cout, int width, int layers, int ksize, uint64_t seed, int device,
+                      qpad_learn** out);
+int qpad_learn_destroy(qpad_learn* net);
+const char* qpad_learn_last_error(const qpad_learn* net);
+int qpad_learn_param_count(const qpad_learn* net, int64_t* n);
+int qpad_learn_get_params(qpad_learn* net, float* params);
+int qpad_learn_set_params(qpad_learn* net, const float* params);
+int qpad_learn_predict(qpad_learn* net, const float* x, int64_t ns, int nr, float* y);
+/* mean squared error of y(x) against t and its gradient w.r.t. every parameter */
+int qpad_learn_grad(qpad_learn* net, const float* x, const float* t, int64_t ns, int nr, double* loss,
+                    float* grad);
+/* Adam, `epochs` shuffled passes in mini-batches; losses[epoch] = mean training loss */
+int qpad_learn_train(qpad_learn* net, const float* x, const float* t, int64_t ns, int nr, int epochs,
+                     int batch, float lr, uint64_t seed, double* losses);
+/* Replaces the carried initial b_spe (simulation_class.f03:324-326, 360) and the J-perp
+ * predictor (:425-426) of every slice j >= 3 by the nets' guess from slices j-1, j-2:
+ * net0 (10 -> 4 channels) for m = 0, net1 (20 -> 8) for the modes m >= 1.  The iteration
+ * still runs to iter_reltol.  Null net0 detaches.  The nets must outlive the attachment. */
+int qpad_guess_attach(qpad_ctx* ctx, qpad_learn* net0, qpad_learn* net1);
+/* Which parts of the guess are applied (bit 0: B-perp, bit 1: the J-perp predictor; both by
+ * default) and the weight w in [0, 1] of the net's correction: guess = carried + w (net - carried). */
+int qpad_guess_config(qpad_ctx* ctx, int apply, double weight);
+/* One training sample of mode m at slice j (3 <= j <= nz) from the 3D stores of the last
+ * step: inputs x [10 or 20][nr], targets t [4 or 8][nr], both in units of *scale. */
+int qpad_guess_sample(qpad_ctx* ctx, int j, int m, float* x, float* t, float* scale);
+
 #ifdef __cplusplus
 }
 #endif

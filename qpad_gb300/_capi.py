@@ -11,6 +11,7 @@ import os
 from . import build as _build
 
 D = C.POINTER(C.c_double)
+F = C.POINTER(C.c_float)
 I32P = C.POINTER(C.c_int32)
 I64P = C.POINTER(C.c_int64)
 
@@ -113,6 +114,20 @@ _SIGS = {
     "qpad_beam_push": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "qpad_slice_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(SliceStats)]),
     "qpad_3d_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(SliceStats)]),
+    "qpad_learn_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int,
+                                    C.POINTER(C.c_void_p)]),
+    "qpad_learn_destroy": (C.c_int, [C.c_void_p]),
+    "qpad_learn_last_error": (C.c_char_p, [C.c_void_p]),
+    "qpad_learn_param_count": (C.c_int, [C.c_void_p, I64P]),
+    "qpad_learn_get_params": (C.c_int, [C.c_void_p, F]),
+    "qpad_learn_set_params": (C.c_int, [C.c_void_p, F]),
+    "qpad_learn_predict": (C.c_int, [C.c_void_p, F, C.c_int64, C.c_int, F]),
+    "qpad_learn_grad": (C.c_int, [C.c_void_p, F, F, C.c_int64, C.c_int, D, F]),
+    "qpad_learn_train": (C.c_int, [C.c_void_p, F, F, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_float,
+                                   C.c_uint64, D]),
+    "qpad_guess_attach": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "qpad_guess_sample": (C.c_int, [C.c_void_p, C.c_int, C.c_int, F, F, F]),
+    "qpad_guess_config": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "qpad_rng_seed": (None, [C.POINTER(Rng), C.c_uint64]),
     "qpad_load_plasma": (C.c_int64, [C.c_int, C.c_double, C.POINTER(Rng), C.c_int, C.c_int, C.c_int, C.c_double,
                                      C.c_double, D, D, D, D, D, D, C.c_int64]),

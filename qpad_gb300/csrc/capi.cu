@@ -346,6 +346,7 @@ extern "C" int qpad_ctx_destroy(qpad_ctx* ctx) {
   if (ctx->fac) cudaFree(ctx->fac);
   if (ctx->rtab) cudaFree(ctx->rtab);
   if (ctx->qn) cudaFree(ctx->qn);
+  guess_free(ctx);
   if (ctx->qraw) cudaFree(ctx->qraw);
   if (ctx->raw) cudaFree(ctx->raw);
   if (ctx->iter_tickets) cudaFree(ctx->iter_tickets);
@@ -965,6 +966,7 @@ int enqueue_slice_prologue(qpad_ctx* ctx, cudaGraphConditionalHandle hi, int use
   int any_ntd = 0;
   for (auto* s : ctx->species) any_ntd |= s->neutralized;
   const bool mixed = ctx->precision == QPAD_PREC_MIXED;
+  if (int r = guess_enqueue(ctx)) return r;          // before anything reads b_spe or cu
   if (cudaMemsetAsync(ctx->d_iter, 0, sizeof(int), ctx->stream) != cudaSuccess ||
       cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess)
     return check_launch(ctx, "slice prologue memsets", 0);

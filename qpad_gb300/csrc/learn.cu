@@ -1,0 +1,702 @@
+// learn.cu -- the learned predictor-corrector guess: a radial 1D conv net per azimuthal
+// mode, trained and evaluated on the GPU by this file's own kernels.
+//
+// Network (per mode): L layers of conv1d(kernel K, zero padding K/2) over the radial nodes,
+// widths cin -> W -> ... -> W -> cout, GELU after every layer but the last.  Activations
+// are channel-major [C][N] with N = samples * nr (sample-major, radial node fastest).
+//
+// Every convolution is an im2col GEMM on BF16 tensor cores (mma.sync m16n8k16, FP32
+// accumulation) with FP32 master weights:
+//   forward       Y[co][n]  = b[co] + sum_k Wt[co][k] * cols[k][n]        (k = ci*K + tap)
+//   weight grad   dW[co][k] = sum_n dY[co][n] * cols[k][n]                  (split over n)
+//   data grad     dcols[k][n] = sum_co Wt[co][k] * dY[co][n], then col2im
+// Training is Adam on the mean squared error.  Everything here is FP32 outside the MMA.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+
+#include "qpad_internal.cuh"
+
+namespace qpad {
+
+static constexpr int kGT = 64;       // GEMM CTA tile (M and N)
+static constexpr int kGK = 32;       // GEMM K step
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat16 l = __float2bfloat16_rn(lo), h = __float2bfloat16_rn(hi);
+  return (uint32_t)(*(const uint16_t*)&l) | ((uint32_t)(*(const uint16_t*)&h) << 16);
+}
+
+// D = A(16x16, row) * B(16x8, col) + C, bf16 inputs, f32 accumulate
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// C[M][N] (+)= sum_k A(m,k) B(k,n) over k in [k_begin, k_end), FP32 in global memory.
+// A(m,k) = TA ? A[k*lda + m] : A[m*lda + k];  B(k,n) = TB ? B[n*ldb + k] : B[k*ldb + n].
+// accumulate: atomicAdd into C (split-K), else C = result (+ bias[m] when bias).
+// CTA: 4 warps, tile 64x64; warp w takes rows 32*(w/2).. and columns 32*(w%2)..
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int Kdim, const float* __restrict__ A, int lda,
+                                                   const float* __restrict__ B, int ldb, float* __restrict__ C,
+                                                   int ldc, const float* __restrict__ bias, int accumulate,
+                                                   int k_chunk) {
+  __shared__ float As[kGT][kGK + 1];   // [m][k]
+  __shared__ float Bs[kGK][kGT + 1];   // [k][n]
+  const int m0 = blockIdx.y * kGT, n0 = blockIdx.x * kGT;
+  const int kb = blockIdx.z * k_chunk, ke = min(Kdim, kb + k_chunk);
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.0f;
+  for (int k0 = kb; k0 < ke; k0 += kGK) {
+    for (int q = t; q < kGT * kGK; q += 128) {
+      const int mm = TA ? q % kGT : q / kGK, kk = TA ? q / kGT : q % kGK;
+      const int gm = m0 + mm, gk = k0 + kk;
+      As[mm][kk] = (gm < M && gk < ke) ? (TA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk]) : 0.0f;
+    }
+    for (int q = t; q < kGK * kGT; q += 128) {
+      const int kk = TB ? q % kGK : q / kGT, nn = TB ? q / kGK : q % kGT;
+      const int gk = k0 + kk, gn = n0 + nn;
+      Bs[kk][nn] = (gk < ke && gn < N) ? (TB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn]) : 0.0f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < kGK; ks += 16) {
+      const int r = lane >> 2, c = (lane & 3) * 2;
+      uint32_t af[2][4], bf[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int mr = wm + i * 16 + r;
+        af[i][0] = pack_bf16(As[mr][ks + c], As[mr][ks + c + 1]);
+        af[i][1] = pack_bf16(As[mr + 8][ks + c], As[mr + 8][ks + c + 1]);
+        af[i][2] = pack_bf16(As[mr][ks + c + 8], As[mr][ks + c + 9]);
+        af[i][3] = pack_bf16(As[mr + 8][ks + c + 8], As[mr + 8][ks + c + 9]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int nc = wn + j * 8 + r;
+        bf[j][0] = pack_bf16(Bs[ks + c][nc], Bs[ks + c + 1][nc]);
+        bf[j][1] = pack_bf16(Bs[ks + c + 8][nc], Bs[ks + c + 9][nc]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bf[j]);
+    }
+    __syncthreads();
+  }
+  const int r = lane >> 2, c = (lane & 3) * 2;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const int gm = m0 + wm + i * 16 + r + (h >= 2 ? 8 : 0);
+        const int gn = n0 + wn + j * 8 + c + (h & 1);
+        if (gm >= M || gn >= N) continue;
+        float* dst = C + (size_t)gm * ldc + gn;
+        if (accumulate) atomicAdd(dst, acc[i][j][h]);
+        else *dst = acc[i][j][h] + (bias ? bias[gm] : 0.0f);
+      }
+}
+
+// cols[(ci*K + tap)][n] = X[ci][n + tap - K/2] within the same sample, else 0
+__global__ void k_im2col(const float* __restrict__ X, int C, int N, int nr, int K, float* __restrict__ cols) {
+  const int64_t total = (int64_t)C * K * N;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int n = (int)(q % N);
+    const int row = (int)(q / N);
+    const int ci = row / K, tap = row % K;
+    const int x = n % nr, xs = x + tap - K / 2;
+    cols[q] = (xs >= 0 && xs < nr) ? X[(size_t)ci * N + n - x + xs] : 0.0f;
+  }
+}
+
+// dX[ci][n] = sum_tap dcols[(ci*K + tap)][n - tap + K/2] within the same sample
+__global__ void k_col2im(const float* __restrict__ dcols, int C, int N, int nr, int K, float* __restrict__ dX) {
+  const int64_t total = (int64_t)C * N;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int n = (int)(q % N), ci = (int)(q / N);
+    const int x = n % nr;
+    float s = 0.0f;
+    for (int tap = 0; tap < K; ++tap) {
+      const int xo = x - tap + K / 2;
+      if (xo >= 0 && xo < nr) s += dcols[((size_t)ci * K + tap) * N + n - x + xo];
+    }
+    dX[q] = s;
+  }
+}
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+__global__ void k_gelu(const float* __restrict__ pre, float* __restrict__ out, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    out[q] = gelu(pre[q]);
+}
+
+// dpre = dout * gelu'(pre)
+__global__ void k_gelu_back(const float* pre, const float* dout, float* dpre, int64_t n) {   // dout may be dpre
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    dpre[q] = dout[q] * gelu_grad(pre[q]);
+}
+
+// mean squared error over [C][N]: loss partial sums and dY = 2 (Y - T) / (C N)
+__global__ void k_mse(const float* __restrict__ Y, const float* __restrict__ T, float* __restrict__ dY, int64_t n,
+                      double* __restrict__ loss) {
+  double s = 0.0;
+  const float sc = 2.0f / (float)n;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const float d = Y[q] - T[q];
+    dY[q] = sc * d;
+    s += (double)d * d;
+  }
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, s);
+}
+
+// db[co] = sum_n dY[co][n]
+__global__ void k_bias_grad(const float* __restrict__ dY, int C, int N, float* __restrict__ db) {
+  const int co = blockIdx.x;
+  float s = 0.0f;
+  for (int n = threadIdx.x; n < N; n += blockDim.x) s += dY[(size_t)co * N + n];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  __shared__ float red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float tot = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    db[co] += tot;
+  }
+}
+
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m1, float* __restrict__ m2,
+                       int64_t n, float lr, float b1, float b2, float eps, float c1, float c2) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const float gq = g[q];
+    const float a = b1 * m1[q] + (1.0f - b1) * gq;
+    const float b = b2 * m2[q] + (1.0f - b2) * gq * gq;
+    m1[q] = a;
+    m2[q] = b;
+    w[q] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+  }
+}
+
+static int egrid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+
+}  // namespace qpad
+
+using namespace qpad;
+
+// Work buffers of one forward (and backward) pass over up to `cap` columns.
+struct LearnBufs {
+  int64_t cap = 0;
+  float* act = nullptr;            // layer inputs [layers+1][maxC][cap]
+  float* pre = nullptr;            // pre-activations [layers][maxC][cap]
+  float* cols = nullptr;           // [maxC*K][cap]
+  float* dcur = nullptr;           // [maxC][cap]
+  float* dnext = nullptr;          // [maxC][cap]
+  float* target = nullptr;         // [cout][cap]
+};
+
+struct qpad_learn {
+  int cin, cout, width, layers, ksize;
+  std::vector<int> ci, co;         // channels in / out per layer
+  std::vector<size_t> woff, boff;  // offsets of each layer's weights / biases in the parameter block
+  size_t nparam = 0;
+  float* param = nullptr;          // FP32 master weights [co][ci*K] then biases, layer by layer
+  float* grad = nullptr;
+  float* m1 = nullptr;
+  float* m2 = nullptr;
+  int64_t step = 0;
+  LearnBufs B;                     // training / prediction buffers
+  double* loss = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int maxc = 0;
+};
+
+namespace {
+int lerr(qpad_learn* L, int code, const std::string& m) {
+  if (L) L->err = m;
+  return code;
+}
+int lcheck(qpad_learn* L, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return QPAD_OK;
+  return lerr(L, QPAD_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void free_bufs(LearnBufs& B) {
+  for (float** p : {&B.act, &B.pre, &B.cols, &B.dcur, &B.dnext, &B.target})
+    if (*p) { cudaFree(*p); *p = nullptr; }
+  B.cap = 0;
+}
+
+int alloc_bufs(const qpad_learn* L, LearnBufs& B, int64_t cols, bool train) {
+  free_bufs(B);
+  const size_t mc = (size_t)L->maxc;
+  cudaError_t e = cudaMalloc(&B.act, sizeof(float) * (L->layers + 1) * mc * cols);
+  if (e == cudaSuccess) e = cudaMalloc(&B.pre, sizeof(float) * L->layers * mc * cols);
+  if (e == cudaSuccess) e = cudaMalloc(&B.cols, sizeof(float) * mc * L->ksize * cols);
+  if (train) {
+    if (e == cudaSuccess) e = cudaMalloc(&B.dcur, sizeof(float) * mc * cols);
+    if (e == cudaSuccess) e = cudaMalloc(&B.dnext, sizeof(float) * mc * cols);
+    if (e == cudaSuccess) e = cudaMalloc(&B.target, sizeof(float) * L->cout * cols);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    free_bufs(B);
+    return QPAD_E_NOMEM;
+  }
+  B.cap = cols;
+  return 0;
+}
+
+int ensure_cap(qpad_learn* L, int64_t cols) {
+  if (cols <= L->B.cap) return 0;
+  if (alloc_bufs(L, L->B, cols, true)) return lerr(L, QPAD_E_NOMEM, "learn work buffers");
+  return 0;
+}
+
+template <bool TA, bool TB>
+void gemm(cudaStream_t st, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+          const float* bias, bool accumulate, int ksplit = 1) {
+  const int k_chunk = ((K + ksplit - 1) / ksplit + kGK - 1) / kGK * kGK;
+  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, (K + k_chunk - 1) / k_chunk);
+  k_gemm_bf16<TA, TB><<<grid, 128, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, accumulate ? 1 : 0, k_chunk);
+}
+
+float* act_of(const qpad_learn* L, const LearnBufs& B, int layer) { return B.act + (size_t)layer * L->maxc * B.cap; }
+float* pre_of(const qpad_learn* L, const LearnBufs& B, int layer) { return B.pre + (size_t)layer * L->maxc * B.cap; }
+
+}  // namespace
+
+// forward pass over N columns already in act layer 0 of B; output in act[layers]
+int learn_forward(const qpad_learn* L, const LearnBufs& B, cudaStream_t st, int N, int nr) {
+  for (int l = 0; l < L->layers; ++l) {
+    const int ci = L->ci[l], co = L->co[l], K = L->ksize;
+    k_im2col<<<egrid((int64_t)ci * K * N), 256, 0, st>>>(act_of(L, B, l), ci, N, nr, K, B.cols);
+    float* out = (l == L->layers - 1) ? act_of(L, B, l + 1) : pre_of(L, B, l);
+    gemm<false, false>(st, co, N, ci * K, L->param + L->woff[l], ci * K, B.cols, N, out, N, L->param + L->boff[l],
+                       false);
+    if (l < L->layers - 1) k_gelu<<<egrid((int64_t)co * N), 256, 0, st>>>(out, act_of(L, B, l + 1), (int64_t)co * N);
+  }
+  return 3 * L->layers - 1;   // kernels launched
+}
+
+namespace {
+// backward from dY (in B.dcur) to the parameter gradients (accumulated into grad)
+void backward(qpad_learn* L, int N, int nr) {
+  LearnBufs& B = L->B;
+  for (int l = L->layers - 1; l >= 0; --l) {
+    const int ci = L->ci[l], co = L->co[l], K = L->ksize;
+    if (l < L->layers - 1)   // through the GELU of this layer's output
+      k_gelu_back<<<egrid((int64_t)co * N), 256, 0, L->stream>>>(pre_of(L, B, l), B.dcur, B.dcur, (int64_t)co * N);
+    k_bias_grad<<<co, 256, 0, L->stream>>>(B.dcur, co, N, L->grad + L->boff[l]);
+    k_im2col<<<egrid((int64_t)ci * K * N), 256, 0, L->stream>>>(act_of(L, B, l), ci, N, nr, K, B.cols);
+    const int ksplit = std::max(1, std::min(64, N / 2048));
+    gemm<false, true>(L->stream, co, ci * K, N, B.dcur, N, B.cols, N, L->grad + L->woff[l], ci * K, nullptr, true,
+                      ksplit);
+    if (l > 0) {
+      gemm<true, false>(L->stream, ci * K, N, co, L->param + L->woff[l], ci * K, B.dcur, N, B.cols, N, nullptr, false);
+      k_col2im<<<egrid((int64_t)ci * N), 256, 0, L->stream>>>(B.cols, ci, N, nr, K, B.dnext);
+      std::swap(B.dcur, B.dnext);
+    }
+  }
+}
+}  // namespace
+
+extern "C" int qpad_learn_create(int cin, int cout, int width, int layers, int ksize, uint64_t seed, int device,
+                                 qpad_learn** out) {
+  if (!out || cin < 1 || cout < 1 || width < 1 || layers < 1 || ksize < 1 || ksize % 2 == 0 || layers > 16)
+    return QPAD_E_ARG;
+  *out = nullptr;
+  qpad_learn* L = new (std::nothrow) qpad_learn();
+  if (!L) return QPAD_E_NOMEM;
+  L->cin = cin; L->cout = cout; L->width = width; L->layers = layers; L->ksize = ksize;
+  L->maxc = std::max(std::max(cin, cout), width);
+  size_t off = 0;
+  for (int l = 0; l < layers; ++l) {
+    L->ci.push_back(l == 0 ? cin : width);
+    L->co.push_back(l == layers - 1 ? cout : width);
+    L->woff.push_back(off);
+    off += (size_t)L->co[l] * L->ci[l] * ksize;
+    L->boff.push_back(off);
+    off += (size_t)L->co[l];
+  }
+  L->nparam = off;
+  int r = lcheck(L, cudaSetDevice(device), "cudaSetDevice");
+  if (!r) r = lcheck(L, cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking), "stream");
+  for (float** p : {&L->param, &L->grad, &L->m1, &L->m2})
+    if (!r) r = lcheck(L, cudaMalloc(p, sizeof(float) * L->nparam), "cudaMalloc(params)");
+  if (!r) r = lcheck(L, cudaMalloc(&L->loss, sizeof(double)), "cudaMalloc(loss)");
+  if (!r) {
+    // He-style initialisation, last layer scaled down so that the initial guess is ~0
+    std::mt19937_64 g(seed);
+    std::vector<float> h(L->nparam, 0.0f);
+    for (int l = 0; l < layers; ++l) {
+      const size_t nw = (size_t)L->co[l] * L->ci[l] * ksize;
+      const double sd = std::sqrt(2.0 / (double)(L->ci[l] * ksize)) * (l == layers - 1 ? 0.1 : 1.0);
+      std::normal_distribution<double> nd(0.0, sd);
+      for (size_t q = 0; q < nw; ++q) h[L->woff[l] + q] = (float)nd(g);
+    }
+    r = lcheck(L, cudaMemcpy(L->param, h.data(), sizeof(float) * L->nparam, cudaMemcpyHostToDevice), "upload params");
+    if (!r) r = lcheck(L, cudaMemset(L->m1, 0, sizeof(float) * L->nparam), "memset");
+    if (!r) r = lcheck(L, cudaMemset(L->m2, 0, sizeof(float) * L->nparam), "memset");
+  }
+  if (r) {
+    qpad_learn_destroy(L);
+    return r;
+  }
+  *out = L;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_learn_destroy(qpad_learn* L) {
+  if (!L) return QPAD_OK;
+  for (float* p : {L->param, L->grad, L->m1, L->m2})
+    if (p) cudaFree(p);
+  free_bufs(L->B);
+  if (L->loss) cudaFree(L->loss);
+  if (L->stream) cudaStreamDestroy(L->stream);
+  delete L;
+  return QPAD_OK;
+}
+
+extern "C" const char* qpad_learn_last_error(const qpad_learn* L) { return L ? L->err.c_str() : "null net"; }
+
+extern "C" int qpad_learn_param_count(const qpad_learn* L, int64_t* n) {
+  if (!L || !n) return QPAD_E_ARG;
+  *n = (int64_t)L->nparam;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_learn_get_params(qpad_learn* L, float* host) {
+  if (!L || !host) return QPAD_E_ARG;
+  return lcheck(L, cudaMemcpy(host, L->param, sizeof(float) * L->nparam, cudaMemcpyDeviceToHost), "download params");
+}
+
+extern "C" int qpad_learn_set_params(qpad_learn* L, const float* host) {
+  if (!L || !host) return QPAD_E_ARG;
+  return lcheck(L, cudaMemcpy(L->param, host, sizeof(float) * L->nparam, cudaMemcpyHostToDevice), "upload params");
+}
+
+// Y[s][cout][nr] = net(X[s][cin][nr]) for ns samples (host arrays, sample-major)
+extern "C" int qpad_learn_predict(qpad_learn* L, const float* X, int64_t ns, int nr, float* Y) {
+  if (!L || !X || !Y || ns < 1 || nr < 1) return QPAD_E_ARG;
+  const int64_t N = ns * nr;
+  if (N > INT32_MAX / 8) return lerr(L, QPAD_E_CAPACITY, "too many columns");
+  if (int r = ensure_cap(L, N)) return r;
+  // host [s][c][x] -> device channel-major [c][s*nr + x]
+  for (int c = 0; c < L->cin; ++c)
+    for (int64_t s = 0; s < ns; ++s)
+      if (int r = lcheck(L, cudaMemcpyAsync(act_of(L, L->B, 0) + (size_t)c * N + s * nr, X + ((size_t)s * L->cin + c) * nr,
+                                            sizeof(float) * nr, cudaMemcpyHostToDevice, L->stream), "upload X"))
+        return r;
+  learn_forward(L, L->B, L->stream, (int)N, nr);
+  for (int c = 0; c < L->cout; ++c)
+    for (int64_t s = 0; s < ns; ++s)
+      if (int r = lcheck(L, cudaMemcpyAsync(Y + ((size_t)s * L->cout + c) * nr, act_of(L, L->B, L->layers) + (size_t)c * N + s * nr,
+                                            sizeof(float) * nr, cudaMemcpyDeviceToHost, L->stream), "download Y"))
+        return r;
+  return lcheck(L, cudaStreamSynchronize(L->stream), "predict");
+}
+
+namespace {
+int upload_batch(qpad_learn* L, const float* X, const float* T, const int64_t* idx, int64_t nb, int nr) {
+  const int64_t N = nb * nr;
+  std::vector<float> hx((size_t)L->cin * N), ht((size_t)L->cout * N);
+  for (int64_t b = 0; b < nb; ++b) {
+    const int64_t s = idx ? idx[b] : b;
+    for (int c = 0; c < L->cin; ++c)
+      std::memcpy(&hx[(size_t)c * N + b * nr], X + ((size_t)s * L->cin + c) * nr, sizeof(float) * nr);
+    for (int c = 0; c < L->cout; ++c)
+      std::memcpy(&ht[(size_t)c * N + b * nr], T + ((size_t)s * L->cout + c) * nr, sizeof(float) * nr);
+  }
+  int r = lcheck(L, cudaMemcpyAsync(act_of(L, L->B, 0), hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice,
+                                    L->stream), "upload batch");
+  if (!r) r = lcheck(L, cudaMemcpyAsync(L->B.target, ht.data(), sizeof(float) * ht.size(), cudaMemcpyHostToDevice,
+                                        L->stream), "upload target");
+  if (!r) r = lcheck(L, cudaStreamSynchronize(L->stream), "batch sync");
+  return r;
+}
+
+// loss and gradient (into L->grad, zeroed first) of one uploaded batch of N columns
+int loss_grad(qpad_learn* L, int64_t N, int nr, double* loss_out) {
+  if (int r = lcheck(L, cudaMemsetAsync(L->grad, 0, sizeof(float) * L->nparam, L->stream), "zero grad")) return r;
+  if (int r = lcheck(L, cudaMemsetAsync(L->loss, 0, sizeof(double), L->stream), "zero loss")) return r;
+  learn_forward(L, L->B, L->stream, (int)N, nr);
+  const int64_t ny = (int64_t)L->cout * N;
+  k_mse<<<egrid(ny), 256, 0, L->stream>>>(act_of(L, L->B, L->layers), L->B.target, L->B.dcur, ny, L->loss);
+  backward(L, (int)N, nr);
+  double h = 0.0;
+  if (int r = lcheck(L, cudaMemcpyAsync(&h, L->loss, sizeof(double), cudaMemcpyDeviceToHost, L->stream), "loss"))
+    return r;
+  if (int r = lcheck(L, cudaStreamSynchronize(L->stream), "loss sync")) return r;
+  if (loss_out) *loss_out = h / (double)ny;
+  return 0;
+}
+}  // namespace
+
+// Mean squared error of the first ns samples and its gradient with respect to every
+// parameter (host arrays; grad has qpad_learn_param_count entries).
+extern "C" int qpad_learn_grad(qpad_learn* L, const float* X, const float* T, int64_t ns, int nr, double* loss,
+                               float* grad) {
+  if (!L || !X || !T || ns < 1 || nr < 1) return QPAD_E_ARG;
+  const int64_t N = ns * nr;
+  if (int r = ensure_cap(L, N)) return r;
+  if (int r = upload_batch(L, X, T, nullptr, ns, nr)) return r;
+  if (int r = loss_grad(L, N, nr, loss)) return r;
+  if (grad)
+    return lcheck(L, cudaMemcpy(grad, L->grad, sizeof(float) * L->nparam, cudaMemcpyDeviceToHost), "download grad");
+  return 0;
+}
+
+// Adam training on ns samples: `epochs` passes in shuffled mini-batches of `batch` samples.
+// losses[e] receives the mean training loss of epoch e.
+extern "C" int qpad_learn_train(qpad_learn* L, const float* X, const float* T, int64_t ns, int nr, int epochs,
+                                int batch, float lr, uint64_t seed, double* losses) {
+  if (!L || !X || !T || ns < 1 || nr < 1 || epochs < 1 || batch < 1 || !(lr > 0.0f)) return QPAD_E_ARG;
+  const int64_t nb = std::min<int64_t>(batch, ns);
+  if (int r = ensure_cap(L, nb * nr)) return r;
+  std::mt19937_64 g(seed);
+  std::vector<int64_t> perm(ns);
+  for (int64_t i = 0; i < ns; ++i) perm[i] = i;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int e = 0; e < epochs; ++e) {
+    std::shuffle(perm.begin(), perm.end(), g);
+    double tot = 0.0;
+    int64_t cnt = 0;
+    for (int64_t b0 = 0; b0 + nb <= ns; b0 += nb) {
+      if (int r = upload_batch(L, X, T, perm.data() + b0, nb, nr)) return r;
+      double l = 0.0;
+      if (int r = loss_grad(L, nb * nr, nr, &l)) return r;
+      ++L->step;
+      const float c1 = 1.0f - std::pow(b1, (float)L->step), c2 = 1.0f - std::pow(b2, (float)L->step);
+      k_adam<<<egrid((int64_t)L->nparam), 256, 0, L->stream>>>(L->param, L->grad, L->m1, L->m2, (int64_t)L->nparam,
+                                                                lr, b1, b2, eps, c1, c2);
+      if (int r = lcheck(L, cudaGetLastError(), "adam")) return r;
+      tot += l;
+      ++cnt;
+    }
+    if (losses) losses[e] = cnt ? tot / (double)cnt : 0.0;
+  }
+  return lcheck(L, cudaStreamSynchronize(L->stream), "train sync");
+}
+
+// =====================================================================================
+// The guess hook of the slice loop
+// =====================================================================================
+// Inputs of mode m at slice j: the previous two slices' B-perp, J-perp and rho - Jz from the
+// 3D stores (b_spe, cu, q_spe), channel (d-1)*5*nh + q*nh + h for slice j-d, quantity q in
+// {B_r, B_phi, J_r, J_phi, rho-Jz} and part h (Re, Im; m = 0 has Re only), over nodes
+// 1..nr, divided by their root mean square s.  Outputs (and training targets), channel
+// q*nh + h: q in {dB_r, dB_phi} = B-perp(j) - B-perp(j-1) and q in {dJ_r, dJ_phi} =
+// (J-perp(j) - J-perp(j-1)) / dxi, also in units of s.  The guess for slice j is then
+// b_spe = B-perp(j-1) + s dB and J-perp = J-perp(j-1) + dxi s dJ (the latter replaces the
+// carried predictor J-perp(j-1) + dxi dcu(j-1)).
+namespace qpad {
+
+struct GuessStores {
+  const double* b2;
+  const double* cu2;
+  const double* q2;
+};
+
+__device__ __forceinline__ double st2(const GridDev& G, const double* f2, int nc, int s, int p, int c, int i) {
+  return f2[((((size_t)(s - 1) * G.P + p) * nc + c) * G.ld) + i];
+}
+
+__device__ __forceinline__ double guess_raw_in(const GridDev& G, const GuessStores& S, int j, int m, int ch, int i) {
+  const int nh = m == 0 ? 1 : 2;
+  const int d = ch / (5 * nh) + 1, q = (ch / nh) % 5, h = ch % nh;
+  const int p = h == 0 ? part_re(m) : part_im(m), s = j - d;
+  if (q < 2) return st2(G, S.b2, 3, s, p, q, i);
+  if (q < 4) return st2(G, S.cu2, 3, s, p, q - 2, i);
+  return st2(G, S.q2, 1, s, p, 0, i) - st2(G, S.cu2, 3, s, p, 2, i);
+}
+
+// One CTA per mode (blockIdx.x = m, or m_fixed >= 0 for a single mode).  X rows have
+// length ldx (columns), mode m writes at column (m - 1) * nr of X1 (m >= 1) or at 0 of X0.
+__global__ void __launch_bounds__(256) k_guess_in(GridDev G, GuessStores S, const int* __restrict__ jp, int j_fixed,
+                                                  int m_fixed, float* __restrict__ X0, float* __restrict__ X1, int ldx1,
+                                                  float* __restrict__ scale, float* __restrict__ T) {
+  const int j = jp ? *jp : j_fixed;
+  const int m = m_fixed >= 0 ? m_fixed : (int)blockIdx.x;
+  if (j < 3) return;
+  const int nr = G.nr, nh = m == 0 ? 1 : 2, cin = 10 * nh;
+  float* X = m == 0 ? X0 : X1 + (size_t)(m_fixed >= 0 ? 0 : (m - 1) * nr);
+  const int ldx = m == 0 ? nr : ldx1;
+  double ss = 0.0;
+  for (int q = threadIdx.x; q < cin * nr; q += blockDim.x) {
+    const int ch = q / nr, x = q % nr;
+    const double v = guess_raw_in(G, S, j, m, ch, x + 1);
+    ss += v * v;
+    X[(size_t)ch * ldx + x] = (float)v;
+  }
+  __shared__ double red[8];
+  for (int off = 16; off > 0; off >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  __shared__ float s_inv;
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    const double sc = sqrt(tot / (double)(cin * nr)) + 1e-30;
+    scale[m_fixed >= 0 ? 0 : m] = (float)sc;
+    s_inv = (float)(1.0 / sc);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < cin * nr; q += blockDim.x) X[(size_t)(q / nr) * ldx + q % nr] *= s_inv;
+  if (!T) return;
+  for (int q = threadIdx.x; q < 4 * nh * nr; q += blockDim.x) {   // training targets of slice j
+    const int ch = q / nr, x = q % nr, i = x + 1;
+    const int qq = ch / nh, h = ch % nh, p = h == 0 ? part_re(m) : part_im(m);
+    double v;
+    if (qq < 2) v = st2(G, S.b2, 3, j, p, qq, i) - st2(G, S.b2, 3, j - 1, p, qq, i);
+    else v = (st2(G, S.cu2, 3, j, p, qq - 2, i) - st2(G, S.cu2, 3, j - 1, p, qq - 2, i)) / G.dxi;
+    T[(size_t)ch * nr + x] = (float)(v * s_inv);
+  }
+}
+
+// Applies the net's outputs of every mode (blockIdx.x = m) as the guess of slice j.
+__global__ void __launch_bounds__(256) k_guess_out(GridDev G, GuessStores S, const int* __restrict__ jp,
+                                                   const float* __restrict__ Y0, const float* __restrict__ Y1, int ldy1,
+                                                   const float* __restrict__ scale, double* __restrict__ b_spe,
+                                                   double* __restrict__ cu, int apply, double weight) {
+  const int j = *jp;
+  const int m = blockIdx.x;
+  if (j < 3) return;
+  const int nr = G.nr, nh = m == 0 ? 1 : 2;
+  const float* Y = m == 0 ? Y0 : Y1 + (size_t)(m - 1) * nr;
+  const int ldy = m == 0 ? nr : ldy1;
+  const double s = (double)scale[m];
+  for (int q = threadIdx.x; q < 2 * nh * nr; q += blockDim.x) {
+    const int ch = q / nr, x = q % nr, i = x + 1;
+    if (i == 1) continue;                        // the axis node keeps the carried value
+    const int c = ch / nh, h = ch % nh, p = h == 0 ? part_re(m) : part_im(m);
+    if (apply & 1)
+      b_spe[fidx(G.ld, 3, p, c, i)] = st2(G, S.b2, 3, j - 1, p, c, i) + weight * s * (double)Y[(size_t)ch * ldy + x];
+    if (apply & 2) {     // a blend of the carried predictor and the net's dJ-perp/dxi
+      const double carried = cu[fidx(G.ld, 3, p, c, i)];
+      const double net = st2(G, S.cu2, 3, j - 1, p, c, i) + G.dxi * s * (double)Y[(size_t)(2 * nh + ch) * ldy + x];
+      cu[fidx(G.ld, 3, p, c, i)] = carried + weight * (net - carried);
+    }
+  }
+}
+
+}  // namespace qpad
+
+struct qpad_guess_state {
+  qpad_learn* net0 = nullptr;     // m = 0
+  qpad_learn* net1 = nullptr;     // m >= 1, all modes as one batch
+  LearnBufs b0, b1;
+  float* scale = nullptr;         // [M+1]
+  int apply = 3;                  // bit 0: B-perp guess, bit 1: J-perp predictor
+  double weight = 1.0;            // fraction of the net's correction that is applied
+};
+
+namespace qpad {
+
+static GuessStores guess_stores(const qpad_ctx* ctx) {
+  return GuessStores{ctx->f2[QPAD_F_B_SPE], ctx->f2[QPAD_F_CU], ctx->f2[QPAD_F_Q_SPE]};
+}
+
+void guess_free(qpad_ctx* ctx) {
+  if (!ctx->guess) return;
+  free_bufs(ctx->guess->b0);
+  free_bufs(ctx->guess->b1);
+  if (ctx->guess->scale) cudaFree(ctx->guess->scale);
+  delete ctx->guess;
+  ctx->guess = nullptr;
+}
+
+// Graph-capturable: the guess of the slice in ctx->d_j (slices 1 and 2 keep the carried one).
+int guess_enqueue(qpad_ctx* ctx) {
+  qpad_guess_state* g = ctx->guess;
+  if (!g) return 0;
+  const GridDev& G = ctx->g;
+  const int nr = G.nr, M = G.M;
+  k_guess_in<<<M + 1, 256, 0, ctx->stream>>>(G, guess_stores(ctx), ctx->d_j, 0, -1, g->b0.act, g->b1.act,
+                                             M * nr, g->scale, nullptr);
+  int n = 1;
+  n += learn_forward(g->net0, g->b0, ctx->stream, nr, nr);
+  if (M >= 1) n += learn_forward(g->net1, g->b1, ctx->stream, M * nr, nr);
+  const float* y0 = g->b0.act + (size_t)g->net0->layers * g->net0->maxc * g->b0.cap;
+  const float* y1 = M >= 1 ? g->b1.act + (size_t)g->net1->layers * g->net1->maxc * g->b1.cap : nullptr;
+  k_guess_out<<<M + 1, 256, 0, ctx->stream>>>(G, guess_stores(ctx), ctx->d_j, y0, y1, M * nr, g->scale,
+                                              ctx->f[QPAD_F_B_SPE], ctx->f[QPAD_F_CU], g->apply, g->weight);
+  return check_launch(ctx, "guess", n + 1);
+}
+
+}  // namespace qpad
+
+extern "C" int qpad_guess_attach(qpad_ctx* ctx, qpad_learn* net0, qpad_learn* net1) {
+  if (!ctx) return QPAD_E_ARG;
+  guess_free(ctx);
+  ctx->step_key.clear();                       // the step graph is rebuilt with or without the guess
+  if (ctx->step_exec) {
+    cudaGraphExecDestroy(ctx->step_exec);
+    ctx->step_exec = nullptr;
+  }
+  if (!net0) return QPAD_OK;                   // detached
+  const int M = ctx->g.M, nr = ctx->g.nr;
+  if (net0->cin != 10 || net0->cout != 4 || (M >= 1 && (!net1 || net1->cin != 20 || net1->cout != 8)))
+    return set_err(ctx, QPAD_E_ARG, "guess nets: m=0 needs 10 -> 4 channels, m>=1 needs 20 -> 8");
+  qpad_guess_state* g = new (std::nothrow) qpad_guess_state();
+  if (!g) return set_err(ctx, QPAD_E_NOMEM, "guess state");
+  ctx->guess = g;
+  g->net0 = net0;
+  g->net1 = M >= 1 ? net1 : nullptr;
+  int r = alloc_bufs(net0, g->b0, nr, false) ? set_err(ctx, QPAD_E_NOMEM, "guess buffers") : 0;
+  if (!r && M >= 1 && alloc_bufs(net1, g->b1, (int64_t)M * nr, false)) r = set_err(ctx, QPAD_E_NOMEM, "guess buffers");
+  if (!r) r = cuda_check(ctx, cudaMalloc(&g->scale, sizeof(float) * (M + 1)), "guess scale");
+  if (r) guess_free(ctx);
+  return r;
+}
+
+extern "C" int qpad_guess_sample(qpad_ctx* ctx, int j, int m, float* x, float* t, float* scale) {
+  if (!ctx || !x || !t || m < 0 || m > ctx->g.M || j < 3 || j > ctx->g.nz)
+    return ctx ? set_err(ctx, QPAD_E_ARG, "guess sample: needs 3 <= j <= nz, 0 <= m <= max_mode") : QPAD_E_ARG;
+  const int nr = ctx->g.nr, nh = m == 0 ? 1 : 2;
+  const size_t nx = (size_t)10 * nh * nr, nt = (size_t)4 * nh * nr;
+  float* d = nullptr;
+  if (int r = cuda_check(ctx, cudaMalloc(&d, sizeof(float) * (nx + nt + 1)), "guess sample buffer")) return r;
+  k_guess_in<<<1, 256, 0, ctx->stream>>>(ctx->g, guess_stores(ctx), nullptr, j, m, d, d, nr, d + nx + nt, d + nx);
+  int r = check_launch(ctx, "k_guess_in");
+  if (!r) r = cuda_check(ctx, cudaMemcpyAsync(x, d, sizeof(float) * nx, cudaMemcpyDeviceToHost, ctx->stream), "x");
+  if (!r) r = cuda_check(ctx, cudaMemcpyAsync(t, d + nx, sizeof(float) * nt, cudaMemcpyDeviceToHost, ctx->stream), "t");
+  if (!r && scale)
+    r = cuda_check(ctx, cudaMemcpyAsync(scale, d + nx + nt, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "s");
+  if (!r) r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "guess sample");
+  cudaFree(d);
+  return r;
+}
+
+extern "C" int qpad_guess_config(qpad_ctx* ctx, int apply, double weight) {
+  if (!ctx || apply < 0 || apply > 3 || !(weight >= 0.0 && weight <= 1.0))
+    return ctx ? set_err(ctx, QPAD_E_ARG, "guess config: apply in 0..3, weight in [0, 1]") : QPAD_E_ARG;
+  if (!ctx->guess) return set_err(ctx, QPAD_E_STATE, "guess config: no nets attached");
+  ctx->guess->apply = apply;
+  ctx->guess->weight = weight;
+  return QPAD_OK;
+}

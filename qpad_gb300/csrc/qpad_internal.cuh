@@ -89,6 +89,7 @@ struct qpad_ctx {
   double* raw = nullptr;                       // raw current deposits of the loop [cu 3|amu 3|acu 2] x P x ld
   unsigned int* iter_tickets = nullptr;        // convergence tickets and maxima of k_iterate
   int iter_cl = 0, iter_rows = 0;              // cluster size and rows per CTA of k_iterate
+  struct qpad_guess_state* guess = nullptr;    // learned predictor-corrector guess (learn.cu)
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
   float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
   double* scratch = nullptr;                   // per-call deposit scratch (cu, amu, acu)
@@ -201,6 +202,9 @@ int launch_iter_b(qpad_ctx* ctx);
 int launch_slice_end(qpad_ctx* ctx);
 int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn);
 int launch_finish_amj(qpad_ctx* ctx, double* cu, double* amu, double* acu);
+// learned guess of the slice's initial B-perp and J-perp predictor (learn.cu)
+int guess_enqueue(qpad_ctx* ctx);
+void guess_free(qpad_ctx* ctx);
 // one predictor-corrector iteration after the deposit, as a cluster kernel (iterate.cu)
 int iterate_setup(qpad_ctx* ctx);
 int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h);

@@ -1,0 +1,141 @@
+"""The learned guess: GPU forward/backward of the conv net against the NumPy reference, GPU
+training, the training samples against the 3D stores, and the guess in the slice loop."""
+import numpy as np
+import pytest
+
+import qpad_gb300 as Q
+from qpad_gb300 import learned as LR
+from tests import nn_ref
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+SHAPE = dict(cin=3, cout=2, width=16, layers=3, K=5)
+
+
+def _toy(seed, ns=4, nr=40):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((ns, SHAPE["cin"], nr)).astype(np.float32)
+    t = rng.standard_normal((ns, SHAPE["cout"], nr)).astype(np.float32)
+    net = LR.ConvNet(SHAPE["cin"], SHAPE["cout"], SHAPE["width"], SHAPE["layers"], SHAPE["K"], seed=seed)
+    return net, x, t
+
+
+def test_forward_matches_numpy():
+    net, x, _ = _toy(1)
+    p = net.get_params()
+    y = net.predict(x)
+    yr, _ = nn_ref.forward(p, x, **SHAPE)
+    assert rel_l2(y, yr) < 2e-3
+
+
+def test_gradient_matches_numpy():
+    net, x, t = _toy(2)
+    p = net.get_params()
+    loss, g = net.grad(x, t)
+    lr_, gr = nn_ref.loss_grad(p, x, t, **SHAPE)
+    assert abs(loss - lr_) <= 2e-3 * abs(lr_)
+    lay, _ = LR.layout(SHAPE["cin"], SHAPE["cout"], SHAPE["width"], SHAPE["layers"], SHAPE["K"])
+    for wo, sh, bo in lay:                 # every layer's weights and biases
+        n = int(np.prod(sh))
+        assert rel_l2(g[wo:wo + n], gr[wo:wo + n]) < 2e-2, (wo, sh)
+        assert rel_l2(g[bo:bo + sh[0]], gr[bo:bo + sh[0]]) < 2e-2, (bo, sh)
+
+
+def test_training_reduces_loss():
+    rng = np.random.default_rng(3)
+    ns, nr = 64, 48
+    x = rng.standard_normal((ns, SHAPE["cin"], nr)).astype(np.float32)
+    k = np.array([0.25, 0.5, 0.25])
+    t = np.stack([np.stack([np.convolve(x[s, 0] + 0.5 * x[s, 1], k, mode="same"),
+                            np.tanh(x[s, 2])]) for s in range(ns)]).astype(np.float32)
+    net = LR.ConvNet(SHAPE["cin"], SHAPE["cout"], SHAPE["width"], SHAPE["layers"], SHAPE["K"], seed=3)
+    losses = net.train(x, t, epochs=60, batch=16, lr=3e-3, seed=3)
+    assert losses[-1] < 0.1 * losses[0], losses
+
+
+def _deck(M=1, nz=24, n_b=2.0, seed=3):
+    return Q.decks.Deck("guess_test", nr=64, nz=nz, max_mode=M, dr=0.04, dxi=0.04, ppc=(2, 1), num_theta=8,
+                        uth=2e-3, seed=seed, beams=[Q.decks.BeamSpec(n_b, 0.4, 0.3, 0.5, 20000, x0=0.04)],
+                        iter_max=30, iter_reltol=1e-6)
+
+
+def test_guess_samples_match_stores():
+    deck = _deck()
+    sim = Q.build_simulation(deck)
+    sim.run_3d_step()
+    b = np.stack([sim.b_spe.store(s) for s in range(1, deck.nz + 1)])
+    cu = np.stack([sim.cu.store(s) for s in range(1, deck.nz + 1)])
+    q = np.stack([sim.q_spe.store(s) for s in range(1, deck.nz + 1)])
+    for m in (0, 1):
+        parts = [0] if m == 0 else [1, 2]
+        x, t, sc = LR.samples(sim, m, [5, 11])
+        for k, j in enumerate([5, 11]):
+            rows = []
+            for d in (1, 2):
+                s = j - d - 1
+                for qq in range(5):
+                    for p in parts:
+                        if qq < 2:
+                            rows.append(b[s, p, qq, 1:-1])
+                        elif qq < 4:
+                            rows.append(cu[s, p, qq - 2, 1:-1])
+                        else:
+                            rows.append(q[s, p, 0, 1:-1] - cu[s, p, 2, 1:-1])
+            raw = np.array(rows)
+            scale = np.sqrt(np.mean(raw ** 2))
+            assert abs(sc[k] - scale) <= 1e-5 * scale
+            assert rel_l2(x[k], raw / scale) < 1e-6
+            tr = []
+            for qq in range(4):
+                for p in parts:
+                    if qq < 2:
+                        tr.append(b[j - 1, p, qq, 1:-1] - b[j - 2, p, qq, 1:-1])
+                    else:
+                        tr.append((cu[j - 1, p, qq - 2, 1:-1] - cu[j - 2, p, qq - 2, 1:-1]) / deck.dxi)
+            assert rel_l2(t[k], np.array(tr) / scale) < 1e-5
+    sim.close()
+
+
+def test_guess_hook_with_zero_net_keeps_the_answer():
+    deck = _deck()
+    a = Q.build_simulation(deck)
+    ia, _ = a.run_3d_step()
+    b = Q.build_simulation(deck)
+    n0, n1 = LR.ConvNet(*LR.CHANNELS[0]), LR.ConvNet(*LR.CHANNELS[1])
+    n0.set_params(np.zeros(n0.nparam, np.float32))
+    n1.set_params(np.zeros(n1.nparam, np.float32))
+    LR.attach(b, n0, n1)
+    ib, _ = b.run_3d_step()
+    # the iteration still runs to iter_reltol from the different guess
+    for s in range(1, deck.nz + 1, 5):
+        assert rel_l2(b.e.store(s), a.e.store(s)) < 1e-4
+        assert rel_l2(b.b.store(s), a.b.store(s)) < 1e-4
+    assert abs(ib.mean() - ia.mean()) < 3.0
+    LR.attach(b, None, None)
+    a.close()
+    b.close()
+
+
+def test_trained_guess_effect_on_iterations(record_property):
+    """What the committed c2 guess nets change on a held-out c2-shaped driver (first 192
+    slices): iterations per slice with and without them, and the fields still agree."""
+    import os
+    from qpad_gb300.train_guess import DEFAULT_OUT, c2_variant
+    if not os.path.exists(DEFAULT_OUT):
+        pytest.skip("no trained weights")
+    net0, net1 = LR.load(DEFAULT_OUT, 2)
+    d = c2_variant(3.0, 999, nz=192)
+    a = Q.build_simulation(d, precision=Q._capi.PREC_MIXED)
+    ia, _ = a.run_3d_step()
+    b = Q.build_simulation(d, precision=Q._capi.PREC_MIXED)
+    LR.attach(b, net0, net1)
+    ib, _ = b.run_3d_step()
+    record_property("iters_per_slice_plain", float(ia.mean()))
+    record_property("iters_per_slice_guess", float(ib.mean()))
+    print(f"iterations per slice: plain {ia.mean():.3f}, with the learned guess {ib.mean():.3f}")
+    for s in range(8, d.nz + 1, 23):
+        assert rel_l2(b.e.store(s), a.e.store(s)) < 2e-2
+    assert ib.max() <= d.iter_max
+    a.close()
+    b.close()
