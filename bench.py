@@ -242,6 +242,69 @@ def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
     return out
 
 
+def run_batch(args):
+    """c3: 64 independent simulations of uneven size advanced together, one graph launch of
+    all their slice loops per 3D step, launch shapes picked by the autotuner; beside it the
+    same simulations stepped one after another."""
+    import numpy as np
+
+    import qpad_gb300 as Q
+    from qpad_gb300 import _capi as K
+    prec = K.PREC_FP64 if args.precision == "fp64" else K.PREC_MIXED
+    decks = Q.decks.c3()
+    if args.slices:
+        for d in decks:
+            d.nz = args.slices
+    sims = [Q.build_simulation(d, precision=prec) for d in decks]
+    tune = [s.autotune(reps=10) for s in sims]
+    pushes = sum(s.species[0].count() * d.nz for s, d in zip(sims, decks))
+    batch = Q.Batch(sims)
+    for _ in range(args.warmup):
+        for s in sims:
+            s.species[0].reset()
+        batch.step()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        iters = []
+        for _ in range(args.steps):
+            for s in sims:
+                s.species[0].reset()
+            its = batch.step()
+            iters.append(float(np.mean(np.concatenate(its))))
+        wall = time.perf_counter() - t0
+    value = pushes * args.steps / wall
+    seq = None
+    if not args.no_compare:                     # the same simulations one after another
+        for s in sims:
+            s.species[0].reset()
+        t1 = time.perf_counter()
+        for s in sims:
+            s.run_3d_step()
+        seq = pushes / (time.perf_counter() - t1)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == K.PREC_FP64 else "f32 particles / f64 solves",
+        "data": "synthetic (seeded decks, no dataset)",
+        "config": {"workload": f"c3_batch{len(decks)}_nz{decks[0].nz}", "simulations": len(decks),
+                   "nr": sorted({d.nr for d in decks}), "max_mode": sorted({d.max_mode for d in decks}),
+                   "plasma_pushes_per_step": pushes, "path": args.precision,
+                   "l2": "step working set above L2 (64 simulations' stores and beams)"},
+        "iters_per_slice": float(np.mean(iters)),
+        "timing": "host wall clock around qpad_batch_step, which synchronises every simulation",
+        "autotune": {"iter_cluster": sorted({t["iter_cluster"] for t in tune}),
+                     "item_ppl": sorted({t["item_ppl"] for t in tune})},
+        "clocks": clk.summary(),
+    }
+    if seq is not None:
+        line["sequential"] = {"value": seq, "speedup_of_batch": value / seq}
+    print(json.dumps(line), flush=True)
+    batch.close()
+    for s in sims:
+        s.close()
+    return 0
+
+
 def run_ours(args):
     import qpad_gb300 as Q
     from qpad_gb300 import _capi as K
@@ -353,6 +416,8 @@ def main():
     ap.add_argument("--graph", default="on", choices=["on", "off"],
                     help="off: host-driven slice loop (one launch per kernel, visible to per-kernel profilers)")
     args = ap.parse_args()
+    if args.impl == "ours" and args.deck == "c3":
+        return run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

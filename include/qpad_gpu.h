@@ -207,6 +207,32 @@ int qpad_slice_step(qpad_ctx* ctx, int j, qpad_slice_stats* stats);
  * slices 1..nz, beam push; per-slice stats into stats[nz] (may be NULL). */
 int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* stats);
 
+/* ---- batches of independent simulations (no counterpart in the reference) -----------
+ * A scan over drivers runs as many contexts on one GPU.  qpad_batch_step advances every
+ * context of the batch by one 3D step (qpad_3d_step semantics for each); the slice loops
+ * of all of them, every slice and predictor-corrector iteration, run as ONE CUDA graph
+ * launch, each simulation an independent branch with its own device-side loop conditions.
+ * The contexts must share a device and must not sort every few slices (sort_freq = 0). */
+typedef struct qpad_batch qpad_batch;
+int qpad_batch_create(qpad_ctx* const* ctxs, int n, qpad_batch** out);
+int qpad_batch_destroy(qpad_batch* batch);
+const char* qpad_batch_last_error(const qpad_batch* batch);
+/* stats[i] receives context i's nz per-slice statistics (stats or stats[i] may be null) */
+int qpad_batch_step(qpad_batch* batch, int push_beams, qpad_slice_stats* const* stats);
+
+/* ---- autotuner (no counterpart in the reference) ---------------------------------------
+ * Times the launch shapes this context can use on this GPU and keeps the fastest: the
+ * cluster size of the fused predictor-corrector kernel (16, 8, 4, 2, 1 CTAs per mode) and,
+ * on the mixed path, the particles per lane of the deposit work items (2 or 4).  Runs
+ * `reps` timed launches of each; overwrites the slice fields (call it before a 3D step). */
+typedef struct qpad_tune_result {
+  int32_t iter_cluster;       /* CTAs per mode of the iteration kernel */
+  double iter_us;             /* its time per launch */
+  int32_t item_ppl;           /* particles per lane of a mixed deposit work item */
+  double deposit_us;          /* the mixed deposit's time per launch (0 on the FP64 path) */
+} qpad_tune_result;
+int qpad_autotune(qpad_ctx* ctx, int reps, qpad_tune_result* out);
+
 /* ---- loaders (host; project RNG substituting gfortran random_number) ------------- */
 typedef struct qpad_rng { uint64_t s; int32_t have; double next; } qpad_rng;
 void qpad_rng_seed(qpad_rng* r, uint64_t seed);

@@ -37,6 +37,11 @@ class SliceStats(C.Structure):
     _fields_ = [("iters", C.c_int32), ("rel_res", C.c_double), ("abs_res", C.c_double)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("iter_cluster", C.c_int32), ("iter_us", C.c_double), ("item_ppl", C.c_int32),
+                ("deposit_us", C.c_double)]
+
+
 class Rng(C.Structure):
     _fields_ = [("s", C.c_uint64), ("have", C.c_int32), ("next", C.c_double)]
 
@@ -128,6 +133,11 @@ _SIGS = {
     "qpad_guess_attach": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "qpad_guess_sample": (C.c_int, [C.c_void_p, C.c_int, C.c_int, F, F, F]),
     "qpad_guess_config": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "qpad_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
+    "qpad_batch_destroy": (C.c_int, [C.c_void_p]),
+    "qpad_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "qpad_batch_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.POINTER(SliceStats))]),
+    "qpad_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(TuneResult)]),
     "qpad_rng_seed": (None, [C.POINTER(Rng), C.c_uint64]),
     "qpad_load_plasma": (C.c_int64, [C.c_int, C.c_double, C.POINTER(Rng), C.c_int, C.c_int, C.c_int, C.c_double,
                                      C.c_double, D, D, D, D, D, D, C.c_int64]),

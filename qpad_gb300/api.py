@@ -229,6 +229,42 @@ class Simulation:
         self._check(self.lib.qpad_3d_step(self.h, int(push_beams), st))
         return (np.array([s.iters for s in st], np.int32), np.array([s.rel_res for s in st]))
 
+    def autotune(self, reps=20) -> dict:
+        """Picks the fastest launch shapes of this simulation's kernels on this GPU."""
+        r = K.TuneResult()
+        self._check(self.lib.qpad_autotune(self.h, reps, C.byref(r)))
+        return {"iter_cluster": r.iter_cluster, "iter_us": r.iter_us, "item_ppl": r.item_ppl,
+                "deposit_us": r.deposit_us}
+
+
+class Batch:
+    """Independent simulations on one GPU advanced together: one 3D step of all of them is
+    one CUDA graph launch of their slice loops (qpad_batch_step)."""
+
+    def __init__(self, sims):
+        self.sims = list(sims)
+        self.lib = K.load()
+        arr = (C.c_void_p * len(self.sims))(*[s.h.value for s in self.sims])
+        h = C.c_void_p()
+        r = self.lib.qpad_batch_create(arr, len(self.sims), C.byref(h))
+        if r != 0:
+            raise QpadError(f"qpad_batch_create failed ({r})")
+        self.h = h
+
+    def step(self, push_beams=True):
+        """One 3D step of every simulation; returns the iterations per slice of each."""
+        bufs = [(K.SliceStats * s.nz)() for s in self.sims]
+        ptrs = (C.POINTER(K.SliceStats) * len(bufs))(*[C.cast(b, C.POINTER(K.SliceStats)) for b in bufs])
+        r = self.lib.qpad_batch_step(self.h, int(push_beams), ptrs)
+        if r != 0:
+            raise QpadError(f"qpad_batch_step failed ({r}): {self.lib.qpad_batch_last_error(self.h).decode()}")
+        return [np.array([s.iters for s in b], np.int32) for b in bufs]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qpad_batch_destroy(self.h)
+            self.h = None
+
 
 class Species2D:
     def __init__(self, sim: Simulation, x, p, gamma, psi, q, *, qbm, push_type, neutralized, npmax, sort_freq):

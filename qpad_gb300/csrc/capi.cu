@@ -1017,29 +1017,49 @@ int enqueue_slice_epilogue(qpad_ctx* ctx, int sort_now) {
 
 // Graph of the whole slice loop: WHILE(j <= nz) { prologue; WHILE(not converged) { iteration }; epilogue; ++j }.
 // The iteration condition is set by the convergence kernel, the slice condition by k_advance.
-int build_step_graph(qpad_ctx* ctx) {
-  cudaGraph_t top = nullptr;
+// Adds to `top` one simulation's slice loop: a kernel that sets its slice index to 1, then
+// WHILE(j <= nz) { prologue; WHILE(not converged) { iteration }; epilogue; ++j }.  The
+// iteration condition is set by the convergence test, the slice condition by k_advance.
+// Branches added for different contexts are independent and run concurrently.
+int add_slice_loop(qpad_ctx* ctx, cudaGraph_t top) {
   cudaGraphConditionalHandle hs = 0, hi = 0;
   cudaGraphNode_t nslice = nullptr, niter = nullptr;
   cudaGraph_t sbody = nullptr, ibody = nullptr;
   const bool prof = ctx->prof_on;
   ctx->prof_on = false;                          // event nodes are not allowed in conditional bodies
-  int r = cuda_check(ctx, cudaGraphCreate(&top, 0), "graph create");
-  if (!r) r = cuda_check(ctx, cudaGraphConditionalHandleCreate(&hs, top, 1, cudaGraphCondAssignDefault), "slice handle");
+  const int64_t l0 = ctx->launches;
+  int64_t l1 = l0, l2 = l0, l3 = l0;
+  int r = cuda_check(ctx, cudaGraphConditionalHandleCreate(&hs, top, 1, cudaGraphCondAssignDefault), "slice handle");
+  if (!r) r = cuda_check(ctx, cudaStreamBeginCaptureToGraph(ctx->stream, top, nullptr, nullptr, 0,
+                                                            cudaStreamCaptureModeThreadLocal), "capture step");
   if (!r) {
-    cudaGraphNodeParams p = {};
-    p.type = cudaGraphNodeTypeConditional;
-    p.conditional.handle = hs;
-    p.conditional.type = cudaGraphCondTypeWhile;
-    p.conditional.size = 1;
-    r = cuda_check(ctx, cudaGraphAddNode(&nslice, top, nullptr, nullptr, 0, &p), "slice while node");
-    if (!r) sbody = p.conditional.phGraph_out[0];
+    r = launch_set_slice(ctx, 1);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (!r) r = cuda_check(ctx, cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &cg, &deps, nullptr, &nd), "capture info");
+    if (!r) {
+      cudaGraphNodeParams p = {};
+      p.type = cudaGraphNodeTypeConditional;
+      p.conditional.handle = hs;
+      p.conditional.type = cudaGraphCondTypeWhile;
+      p.conditional.size = 1;
+      r = cuda_check(ctx, cudaGraphAddNode(&nslice, cg, deps, nullptr, nd, &p), "slice while node");
+      if (!r) sbody = p.conditional.phGraph_out[0];
+      if (!r)
+        r = cuda_check(ctx, cudaStreamUpdateCaptureDependencies(ctx->stream, &nslice, nullptr, 1,
+                                                                cudaStreamSetCaptureDependencies), "capture deps");
+    }
+    cudaGraph_t out = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &out);
+    if (!r) r = cuda_check(ctx, e, "end capture step");
   }
+  const int64_t lset = ctx->launches;
   if (!r) r = cuda_check(ctx, cudaGraphConditionalHandleCreate(&hi, sbody, 1, cudaGraphCondAssignDefault), "iter handle");
   if (!r) r = cuda_check(ctx, cudaStreamBeginCaptureToGraph(ctx->stream, sbody, nullptr, nullptr, 0,
                                                             cudaStreamCaptureModeThreadLocal), "capture slice");
-  const int64_t l0 = ctx->launches;
-  int64_t l1 = l0, l2 = l0, l3 = l0;
+  l1 = l2 = l3 = lset;
   if (!r) {
     r = enqueue_slice_prologue(ctx, hi, 1);
     l1 = ctx->launches;
@@ -1080,14 +1100,25 @@ int build_step_graph(qpad_ctx* ctx) {
     if (!r) r = cuda_check(ctx, e, "end capture iteration");
   }
   // captured launches are not executions: keep the per-phase counts, undo the increments
-  ctx->g_pro = l1 - l0;
+  ctx->g_once = lset - l0;                        // the slice-index kernel, once per step
+  ctx->g_pro = l1 - lset;
   ctx->g_epi = l2 - l1;
   ctx->g_it = l3 - l2;
   ctx->launches = l0;
+  ctx->prof_on = prof;
+  cudaGetLastError();
+  return r;
+}
+
+int build_step_graph(qpad_ctx* ctx) {
+  cudaGraph_t top = nullptr;
+  int r = cuda_check(ctx, cudaGraphCreate(&top, 0), "graph create");
+  if (!r) r = add_slice_loop(ctx, top);
   cudaGraphExec_t exec = nullptr;
   if (!r) r = cuda_check(ctx, cudaGraphInstantiate(&exec, top, 0), "graph instantiate");
-  if (top) cudaGraphDestroy(top);
-  ctx->prof_on = prof;
+  // a graph whose conditional body saw an invalidated capture is left alone (its
+  // destruction is not safe); only the error path leaks it
+  if (top && !r) cudaGraphDestroy(top);
   cudaGetLastError();
   if (r) return r;
   if (ctx->step_exec) cudaGraphExecDestroy(ctx->step_exec);
@@ -1096,7 +1127,8 @@ int build_step_graph(qpad_ctx* ctx) {
 }
 
 std::string step_key(const qpad_ctx* ctx) {
-  std::string k = std::to_string(ctx->precision);
+  std::string k = std::to_string(ctx->precision) + "/" + std::to_string(ctx->iter_cl) + "/" +
+                  std::to_string(ctx->item_ppl) + "/" + std::to_string(ctx->guess != nullptr);
   for (auto* s : ctx->species)
     k += "|" + std::to_string((long long)s->np) + ":" + std::to_string(s->push_type) + ":" +
          std::to_string(s->neutralized) + ":" + std::to_string(s->sort_freq);
@@ -1138,10 +1170,10 @@ extern "C" int qpad_slice_step(qpad_ctx* ctx, int j, qpad_slice_stats* stats) {
   return slice_step(ctx, j, stats);
 }
 
-extern "C" int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* stats) {
-  if (!ctx) return QPAD_E_ARG;
-  prof_begin(ctx, "step");
-  // simulation_class.f03:309-341
+namespace {
+// 3D-step work before the slice loop (simulation_class.f03:309-341): beam charge deposit
+// into the store, zeroed slice fields.
+int step_begin(qpad_ctx* ctx) {
   if (int r = qpad_store_fill(ctx, QPAD_F_Q_BEAM, 0.0)) return r;
   if (int r = qpad_store_fill(ctx, QPAD_F_Q_SPE, 0.0)) return r;
   for (auto* b : ctx->beams)
@@ -1153,10 +1185,49 @@ extern "C" int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* sta
   for (int f : zero_fields)
     if (cudaMemsetAsync(ctx->f[f], 0, f1_elems(ctx, f) * sizeof(double), ctx->stream) != cudaSuccess)
       return check_launch(ctx, "zero fields");
+  return 0;
+}
+
+bool graph_ok(const qpad_ctx* ctx) {
+  bool ok = ctx->use_graph;
+  for (auto* s : ctx->species) ok &= (s->sort_freq == 0);
+  return ok;
+}
+
+// After a graph-run slice loop has been enqueued: its statistics, counted launches.
+int step_graph_stats(qpad_ctx* ctx, qpad_slice_stats* stats) {
+  ctx->h_stats.resize(ctx->g.nz);
+  if (int r = cuda_check(ctx, cudaMemcpyAsync(ctx->h_stats.data(), ctx->d_stats, sizeof(qpad_slice_stats) * ctx->g.nz,
+                                              cudaMemcpyDeviceToHost, ctx->stream), "stats"))
+    return r;
+  if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "graph step")) return r;
+  // kernels the graph ran: per slice the prologue and epilogue, per iteration the body
+  int64_t iters = 0;
+  for (const auto& s : ctx->h_stats) iters += s.iters;
+  ctx->launches += ctx->g_once + (int64_t)ctx->g.nz * (ctx->g_pro + ctx->g_epi) + iters * ctx->g_it;
+  if (stats) std::copy(ctx->h_stats.begin(), ctx->h_stats.end(), stats);
+  return 0;
+}
+
+// 3D-step work after the slice loop (simulation_class.f03:487-492): beam push, counts.
+int step_end(qpad_ctx* ctx, int push_beams) {
+  if (push_beams)
+    for (auto* b : ctx->beams)
+      if (int r = beam_push(b, ctx->f2[QPAD_F_E], ctx->f2[QPAD_F_B])) return r;
+  prof_end(ctx, "step");
+  for (auto* s : ctx->species)
+    if (int r = species_sync_count(s)) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "3d step");
+}
+}  // namespace
+
+extern "C" int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* stats) {
+  if (!ctx) return QPAD_E_ARG;
+  prof_begin(ctx, "step");
+  if (int r = step_begin(ctx)) return r;
   // the slice loop runs as one CUDA graph when the configuration allows it (sorting every
   // few slices is host-driven); otherwise the host drives it slice by slice
-  bool use_graph = ctx->use_graph;
-  for (auto* s : ctx->species) use_graph &= (s->sort_freq == 0);
+  bool use_graph = graph_ok(ctx);
   if (use_graph) {
     const std::string key = step_key(ctx);
     if (!ctx->step_exec || ctx->step_key != key) {
@@ -1171,30 +1242,206 @@ extern "C" int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* sta
     }
   }
   if (use_graph) {
-    *ctx->h_j = 1;
-    if (cudaMemcpyAsync(ctx->d_j, ctx->h_j, sizeof(int), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
-      return check_launch(ctx, "slice index", 0);
     if (int r = cuda_check(ctx, cudaGraphLaunch(ctx->step_exec, ctx->stream), "graph launch")) return r;
-    ctx->h_stats.resize(ctx->g.nz);
-    if (int r = cuda_check(ctx, cudaMemcpyAsync(ctx->h_stats.data(), ctx->d_stats,
-                                                sizeof(qpad_slice_stats) * ctx->g.nz, cudaMemcpyDeviceToHost,
-                                                ctx->stream), "stats"))
-      return r;
-    if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "graph step")) return r;
-    // kernels the graph ran: per slice the prologue and epilogue, per iteration the body
-    int64_t iters = 0;
-    for (const auto& s : ctx->h_stats) iters += s.iters;
-    ctx->launches += (int64_t)ctx->g.nz * (ctx->g_pro + ctx->g_epi) + iters * ctx->g_it;
-    if (stats) std::copy(ctx->h_stats.begin(), ctx->h_stats.end(), stats);
+    if (int r = step_graph_stats(ctx, stats)) return r;
   } else {
     for (int j = 1; j <= ctx->g.nz; ++j)
       if (int r = slice_step(ctx, j, stats ? stats + (j - 1) : nullptr)) return r;
   }
-  if (push_beams)
-    for (auto* b : ctx->beams)
-      if (int r = beam_push(b, ctx->f2[QPAD_F_E], ctx->f2[QPAD_F_B])) return r;
-  prof_end(ctx, "step");
-  for (auto* s : ctx->species)
-    if (int r = species_sync_count(s)) return r;
-  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "3d step");
+  return step_end(ctx, push_beams);
+}
+
+// =====================================================================================
+// batches of independent simulations
+// =====================================================================================
+struct qpad_batch {
+  std::vector<qpad_ctx*> ctxs;
+  std::vector<std::string> keys;
+  std::vector<cudaEvent_t> ev;      // per simulation: its pre-loop work is done
+  cudaEvent_t done = nullptr;       // the batch graph is done
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::string err;
+};
+
+extern "C" int qpad_batch_create(qpad_ctx* const* ctxs, int n, qpad_batch** out) {
+  if (!ctxs || n < 1 || !out) return QPAD_E_ARG;
+  *out = nullptr;
+  for (int i = 0; i < n; ++i)
+    if (!ctxs[i] || ctxs[i]->device != ctxs[0]->device) return QPAD_E_ARG;
+  qpad_batch* b = new (std::nothrow) qpad_batch();
+  if (!b) return QPAD_E_NOMEM;
+  b->ctxs.assign(ctxs, ctxs + n);
+  b->keys.resize(n);
+  b->ev.resize(n, nullptr);
+  cudaError_t e = cudaSetDevice(ctxs[0]->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&b->ev[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    qpad_batch_destroy(b);
+    return QPAD_E_CUDA;
+  }
+  *out = b;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_batch_destroy(qpad_batch* b) {
+  if (!b) return QPAD_OK;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (cudaEvent_t e : b->ev)
+    if (e) cudaEventDestroy(e);
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return QPAD_OK;
+}
+
+extern "C" const char* qpad_batch_last_error(const qpad_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+// One 3D step of every simulation of the batch; their slice loops (every slice, every
+// predictor-corrector iteration of all of them) run as one CUDA graph launch, the
+// simulations in independent branches.  stats[i] (nz entries) may be null.
+extern "C" int qpad_batch_step(qpad_batch* b, int push_beams, qpad_slice_stats* const* stats) {
+  if (!b) return QPAD_E_ARG;
+  const int n = (int)b->ctxs.size();
+  for (int i = 0; i < n; ++i)
+    if (!graph_ok(b->ctxs[i])) {
+      b->err = "simulation " + std::to_string(i) + " cannot run as a graph (sorting every few slices or graph off)";
+      return QPAD_E_STATE;
+    }
+  bool rebuild = !b->exec;
+  for (int i = 0; i < n; ++i) rebuild |= (b->keys[i] != step_key(b->ctxs[i]));
+  if (rebuild) {
+    if (b->exec) {
+      cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+    }
+    cudaGraph_t top = nullptr;
+    int r = cudaGraphCreate(&top, 0) == cudaSuccess ? 0 : QPAD_E_CUDA;
+    for (int i = 0; i < n && !r; ++i) {
+      r = add_slice_loop(b->ctxs[i], top);
+      if (r) b->err = "simulation " + std::to_string(i) + ": " + b->ctxs[i]->err;
+    }
+    if (!r && cudaGraphInstantiate(&b->exec, top, 0) != cudaSuccess) {
+      b->err = "batch graph instantiate failed";
+      r = QPAD_E_CUDA;
+    }
+    if (top && !r) cudaGraphDestroy(top);        // left alone after a failed capture, as above
+    cudaGetLastError();
+    if (r) return r;
+    for (int i = 0; i < n; ++i) b->keys[i] = step_key(b->ctxs[i]);
+  }
+  for (int i = 0; i < n; ++i) {
+    qpad_ctx* c = b->ctxs[i];
+    prof_begin(c, "step");
+    if (int r = step_begin(c)) {
+      b->err = "simulation " + std::to_string(i) + ": " + c->err;
+      return r;
+    }
+    if (cudaEventRecord(b->ev[i], c->stream) != cudaSuccess || cudaStreamWaitEvent(b->stream, b->ev[i], 0) != cudaSuccess)
+      return QPAD_E_CUDA;
+  }
+  if (cudaGraphLaunch(b->exec, b->stream) != cudaSuccess || cudaEventRecord(b->done, b->stream) != cudaSuccess) {
+    b->err = "batch graph launch failed";
+    return QPAD_E_CUDA;
+  }
+  for (int i = 0; i < n; ++i) {
+    qpad_ctx* c = b->ctxs[i];
+    if (cudaStreamWaitEvent(c->stream, b->done, 0) != cudaSuccess) return QPAD_E_CUDA;
+    int r = step_graph_stats(c, stats ? stats[i] : nullptr);
+    if (!r) r = step_end(c, push_beams);
+    if (r) {
+      b->err = "simulation " + std::to_string(i) + ": " + c->err;
+      return r;
+    }
+  }
+  return QPAD_OK;
+}
+
+// =====================================================================================
+// autotuner
+// =====================================================================================
+extern "C" int qpad_autotune(qpad_ctx* ctx, int reps, qpad_tune_result* out) {
+  if (!ctx || reps < 1) return QPAD_E_ARG;
+  // the slice fields are scratch for the timing runs (a 3D step zeroes them anyway)
+  const int zero_fields[] = {QPAD_F_B, QPAD_F_E, QPAD_F_B_SPE, QPAD_F_E_SPE, QPAD_F_PSI, QPAD_F_CU,
+                             QPAD_F_ACU, QPAD_F_AMU, QPAD_F_DCU, QPAD_F_B_BEAM};
+  for (int f : zero_fields)
+    if (cudaMemsetAsync(ctx->f[f], 0, f1_elems(ctx, f) * sizeof(double), ctx->stream) != cudaSuccess)
+      return check_launch(ctx, "autotune zero", 0);
+  if (ctx->gtab && cudaMemsetAsync(ctx->gtab, 0, (size_t)ctx->g.ld * ctx->g.P * 6 * sizeof(float), ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "autotune zero", 0);
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return QPAD_E_CUDA;
+  auto timed = [&](auto&& body, double* us) -> int {
+    for (int w = 0; w < 3; ++w)
+      if (int r = body()) return r;
+    cudaEventRecord(e0, ctx->stream);
+    for (int k = 0; k < reps; ++k)
+      if (int r = body()) return r;
+    cudaEventRecord(e1, ctx->stream);
+    if (int r = cuda_check(ctx, cudaEventSynchronize(e1), "autotune sync")) return r;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    *us = 1e3 * ms / reps;
+    return 0;
+  };
+  qpad_tune_result res{};
+  int r = 0;
+  // cluster size of the iteration kernel
+  const int64_t l0 = ctx->launches;
+  double best = 1e30;
+  int best_cl = ctx->iter_cl;
+  for (int cl = 16; cl >= 1 && !r; cl /= 2) {
+    if (iterate_try_cluster(ctx, cl)) continue;
+    double us = 0.0;
+    r = timed([&]() { return launch_iterate(ctx, 0, 0, 0); }, &us);
+    if (!r && us < best) {
+      best = us;
+      best_cl = cl;
+    }
+  }
+  if (!r) r = iterate_try_cluster(ctx, best_cl);
+  res.iter_cluster = best_cl;
+  res.iter_us = best;
+  // work-item size of the mixed deposit
+  res.item_ppl = ctx->item_ppl;
+  res.deposit_us = 0.0;
+  bool mixed = ctx->precision == QPAD_PREC_MIXED && !ctx->species.empty();
+  if (!r && mixed) {
+    const size_t P1 = (size_t)ctx->g.P * ctx->g.ld;
+    double bestd = 1e30;
+    int best_ppl = ctx->item_ppl;
+    for (int ppl : {2, 4}) {
+      ctx->item_ppl = ppl;
+      for (auto* s : ctx->species)
+        if (!r) r = mixed_index(s);
+      double us = 0.0;
+      if (!r)
+        r = timed([&]() {
+          for (auto* s : ctx->species)
+            if (int q = mixed_amjdp_raw(s, ctx->gtab, ctx->raw, ctx->raw + 3 * P1, ctx->raw + 6 * P1, ctx->g.dxi))
+              return q;
+          return 0;
+        }, &us);
+      if (!r && us < bestd) {
+        bestd = us;
+        best_ppl = ppl;
+      }
+    }
+    ctx->item_ppl = best_ppl;
+    for (auto* s : ctx->species)
+      if (!r) r = mixed_index(s);
+    res.item_ppl = best_ppl;
+    res.deposit_us = bestd;
+  }
+  if (!r && cudaMemsetAsync(ctx->raw, 0, 8 * (size_t)ctx->g.P * ctx->g.ld * sizeof(double), ctx->stream) != cudaSuccess)
+    r = check_launch(ctx, "autotune raw", 0);
+  if (!r) r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "autotune");
+  ctx->launches = l0;                            // tuning launches are not part of the simulation
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (out) *out = res;
+  return r;
 }

@@ -13,6 +13,9 @@
 // the same kernel with the radial lines held in shared memory.
 #include <cmath>
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "stencils.cuh"
@@ -766,15 +769,28 @@ __global__ void k_advance(int* __restrict__ jp, int nz, cudaGraphConditionalHand
 // ------------------------------------------------------------------------------------
 static size_t field_smem(const qpad_ctx* ctx) { return (size_t)4 * (ctx->g.nr + 2) * sizeof(double); }
 
+// The dynamic shared-memory limit is an attribute of the kernel (per device), shared by
+// every context in the process: it is only ever raised, so that a context with a shorter
+// radial line never lowers the limit another context's launches rely on.
+int raise_dyn_smem(qpad_ctx* ctx, const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> cur;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& have = cur[{func, ctx->device}];
+  if (bytes <= have) return 0;
+  cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cudaFuncSetAttribute(smem)");
+  have = bytes;
+  return 0;
+}
+
 static int ensure_smem_attr(qpad_ctx* ctx) {
   if (ctx->field_attr_done) return 0;
   const size_t need = field_smem(ctx);
   const void* ks[] = {(const void*)k_field_op, (const void*)k_slice_begin, (const void*)k_iter_e,
                       (const void*)k_iter_b, (const void*)k_slice_end};
-  for (const void* k : ks) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-    if (e != cudaSuccess) return cuda_check(ctx, e, "cudaFuncSetAttribute(smem)");
-  }
+  for (const void* k : ks)
+    if (int r = raise_dyn_smem(ctx, k, need)) return r;
   ctx->field_attr_done = true;
   return 0;
 }
@@ -800,6 +816,13 @@ int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op, int loop_state
   k_conv<<<1, 1024, 0, ctx->stream>>>(ctx->g, b, comp, op, ctx->conv, ctx->reltol, ctx->abstol, L);
   prof_end(ctx, "conv");
   return check_launch(ctx, "k_conv");
+}
+
+__global__ void k_set_slice(int* __restrict__ jp, int j) { *jp = j; }
+
+int launch_set_slice(qpad_ctx* ctx, int j) {
+  k_set_slice<<<1, 1, 0, ctx->stream>>>(ctx->d_j, j);
+  return check_launch(ctx, "k_set_slice");
 }
 
 int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle h) {

@@ -554,6 +554,37 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
 // ------------------------------------------------------------------------------------
 static int cluster_for(int nr) { return std::max(1, std::min(16, nr / 32)); }
 
+// Uses cluster size cl for k_iterate if the kernel can launch with it; nonzero otherwise.
+int iterate_try_cluster(qpad_ctx* ctx, int cl) {
+  if (cl < 1 || cl > 16 || cl > ctx->g.nr) return QPAD_E_ARG;
+  cudaError_t e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cluster attribute");
+  const int R = (ctx->g.nr + cl - 1) / cl;
+  const size_t smem = iterate_smem_doubles(R, ctx->g.ld) * sizeof(double);
+  if (smem > 200 * 1024) return QPAD_E_CAPACITY;
+  if (int r = raise_dyn_smem(ctx, (const void*)k_iterate, smem)) return r;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cl * (ctx->g.M + 1));
+  cfg.blockDim = dim3(kIterThreads);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cl;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int ncl = 0;
+  e = cudaOccupancyMaxActiveClusters(&ncl, k_iterate, &cfg);
+  if (e != cudaSuccess || ncl < 1) {
+    cudaGetLastError();
+    return QPAD_E_CAPACITY;
+  }
+  ctx->iter_cl = cl;
+  ctx->iter_rows = R;
+  return 0;
+}
+
 int iterate_setup(qpad_ctx* ctx) {
   if (ctx->iter_cl > 0) return 0;
   cudaError_t e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -561,10 +592,7 @@ int iterate_setup(qpad_ctx* ctx) {
   for (int cl = cluster_for(ctx->g.nr); cl >= 1; cl /= 2) {
     const int R = (ctx->g.nr + cl - 1) / cl;
     const size_t smem = iterate_smem_doubles(R, ctx->g.ld) * sizeof(double);
-    if (smem > 48 * 1024) {
-      e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return cuda_check(ctx, e, "iterate smem");
-    }
+    if (int r = raise_dyn_smem(ctx, (const void*)k_iterate, smem)) return r;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cl * (ctx->g.M + 1));
     cfg.blockDim = dim3(kIterThreads);

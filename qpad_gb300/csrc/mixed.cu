@@ -25,8 +25,9 @@
 namespace qpad {
 
 static constexpr int kMixThreads = 256;
-static constexpr int kItem = 128;                         // particles per deposit work item (one warp)
-static constexpr int kPPL = kItem / 32;                   // particles per lane in a work item
+// A deposit work item is one warp's worth of particles of one cell: 32 * PPL of them,
+// PPL = ctx->item_ppl in {2, 4} (chosen by qpad_autotune, 4 by default).
+static constexpr int kMinItem = 64;                       // smallest work item (sizes the item list)
 static constexpr int kItemThreads = 128;                  // four work items per CTA
 #define FULL 0xffffffffu
 
@@ -128,6 +129,7 @@ __device__ __forceinline__ void butterfly32(float (&a)[32], int lane) {
 // ------------------------------------------------------------------------------------
 // charge deposit (rho - Jz), one warp per work item (kItem particles of one cell)
 // ------------------------------------------------------------------------------------
+template <int kPPL>
 __global__ void __launch_bounds__(kItemThreads) k_mqdeposit(GridDev G, const int4* __restrict__ items,
                                                             const int* __restrict__ n_items, MArr A,
                                                             double* __restrict__ qraw) {
@@ -272,6 +274,7 @@ __device__ __forceinline__ void mpredict(const GridDev& G, int push_type, float 
 // [node 0/1][Re/Im][cu 0..2, acu 3..4, amu 5..7] in registers, one butterfly sums them
 // over the warp, and each lane adds one total into the FP64 arrays.
 // ------------------------------------------------------------------------------------
+template <int kPPL>
 __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_type, float qbm, float dt,
                                                          const int4* __restrict__ items, const int* __restrict__ n_items,
                                                          MArr A, const float* __restrict__ T, double* __restrict__ cu,
@@ -430,7 +433,8 @@ __global__ void __launch_bounds__(kMixThreads) k_mhist(const int64_t* __restrict
 // {k, first particle, count}.  One CTA.
 __global__ void __launch_bounds__(1024) k_mscan(int nk, int nr, const int32_t* __restrict__ hist,
                                                 int32_t* __restrict__ cursor, int64_t* __restrict__ n_ptr,
-                                                int dead_key, int4* __restrict__ items, int* __restrict__ n_items) {
+                                                int dead_key, int4* __restrict__ items, int* __restrict__ n_items,
+                                                int kItem) {
   __shared__ int sh[64], shi[64];
   int carry = 0, carry_i = 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -580,7 +584,7 @@ int mixed_alloc(qpad_species* sp) {
   if (e != cudaSuccess) { cudaGetLastError(); return set_err(ctx, QPAD_E_NOMEM, "cudaMalloc(mixed pristine)"); }
   e = cudaMalloc(&sp->hist, sizeof(int32_t) * (ctx->g.nr + 4));
   if (e == cudaSuccess) e = cudaMalloc(&sp->cursor, sizeof(int32_t) * (ctx->g.nr + 4));
-  sp->items_cap = (int64_t)(cap / kItem) + ctx->g.nr + 2;
+  sp->items_cap = (int64_t)(cap / kMinItem) + ctx->g.nr + 2;
   if (e == cudaSuccess) e = cudaMalloc(&sp->items, sizeof(int4) * (size_t)sp->items_cap);
   if (e == cudaSuccess) e = cudaMalloc(&sp->d_nitems, sizeof(int) * 2);
   if (e == cudaSuccess) e = cudaMemset(sp->d_nitems, 0, sizeof(int) * 2);
@@ -612,7 +616,7 @@ static int mixed_sort(qpad_species* sp) {
   k_mhist<<<mgrid(n, kMixThreads), kMixThreads, 0, ctx->stream>>>(sp->d_count, sp->mkey[0], sp->hist);
   k_copy_count<<<1, 1, 0, ctx->stream>>>(sp->d_count, sp->d_total);      // old count for the scatter
   k_mscan<<<1, 1024, 0, ctx->stream>>>(nk, ctx->g.nr, sp->hist, sp->cursor, sp->d_count, ctx->g.nr + 1, sp->items,
-                                       sp->d_nitems);
+                                       sp->d_nitems, 32 * ctx->item_ppl);
   k_mscatter<<<mgrid(n, kMixThreads), kMixThreads, 0, ctx->stream>>>(sp->d_total, marr(sp, 0), marr(sp, 1),
                                                                       sp->cursor);
   if (int r = check_launch(ctx, "mixed sort", 4)) return r;
@@ -631,12 +635,12 @@ int mixed_index(qpad_species* sp) {
   if (cudaMemsetAsync(sp->hist, 0, sizeof(int32_t) * nk, ctx->stream) != cudaSuccess) return check_launch(ctx, "hist0", 0);
   k_mhist<<<mgrid(n, kMixThreads), kMixThreads, 0, ctx->stream>>>(sp->d_count, sp->mkey[0], sp->hist);
   k_mscan<<<1, 1024, 0, ctx->stream>>>(nk, ctx->g.nr, sp->hist, sp->cursor, sp->d_count, ctx->g.nr + 1, sp->items,
-                                       sp->d_nitems);
+                                       sp->d_nitems, 32 * ctx->item_ppl);
   return check_launch(ctx, "mixed index", 2);
 }
 
 static int item_blocks(const qpad_species* sp) {
-  const int64_t bound = sp->np / kItem + sp->ctx->g.nr + 2;     // >= sum over cells of ceil(n_k / kItem)
+  const int64_t bound = sp->np / (32 * sp->ctx->item_ppl) + sp->ctx->g.nr + 2;   // >= sum over cells of ceil(n_k / item)
   return (int)((std::min<int64_t>(bound, sp->items_cap) + kItemThreads / 32 - 1) / (kItemThreads / 32));
 }
 
@@ -689,7 +693,10 @@ int mixed_qdeposit_raw(qpad_species* sp, double* qraw) {
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
   prof_begin(ctx, "qdeposit");
-  k_mqdeposit<<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
+  if (ctx->item_ppl == 2)
+    k_mqdeposit<2><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
+  else
+    k_mqdeposit<4><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
   prof_end(ctx, "qdeposit");
   return check_launch(ctx, "k_mqdeposit");
 }
@@ -698,9 +705,14 @@ int mixed_amjdp_raw(qpad_species* sp, const float* gtab, double* cu, double* amu
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
   prof_begin(ctx, "amjdp");
-  k_mamjdp<<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
-                                                              sp->items, sp->d_nitems, marr(sp, 0), gtab, cu, amu,
-                                                              acu, 0);
+  if (ctx->item_ppl == 2)
+    k_mamjdp<2><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
+                                                                   sp->items, sp->d_nitems, marr(sp, 0), gtab, cu, amu,
+                                                                   acu, 0);
+  else
+    k_mamjdp<4><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
+                                                                   sp->items, sp->d_nitems, marr(sp, 0), gtab, cu, amu,
+                                                                   acu, 0);
   prof_end(ctx, "amjdp");
   return check_launch(ctx, "k_mamjdp");
 }

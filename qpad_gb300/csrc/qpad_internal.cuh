@@ -89,6 +89,7 @@ struct qpad_ctx {
   double* raw = nullptr;                       // raw current deposits of the loop [cu 3|amu 3|acu 2] x P x ld
   unsigned int* iter_tickets = nullptr;        // convergence tickets and maxima of k_iterate
   int iter_cl = 0, iter_rows = 0;              // cluster size and rows per CTA of k_iterate
+  int item_ppl = 4;                            // particles per lane of a mixed deposit work item
   struct qpad_guess_state* guess = nullptr;    // learned predictor-corrector guess (learn.cu)
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
   float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
@@ -112,6 +113,7 @@ struct qpad_ctx {
   std::string graph_status;                    // why the graph path is off, if it is
   bool use_graph = true;
   int64_t g_pro = 0, g_it = 0, g_epi = 0;      // kernels per slice prologue / iteration / epilogue
+  int64_t g_once = 0;                          // kernels once per graph step
   std::vector<qpad_slice_stats> h_stats;       // per-slice statistics read back after a graph step
   int64_t launches = 0;                        // kernels launched on this context
   // per-kernel-family CUDA-event timing (qpad_profile_enable / qpad_profile_read)
@@ -182,6 +184,8 @@ void prof_collect(qpad_ctx* ctx);   // folds completed pairs into the totals (st
 
 // ---- field kernels (fields.cu) ----------------------------------------------------------
 int build_factors(qpad_ctx* ctx);
+// raises (never lowers) a kernel's dynamic shared-memory limit on the context's device
+int raise_dyn_smem(qpad_ctx* ctx, const void* func, size_t bytes);
 enum FieldOp {
   FOP_PSI = 0, FOP_BZ, FOP_BT_BEAM, FOP_BT_ITER, FOP_EZ, FOP_ET, FOP_DJDXI
 };
@@ -195,6 +199,7 @@ int launch_field_op(qpad_ctx* ctx, int op, FieldArgs a);
 int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op, int loop_state = 0,
                 cudaGraphConditionalHandle h = 0, int use_h = 0);
 int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle h);   // ++slice, set slice WHILE condition
+int launch_set_slice(qpad_ctx* ctx, int j);                         // slice index = j on the device
 // fused phases of one slice
 int launch_slice_begin(qpad_ctx* ctx, int neutralized_any);   // slice index read from ctx->d_j
 int launch_iter_e(qpad_ctx* ctx);
@@ -207,6 +212,7 @@ int guess_enqueue(qpad_ctx* ctx);
 void guess_free(qpad_ctx* ctx);
 // one predictor-corrector iteration after the deposit, as a cluster kernel (iterate.cu)
 int iterate_setup(qpad_ctx* ctx);
+int iterate_try_cluster(qpad_ctx* ctx, int cl);
 int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h);
 
 // ---- particle kernels (plasma.cu, beam.cu) ---------------------------------------------

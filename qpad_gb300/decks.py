@@ -98,4 +98,24 @@ def c5() -> Deck:
                        BeamSpec(20.0, 0.1, 0.3, 5.5, 50_000_000, gamma=40000.0)], n_steps=10)
 
 
+def c3(n: int = 64, seed: int = 2) -> list:
+    """Batched scan: n independent simulations of uneven size (seed 2).  nr uniform in
+    {128, 256, 512, 1024} with dr = 10.24 / nr, max mode uniform in 0..4, particles per cell
+    a x b with a uniform in 4..8 and b in {8, 16}, driver peak density log-uniform in
+    [0.5, 20], sigma_r uniform in [0.2, 1.0], sigma_xi = 1, 512 slices of dxi = 0.04, the
+    driver centre 3 sigma_xi behind the box head, 200,000 beam particles per simulation."""
+    import random
+    rng = random.Random(seed)
+    out = []
+    for k in range(n):
+        nr = rng.choice([128, 256, 512, 1024])
+        M = rng.randint(0, 4)
+        a, b = rng.randint(4, 8), rng.choice([8, 16])
+        n_b = math.exp(rng.uniform(math.log(0.5), math.log(20.0)))
+        sig_r = rng.uniform(0.2, 1.0)
+        out.append(Deck(f"c3_{k:02d}_m{M}_nr{nr}", nr, 512, M, 10.24 / nr, 0.04, (a, b // 8), 8, 0.0,
+                        seed * 1000 + k, beams=[BeamSpec(n_b, sig_r, 1.0, 3.0, 200_000)]))
+    return out
+
+
 DECKS = {"c1": c1, "c2": c2, "c5": c5}
