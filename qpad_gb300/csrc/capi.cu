@@ -979,6 +979,10 @@ int enqueue_slice_prologue(qpad_ctx* ctx, cudaGraphConditionalHandle hi, int use
     if (s->push_type == QPAD_PUSH2_STD)
       if (int r = mixed ? mixed_interp_psi(s, ctx->f[QPAD_F_PSI]) : species_interp_psi(s, ctx->f[QPAD_F_PSI]))
         return r;
+  // the convergence record of B_phi: in the graph the last iteration of the previous slice
+  // left it (nothing changes B_phi in between; the step start zeroes both), unless the
+  // learned guess has just replaced b_spe
+  if (use_h && !ctx->guess) return 0;
   return launch_conv(ctx, ctx->f[QPAD_F_B_SPE], 1, 0, use_h, hi, use_h);
 }
 
@@ -1083,7 +1087,7 @@ int add_slice_loop(qpad_ctx* ctx, cudaGraph_t top) {
       }
     }
     if (!r) r = enqueue_slice_epilogue(ctx, 1);
-    if (!r) r = launch_advance(ctx, hs);
+    if (!r) r = launch_advance(ctx, hs, hi);
     l2 = ctx->launches;
     cudaGraph_t out = nullptr;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &out);
@@ -1185,6 +1189,9 @@ int step_begin(qpad_ctx* ctx) {
   for (int f : zero_fields)
     if (cudaMemsetAsync(ctx->f[f], 0, f1_elems(ctx, f) * sizeof(double), ctx->stream) != cudaSuccess)
       return check_launch(ctx, "zero fields");
+  // the convergence record of the zeroed B_phi
+  if (cudaMemsetAsync(ctx->conv, 0, 2 * (size_t)ctx->g.nr * sizeof(double), ctx->stream) != cudaSuccess)
+    return check_launch(ctx, "zero record");
   return 0;
 }
 

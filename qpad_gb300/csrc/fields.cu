@@ -667,47 +667,63 @@ __global__ void __launch_bounds__(kFieldThreads) k_iter_b(GridDev G, const doubl
   op_bz(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_B_SPE]);
 }
 
-// End of slice j (simulation_class.f03:403-456 without the particle push): cbq and the
-// stores of cu and rho, total and species fields, the J-perp predictor for slice j+1.
-__global__ void __launch_bounds__(kFieldThreads) k_slice_end(GridDev G, const double* __restrict__ fac,
-                                                             SliceFields F, const int* __restrict__ jp) {
-  extern __shared__ double sm[];
-  __shared__ double sc[6 * 32 + 8];
+// End of slice j (simulation_class.f03:403-456 without the particle push), one thread per
+// (mode part, node): cbq (rho = (rho - Jz) + Jz), the stores of cu, rho, E, B, psi, b_spe
+// and e_spe = E-perp(b_spe, psi), then the J-perp predictor dcu *= dxi, cu += dcu.  E and B
+// of the slice, b = b_spe + b_beam and the FP32 gather table are those the last
+// predictor-corrector iteration (k_iterate) left: the reference's e%solve(cu) and
+// e%solve(b, psi) at the slice end see the same inputs.
+__global__ void __launch_bounds__(256) k_slice_end(GridDev G, SliceFields F, const int* __restrict__ jp) {
   const int j = *jp;
-  const int m = blockIdx.x;
-  const int npart = m == 0 ? 1 : 2;
+  const int ld = G.ld;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= G.P * ld) return;
+  const int p = q / ld, i = q % ld;
+  const int m = (p + 1) / 2;
   double* cu = F.f[QPAD_F_CU];
   double* qs = F.f[QPAD_F_Q_SPE];
-  // q_spe(1,:) += cu(3,:) over all nodes, then the stores of cu and q_spe
-  for (int h = 0; h < npart; ++h) {
-    const int p = h == 0 ? part_re(m) : part_im(m);
-    for (int i = threadIdx.x; i < G.ld; i += blockDim.x) FLD(qs, 1, p, 0, i) = FLD(qs, 1, p, 0, i) + FLD(cu, 3, p, 2, i);
+  const size_t s1 = (size_t)(j - 1) * G.P;      // slice block of the 3D stores
+  // q_spe(1,:) += cu(3,:), then the stores of cu and q_spe
+  const double qv = FLD(qs, 1, p, 0, i) + FLD(cu, 3, p, 2, i);
+  FLD(qs, 1, p, 0, i) = qv;
+  F.f2[QPAD_F_Q_SPE][(s1 + p) * ld + i] = qv;
+  for (int c = 0; c < 3; ++c) {
+    F.f2[QPAD_F_CU][((s1 + p) * 3 + c) * ld + i] = FLD(cu, 3, p, c, i);
+    F.f2[QPAD_F_E][((s1 + p) * 3 + c) * ld + i] = FLD(F.f[QPAD_F_E], 3, p, c, i);
+    F.f2[QPAD_F_B][((s1 + p) * 3 + c) * ld + i] = FLD(F.f[QPAD_F_B], 3, p, c, i);
+    F.f2[QPAD_F_B_SPE][((s1 + p) * 3 + c) * ld + i] = FLD(F.f[QPAD_F_B_SPE], 3, p, c, i);
   }
-  __syncthreads();
-  op_copy(G, m, 3, cu, store_slice(G, F.f2[QPAD_F_CU], 3, j));
-  op_copy(G, m, 1, qs, store_slice(G, F.f2[QPAD_F_Q_SPE], 1, j));
-  op_add(G, m, 3, F.f[QPAD_F_B_SPE], F.f[QPAD_F_B_BEAM], F.f[QPAD_F_B]);
-  op_et(G, m, F.f[QPAD_F_B_SPE], F.f[QPAD_F_PSI], F.f[QPAD_F_E_SPE]);
-  op_ez(G, m, fac, sm, sc, cu, F.f[QPAD_F_E]);
-  op_et(G, m, F.f[QPAD_F_B], F.f[QPAD_F_PSI], F.f[QPAD_F_E]);
+  F.f2[QPAD_F_PSI][(s1 + p) * ld + i] = FLD(F.f[QPAD_F_PSI], 1, p, 0, i);
+  // e_spe = E-perp(b_spe, psi) on nodes 1..nr (field_e_class.f03:412-514)
+  double* es = F.f[QPAD_F_E_SPE];
+  if (i >= 1 && i <= G.nr && (m == 0 || p == part_re(m))) {
+    double o[4];
+    row_et(G, m, i, GlobalF{F.f[QPAD_F_B_SPE], ld, 3}, GlobalF{F.f[QPAD_F_PSI], ld, 1}, o);
+    if (m == 0) {
+      FLD(es, 3, 0, 0, i) = o[0];
+      FLD(es, 3, 0, 1, i) = o[1];
+    } else {
+      FLD(es, 3, part_re(m), 0, i) = o[0];
+      FLD(es, 3, part_im(m), 0, i) = o[1];
+      FLD(es, 3, part_re(m), 1, i) = o[2];
+      FLD(es, 3, part_im(m), 1, i) = o[3];
+    }
+  }
   // dcu *= dxi ; cu(1:2) += dcu(1:2)   (simulation_class.f03:425-426)
   double* dcu = F.f[QPAD_F_DCU];
-  for (int h = 0; h < npart; ++h) {
-    const int p = h == 0 ? part_re(m) : part_im(m);
-    for (int i = threadIdx.x; i < G.ld; i += blockDim.x)
-      for (int c = 0; c < 2; ++c) {
-        const double d = FLD(dcu, 2, p, c, i) * G.dxi;
-        FLD(dcu, 2, p, c, i) = d;
-        FLD(cu, 3, p, c, i) = FLD(cu, 3, p, c, i) + d;
-      }
+  for (int c = 0; c < 2; ++c) {
+    const double d = FLD(dcu, 2, p, c, i) * G.dxi;
+    FLD(dcu, 2, p, c, i) = d;
+    FLD(cu, 3, p, c, i) = FLD(cu, 3, p, c, i) + d;
   }
-  __syncthreads();
-  if (F.gtab) op_write_gtab(G, m, F.f[QPAD_F_E], F.f[QPAD_F_B], F.gtab);
-  op_copy(G, m, 3, F.f[QPAD_F_E], store_slice(G, F.f2[QPAD_F_E], 3, j));
-  op_copy(G, m, 3, F.f[QPAD_F_B], store_slice(G, F.f2[QPAD_F_B], 3, j));
-  op_copy(G, m, 1, F.f[QPAD_F_PSI], store_slice(G, F.f2[QPAD_F_PSI], 1, j));
-  op_copy(G, m, 3, F.f[QPAD_F_B_SPE], store_slice(G, F.f2[QPAD_F_B_SPE], 3, j));
-  op_copy(G, m, 3, F.f[QPAD_F_E_SPE], store_slice(G, F.f2[QPAD_F_E_SPE], 3, j));
+}
+
+// e_spe of the slice into its store; needs every part of e_spe, so it follows k_slice_end
+__global__ void __launch_bounds__(256) k_store_espe(GridDev G, SliceFields F, const int* __restrict__ jp) {
+  const int j = *jp;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= G.P * 3 * G.ld) return;
+  F.f2[QPAD_F_E_SPE][(size_t)(j - 1) * G.P * 3 * G.ld + q] = F.f[QPAD_F_E_SPE][q];
 }
 
 __global__ void __launch_bounds__(kFieldThreads) k_finish_q(GridDev G, const double* raw, const double* qn,
@@ -758,10 +774,13 @@ __global__ void __launch_bounds__(1024) k_conv(GridDev G, const double* __restri
 }
 
 // Advances the slice counter and sets the condition of the slice WHILE node.
-__global__ void k_advance(int* __restrict__ jp, int nz, cudaGraphConditionalHandle h) {
+__global__ void k_advance(int* __restrict__ jp, int nz, cudaGraphConditionalHandle hs, cudaGraphConditionalHandle hi) {
   const int j = *jp + 1;
   *jp = j;
-  cudaGraphSetConditional(h, j <= nz ? 1u : 0u);
+  cudaGraphSetConditional(hs, j <= nz ? 1u : 0u);
+  // re-arm the iteration WHILE node for the next slice (a nested conditional keeps its
+  // last value between entries within one graph launch)
+  cudaGraphSetConditional(hi, 1u);
 }
 
 // ------------------------------------------------------------------------------------
@@ -788,7 +807,7 @@ static int ensure_smem_attr(qpad_ctx* ctx) {
   if (ctx->field_attr_done) return 0;
   const size_t need = field_smem(ctx);
   const void* ks[] = {(const void*)k_field_op, (const void*)k_slice_begin, (const void*)k_iter_e,
-                      (const void*)k_iter_b, (const void*)k_slice_end};
+                      (const void*)k_iter_b};
   for (const void* k : ks)
     if (int r = raise_dyn_smem(ctx, k, need)) return r;
   ctx->field_attr_done = true;
@@ -825,8 +844,8 @@ int launch_set_slice(qpad_ctx* ctx, int j) {
   return check_launch(ctx, "k_set_slice");
 }
 
-int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle h) {
-  k_advance<<<1, 1, 0, ctx->stream>>>(ctx->d_j, ctx->g.nz, h);
+int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle hs, cudaGraphConditionalHandle hi) {
+  k_advance<<<1, 1, 0, ctx->stream>>>(ctx->d_j, ctx->g.nz, hs, hi);
   return check_launch(ctx, "k_advance");
 }
 
@@ -854,12 +873,12 @@ int launch_iter_b(qpad_ctx* ctx) {
 }
 
 int launch_slice_end(qpad_ctx* ctx) {
-  if (int r = ensure_smem_attr(ctx)) return r;
+  const int n = ctx->g.P * ctx->g.ld;
   prof_begin(ctx, "slice_end");
-  k_slice_end<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac, slice_fields(ctx),
-                                                                              ctx->d_j);
+  k_slice_end<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->g, slice_fields(ctx), ctx->d_j);
+  k_store_espe<<<(3 * n + 255) / 256, 256, 0, ctx->stream>>>(ctx->g, slice_fields(ctx), ctx->d_j);
   prof_end(ctx, "slice_end");
-  return check_launch(ctx, "k_slice_end");
+  return check_launch(ctx, "k_slice_end", 2);
 }
 
 int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn) {

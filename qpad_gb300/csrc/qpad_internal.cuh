@@ -198,7 +198,8 @@ int launch_field_op(qpad_ctx* ctx, int op, FieldArgs a);
 // loop_state: count iterations, store per-slice stats, and (use_h) drive the WHILE node h
 int launch_conv(qpad_ctx* ctx, const double* b, int comp, int op, int loop_state = 0,
                 cudaGraphConditionalHandle h = 0, int use_h = 0);
-int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle h);   // ++slice, set slice WHILE condition
+// ++slice, set the slice WHILE condition, re-arm the iteration WHILE condition
+int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle hs, cudaGraphConditionalHandle hi);
 int launch_set_slice(qpad_ctx* ctx, int j);                         // slice index = j on the device
 // fused phases of one slice
 int launch_slice_begin(qpad_ctx* ctx, int neutralized_any);   // slice index read from ctx->d_j

@@ -95,9 +95,11 @@ def test_graph_and_host_driven_loops_agree(precision):
         for x, y in zip(ea, eb):
             assert field_errors(x, y).max() < 1e-12
     else:
+        # FP32 atomics make the two runs differ in summation order only; components far below
+        # the field (E_phi of m = 0) are rated against 1e-3 of the field's norm
         assert abs(float(ia.mean()) - float(ib.mean())) < 0.5
         for x, y in zip(ea, eb):
-            assert field_errors(x, y).max() < 1e-4
+            assert field_errors(x, y, floor_rel=1e-3).max() < 1e-4
     sa.close()
     sb.close()
 
