@@ -172,6 +172,7 @@ def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
     from qpad_gb300.replicas import reduce_timing
     sim = Q.build_simulation(deck, precision=prec, device=local, inputs=inputs)
     sim.use_graph(args.graph == "on")
+    tune = sim.autotune(reps=20) if not args.no_autotune else None
     if guess:
         from qpad_gb300 import learned as LR
         from qpad_gb300.train_guess import DEFAULT_OUT
@@ -208,7 +209,7 @@ def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
     barrier()
     pushes_step = npl * deck.nz
     dev_s, total_pushes = reduce_timing(dev_s, float(pushes_step * args.steps), dist)
-    out = {"value": total_pushes / dev_s, "ms_per_step": dev_s * 1e3 / args.steps,
+    out = {"tune": tune, "value": total_pushes / dev_s, "ms_per_step": dev_s * 1e3 / args.steps,
            "iters_per_slice": iters_tot / (args.steps * deck.nz), "wall_s": wall, "launches": launches,
            "graph": {"active": graph_on, "status": graph_why}, "clocks": clk.summary(), "dev_s": dev_s,
            "pushes_step": pushes_step}
@@ -380,6 +381,7 @@ def run_ours(args):
                      "bytes_per_launch": bytes_per_particle * npl, "avg_launch_us": amj_avg_s * 1e6},
         "clocks": r["clocks"],
         "graph": r["graph"],
+        "autotune": r["tune"],
         "kernel_ms_per_step": {k: round(v[0], 3) for k, v in kern.items()},
         "kernel_launches_per_step": {k: v[1] for k, v in kern.items()},
     }
@@ -410,6 +412,7 @@ def main():
     ap.add_argument("--deck", default="c2")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP64 (or mixed) comparison arm")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--cpu-slices", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slices", type=int, default=0, help="override the deck's slice count (profiling runs)")

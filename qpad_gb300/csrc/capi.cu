@@ -1224,7 +1224,16 @@ int step_end(qpad_ctx* ctx, int push_beams) {
   prof_end(ctx, "step");
   for (auto* s : ctx->species)
     if (int r = species_sync_count(s)) return r;
-  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "3d step");
+  if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "3d step")) return r;
+  unsigned int werr = 0;
+  if (int r = cuda_check(ctx, cudaMemcpy(&werr, ctx->iter_tickets + kIterErrWord, sizeof(werr), cudaMemcpyDeviceToHost),
+                         "iteration error word"))
+    return r;
+  if (werr) {
+    cudaMemsetAsync(ctx->iter_tickets + kIterErrWord, 0, sizeof(werr), ctx->stream);
+    return set_err(ctx, QPAD_E_CUDA, "field iteration: a bulk-copy wait gave up (staging incomplete)");
+  }
+  return QPAD_OK;
 }
 }  // namespace
 

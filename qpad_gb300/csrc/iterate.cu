@@ -14,7 +14,7 @@
 //   convergence test (:394-396, simulation_class.f03:522-606).
 //
 // Solves.  Both substitutions of a factored tridiagonal system are first-order affine
-// recurrences.  Within a CTA, each right-hand side is taken by a group of kLanes lanes,
+// recurrences.  Within a CTA, each right-hand side is taken by a group of gw lanes,
 // each composing a contiguous run of rows, combined by a shuffle scan inside the group;
 // the CTA's composite map is published in shared memory, and after a cluster barrier
 // every CTA composes the maps of the CTAs before it (after it, for the back
@@ -37,7 +37,7 @@ namespace cg = cooperative_groups;
 namespace qpad {
 
 static constexpr int kIterThreads = 256;
-static constexpr int kLanes = 4;           // lanes per right-hand side in the solves
+static constexpr int kMaxRL = 8;           // rows per lane in the solves, at most
 static constexpr int kMaxRhs = 8;          // B+ (re, im), B- (re, im), Bz (re, im), Ez (re, im)
 static constexpr int kCompConv = 1;        // convergence on B_phi
 
@@ -57,6 +57,9 @@ struct IterArgs {
   ConvLoop L;
   double reltol, abstol;
   int R;                  // rows per CTA
+  int gw;                 // lanes per right-hand side in the solves
+  int tma;                // stage with bulk copies (even nr and R: every row 16-byte aligned)
+  unsigned int* err;      // device error word: 1 = a bulk-copy wait gave up
 };
 
 __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release;\n" ::: "memory"); }
@@ -74,34 +77,35 @@ struct RawFin {
 
 // Composite of the per-CTA maps (B, A) published in maps[rhs] by the other CTAs of the
 // cluster, applied to 0: forward, the CTAs before `rank` in increasing order; backward,
-// the CTAs after it in decreasing order.  Lane l of the right-hand side's group composes
-// a block of up to kQB consecutive maps (their remote loads all in flight together) and a
-// shuffle scan over the group joins the blocks.  Every lane of the warp must call it.
-static constexpr int kQB = (16 + kLanes - 1) / kLanes;
+// the CTAs after it in decreasing order.  Lane l of the right-hand side's group (gw lanes)
+// composes a block of up to kMaxQB consecutive maps (their remote loads all in flight
+// together) and a shuffle scan over the group joins the blocks.  Every lane of the warp
+// must call it.
+static constexpr int kMaxQB = 4;
 __device__ __forceinline__ double compose_maps(const cg::cluster_group& cluster, double* maps, int rhs, bool act,
-                                               int l, int rank, int CL, bool forward) {
+                                               int l, int gw, int rank, int CL, bool forward) {
+  const int qb = (CL + gw - 1) / gw;                   // <= kMaxQB for CL <= 16, gw >= 4
   double cA = 0.0, cB = 1.0;
 #pragma unroll
-  for (int j = 0; j < kQB; ++j) {
-    const int n = l * kQB + j;                       // position in the composition order
+  for (int j = 0; j < kMaxQB; ++j) {
+    const int n = l * qb + j;                          // position in the composition order
     const int q = forward ? n : CL - 1 - n;
-    if (act && (forward ? q < rank : q > rank)) {
+    if (act && j < qb && (forward ? q < rank : (q > rank && q >= 0))) {
       const double* mq = cluster.map_shared_rank(maps + 2 * rhs, q);
       const double Bq = mq[0], Aq = mq[1];
       cA = Aq + Bq * cA;
       cB = Bq * cB;
     }
   }
-#pragma unroll
-  for (int off = 1; off < kLanes; off <<= 1) {
-    const double Ao = __shfl_up_sync(0xffffffffu, cA, off, kLanes);
-    const double Bo = __shfl_up_sync(0xffffffffu, cB, off, kLanes);
+  for (int off = 1; off < gw; off <<= 1) {
+    const double Ao = __shfl_up_sync(0xffffffffu, cA, off, gw);
+    const double Bo = __shfl_up_sync(0xffffffffu, cB, off, gw);
     if (l >= off) {
       cA = cA + cB * Ao;
       cB = cB * Bo;
     }
   }
-  return __shfl_sync(0xffffffffu, cA, kLanes - 1, kLanes);
+  return __shfl_sync(0xffffffffu, cA, gw - 1, gw);
 }
 
 // Shared-memory view of a staged node window: component `c0 + c` of part p (the Re or
@@ -118,9 +122,22 @@ struct WinF {
 // [r0-1, r1+2] (cu 0..2, amu 3..5, acu 6..7), b_spe components 0..1 and b_beam on the owned
 // nodes, psi on the window, the factor rows of the three matrices, the right-hand sides.
 __host__ __device__ inline size_t iterate_smem_doubles(int R, int ld) {
-  const size_t W = (size_t)R + 4;
+  const size_t W = (size_t)R + 6;                // node window [r0-2, r0+R+4)
   (void)ld;
-  return 16 * W + 4 * (size_t)R + 6 * (size_t)R + 2 * W + 9 * (size_t)R + (size_t)kMaxRhs * R + 2 * W + 4 * (size_t)R;
+  return 30 * W + 21 * (size_t)R;
+}
+
+// Bulk (TMA) copy global -> this CTA's shared memory, completing on an mbarrier.
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(mbar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, unsigned parity) {
+  unsigned ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(ok) : "r"(smem_u32(mbar)), "r"(parity) : "memory");
+  return ok != 0;
 }
 
 // 8-byte asynchronous copy global -> shared (cp.async), and the wait for all of them
@@ -133,7 +150,8 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 
 __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
-  extern __shared__ double smem[];
+  extern __shared__ __align__(16) double smem[];
+  __shared__ __align__(8) uint64_t mbar;
   __shared__ double fwd[kMaxRhs][2], bwd[kMaxRhs][2];
   __shared__ double wpart[kIterThreads / 32];
   __shared__ double divp;
@@ -141,24 +159,26 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   cg::cluster_group cluster = cg::this_cluster();
   const int CL = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
-  const int m = blockIdx.x / CL;
+  // two clusters per mode: group 0 solves B+ / B- (B-perp, E-perp, the convergence test),
+  // group 1 solves Bz and Ez; they read and write disjoint components
+  const int m = blockIdx.x / (2 * CL), grp = (blockIdx.x / CL) % 2;
   const int nr = a.G.nr, ld = a.G.ld, P = a.G.P;
   const int pr = part_re(m), pi = part_im(m);
   const int nh = m == 0 ? 1 : 2;                 // parts of this mode
-  const int nrhs = m == 0 ? 4 : 8;
+  const int nrhs = m == 0 ? 2 : 4;               // right-hand sides of this group
   const int R = a.R;
   const int r0 = min(rank * R, nr), r1 = min(r0 + R, nr);
   const int Rc = r1 - r0;
   const int t = threadIdx.x;
-  const int W = R + 4, wb = r0 - 1;
+  const int W = R + 6, wb = r0 - 2;              // node window [wb, wb + W): even start for 16-byte rows
   const size_t P1 = (size_t)P * ld;
   double* raw_cu = a.raw;
   double* raw_amu = a.raw + 3 * P1;
   double* raw_acu = a.raw + 6 * P1;
   double* win = smem;                            // [8][2][W]
-  double* bo = win + 16 * W;                     // [2][2][R]
-  double* bbm = bo + 4 * R;                      // [3][2][R]
-  double* psw = bbm + 6 * R;                     // [2][W]
+  double* bo = win + 16 * W;                     // [2][2][W]
+  double* bbm = bo + 4 * W;                      // [3][2][W]
+  double* psw = bbm + 6 * W;                     // [2][W]
   double* facs = psw + 2 * W;                    // [3 kinds][w, ib, g][R]
   double* dsm = facs + 9 * R;                    // [kMaxRhs][R]
   double* tab = dsm + kMaxRhs * R;               // node tables ir, inv on the window
@@ -168,52 +188,127 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   G.inv = tab + W;
   G.toff = wb;
 
-  // ---- staging: every copy of the iteration's inputs in flight at once (cp.async) -------
-  for (int k = t; k < W; k += blockDim.x) {
-    const int node = wb + k;
-    if (node >= 0 && node <= nr + 1) {
-      cp_async8(tab + k, a.G.ir + node);
-      cp_async8(tab + W + k, a.G.inv + node);
-    } else {
-      tab[k] = 0.0;
-      tab[W + k] = 0.0;
+  // ---- staging: every copy of the iteration's inputs in flight at once --------------------
+  // Rows on the node window: the node tables, the group's raw deposit components, psi
+  // (group 0), B_old (group 0) and b_beam; then the factor rows of the group's matrices.
+  // With even nr and R every row is 16-byte aligned and one thread issues one bulk (TMA)
+  // copy per row onto an mbarrier; otherwise each thread issues 8-byte cp.async copies.
+  const int c8_lo = grp == 0 ? 2 : 0, c8_n = grp == 0 ? 6 : 2;   // cu_z, amu, acu | cu_r, cu_phi
+  const int c5_lo = grp == 0 ? 0 : 4, c5_n = grp == 0 ? 4 : 1;   // B_old r, phi and b_beam r, phi | b_beam z
+  const int n0 = max(0, wb), n1 = min(ld, wb + W);               // window nodes that exist
+  const int nwin = 2 + c8_n * nh + (grp == 0 ? nh : 0) + c5_n * nh;   // window rows of this CTA
+  const int fr0 = grp == 0 ? 0 : 6, fr1 = grp == 0 ? 6 : 9;      // factor rows of this CTA
+  // window row k: (destination, source row base at node 0)
+  const auto win_row = [&](int k, double*& dst, const double*& src) {
+    if (k < 2) {
+      dst = tab + k * W;
+      src = k == 0 ? a.G.ir : a.G.inv;
+      return;
     }
-  }
-  for (int row = 0; row < 8 * nh; ++row) {       // raw deposits on the window
-    const int c8 = row / nh, h = row % nh, p = h == 0 ? pr : pi;
-    const double* src = c8 < 3 ? raw_cu + fidx(ld, 3, p, c8, 0)
-                               : (c8 < 6 ? raw_amu + fidx(ld, 3, p, c8 - 3, 0) : raw_acu + fidx(ld, 2, p, c8 - 6, 0));
-    double* dst = win + (c8 * 2 + h) * W;
-    for (int k = t; k < W; k += blockDim.x) {
-      const int node = wb + k;
-      if (node >= 0 && node <= nr + 1) cp_async8(dst + k, src + node);
-      else dst[k] = 0.0;
+    k -= 2;
+    if (k < c8_n * nh) {
+      const int c8 = c8_lo + k / nh, h = k % nh, p = h == 0 ? pr : pi;
+      dst = win + (c8 * 2 + h) * W;
+      src = c8 < 3 ? raw_cu + fidx(ld, 3, p, c8, 0)
+                   : (c8 < 6 ? raw_amu + fidx(ld, 3, p, c8 - 3, 0) : raw_acu + fidx(ld, 2, p, c8 - 6, 0));
+      return;
     }
-  }
-  for (int h = 0; h < nh; ++h) {                 // psi on the window
-    const double* src = a.psi + fidx(ld, 1, h == 0 ? pr : pi, 0, 0);
-    for (int k = t; k < W; k += blockDim.x) {
-      const int node = wb + k;
-      if (node >= 0 && node <= nr + 1) cp_async8(psw + h * W + k, src + node);
-      else psw[h * W + k] = 0.0;
+    k -= c8_n * nh;
+    if (grp == 0 && k < nh) {
+      dst = psw + k * W;
+      src = a.psi + fidx(ld, 1, k == 0 ? pr : pi, 0, 0);
+      return;
     }
-  }
-  for (int row = 0; row < 5 * nh; ++row) {       // b_spe (B_old) and b_beam on the owned nodes
-    const int c5 = row / nh, h = row % nh, p = h == 0 ? pr : pi;
-    const double* src = c5 < 2 ? a.b_spe + fidx(ld, 3, p, c5, r0 + 1) : a.b_beam + fidx(ld, 3, p, c5 - 2, r0 + 1);
-    double* dst = c5 < 2 ? bo + (c5 * 2 + h) * R : bbm + ((c5 - 2) * 2 + h) * R;
-    for (int k = t; k < Rc; k += blockDim.x) cp_async8(dst + k, src + k);
-  }
-  for (int row = 0; row < 9; ++row) {            // factor rows
+    if (grp == 0) k -= nh;
+    const int c5 = c5_lo + k / nh, h = k % nh, p = h == 0 ? pr : pi;
+    dst = c5 < 2 ? bo + (c5 * 2 + h) * W : bbm + ((c5 - 2) * 2 + h) * W;
+    src = c5 < 2 ? a.b_spe + fidx(ld, 3, p, c5, 0) : a.b_beam + fidx(ld, 3, p, c5 - 2, 0);
+  };
+  const auto fac_src = [&](int row) {
     const int ka = row / 3, arr = row % 3;
     const int kind = ka == 0 ? OK_BPLUS : ka == 1 ? OK_BMINUS : OK_GEN;
-    const double* src = a.fac + fac_off(nr, G.M, kind, m) + (size_t)arr * nr + r0;
-    for (int k = t; k < Rc; k += blockDim.x) cp_async8(facs + row * R + k, src + k);
+    return a.fac + fac_off(nr, a.G.M, kind, m) + (size_t)arr * nr + r0;
+  };
+  // window slots outside the grid are zero
+  for (int q = t; q < nwin * W; q += blockDim.x) {
+    const int k = q / W, x = q % W;
+    if (x >= n0 - wb && x < n1 - wb) continue;
+    double* dst;
+    const double* src;
+    win_row(k, dst, src);
+    dst[x] = 0.0;
   }
-  cp_async_wait_all();
+  __shared__ int s_bulk;
+  if (t < 32) {
+    // warp 0 issues one bulk copy per row (lane k: rows k, k + 32, ...), only when every
+    // copy is 16-byte aligned (each lane checks its rows before any copy is issued)
+    const int nf = fr1 - fr0, ncp = nwin + nf;
+    const unsigned wbytes = (unsigned)(n1 - n0) * 8u, fbytes = (unsigned)Rc * 8u;
+    const auto row_copy = [&](int k, void*& dst, const void*& src, unsigned& bytes) {
+      if (k < nwin) {
+        double* d;
+        const double* sr;
+        win_row(k, d, sr);
+        dst = d + (n0 - wb);
+        src = sr + n0;
+        bytes = wbytes;
+      } else {
+        dst = facs + (fr0 + k - nwin) * R;
+        src = fac_src(fr0 + k - nwin);
+        bytes = fbytes;
+      }
+    };
+    bool mine = true;
+    for (int k = t; k < ncp; k += 32) {
+      void* dst;
+      const void* src;
+      unsigned bytes;
+      row_copy(k, dst, src, bytes);
+      mine &= (((uintptr_t)src | (uintptr_t)smem_u32(dst) | bytes) & 15u) == 0;
+    }
+    const bool ok = __all_sync(0xffffffffu, mine) && a.tma;
+    if (ok && t == 0) {
+      const unsigned total = (unsigned)nwin * wbytes + (unsigned)nf * fbytes;
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar)) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(&mbar)), "r"(total)
+                   : "memory");
+    }
+    __syncwarp();
+    if (ok)
+      for (int k = t; k < ncp; k += 32) {
+        void* dst;
+        const void* src;
+        unsigned bytes;
+        row_copy(k, dst, src, bytes);
+        if (bytes) bulk_g2s(dst, src, bytes, &mbar);
+      }
+    if (t == 0) s_bulk = ok;
+  }
+  __syncthreads();                                    // s_bulk and the mbarrier are set up
+  if (s_bulk) {
+    int spins = 0;
+    while (!mbar_try_wait(&mbar, 0u))
+      if (++spins > (1 << 20)) {                     // bounded wait: flag the error and go on
+        if (t == 0) atomicExch(a.err, 1);
+        break;
+      }
+  } else {
+    for (int k = 0; k < nwin; ++k) {
+      double* dst;
+      const double* src;
+      win_row(k, dst, src);
+      for (int x = n0 - wb + t; x < n1 - wb; x += blockDim.x) cp_async8(dst + x, src + wb + x);
+    }
+    for (int row = fr0; row < fr1; ++row) {
+      const double* src = fac_src(row);
+      for (int k = t; k < Rc; k += blockDim.x) cp_async8(facs + row * R + k, src + k);
+    }
+    cp_async_wait_all();
+  }
   __syncthreads();
-  for (int q = t; q < 8 * nh * W; q += blockDim.x) {   // finish the deposits in place
-    const int row = q / W, k = q % W, c8 = row / nh, node = wb + k;
+  for (int q = t; q < c8_n * nh * W; q += blockDim.x) {   // finish the deposits in place
+    const int row = q / W, k = q % W, c8 = c8_lo + row / nh, node = wb + k;
     if (node < 0 || node > nr + 1) continue;
     double& v = win[(c8 * 2 + row % nh) * W + k];
     v = c8 < 3 ? finish_amj(G, m, 0, c8, node, v) : (c8 < 6 ? finish_amj(G, m, 1, c8 - 3, node, v)
@@ -222,13 +317,13 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   __syncthreads();
   const WinF CU{win, W, wb, pr, 0}, AMU{win, W, wb, pr, 3}, ACU{win, W, wb, pr, 6};
   const WinF PS{psw, W, wb, pr, 0};
-  const auto BO = [&](int p, int c, int i) { return bo[(c * 2 + (p == pr ? 0 : 1)) * R + (i - r0 - 1)]; };
+  const auto BO = [&](int p, int c, int i) { return bo[(c * 2 + (p == pr ? 0 : 1)) * W + (i - wb)]; };
 
   // ---- sources: (node, equation group) per thread ---------------------------------------
   // group 0: dJ/dxi and the B+ / B- right-hand sides; group 1: Bz; group 2: Ez
   double div = 0.0;
-  for (int q = t; q < 3 * Rc; q += blockDim.x) {
-    const int job = q / Rc, k = q % Rc, i = r0 + k + 1;
+  for (int q = t; q < (grp == 0 ? 1 : 2) * Rc; q += blockDim.x) {
+    const int job = (grp == 0 ? 0 : 1) + q / Rc, k = q % Rc, i = r0 + k + 1;
     if (job == 0) {
       double dj[4];
       row_djdxi(G, m, i, ACU, AMU, dj);
@@ -260,7 +355,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     }
   }
   // the m = 0 axis row of Ez needs the weighted sum over the whole line
-  if (m == 0) {
+  if (m == 0 && grp == 1) {
     for (int off = 16; off > 0; off >>= 1) div += __shfl_down_sync(0xffffffffu, div, off);
     if ((t & 31) == 0) wpart[t >> 5] = div;
     __syncthreads();
@@ -280,78 +375,97 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   __syncthreads();
 
   // ---- forward substitution y_k = d_k - w_k y_{k-1} ------------------------------------
-  const int rhs = t / kLanes, l = t % kLanes;
-  const bool solver = t < 32 * ((kMaxRhs * kLanes + 31) / 32);   // whole warps take part in the shuffles
-  const bool act = rhs < nrhs;
-  const int RL = (Rc + kLanes - 1) / kLanes;
-  const int k0 = min(l * RL, Rc), k1 = min(k0 + RL, Rc);
+  // gw lanes per right-hand side (a power of two, host-chosen so that RL <= kMaxRL); a
+  // lane's rows and factors are read into registers before its dependent FP64 chain
+  const int gw = a.gw;
+  const int rl = t / gw, l = t % gw;
+  // slot of local right-hand side rl: group 0 {B+ re, B- re, B+ im, B- im} = {0, 1, 4, 5},
+  // group 1 {Bz re, Ez re, Bz im, Ez im} = {2, 3, 6, 7}
+  const int rhs = ((rl & 1) | ((rl >> 1) << 2)) + 2 * grp;
+  const bool solver = t < 32 * ((kMaxRhs / 2 * gw + 31) / 32);   // whole warps take part in the shuffles
+  const bool act = rl < nrhs;
+  const int RL = (Rc + gw - 1) / gw;
+  const int k0 = min(l * RL, Rc), cnt = min(RL, Rc - k0);
   const int ka = (rhs & 3) < 2 ? (rhs & 3) : 2;          // B+, B-, then the shared Bz / Ez matrix
-  const double* fw = facs + ka * 3 * R;
-  const double* fib = fw + R;
-  const double* fg = fib + R;
-  double* d = dsm + (size_t)(act ? rhs : 0) * R;
+  const double* fw = facs + ka * 3 * R + k0;
+  const double* fib = facs + ka * 3 * R + R + k0;
+  const double* fg = facs + ka * 3 * R + 2 * R + k0;
+  double* d = dsm + (size_t)(act ? rhs : 2 * grp) * R + k0;
+  double dv[kMaxRL], cv[kMaxRL];
+#pragma unroll
+  for (int j = 0; j < kMaxRL; ++j) {
+    const bool in = act && j < cnt;
+    dv[j] = in ? d[j] : 0.0;
+    cv[j] = in ? fw[j] : 0.0;
+  }
   double Aex = 0.0, Bex = 1.0;
   if (solver) {
     double A = 0.0, B = 1.0;
-    if (act)
-      for (int k = k0; k < k1; ++k) {
-        const double w = fw[k];
-        A = d[k] - w * A;
-        B = -w * B;
-      }
 #pragma unroll
-    for (int off = 1; off < kLanes; off <<= 1) {
-      const double Ao = __shfl_up_sync(0xffffffffu, A, off, kLanes);
-      const double Bo = __shfl_up_sync(0xffffffffu, B, off, kLanes);
+    for (int j = 0; j < kMaxRL; ++j)
+      if (j < cnt) {
+        A = dv[j] - cv[j] * A;
+        B = -cv[j] * B;
+      }
+    for (int off = 1; off < gw; off <<= 1) {
+      const double Ao = __shfl_up_sync(0xffffffffu, A, off, gw);
+      const double Bo = __shfl_up_sync(0xffffffffu, B, off, gw);
       if (l >= off) {
         A = A + B * Ao;
         B = B * Bo;
       }
     }
-    Aex = __shfl_up_sync(0xffffffffu, A, 1, kLanes);
-    Bex = __shfl_up_sync(0xffffffffu, B, 1, kLanes);
+    Aex = __shfl_up_sync(0xffffffffu, A, 1, gw);
+    Bex = __shfl_up_sync(0xffffffffu, B, 1, gw);
     if (l == 0) {
       Aex = 0.0;
       Bex = 1.0;
     }
-    if (act && l == kLanes - 1) {
+    if (act && l == gw - 1) {
       fwd[rhs][0] = B;
       fwd[rhs][1] = A;
     }
   }
   cluster.sync();
   double carry = 0.0;                                 // y at the row before this CTA
-  if (solver) carry = compose_maps(cluster, &fwd[0][0], rhs, act, l, rank, CL, true);
+  if (solver) carry = compose_maps(cluster, &fwd[0][0], rhs, act, l, gw, rank, CL, true);
   if (solver && act) {
     double y = Aex + Bex * carry;
-    for (int k = k0; k < k1; ++k) {
-      y = d[k] - fw[k] * y;
-      d[k] = y;
-    }
+#pragma unroll
+    for (int j = 0; j < kMaxRL; ++j)
+      if (j < cnt) {
+        y = dv[j] - cv[j] * y;
+        dv[j] = y;
+      }
   }
-  __syncthreads();
 
   // ---- back substitution x_k = y_k ib_k - g_k x_{k+1} -----------------------------------
+  double ibv[kMaxRL];
+#pragma unroll
+  for (int j = 0; j < kMaxRL; ++j) {
+    const bool in = act && j < cnt;
+    ibv[j] = in ? fib[j] : 0.0;
+    cv[j] = in ? fg[j] : 0.0;
+  }
   if (solver) {
     double A = 0.0, B = 1.0;
-    if (act)
-      for (int k = k1 - 1; k >= k0; --k) {
-        const double g = fg[k];
-        A = d[k] * fib[k] - g * A;
-        B = -g * B;
-      }
 #pragma unroll
-    for (int off = 1; off < kLanes; off <<= 1) {
-      const double Ao = __shfl_down_sync(0xffffffffu, A, off, kLanes);
-      const double Bo = __shfl_down_sync(0xffffffffu, B, off, kLanes);
-      if (l + off < kLanes) {
+    for (int j = kMaxRL - 1; j >= 0; --j)
+      if (j < cnt) {
+        A = dv[j] * ibv[j] - cv[j] * A;
+        B = -cv[j] * B;
+      }
+    for (int off = 1; off < gw; off <<= 1) {
+      const double Ao = __shfl_down_sync(0xffffffffu, A, off, gw);
+      const double Bo = __shfl_down_sync(0xffffffffu, B, off, gw);
+      if (l + off < gw) {
         A = A + B * Ao;
         B = B * Bo;
       }
     }
-    Aex = __shfl_down_sync(0xffffffffu, A, 1, kLanes);
-    Bex = __shfl_down_sync(0xffffffffu, B, 1, kLanes);
-    if (l == kLanes - 1) {
+    Aex = __shfl_down_sync(0xffffffffu, A, 1, gw);
+    Bex = __shfl_down_sync(0xffffffffu, B, 1, gw);
+    if (l == gw - 1) {
       Aex = 0.0;
       Bex = 1.0;
     }
@@ -362,13 +476,15 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   }
   cluster.sync();
   carry = 0.0;                                        // x at the row after this CTA
-  if (solver) carry = compose_maps(cluster, &bwd[0][0], rhs, act, l, rank, CL, false);
+  if (solver) carry = compose_maps(cluster, &bwd[0][0], rhs, act, l, gw, rank, CL, false);
   if (solver && act) {
     double x = Aex + Bex * carry;
-    for (int k = k1 - 1; k >= k0; --k) {
-      x = d[k] * fib[k] - fg[k] * x;
-      d[k] = x;
-    }
+#pragma unroll
+    for (int j = kMaxRL - 1; j >= 0; --j)
+      if (j < cnt) {
+        x = dv[j] * ibv[j] - cv[j] * x;
+        d[j] = x;
+      }
   }
   // last access to another CTA's shared memory is done; the matching wait sits at the end
   cluster_arrive();
@@ -376,8 +492,8 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
 
   // ---- fields of the owned nodes: (node, group) per thread ------------------------------
   // group 0: B-perp from B+ / B-, b = b_spe + b_beam and E-perp; group 1: Bz and Ez
-  for (int q = t; q < 2 * Rc; q += blockDim.x) {
-    const int job = q / Rc, k = q % Rc, i = r0 + k + 1;
+  for (int q = t; q < Rc; q += blockDim.x) {
+    const int job = grp, k = q, i = r0 + k + 1;
     if (job == 0) {
       double bs[2][2], bb[2][2];
       if (m == 0) {
@@ -393,7 +509,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
         bs[1][1] = zero ? 0.0 : 0.5 * (-b1re + b2re);
       }
       for (int h = 0; h < nh; ++h)
-        for (int c = 0; c < 2; ++c) bb[h][c] = bs[h][c] + bbm[(c * 2 + h) * R + k];
+        for (int c = 0; c < 2; ++c) bb[h][c] = bs[h][c] + bbm[(c * 2 + h) * W + (i - wb)];
       const auto Bn = [&](int p, int c, int) { return p == pr ? bb[0][c] : bb[1][c]; };
       double et[4];
       row_et(G, m, i, Bn, PS, et);
@@ -435,7 +551,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
       }
       for (int h = 0; h < nh; ++h) {
         const int p = h == 0 ? pr : pi;
-        const double bzt = bz[h] + bbm[(2 * 2 + h) * R + k];
+        const double bzt = bz[h] + bbm[(2 * 2 + h) * W + (i - wb)];
         a.b_spe[fidx(ld, 3, p, 2, i)] = bz[h];
         a.b[fidx(ld, 3, p, 2, i)] = bzt;
         a.e[fidx(ld, 3, p, 2, i)] = ez[h];
@@ -452,7 +568,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     const int i = t == 0 ? 0 : nr + 1;
     for (int h = 0; h < nh; ++h) {
       const int p = h == 0 ? pr : pi;
-      for (int c = 0; c < 3; ++c) {
+      for (int c = (grp == 0 ? 0 : 2); c < (grp == 0 ? 2 : 3); ++c) {   // the group's components
         const double v = a.b_spe[fidx(ld, 3, p, c, i)] + a.b_beam[fidx(ld, 3, p, c, i)];
         a.b[fidx(ld, 3, p, c, i)] = v;
         if (a.gtab) {
@@ -463,7 +579,8 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     }
   }
 
-  // ---- convergence test -----------------------------------------------------------------
+  // ---- convergence test (group 0, which owns B-perp) ------------------------------------
+  if (grp == 0) {
   __threadfence();                                    // this CTA's B-perp, visible device-wide
   __syncthreads();
   if (t == 0) s_ticket = atomicAdd(&a.tickets[rank], 1u);
@@ -520,14 +637,16 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
       }
     }
   }
+  }
+
   // ---- stores nothing in this kernel waits for: the finished deposits, dJ/dxi, and the
   // cleared raw deposits (every CTA of the cluster staged its window before the forward
   // barrier)
   {
     const int i0 = rank == 0 ? 0 : r0 + 1, i1 = rank == CL - 1 ? nr + 1 : r1;
     const int nn = i1 - i0 + 1;
-    for (int q = t; q < 8 * nh * nn; q += blockDim.x) {
-      const int c8 = q / (nh * nn), h = (q / nn) % nh, i = i0 + q % nn;
+    for (int q = t; q < c8_n * nh * nn; q += blockDim.x) {
+      const int c8 = c8_lo + q / (nh * nn), h = (q / nn) % nh, i = i0 + q % nn;
       const int p = h == 0 ? pr : pi;
       const double v = win[(c8 * 2 + h) * W + (i - wb)];
       if (c8 < 3) {
@@ -541,7 +660,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
         raw_acu[fidx(ld, 2, p, c8 - 6, i)] = 0.0;
       }
     }
-    for (int q = t; q < 2 * nh * Rc; q += blockDim.x) {
+    for (int q = t; q < (grp == 0 ? 2 * nh * Rc : 0); q += blockDim.x) {
       const int c = q / (nh * Rc), h = (q / Rc) % nh, k = q % Rc;
       a.dcu[fidx(ld, 2, h == 0 ? pr : pi, c, r0 + k + 1)] = djs[(2 * h + c) * R + k];
     }
@@ -554,9 +673,18 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
 // ------------------------------------------------------------------------------------
 static int cluster_for(int nr) { return std::max(1, std::min(16, nr / 32)); }
 
+// Lanes per right-hand side for R rows per CTA: a power of two in 4..32 giving at most 4
+// rows per lane where possible (and at most kMaxRL); 8 right-hand sides fit 256 threads.
+static int solve_lanes(int R) {
+  int g = 4;
+  while (g < 32 && (R + g - 1) / g > 4) g *= 2;
+  return g;
+}
+
 // Uses cluster size cl for k_iterate if the kernel can launch with it; nonzero otherwise.
 int iterate_try_cluster(qpad_ctx* ctx, int cl) {
   if (cl < 1 || cl > 16 || cl > ctx->g.nr) return QPAD_E_ARG;
+  if ((ctx->g.nr + cl - 1) / cl > 32 * kMaxRL) return QPAD_E_CAPACITY;      // rows per CTA beyond the solver
   cudaError_t e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return cuda_check(ctx, e, "cluster attribute");
   const int R = (ctx->g.nr + cl - 1) / cl;
@@ -564,7 +692,7 @@ int iterate_try_cluster(qpad_ctx* ctx, int cl) {
   if (smem > 200 * 1024) return QPAD_E_CAPACITY;
   if (int r = raise_dyn_smem(ctx, (const void*)k_iterate, smem)) return r;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cl * (ctx->g.M + 1));
+  cfg.gridDim = dim3(2 * cl * (ctx->g.M + 1));
   cfg.blockDim = dim3(kIterThreads);
   cfg.dynamicSmemBytes = smem;
   cudaLaunchAttribute at[1];
@@ -587,33 +715,10 @@ int iterate_try_cluster(qpad_ctx* ctx, int cl) {
 
 int iterate_setup(qpad_ctx* ctx) {
   if (ctx->iter_cl > 0) return 0;
-  cudaError_t e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  if (e != cudaSuccess) return cuda_check(ctx, e, "cluster attribute");
-  for (int cl = cluster_for(ctx->g.nr); cl >= 1; cl /= 2) {
-    const int R = (ctx->g.nr + cl - 1) / cl;
-    const size_t smem = iterate_smem_doubles(R, ctx->g.ld) * sizeof(double);
-    if (int r = raise_dyn_smem(ctx, (const void*)k_iterate, smem)) return r;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(cl * (ctx->g.M + 1));
-    cfg.blockDim = dim3(kIterThreads);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = cl;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    int ncl = 0;
-    e = cudaOccupancyMaxActiveClusters(&ncl, k_iterate, &cfg);
-    if (e == cudaSuccess && ncl >= 1) {
-      ctx->iter_cl = cl;
-      ctx->iter_rows = R;
-      return 0;
-    }
-    cudaGetLastError();
-  }
-  return set_err(ctx, QPAD_E_CUDA, "no cluster shape of the iteration kernel fits this GPU");
+  for (int cl = cluster_for(ctx->g.nr); cl >= 1; cl /= 2)
+    if (iterate_try_cluster(ctx, cl) == 0) return 0;
+  cudaGetLastError();
+  return set_err(ctx, QPAD_E_CUDA, "no cluster shape of the iteration kernel fits this grid and GPU");
 }
 
 int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h) {
@@ -647,9 +752,12 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   a.reltol = ctx->reltol;
   a.abstol = ctx->abstol;
   a.R = ctx->iter_rows;
+  a.gw = solve_lanes(a.R);
+  a.tma = (ctx->g.nr % 2 == 0 && a.R % 2 == 0) ? 1 : 0;
+  a.err = ctx->iter_tickets + kIterErrWord;
   const int cl = ctx->iter_cl;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cl * (ctx->g.M + 1));
+  cfg.gridDim = dim3(2 * cl * (ctx->g.M + 1));
   cfg.blockDim = dim3(kIterThreads);
   cfg.dynamicSmemBytes = iterate_smem_doubles(a.R, ctx->g.ld) * sizeof(double);
   cfg.stream = ctx->stream;

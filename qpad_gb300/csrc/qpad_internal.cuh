@@ -73,6 +73,8 @@ struct Beam;
 
 }  // namespace qpad
 
+static constexpr int kIterErrWord = 127;       // k_iterate's error word in the ticket buffer
+
 struct qpad_ctx {
   qpad::GridDev g;
   int iter_max;
@@ -87,7 +89,7 @@ struct qpad_ctx {
   double* qn = nullptr;                        // neutralising background (sum over species)
   double* qraw = nullptr;                      // raw charge deposit scratch
   double* raw = nullptr;                       // raw current deposits of the loop [cu 3|amu 3|acu 2] x P x ld
-  unsigned int* iter_tickets = nullptr;        // convergence tickets and maxima of k_iterate
+  unsigned int* iter_tickets = nullptr;        // [0,32) tickets, [32,96) maxima, [kIterErrWord] error word of k_iterate
   int iter_cl = 0, iter_rows = 0;              // cluster size and rows per CTA of k_iterate
   int item_ppl = 4;                            // particles per lane of a mixed deposit work item
   struct qpad_guess_state* guess = nullptr;    // learned predictor-corrector guess (learn.cu)
@@ -96,7 +98,6 @@ struct qpad_ctx {
   double* scratch = nullptr;                   // per-call deposit scratch (cu, amu, acu)
   double* beam_scratch = nullptr;              // per-beam charge store scratch
   double* h_res = nullptr;                     // pinned mirror of res
-  int* d_err = nullptr;                        // device error word
   std::vector<qpad_species*> species;
   std::vector<qpad_beam*> beams;
   std::string err;
