@@ -2,16 +2,22 @@
 //
 // GB300 executes FP64 at 1/64 of its FP32 rate, so the FP64 field work of an iteration
 // has to be spread over many SMs instead of one CTA per mode.  Here each azimuthal mode m
-// is one thread-block cluster of CL CTAs; CTA `rank` of the cluster owns the radial rows
-// [rank*R, (rank+1)*R) of that mode (row k = node k+1).  After the plasma deposit the
-// kernel does, per node it owns:
+// is two thread-block clusters of CL CTAs: group 0 solves B+ / B- (B-perp, E-perp and
+// the convergence test), group 1 solves Bz and Ez; they read and write disjoint
+// components.  CTA `rank` of a cluster owns the radial rows [rank*R, (rank+1)*R) of the
+// mode (row k = node k+1).  After the plasma deposit the kernel does, per node it owns:
 //
 //   finish the raw deposits (axis rule, 1/(i-1)), dJ/dxi, and the right-hand sides of
 //   B+ / B- (the B-perp predictor-corrector), Bz and Ez (simulation_class.f03:386-392,
 //   and the Ez of the next iteration, :375-378, which depends only on the same current);
-//   the tridiagonal solves of all of them at once, split across the cluster;
+//   the tridiagonal solves of the group's systems, split across the cluster;
 //   B-perp, Bz, Ez, b = b_spe + b_beam, E-perp, the FP32 gather table; and the
 //   convergence test (:394-396, simulation_class.f03:522-606).
+//
+// Staging.  A CTA's inputs are rows on an even-aligned node window; warp 0 issues one
+// bulk copy per row onto an mbarrier when every row is 16-byte aligned (even nr and R),
+// otherwise every thread issues 8-byte cp.async copies.  The wait is bounded; a wait
+// that gives up sets an error word that the host reads after the step.
 //
 // Solves.  Both substitutions of a factored tridiagonal system are first-order affine
 // recurrences.  Within a CTA, each right-hand side is taken by a group of gw lanes,
@@ -21,11 +27,11 @@
 // substitution) through distributed shared memory and replays its rows.
 //
 // Convergence.  The record is a per-node sum over all modes, so it cannot be formed
-// inside one cluster.  Each CTA counts in on a per-node-range ticket after writing its
-// B-perp; the last of the M+1 CTAs of a node range evaluates the record there and folds
-// its maxima into two global words (atomicMax on the bit patterns of non-negative
-// doubles, which is exact and order independent); the last node range to finish takes
-// the verdict, drives the loop state and resets the tickets.  No CTA waits on another.
+// inside one cluster.  Each group-0 CTA takes its node range's ticket after writing its
+// B-perp; the last of the M+1 CTAs of a range evaluates the record there and folds its
+// maxima into two global words (max on the bit patterns of non-negative doubles, which is
+// exact and order independent); the last range to finish takes the verdict, drives the
+// loop state and resets the tickets.  No CTA waits on another.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -52,8 +58,8 @@ struct IterArgs {
   const double* psi;
   float* gtab;            // FP32 gather table (mixed path) or null
   double* conv;           // s_re[nr], s_im[nr], res[..]
-  unsigned int* tickets;  // [0, CL): node-range tickets; [CL]: range counter
-  double* slots;           // per node range: the two maxima of the convergence test
+  unsigned int* tickets;  // [0, CL): modes through each node range; [CL]: node ranges through the test
+  unsigned long long* maxima;  // the test's two maxima (bit patterns of non-negative doubles)
   ConvLoop L;
   double reltol, abstol;
   int R;                  // rows per CTA
@@ -62,6 +68,14 @@ struct IterArgs {
   unsigned int* err;      // device error word: 1 = a bulk-copy wait gave up
 };
 
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;\n" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ void red_max_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.max.u64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release;\n" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory"); }
 
@@ -581,20 +595,26 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
 
   // ---- convergence test (group 0, which owns B-perp) ------------------------------------
   if (grp == 0) {
-  __threadfence();                                    // this CTA's B-perp, visible device-wide
+  __syncthreads();                                    // this CTA's B-perp is written
+  if (t == 0) s_ticket = atom_add_acq_rel(&a.tickets[rank], 1u);   // releases it, acquires the others'
   __syncthreads();
-  if (t == 0) s_ticket = atomicAdd(&a.tickets[rank], 1u);
-  __syncthreads();
-  if (s_ticket == (unsigned)G.M) {                    // the last mode of this node range
-    __threadfence();
+  if (s_ticket == (unsigned)G.M) {                    // the last mode of this node range: its record
     double* s_re = a.conv;
     double* s_im = a.conv + nr;
-    double mx_old = 0.0, mx_new = 0.0;
+    int it_prev = 0, jp = 1;
+    if (t == 0 && a.L.iter_ctr) {                     // loop state, read in case this CTA decides
+      it_prev = __ldcg(a.L.iter_ctr);
+      if (a.L.stats && a.L.jp) jp = __ldcg(a.L.jp);
+    }
+    // maxima as the bit patterns of non-negative doubles: integer order is numeric order,
+    // so the max over nodes is exact, order independent and off the FP64 pipe
+    unsigned long long mo = 0ull, mn = 0ull;
     for (int k = t; k < Rc; k += blockDim.x) {
       const int i = r0 + k + 1;
       double bv[QPAD_MAX_PARTS];                     // every mode's B_phi here, loads in flight together
 #pragma unroll
       for (int p = 0; p < QPAD_MAX_PARTS; ++p) bv[p] = p < P ? __ldcg(a.b_spe + fidx(ld, 3, p, kCompConv, i)) : 0.0;
+      const double ore = __ldcg(s_re + i - 1), oim = __ldcg(s_im + i - 1);
       const auto Bc = [&](int p, int, int) {
         double v = 0.0;
 #pragma unroll
@@ -602,38 +622,39 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
           if (q == p) v = bv[q];
         return v;
       };
-      conv_node(G, Bc, kCompConv, i, s_re, s_im, true, mx_old, mx_new);
+      double nre, nim, xo = 0.0, xn = 0.0;
+      conv_node_v(G, Bc, kCompConv, i, ore, oim, true, nre, nim, xo, xn);
+      s_re[i - 1] = nre;
+      s_im[i - 1] = nim;
+      mo = max(mo, (unsigned long long)__double_as_longlong(xo));
+      mn = max(mn, (unsigned long long)__double_as_longlong(xn));
     }
     for (int off = 16; off > 0; off >>= 1) {
-      mx_old = fmax(mx_old, __shfl_down_sync(0xffffffffu, mx_old, off));
-      mx_new = fmax(mx_new, __shfl_down_sync(0xffffffffu, mx_new, off));
+      mo = max(mo, __shfl_down_sync(0xffffffffu, mo, off));
+      mn = max(mn, __shfl_down_sync(0xffffffffu, mn, off));
     }
-    __shared__ double rmo[kIterThreads / 32], rmn[kIterThreads / 32];
+    __shared__ unsigned long long rmo[kIterThreads / 32], rmn[kIterThreads / 32];
     if ((t & 31) == 0) {
-      rmo[t >> 5] = mx_old;
-      rmn[t >> 5] = mx_new;
+      rmo[t >> 5] = mo;
+      rmn[t >> 5] = mn;
     }
-    __syncthreads();
+    __syncthreads();                                  // also orders this CTA's record stores
     if (t == 0) {
       for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-        mx_old = fmax(mx_old, rmo[w]);
-        mx_new = fmax(mx_new, rmn[w]);
+        mo = max(mo, rmo[w]);
+        mn = max(mn, rmn[w]);
       }
-      a.slots[2 * rank] = mx_old;
-      a.slots[2 * rank + 1] = mx_new;
+      unsigned long long* mx = a.maxima;
+      if (mo) red_max_u64(mx, mo);
+      if (mn) red_max_u64(mx + 1, mn);
       a.tickets[rank] = 0u;
-      __threadfence();
-      const unsigned int done = atomicAdd(&a.tickets[CL], 1u);
-      if (done == (unsigned)(CL - 1)) {               // the last node range: the verdict
-        __threadfence();
-        double vo = 0.0, vn = 0.0;                      // max over the ranges (exact, any order)
-        for (int q = 0; q < CL; ++q) {
-          vo = fmax(vo, __ldcg(a.slots + 2 * q));
-          vn = fmax(vn, __ldcg(a.slots + 2 * q + 1));
-        }
-        conv_decide(vo, vn, a.reltol, a.abstol, a.conv + 2 * nr, a.L);
+      if (atom_add_acq_rel(&a.tickets[CL], 1u) == (unsigned)(CL - 1)) {   // the last range: the verdict
+        const unsigned long long vo = __ldcg(mx), vn = __ldcg(mx + 1);
+        mx[0] = 0ull;
+        mx[1] = 0ull;
         a.tickets[CL] = 0u;
-        __threadfence();
+        conv_decide_at(__longlong_as_double((long long)vo), __longlong_as_double((long long)vn), a.reltol, a.abstol,
+                       a.conv + 2 * nr, a.L, it_prev, jp);
       }
     }
   }
@@ -739,7 +760,7 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   a.gtab = ctx->precision == QPAD_PREC_MIXED ? ctx->gtab : nullptr;
   a.conv = ctx->conv;
   a.tickets = ctx->iter_tickets;
-  a.slots = reinterpret_cast<double*>(ctx->iter_tickets + 32);
+  a.maxima = reinterpret_cast<unsigned long long*>(ctx->iter_tickets + kIterMaxWords);
   a.L = ConvLoop{};
   if (loop_state) {
     a.L.iter_ctr = ctx->d_iter;

@@ -73,6 +73,7 @@ struct Beam;
 
 }  // namespace qpad
 
+static constexpr int kIterMaxWords = 64;      // k_iterate's two 64-bit maxima in the ticket buffer
 static constexpr int kIterErrWord = 127;       // k_iterate's error word in the ticket buffer
 
 struct qpad_ctx {
@@ -89,7 +90,7 @@ struct qpad_ctx {
   double* qn = nullptr;                        // neutralising background (sum over species)
   double* qraw = nullptr;                      // raw charge deposit scratch
   double* raw = nullptr;                       // raw current deposits of the loop [cu 3|amu 3|acu 2] x P x ld
-  unsigned int* iter_tickets = nullptr;        // [0,32) tickets, [32,96) maxima, [kIterErrWord] error word of k_iterate
+  unsigned int* iter_tickets = nullptr;        // [0,17) tickets, [64,68) maxima, [127] error word of k_iterate
   int iter_cl = 0, iter_rows = 0;              // cluster size and rows per CTA of k_iterate
   int item_ppl = 4;                            // particles per lane of a mixed deposit work item
   struct qpad_guess_state* guess = nullptr;    // learned predictor-corrector guess (learn.cu)

@@ -305,10 +305,10 @@ __device__ __forceinline__ void row_et(const GridDev& G, int m, int i, const BF&
 // squared distance of the old record from the new one (accumulated by the same sequential
 // subtraction) and the squared old record are folded into the running maxima.
 template <class BF>
-__device__ __forceinline__ void conv_node(const GridDev& G, const BF& B, int comp, int i, double* s_re, double* s_im,
-                                          bool compare, double& mx_old, double& mx_new) {
-  double nre = 0.0, nim = 0.0;
-  double ore = s_re[i - 1], oim = s_im[i - 1];
+__device__ __forceinline__ void conv_node_v(const GridDev& G, const BF& B, int comp, int i, double ore, double oim,
+                                            bool compare, double& nre, double& nim, double& mx_old, double& mx_new) {
+  nre = 0.0;
+  nim = 0.0;
   if (compare) mx_old = fmax(mx_old, ore * ore + oim * oim);
   for (int m = 0; m <= G.M; ++m) {
     const double vr = fabs(B(part_re(m), comp, i));
@@ -320,14 +320,21 @@ __device__ __forceinline__ void conv_node(const GridDev& G, const BF& B, int com
     if (compare) oim = oim - vi;
   }
   if (compare) mx_new = fmax(mx_new, ore * ore + oim * oim);
+}
+
+template <class BF>
+__device__ __forceinline__ void conv_node(const GridDev& G, const BF& B, int comp, int i, double* s_re, double* s_im,
+                                          bool compare, double& mx_old, double& mx_new) {
+  double nre, nim;
+  conv_node_v(G, B, comp, i, s_re[i - 1], s_im[i - 1], compare, nre, nim, mx_old, mx_new);
   s_re[i - 1] = nre;
   s_im[i - 1] = nim;
 }
 
 // The verdict from the maxima over nodes: relative and absolute residuals, convergence,
 // and the loop state (iteration count, statistics, WHILE condition).  One thread.
-__device__ inline void conv_decide(double mx_old, double mx_new, double reltol, double abstol, double* res,
-                                   const ConvLoop& L) {
+__device__ inline void conv_decide_at(double mx_old, double mx_new, double reltol, double abstol, double* res,
+                                      const ConvLoop& L, int it_prev, int jp) {
   const double old_norm = sqrt(mx_old), abs_res = sqrt(mx_new);
   const double rel = old_norm > 2.220446049250313e-16 ? abs_res / old_norm : 1.7976931348623157e308;
   const bool converged = rel < reltol || abs_res < abstol;
@@ -335,17 +342,23 @@ __device__ inline void conv_decide(double mx_old, double mx_new, double reltol, 
   res[1] = abs_res;
   res[2] = converged ? 1.0 : 0.0;
   if (L.iter_ctr) {
-    const int it = *L.iter_ctr + 1;
+    const int it = it_prev + 1;
     *L.iter_ctr = it;
     if (L.stats && L.jp) {
       qpad_slice_stats s;
       s.iters = it;
       s.rel_res = rel;
       s.abs_res = abs_res;
-      L.stats[*L.jp - 1] = s;
+      L.stats[jp - 1] = s;
     }
     if (L.use_h) cudaGraphSetConditional(L.h, (!converged && it < L.iter_max) ? 1u : 0u);
   }
+}
+
+__device__ inline void conv_decide(double mx_old, double mx_new, double reltol, double abstol, double* res,
+                                   const ConvLoop& L) {
+  conv_decide_at(mx_old, mx_new, reltol, abstol, res, L, L.iter_ctr ? *L.iter_ctr : 0,
+                 (L.iter_ctr && L.stats && L.jp) ? *L.jp : 1);
 }
 
 }  // namespace qpad
