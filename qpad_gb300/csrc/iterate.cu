@@ -580,17 +580,29 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   // guard nodes: b = b_spe + b_beam there too, and their gather-table records
   if (t < 2 && ((t == 0 && rank == 0) || (t == 1 && rank == CL - 1))) {
     const int i = t == 0 ? 0 : nr + 1;
-    for (int h = 0; h < nh; ++h) {
-      const int p = h == 0 ? pr : pi;
-      for (int c = (grp == 0 ? 0 : 2); c < (grp == 0 ? 2 : 3); ++c) {   // the group's components
-        const double v = a.b_spe[fidx(ld, 3, p, c, i)] + a.b_beam[fidx(ld, 3, p, c, i)];
-        a.b[fidx(ld, 3, p, c, i)] = v;
+    const int c0 = grp == 0 ? 0 : 2, nc = grp == 0 ? 2 : 1;   // the group's components
+    double vb[2][2], ve[2][2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)                       // every load before any store
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int p = h == 0 ? pr : pi;
+        const bool on = h < nh && c < nc;
+        vb[h][c] = on ? __ldcg(a.b_spe + fidx(ld, 3, p, c0 + c, i)) + __ldcg(a.b_beam + fidx(ld, 3, p, c0 + c, i)) : 0.0;
+        ve[h][c] = (on && a.gtab) ? __ldcg(a.e + fidx(ld, 3, p, c0 + c, i)) : 0.0;
+      }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        if (h >= nh || c >= nc) continue;
+        const int p = h == 0 ? pr : pi;
+        a.b[fidx(ld, 3, p, c0 + c, i)] = vb[h][c];
         if (a.gtab) {
-          a.gtab[((size_t)i * P + p) * 6 + 3 + c] = (float)v;
-          a.gtab[((size_t)i * P + p) * 6 + c] = (float)a.e[fidx(ld, 3, p, c, i)];
+          a.gtab[((size_t)i * P + p) * 6 + 3 + c0 + c] = (float)vb[h][c];
+          a.gtab[((size_t)i * P + p) * 6 + c0 + c] = (float)ve[h][c];
         }
       }
-    }
   }
 
   // ---- convergence test (group 0, which owns B-perp) ------------------------------------
