@@ -620,7 +620,9 @@ __device__ __forceinline__ double* store_slice(const GridDev& G, double* f2, int
 }
 
 // Start of slice j (simulation_class.f03:344-360): beam B-perp from the stored beam
-// charge; species charge (+ background) and psi; Bz from the carried current.
+// charge; species charge (+ background) and psi; Bz from the carried current; and the Ez
+// of the first iteration (:375-378), which also depends only on the carried current.
+// One CTA per (job, mode).
 __global__ void __launch_bounds__(kFieldThreads) k_slice_begin(GridDev G, const double* __restrict__ fac,
                                                                SliceFields F, const int* __restrict__ jp,
                                                                int use_qn) {
@@ -635,24 +637,72 @@ __global__ void __launch_bounds__(kFieldThreads) k_slice_begin(GridDev G, const 
   } else if (job == 1) {
     op_finish_q(G, m, F.qraw, use_qn ? F.qn : nullptr, F.f[QPAD_F_Q_SPE]);
     op_psi(G, m, fac, sm, sc, F.f[QPAD_F_Q_SPE], F.f[QPAD_F_PSI]);
-  } else {
+  } else if (job == 2) {
     op_bz(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_B_SPE]);
+  } else {
+    op_ez(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_E]);
   }
 }
 
-// Iteration phase 1 (simulation_class.f03:375-380): b = b_spe + b_beam, Ez(cu), E-perp(b,psi);
-// then cu = acu = amu = 0 for the deposit that follows.
-__global__ void __launch_bounds__(kFieldThreads) k_iter_e(GridDev G, const double* __restrict__ fac, SliceFields F) {
-  extern __shared__ double sm[];
-  __shared__ double sc[6 * 32 + 8];
-  const int m = blockIdx.x;
-  op_add(G, m, 3, F.f[QPAD_F_B_SPE], F.f[QPAD_F_B_BEAM], F.f[QPAD_F_B]);
-  op_ez(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_E]);
-  op_et(G, m, F.f[QPAD_F_B], F.f[QPAD_F_PSI], F.f[QPAD_F_E]);
-  if (F.gtab) op_write_gtab(G, m, F.f[QPAD_F_E], F.f[QPAD_F_B], F.gtab);
-  op_fill(G, m, 3, F.f[QPAD_F_CU], 0.0);
-  op_fill(G, m, 2, F.f[QPAD_F_ACU], 0.0);
-  op_fill(G, m, 3, F.f[QPAD_F_AMU], 0.0);
+// Rest of the first iteration's phase 1 (simulation_class.f03:375-380), one thread per
+// (mode, node): b = b_spe + b_beam, E-perp(b, psi), the FP32 gather table; then
+// cu = acu = amu = 0 for the deposit that follows.  Ez came from k_slice_begin.
+__global__ void __launch_bounds__(256) k_iter_e(GridDev G, SliceFields F) {
+  const int ld = G.ld;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (G.M + 1) * ld) return;
+  const int m = q / ld, i = q % ld;
+  const int nh = m == 0 ? 1 : 2;
+  const int pr = part_re(m), pi = part_im(m);
+  const double* bs = F.f[QPAD_F_B_SPE];
+  const double* bb = F.f[QPAD_F_B_BEAM];
+  double* b = F.f[QPAD_F_B];
+  double* e = F.f[QPAD_F_E];
+  double bv[2][3];
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int p = h == 0 ? pr : pi;
+      bv[h][c] = h < nh ? FLD(bs, 3, p, c, i) + FLD(bb, 3, p, c, i) : 0.0;
+    }
+  double ev[2][3];
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) ev[h][c] = h < nh ? FLD(e, 3, h == 0 ? pr : pi, c, i) : 0.0;
+  if (i >= 1 && i <= G.nr) {
+    const auto B = [&](int p, int c, int) { return p == pr ? bv[0][c] : bv[1][c]; };
+    double o[4];
+    row_et(G, m, i, B, GlobalF{F.f[QPAD_F_PSI], ld, 1}, o);
+    if (m == 0) {
+      ev[0][0] = o[0];
+      ev[0][1] = o[1];
+    } else {
+      ev[0][0] = o[0];
+      ev[1][0] = o[1];
+      ev[0][1] = o[2];
+      ev[1][1] = o[3];
+    }
+  }
+  for (int h = 0; h < nh; ++h) {
+    const int p = h == 0 ? pr : pi;
+    for (int c = 0; c < 3; ++c) FLD(b, 3, p, c, i) = bv[h][c];
+    if (i >= 1 && i <= G.nr)
+      for (int c = 0; c < 2; ++c) FLD(e, 3, p, c, i) = ev[h][c];
+    if (F.gtab) {
+      float* T = F.gtab + ((size_t)i * G.P + p) * 6;
+      for (int c = 0; c < 3; ++c) {
+        T[c] = (float)ev[h][c];
+        T[3 + c] = (float)bv[h][c];
+      }
+    }
+    for (int c = 0; c < 3; ++c) {
+      FLD(F.f[QPAD_F_CU], 3, p, c, i) = 0.0;
+      FLD(F.f[QPAD_F_AMU], 3, p, c, i) = 0.0;
+    }
+    for (int c = 0; c < 2; ++c) FLD(F.f[QPAD_F_ACU], 2, p, c, i) = 0.0;
+  }
 }
 
 // Iteration phase 2 (simulation_class.f03:386-392): finish the deposits, dJ/dxi, B-perp
@@ -806,8 +856,7 @@ int raise_dyn_smem(qpad_ctx* ctx, const void* func, size_t bytes) {
 static int ensure_smem_attr(qpad_ctx* ctx) {
   if (ctx->field_attr_done) return 0;
   const size_t need = field_smem(ctx);
-  const void* ks[] = {(const void*)k_field_op, (const void*)k_slice_begin, (const void*)k_iter_e,
-                      (const void*)k_iter_b};
+  const void* ks[] = {(const void*)k_field_op, (const void*)k_slice_begin, (const void*)k_iter_b};
   for (const void* k : ks)
     if (int r = raise_dyn_smem(ctx, k, need)) return r;
   ctx->field_attr_done = true;
@@ -852,16 +901,16 @@ int launch_advance(qpad_ctx* ctx, cudaGraphConditionalHandle hs, cudaGraphCondit
 int launch_slice_begin(qpad_ctx* ctx, int use_qn) {
   if (int r = ensure_smem_attr(ctx)) return r;
   prof_begin(ctx, "slice_begin");
-  k_slice_begin<<<3 * (ctx->g.M + 1), kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac,
+  k_slice_begin<<<4 * (ctx->g.M + 1), kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac,
                                                                                      slice_fields(ctx), ctx->d_j, use_qn);
   prof_end(ctx, "slice_begin");
   return check_launch(ctx, "k_slice_begin");
 }
 
 int launch_iter_e(qpad_ctx* ctx) {
-  if (int r = ensure_smem_attr(ctx)) return r;
+  const int n = (ctx->g.M + 1) * ctx->g.ld;
   prof_begin(ctx, "iter_e");
-  k_iter_e<<<ctx->g.M + 1, kFieldThreads, field_smem(ctx), ctx->stream>>>(ctx->g, ctx->fac, slice_fields(ctx));
+  k_iter_e<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->g, slice_fields(ctx));
   prof_end(ctx, "iter_e");
   return check_launch(ctx, "k_iter_e");
 }
