@@ -336,8 +336,12 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   // ---- sources: (node, equation group) per thread ---------------------------------------
   // group 0: dJ/dxi and the B+ / B- right-hand sides; group 1: Bz; group 2: Ez
   double div = 0.0;
-  for (int q = t; q < (grp == 0 ? 1 : 2) * Rc; q += blockDim.x) {
-    const int job = (grp == 0 ? 0 : 1) + q / Rc, k = q % Rc, i = r0 + k + 1;
+  // rows 1, 2 and nr take boundary stencils: they go to the last warp's threads so that
+  // the other warps do not wait out their branch
+  const auto special = [&](int i) { return i <= 2 || i == nr; };
+  const int njob = grp == 0 ? 1 : 2;
+  const auto source_row = [&](int job, int k) {
+    const int i = r0 + k + 1;
     if (job == 0) {
       double dj[4];
       row_djdxi(G, m, i, ACU, AMU, dj);
@@ -366,6 +370,23 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
       if (in_div) div += er * (double)(i - 1);
       dsm[3 * R + k] = er;
       if (m > 0) dsm[7 * R + k] = ei;
+    }
+  };
+  for (int q = t; q < njob * Rc; q += blockDim.x) {
+    const int job = (grp == 0 ? 0 : 1) + q / Rc, k = q % Rc;
+    if (!special(r0 + k + 1)) source_row(job, k);
+  }
+  {
+    // this CTA's boundary rows: candidates k = 0, 1, Rc - 1
+    const bool v0 = Rc > 0 && special(r0 + 1), v1 = Rc > 1 && special(r0 + 2), v2 = Rc > 2 && special(r0 + Rc);
+    const int ns = (int)v0 + (int)v1 + (int)v2;
+    const int sidx = (int)blockDim.x - 1 - t;
+    if (sidx < njob * ns) {
+      int w = sidx % ns, k = -1;
+      if (v0) k = w-- == 0 ? 0 : k;
+      if (v1 && k < 0) k = w-- == 0 ? 1 : k;
+      if (v2 && k < 0) k = w == 0 ? Rc - 1 : k;
+      source_row((grp == 0 ? 0 : 1) + sidx / ns, k);
     }
   }
   // the m = 0 axis row of Ez needs the weighted sum over the whole line
@@ -506,8 +527,8 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
 
   // ---- fields of the owned nodes: (node, group) per thread ------------------------------
   // group 0: B-perp from B+ / B-, b = b_spe + b_beam and E-perp; group 1: Bz and Ez
-  for (int q = t; q < Rc; q += blockDim.x) {
-    const int job = grp, k = q, i = r0 + k + 1;
+  const auto field_row = [&](int k) {
+    const int job = grp, i = r0 + k + 1;
     if (job == 0) {
       double bs[2][2], bb[2][2];
       if (m == 0) {
@@ -576,34 +597,24 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
         }
       }
     }
+  };
+  for (int q = t; q < Rc; q += blockDim.x)
+    if (!special(r0 + q + 1)) field_row(q);
+  {
+    const bool v0 = Rc > 0 && special(r0 + 1), v1 = Rc > 1 && special(r0 + 2), v2 = Rc > 2 && special(r0 + Rc);
+    const int ns = (int)v0 + (int)v1 + (int)v2;
+    const int sidx = (int)blockDim.x - 1 - t;
+    if (sidx < ns) {
+      int w = sidx, k = -1;
+      if (v0) k = w-- == 0 ? 0 : k;
+      if (v1 && k < 0) k = w-- == 0 ? 1 : k;
+      if (v2 && k < 0) k = w == 0 ? Rc - 1 : k;
+      field_row(k);
+    }
   }
-  // guard nodes: b = b_spe + b_beam there too, and their gather-table records
-  if (t < 2 && ((t == 0 && rank == 0) || (t == 1 && rank == CL - 1))) {
-    const int i = t == 0 ? 0 : nr + 1;
-    const int c0 = grp == 0 ? 0 : 2, nc = grp == 0 ? 2 : 1;   // the group's components
-    double vb[2][2], ve[2][2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h)                       // every load before any store
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        const int p = h == 0 ? pr : pi;
-        const bool on = h < nh && c < nc;
-        vb[h][c] = on ? __ldcg(a.b_spe + fidx(ld, 3, p, c0 + c, i)) + __ldcg(a.b_beam + fidx(ld, 3, p, c0 + c, i)) : 0.0;
-        ve[h][c] = (on && a.gtab) ? __ldcg(a.e + fidx(ld, 3, p, c0 + c, i)) : 0.0;
-      }
-#pragma unroll
-    for (int h = 0; h < 2; ++h)
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        if (h >= nh || c >= nc) continue;
-        const int p = h == 0 ? pr : pi;
-        a.b[fidx(ld, 3, p, c0 + c, i)] = vb[h][c];
-        if (a.gtab) {
-          a.gtab[((size_t)i * P + p) * 6 + 3 + c0 + c] = (float)vb[h][c];
-          a.gtab[((size_t)i * P + p) * 6 + c0 + c] = (float)ve[h][c];
-        }
-      }
-  }
+
+  // guard nodes (0, nr + 1): nothing here writes b_spe or E there, so b = b_spe + b_beam and
+  // their gather-table records stay as k_iter_e wrote them at the start of the slice
 
   // ---- convergence test (group 0, which owns B-perp) ------------------------------------
   if (grp == 0) {
