@@ -1000,7 +1000,7 @@ int enqueue_iteration(qpad_ctx* ctx, cudaGraphConditionalHandle h, int use_h) {
                         : species_amjdp_raw(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], rcu, ramu, racu, ctx->g.dxi);
     if (r) return r;
   }
-  return launch_iterate(ctx, 1, h, use_h);
+  return launch_iterate(ctx, 1, h, use_h, 1);
 }
 
 // Epilogue (simulation_class.f03:403-456): stores, final fields, J-perp predictor, push.
@@ -1132,7 +1132,8 @@ int build_step_graph(qpad_ctx* ctx) {
 
 std::string step_key(const qpad_ctx* ctx) {
   std::string k = std::to_string(ctx->precision) + "/" + std::to_string(ctx->iter_cl) + "/" +
-                  std::to_string(ctx->item_ppl) + "/" + std::to_string(ctx->guess != nullptr);
+                  std::to_string(ctx->item_ppl) + "/" + std::to_string(ctx->guess != nullptr) + "/" +
+                  std::to_string(ctx->pdl);
   for (auto* s : ctx->species)
     k += "|" + std::to_string((long long)s->np) + ":" + std::to_string(s->push_type) + ":" +
          std::to_string(s->neutralized) + ":" + std::to_string(s->sort_freq);
@@ -1247,13 +1248,19 @@ extern "C" int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* sta
   if (use_graph) {
     const std::string key = step_key(ctx);
     if (!ctx->step_exec || ctx->step_key != key) {
-      if (int r = build_step_graph(ctx)) {
+      int rb = build_step_graph(ctx);
+      if (rb && ctx->pdl) {                          // a graph with programmatic edges was refused:
+        cudaGetLastError();                          // build it with plain edges
+        ctx->pdl = false;
+        rb = build_step_graph(ctx);
+      }
+      if (int r = rb) {
         ctx->graph_status = "graph build failed: " + ctx->err;
         ctx->use_graph = false;
         use_graph = false;
         cudaGetLastError();
       } else {
-        ctx->step_key = key;
+        ctx->step_key = step_key(ctx);
       }
     }
   }
@@ -1333,18 +1340,29 @@ extern "C" int qpad_batch_step(qpad_batch* b, int push_beams, qpad_slice_stats* 
       cudaGraphExecDestroy(b->exec);
       b->exec = nullptr;
     }
-    cudaGraph_t top = nullptr;
-    int r = cudaGraphCreate(&top, 0) == cudaSuccess ? 0 : QPAD_E_CUDA;
-    for (int i = 0; i < n && !r; ++i) {
-      r = add_slice_loop(b->ctxs[i], top);
-      if (r) b->err = "simulation " + std::to_string(i) + ": " + b->ctxs[i]->err;
+    const auto attempt = [&]() {
+      cudaGraph_t top = nullptr;
+      int r = cudaGraphCreate(&top, 0) == cudaSuccess ? 0 : QPAD_E_CUDA;
+      for (int i = 0; i < n && !r; ++i) {
+        r = add_slice_loop(b->ctxs[i], top);
+        if (r) b->err = "simulation " + std::to_string(i) + ": " + b->ctxs[i]->err;
+      }
+      if (!r && cudaGraphInstantiate(&b->exec, top, 0) != cudaSuccess) {
+        b->err = "batch graph instantiate failed";
+        r = QPAD_E_CUDA;
+      }
+      if (top && !r) cudaGraphDestroy(top);      // left alone after a failed capture, as above
+      cudaGetLastError();
+      return r;
+    };
+    int r = attempt();
+    bool any_pdl = false;
+    for (auto* c : b->ctxs) any_pdl |= c->pdl;
+    if (r && any_pdl) {                          // programmatic edges refused: plain edges
+      for (auto* c : b->ctxs) c->pdl = false;
+      b->exec = nullptr;
+      r = attempt();
     }
-    if (!r && cudaGraphInstantiate(&b->exec, top, 0) != cudaSuccess) {
-      b->err = "batch graph instantiate failed";
-      r = QPAD_E_CUDA;
-    }
-    if (top && !r) cudaGraphDestroy(top);        // left alone after a failed capture, as above
-    cudaGetLastError();
     if (r) return r;
     for (int i = 0; i < n; ++i) b->keys[i] = step_key(b->ctxs[i]);
   }

@@ -73,6 +73,10 @@ __device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
   asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;\n" : "=r"(old) : "l"(p), "r"(v) : "memory");
   return old;
 }
+// Programmatic dependent launch: wait for the grid this one depends on (no-op when the
+// launch carried no programmatic dependency).
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
 __device__ __forceinline__ void red_max_u64(unsigned long long* p, unsigned long long v) {
   asm volatile("red.relaxed.gpu.global.max.u64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
 }
@@ -243,6 +247,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     const int kind = ka == 0 ? OK_BPLUS : ka == 1 ? OK_BMINUS : OK_GEN;
     return a.fac + fac_off(nr, a.G.M, kind, m) + (size_t)arr * nr + r0;
   };
+  const auto is_raw_row = [&](int k) { return k >= 2 && k < 2 + c8_n * nh; };   // written by the deposit
   // window slots outside the grid are zero
   for (int q = t; q < nwin * W; q += blockDim.x) {
     const int k = q / W, x = q % W;
@@ -289,17 +294,24 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
                    : "memory");
     }
     __syncwarp();
-    if (ok)
-      for (int k = t; k < ncp; k += 32) {
-        void* dst;
-        const void* src;
-        unsigned bytes;
-        row_copy(k, dst, src, bytes);
-        if (bytes) bulk_g2s(dst, src, bytes, &mbar);
-      }
+    // rows that the deposit before this kernel does not write first; the raw deposit rows
+    // after the programmatic wait (a no-op unless launched as a dependent of the deposit)
+    for (int pass = 0; pass < 2; ++pass) {
+      if (pass == 1) griddep_wait();
+      if (ok)
+        for (int k = t; k < ncp; k += 32) {
+          if (is_raw_row(k) != (pass == 1)) continue;
+          void* dst;
+          const void* src;
+          unsigned bytes;
+          row_copy(k, dst, src, bytes);
+          if (bytes) bulk_g2s(dst, src, bytes, &mbar);
+        }
+    }
     if (t == 0) s_bulk = ok;
   }
   __syncthreads();                                    // s_bulk and the mbarrier are set up
+  griddep_wait();                                     // nothing below runs before the deposit is complete
   if (s_bulk) {
     int spins = 0;
     while (!mbar_try_wait(&mbar, 0u))
@@ -314,6 +326,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
       win_row(k, dst, src);
       for (int x = n0 - wb + t; x < n1 - wb; x += blockDim.x) cp_async8(dst + x, src + wb + x);
     }
+    // (this path issues every row after the programmatic wait)
     for (int row = fr0; row < fr1; ++row) {
       const double* src = fac_src(row);
       for (int k = t; k < Rc; k += blockDim.x) cp_async8(facs + row * R + k, src + k);
@@ -765,7 +778,7 @@ int iterate_setup(qpad_ctx* ctx) {
   return set_err(ctx, QPAD_E_CUDA, "no cluster shape of the iteration kernel fits this grid and GPU");
 }
 
-int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h) {
+int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h, int after_deposit) {
   if (int r = iterate_setup(ctx)) return r;
   IterArgs a;
   a.G = ctx->g;
@@ -805,13 +818,17 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   cfg.blockDim = dim3(kIterThreads);
   cfg.dynamicSmemBytes = iterate_smem_doubles(a.R, ctx->g.ld) * sizeof(double);
   cfg.stream = ctx->stream;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = cl;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  // directly after the plasma deposit: start as its programmatic dependent, so that the
+  // launch and the staging of everything the deposit does not write overlap it
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = (after_deposit && ctx->pdl) ? 2 : 1;
   prof_begin(ctx, "iterate");
   cudaError_t e = cudaLaunchKernelEx(&cfg, k_iterate, a);
   prof_end(ctx, "iterate");

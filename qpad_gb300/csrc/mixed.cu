@@ -280,6 +280,8 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
                                                          MArr A, const float* __restrict__ T, double* __restrict__ cu,
                                                          double* __restrict__ amu, double* __restrict__ acu,
                                                          int write_back) {
+  // the field iteration launched after this kernel may start its own staging now
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   const int lane = threadIdx.x & 31;
   const int it = blockIdx.x * (kItemThreads / 32) + (threadIdx.x >> 5);
   if (it >= *n_items) return;                          // warp-uniform

@@ -68,6 +68,8 @@ __global__ void __launch_bounds__(kPartThreads) k_amjdp(GridDev G, int push_type
                                                         const double* __restrict__ ef, const double* __restrict__ bf,
                                                         double* __restrict__ cu, double* __restrict__ amu,
                                                         double* __restrict__ acu) {
+  // the field iteration launched after this kernel may start its own staging now
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   const int64_t n = *n_ptr;
   const int64_t pp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (pp >= n) return;

@@ -93,6 +93,7 @@ struct qpad_ctx {
   unsigned int* iter_tickets = nullptr;        // [0,17) tickets, [64,68) maxima, [127] error word of k_iterate
   int iter_cl = 0, iter_rows = 0;              // cluster size and rows per CTA of k_iterate
   int item_ppl = 4;                            // particles per lane of a mixed deposit work item
+  bool pdl = true;                             // k_iterate as programmatic dependent of the deposit
   struct qpad_guess_state* guess = nullptr;    // learned predictor-corrector guess (learn.cu)
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
   float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
@@ -216,7 +217,8 @@ void guess_free(qpad_ctx* ctx);
 // one predictor-corrector iteration after the deposit, as a cluster kernel (iterate.cu)
 int iterate_setup(qpad_ctx* ctx);
 int iterate_try_cluster(qpad_ctx* ctx, int cl);
-int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h);
+int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h,
+                   int after_deposit = 0);
 
 // ---- particle kernels (plasma.cu, beam.cu) ---------------------------------------------
 int species_qdeposit_raw(qpad_species* sp, double* qraw);
