@@ -344,20 +344,32 @@ def run_ours(args):
                        "iters_change": g["iters_per_slice"] / r["iters_per_slice"] - 1.0,
                        "weights": os.path.relpath(DEFAULT_OUT, ROOT)}
     kern = r["kern"]
-    amj_ms, namj = kern["amjdp"]
     peak, peak_kind = _peaks()
-    # algorithmic bytes per particle of one amjdp pass: FP64 reads x, y, px, py, pz, q and
-    # writes gamma, psi (64 B); mixed reads the cell word, two offsets, three momenta and q (28 B)
+    traffic = {}
+    tf = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf))["dram_bytes_per_launch"].get(args.precision, {})
+        except Exception:
+            traffic = {}
+    # the dominant kernel, k_iterate: algorithmic bytes of one launch (every mode) -- it reads
+    # the raw deposits (8 components), psi, B_old (2), b_beam (3), the factor rows of its three
+    # matrices and the node tables; it writes the finished deposits (8), zeroes the raw ones
+    # (8), writes dJ/dxi (2), b_spe, b, E (3 each), the convergence record and, on the mixed
+    # path, the FP32 gather table (6 floats per node and part)
+    ld, P = deck.nr + 2, 2 * deck.max_mode + 1
+    it_bytes = 8 * ((8 + 1 + 2 + 3) * P * ld + 9 * deck.nr * (deck.max_mode + 1) + 2 * ld) \
+        + 8 * ((8 + 8 + 2 + 3 + 3 + 3) * P * ld + 2 * deck.nr) + (4 * 6 * P * ld if prec == K.PREC_MIXED else 0)
+    it_ms, nit = kern["iterate"]
+    it_avg_s = (it_ms / 1e3) / max(nit, 1)
+    it_ach = it_bytes / it_avg_s / 1e9 if nit else None
+    # the deposit: algorithmic bytes per particle of one amjdp pass: FP64 reads x, y, px, py,
+    # pz, q and writes gamma, psi (64 B); mixed reads the cell word, two offsets, three
+    # momenta and q (28 B)
+    amj_ms, namj = kern["amjdp"]
     bytes_per_particle = 64 if prec == K.PREC_FP64 else 28
     amj_avg_s = (amj_ms / 1e3) / max(namj, 1)
     achieved = bytes_per_particle * npl / amj_avg_s / 1e9 if namj else None
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "amjdp_traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get(args.precision)
-        except Exception:
-            traffic = None
     dev_s = r["dev_s"]
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -375,10 +387,18 @@ def run_ours(args):
         "wall_s": r["wall_s"],
         "e2e": r["e2e"],
         "gpu_launches": r["launches"],
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "k_amjdp" if prec == K.PREC_FP64 else "k_mamjdp", "peak_kind": peak_kind,
-                     "bytes_per_launch": bytes_per_particle * npl, "avg_launch_us": amj_avg_s * 1e6},
+        "roofline": {"bound": "hbm", "achieved": it_ach, "peak": peak, "unit": "GB/s",
+                     "frac": (it_ach / peak) if it_ach else None, "traffic": traffic.get("k_iterate"),
+                     "kernel": "k_iterate", "peak_kind": peak_kind, "bytes_per_launch": it_bytes,
+                     "avg_launch_us": it_avg_s * 1e6,
+                     "limiter": "latency: dependent FP64 chains and CTA/cluster barriers on an L2-resident "
+                                "per-slice working set"},
+        "roofline_deposit": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": (achieved / peak) if achieved else None,
+                             "traffic": traffic.get("k_amjdp" if prec == K.PREC_FP64 else "k_mamjdp"),
+                             "kernel": "k_amjdp" if prec == K.PREC_FP64 else "k_mamjdp", "peak_kind": peak_kind,
+                             "bytes_per_launch": bytes_per_particle * npl, "avg_launch_us": amj_avg_s * 1e6,
+                             "limiter": "latency: particle and gather-table loads, one warp per cell work item"},
         "clocks": r["clocks"],
         "graph": r["graph"],
         "autotune": r["tune"],

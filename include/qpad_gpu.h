@@ -223,7 +223,7 @@ int qpad_batch_step(qpad_batch* batch, int push_beams, qpad_slice_stats* const* 
 /* ---- autotuner (no counterpart in the reference) ---------------------------------------
  * Times the launch shapes this context can use on this GPU and keeps the fastest: the
  * cluster size of the fused predictor-corrector kernel (16, 8, 4, 2, 1 CTAs per mode) and,
- * on the mixed path, the particles per lane of the deposit work items (2 or 4).  Runs
+ * on the mixed path, the particles per lane of the deposit work items (1, 2 or 4).  Runs
  * `reps` timed launches of each; overwrites the slice fields (call it before a 3D step). */
 typedef struct qpad_tune_result {
   int32_t iter_cluster;       /* CTAs per mode of the iteration kernel */

@@ -1447,7 +1447,7 @@ extern "C" int qpad_autotune(qpad_ctx* ctx, int reps, qpad_tune_result* out) {
     const size_t P1 = (size_t)ctx->g.P * ctx->g.ld;
     double bestd = 1e30;
     int best_ppl = ctx->item_ppl;
-    for (int ppl : {2, 4}) {
+    for (int ppl : {1, 2, 4}) {
       ctx->item_ppl = ppl;
       for (auto* s : ctx->species)
         if (!r) r = mixed_index(s);

@@ -26,8 +26,8 @@ namespace qpad {
 
 static constexpr int kMixThreads = 256;
 // A deposit work item is one warp's worth of particles of one cell: 32 * PPL of them,
-// PPL = ctx->item_ppl in {2, 4} (chosen by qpad_autotune, 4 by default).
-static constexpr int kMinItem = 64;                       // smallest work item (sizes the item list)
+// PPL = ctx->item_ppl in {1, 2, 4} (chosen by qpad_autotune, 4 by default).
+static constexpr int kMinItem = 32;                       // smallest work item (sizes the item list)
 static constexpr int kItemThreads = 128;                  // four work items per CTA
 #define FULL 0xffffffffu
 
@@ -695,7 +695,9 @@ int mixed_qdeposit_raw(qpad_species* sp, double* qraw) {
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
   prof_begin(ctx, "qdeposit");
-  if (ctx->item_ppl == 2)
+  if (ctx->item_ppl == 1)
+    k_mqdeposit<1><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
+  else if (ctx->item_ppl == 2)
     k_mqdeposit<2><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
   else
     k_mqdeposit<4><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
@@ -707,7 +709,11 @@ int mixed_amjdp_raw(qpad_species* sp, const float* gtab, double* cu, double* amu
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
   prof_begin(ctx, "amjdp");
-  if (ctx->item_ppl == 2)
+  if (ctx->item_ppl == 1)
+    k_mamjdp<1><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
+                                                                   sp->items, sp->d_nitems, marr(sp, 0), gtab, cu, amu,
+                                                                   acu, 0);
+  else if (ctx->item_ppl == 2)
     k_mamjdp<2><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
                                                                    sp->items, sp->d_nitems, marr(sp, 0), gtab, cu, amu,
                                                                    acu, 0);

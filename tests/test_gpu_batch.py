@@ -53,7 +53,7 @@ def test_autotune_keeps_results(precision):
     b = Q.build_simulation(d, precision=precision)
     res = b.autotune(reps=5)
     assert res["iter_cluster"] in (1, 2, 4, 8, 16) and res["iter_us"] > 0
-    assert res["item_ppl"] in (2, 4)
+    assert res["item_ppl"] in (1, 2, 4)
     ib, _ = b.run_3d_step()
     tol = 1e-9 if precision == Q._capi.PREC_FP64 else 1e-4
     if precision == Q._capi.PREC_FP64:
