@@ -629,6 +629,34 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   // guard nodes (0, nr + 1): nothing here writes b_spe or E there, so b = b_spe + b_beam and
   // their gather-table records stay as k_iter_e wrote them at the start of the slice
 
+  // ---- stores nothing in this kernel waits for: the finished deposits, dJ/dxi, and the
+  // cleared raw deposits (every CTA of the cluster staged its window before the forward
+  // barrier); threads first, first + stride, ...
+  const auto late_stores = [&](int first, int stride) {
+    const int i0 = rank == 0 ? 0 : r0 + 1, i1 = rank == CL - 1 ? nr + 1 : r1;
+    const int nn = i1 - i0 + 1;
+    for (int q = first; q < c8_n * nh * nn; q += stride) {
+      const int c8 = c8_lo + q / (nh * nn), h = (q / nn) % nh, i = i0 + q % nn;
+      const int p = h == 0 ? pr : pi;
+      const double v = win[(c8 * 2 + h) * W + (i - wb)];
+      if (c8 < 3) {
+        a.cu[fidx(ld, 3, p, c8, i)] = v;
+        raw_cu[fidx(ld, 3, p, c8, i)] = 0.0;
+      } else if (c8 < 6) {
+        a.amu[fidx(ld, 3, p, c8 - 3, i)] = v;
+        raw_amu[fidx(ld, 3, p, c8 - 3, i)] = 0.0;
+      } else {
+        a.acu[fidx(ld, 2, p, c8 - 6, i)] = v;
+        raw_acu[fidx(ld, 2, p, c8 - 6, i)] = 0.0;
+      }
+    }
+    for (int q = first; q < (grp == 0 ? 2 * nh * Rc : 0); q += stride) {
+      const int c = q / (nh * Rc), h = (q / Rc) % nh, k = q % Rc;
+      a.dcu[fidx(ld, 2, h == 0 ? pr : pi, c, r0 + k + 1)] = djs[(2 * h + c) * R + k];
+    }
+  };
+  bool late_done = false;
+
   // ---- convergence test (group 0, which owns B-perp) ------------------------------------
   if (grp == 0) {
   __syncthreads();                                    // this CTA's B-perp is written
@@ -645,7 +673,13 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     // maxima as the bit patterns of non-negative doubles: integer order is numeric order,
     // so the max over nodes is exact, order independent and off the FP64 pipe
     unsigned long long mo = 0ull, mn = 0ull;
-    for (int k = t; k < Rc; k += blockDim.x) {
+    // the warps the record needs take it; the others issue the late stores meanwhile
+    const int rth = min((int)blockDim.x, 32 * ((Rc + 31) / 32));
+    if (rth < (int)blockDim.x) {
+      if (t >= rth) late_stores(t - rth, (int)blockDim.x - rth);
+      late_done = true;
+    }
+    for (int k = t; k < Rc && t < rth; k += rth) {
       const int i = r0 + k + 1;
       double bv[QPAD_MAX_PARTS];                     // every mode's B_phi here, loads in flight together
 #pragma unroll
@@ -696,32 +730,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   }
   }
 
-  // ---- stores nothing in this kernel waits for: the finished deposits, dJ/dxi, and the
-  // cleared raw deposits (every CTA of the cluster staged its window before the forward
-  // barrier)
-  {
-    const int i0 = rank == 0 ? 0 : r0 + 1, i1 = rank == CL - 1 ? nr + 1 : r1;
-    const int nn = i1 - i0 + 1;
-    for (int q = t; q < c8_n * nh * nn; q += blockDim.x) {
-      const int c8 = c8_lo + q / (nh * nn), h = (q / nn) % nh, i = i0 + q % nn;
-      const int p = h == 0 ? pr : pi;
-      const double v = win[(c8 * 2 + h) * W + (i - wb)];
-      if (c8 < 3) {
-        a.cu[fidx(ld, 3, p, c8, i)] = v;
-        raw_cu[fidx(ld, 3, p, c8, i)] = 0.0;
-      } else if (c8 < 6) {
-        a.amu[fidx(ld, 3, p, c8 - 3, i)] = v;
-        raw_amu[fidx(ld, 3, p, c8 - 3, i)] = 0.0;
-      } else {
-        a.acu[fidx(ld, 2, p, c8 - 6, i)] = v;
-        raw_acu[fidx(ld, 2, p, c8 - 6, i)] = 0.0;
-      }
-    }
-    for (int q = t; q < (grp == 0 ? 2 * nh * Rc : 0); q += blockDim.x) {
-      const int c = q / (nh * Rc), h = (q / Rc) % nh, k = q % Rc;
-      a.dcu[fidx(ld, 2, h == 0 ? pr : pi, c, r0 + k + 1)] = djs[(2 * h + c) * R + k];
-    }
-  }
+  if (!late_done) late_stores(t, (int)blockDim.x);
   cluster_wait();
 }
 
