@@ -276,7 +276,8 @@ def run_batch(args):
     value = pushes * args.steps / wall
     seq = None
     if not args.no_compare:                     # the same simulations one after another
-        for s in sims:
+        for s in sims:                          # with their single-simulation (latency) shapes
+            s.autotune(reps=10)
             s.species[0].reset()
         t1 = time.perf_counter()
         for s in sims:

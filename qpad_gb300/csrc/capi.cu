@@ -1284,6 +1284,7 @@ struct qpad_batch {
   cudaEvent_t done = nullptr;       // the batch graph is done
   cudaStream_t stream = nullptr;
   cudaGraphExec_t exec = nullptr;
+  bool shaped = false;              // the iteration kernels' cluster shapes are set for the batch
   std::string err;
 };
 
@@ -1333,6 +1334,21 @@ extern "C" int qpad_batch_step(qpad_batch* b, int push_beams, qpad_slice_stats* 
       b->err = "simulation " + std::to_string(i) + " cannot run as a graph (sorting every few slices or graph off)";
       return QPAD_E_STATE;
     }
+  // a batch is throughput-bound: every simulation's iteration kernel takes the smallest
+  // cluster that fits its grid (the most rows per CTA, the fewest CTAs), which the
+  // single-simulation autotuner, tuning for latency, does not choose
+  if (!b->shaped) {
+    for (auto* c : b->ctxs) {
+      int r = QPAD_E_CUDA;
+      for (int cl = 1; cl <= 16 && r; cl *= 2) r = iterate_try_cluster(c, cl);
+      cudaGetLastError();
+      if (r) {
+        b->err = "no cluster shape of the iteration kernel fits: " + c->err;
+        return r;
+      }
+    }
+    b->shaped = true;
+  }
   bool rebuild = !b->exec;
   for (int i = 0; i < n; ++i) rebuild |= (b->keys[i] != step_key(b->ctxs[i]));
   if (rebuild) {
