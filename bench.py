@@ -350,7 +350,9 @@ def run_ours(args):
     tf = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.json")
     if os.path.exists(tf):
         try:
-            traffic = json.load(open(tf))["dram_bytes_per_launch"].get(args.precision, {})
+            # captured per workload; the profiling runs shorten the deck (same slice workload)
+            wl = deck.name.split("_nz")[0]
+            traffic = json.load(open(tf))["dram_bytes_per_launch"].get(wl, {}).get(args.precision, {})
         except Exception:
             traffic = {}
     # the dominant kernel, k_iterate: algorithmic bytes of one launch (every mode) -- it reads
