@@ -14,8 +14,8 @@ from tests.helpers import beam_to_oracle, field_errors, plasma_to_oracle, sorted
 pytestmark = pytest.mark.gpu
 
 
-def _deck(M, push_type=O.PUSH_ROBUST):
-    d = Q.decks.Deck("loop_test", nr=64, nz=40, max_mode=M, dr=0.04, dxi=0.04, ppc=(2, 1), num_theta=8,
+def _deck(M, push_type=O.PUSH_ROBUST, nr=64):
+    d = Q.decks.Deck("loop_test", nr=nr, nz=40, max_mode=M, dr=0.04, dxi=0.04, ppc=(2, 1), num_theta=8,
                      uth=2e-3, seed=3, beams=[Q.decks.BeamSpec(2.0, 0.4, 0.3, 0.6, 20000, x0=0.04)],
                      iter_max=30, iter_reltol=1e-6)
     return d
@@ -34,9 +34,12 @@ def _oracle_run(deck, pl_in, beams_in, push_type):
     return sim, iters, rel
 
 
-@pytest.mark.parametrize("M,push_type", [(1, O.PUSH_ROBUST), (2, O.PUSH_ROBUST), (2, O.PUSH_STD)])
-def test_3d_step_matches_oracle(M, push_type):
-    deck = _deck(M)
+# nr = 45 (one CTA of 45 rows) and nr = 66 (two CTAs of 33 rows) stage with 8-byte copies:
+# the bulk-copy staging needs every row 16-byte aligned (even nr and rows per CTA)
+@pytest.mark.parametrize("M,push_type,nr", [(1, O.PUSH_ROBUST, 64), (2, O.PUSH_ROBUST, 64), (2, O.PUSH_STD, 64),
+                                            (2, O.PUSH_ROBUST, 45), (1, O.PUSH_STD, 66)])
+def test_3d_step_matches_oracle(M, push_type, nr):
+    deck = _deck(M, nr=nr)
     inputs = Q.deck_inputs(deck)
     pl, beams = inputs
     osim, oiters, orel = _oracle_run(deck, pl, beams, push_type)
