@@ -80,17 +80,16 @@ __device__ __forceinline__ MInterp minterp(int32_t c, float fx, float fy, int nr
 }
 
 // E and B gathered from the FP32 table (interp_field, interp_part2d.f03:67-109)
-__device__ __forceinline__ void mgather(const float* __restrict__ T, int P, int M, const MInterp& ii, float ep[3],
-                                        float bp[3]) {
+// t0: the records of node ii.idx (in the table, or a copy of the two nodes' records)
+__device__ __forceinline__ void mgather_at(const float* t0, int P, int M, const MInterp& ii, float ep[3], float bp[3]) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) { ep[c] = 0.0f; bp[c] = 0.0f; }
   if (!ii.ok) return;
-  const float* t0 = T + (size_t)ii.idx * P * 6;
   const float* t1 = t0 + (size_t)P * 6;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    ep[c] = __ldg(t0 + c) * ii.w0 + __ldg(t1 + c) * ii.w1;
-    bp[c] = __ldg(t0 + 3 + c) * ii.w0 + __ldg(t1 + 3 + c) * ii.w1;
+    ep[c] = t0[c] * ii.w0 + t1[c] * ii.w1;
+    bp[c] = t0[3 + c] * ii.w0 + t1[3 + c] * ii.w1;
   }
   float phr = 1.0f, phi = 0.0f;
   for (int m = 1; m <= M; ++m) {
@@ -104,11 +103,16 @@ __device__ __forceinline__ void mgather(const float* __restrict__ T, int P, int 
     const float* i1 = t1 + (2 * m) * 6;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      ep[c] += (__ldg(r0 + c) * pre - __ldg(i0 + c) * pim) * ii.w0 + (__ldg(r1 + c) * pre - __ldg(i1 + c) * pim) * ii.w1;
-      bp[c] += (__ldg(r0 + 3 + c) * pre - __ldg(i0 + 3 + c) * pim) * ii.w0 +
-               (__ldg(r1 + 3 + c) * pre - __ldg(i1 + 3 + c) * pim) * ii.w1;
+      ep[c] += (r0[c] * pre - i0[c] * pim) * ii.w0 + (r1[c] * pre - i1[c] * pim) * ii.w1;
+      bp[c] += (r0[3 + c] * pre - i0[3 + c] * pim) * ii.w0 +
+               (r1[3 + c] * pre - i1[3 + c] * pim) * ii.w1;
     }
   }
+}
+
+__device__ __forceinline__ void mgather(const float* __restrict__ T, int P, int M, const MInterp& ii, float ep[3],
+                                        float bp[3]) {
+  mgather_at(T + (size_t)(ii.ok ? ii.idx : 0) * P * 6, P, M, ii, ep, bp);
 }
 
 // Sum over the 32 lanes of each of 32 values: after the exchange, lane l holds in a[0]
@@ -195,20 +199,22 @@ __global__ void __launch_bounds__(kItemThreads) k_mqdeposit(GridDev G, const int
 
 // Predictor push of one particle (amjdeposit_robust / _std): the deposit values
 // v = {u0, u1, u2, du0, du1, u0 u0 / (g - u2) .. } and the charge factor qq = q / (g - u2).
+// pv: the particle's px, py, pz, psi, q (loaded by the caller); t0: the gather records of
+// node ii.idx
 __device__ __forceinline__ void mpredict(const GridDev& G, int push_type, float qbm, float dt, const MArr& A,
-                                         const float* __restrict__ T, int64_t i, int write_back, const MInterp& ii,
-                                         float v[8], float& qq) {
+                                         const float* t0, int64_t i, int write_back, const MInterp& ii,
+                                         const float pv[5], float v[8], float& qq) {
   const float idt = 1.0f / dt, qtmh = 0.5f * qbm * dt;
   float ep[3], bp[3], wp[3], u0[3], u[3], ut[3];
-  mgather(T, G.P, G.M, ii, ep, bp);
+  mgather_at(t0, G.P, G.M, ii, ep, bp);
   wp[0] = ep[0] - bp[1];
   wp[1] = ep[1] + bp[0];
   wp[2] = ep[2];
-  const float p1 = A.px[i], p2 = A.py[i];
+  const float p1 = pv[0], p2 = pv[1];
   u0[0] = p1 * ii.pcos + p2 * ii.psin;
   u0[1] = p2 * ii.pcos - p1 * ii.psin;
-  u0[2] = A.pz[i];
-  const float psi_in = A.psi[i];
+  u0[2] = pv[2];
+  const float psi_in = pv[3];
   if (push_type == QPAD_PUSH2_ROBUST) {
     float gam = sqrtf(1.0f + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
     const float qtmh1 = qtmh * gam / (gam - u0[2]);
@@ -264,7 +270,7 @@ __device__ __forceinline__ void mpredict(const GridDev& G, int push_type, float 
   du1 += u[1] * dpsi * ipsi;
   v[0] = u[0]; v[1] = u[1]; v[2] = u[2]; v[3] = du0; v[4] = du1;
   v[5] = u[0] * u[0] * ipsi; v[6] = u[0] * u[1] * ipsi; v[7] = u[1] * u[1] * ipsi;
-  qq = A.q[i] * ipsi;
+  qq = pv[4] * ipsi;
 }
 
 // ------------------------------------------------------------------------------------
@@ -282,12 +288,43 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
                                                          int write_back) {
   // the field iteration launched after this kernel may start its own staging now
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
-  const int lane = threadIdx.x & 31;
-  const int it = blockIdx.x * (kItemThreads / 32) + (threadIdx.x >> 5);
-  if (it >= *n_items) return;                          // warp-uniform
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int it = blockIdx.x * (kItemThreads / 32) + w;
+  // the item and the item count in flight together (the item list holds whole CTAs' worth)
+  const int n_it = *n_items;
   const int4 item = items[it];
+  if (it >= n_it) return;                              // warp-uniform
   const int key = item.x, start = item.y, cnt = item.z;
   const int ld = G.ld;
+  // every particle of an item sits in radial cell `key`: the two gather records (nodes key,
+  // key + 1) load with the particles, then go to this warp's shared slot
+  constexpr int kTV = (12 * QPAD_MAX_PARTS + 31) / 32;
+  __shared__ float tsm[kItemThreads / 32][12 * QPAD_MAX_PARTS];
+  const int nt = 12 * G.P;
+  const float* tb = T + (size_t)min(key, G.nr) * G.P * 6;
+  float tv[kTV];
+#pragma unroll
+  for (int q = 0; q < kTV; ++q) tv[q] = lane + 32 * q < nt ? __ldg(tb + lane + 32 * q) : 0.0f;
+  int32_t pcx[kPPL];
+  float pf[kPPL][2], pv[kPPL][5];
+#pragma unroll
+  for (int j = 0; j < kPPL; ++j) {
+    const int o = j * 32 + lane;
+    const bool in = o < cnt;
+    const int i = start + (in ? o : 0);
+    pcx[j] = in ? A.cxy[i] : 0;
+    pf[j][0] = in ? A.fx[i] : 0.0f;
+    pf[j][1] = in ? A.fy[i] : 0.0f;
+    pv[j][0] = in ? A.px[i] : 0.0f;
+    pv[j][1] = in ? A.py[i] : 0.0f;
+    pv[j][2] = in ? A.pz[i] : 0.0f;
+    pv[j][3] = in ? A.psi[i] : 0.0f;
+    pv[j][4] = in ? A.q[i] : 0.0f;
+  }
+#pragma unroll
+  for (int q = 0; q < kTV; ++q)
+    if (lane + 32 * q < nt) tsm[w][lane + 32 * q] = tv[q];
+  __syncwarp();
   float v[kPPL][8], wq[kPPL][2], pc[kPPL][2];
 #pragma unroll
   for (int j = 0; j < kPPL; ++j) {
@@ -299,10 +336,11 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
     for (int c = 0; c < 8; ++c) v[j][c] = 0.0f;
     if (o < cnt) {
       const int i = start + o;
-      const MInterp ii = minterp(A.cxy[i], A.fx[i], A.fy[i], G.nr);
+      const MInterp ii = minterp(pcx[j], pf[j][0], pf[j][1], G.nr);
       if (ii.ok) {
         float qq;
-        mpredict(G, push_type, qbm, dt, A, T, i, write_back, ii, v[j], qq);
+        const float* t0 = ii.idx == key ? &tsm[w][0] : T + (size_t)ii.idx * G.P * 6;
+        mpredict(G, push_type, qbm, dt, A, t0, i, write_back, ii, pv[j], v[j], qq);
         wq[j][0] = qq * ii.w0;
         wq[j][1] = qq * ii.w1;
         pc[j][0] = ii.pcos;
@@ -586,7 +624,8 @@ int mixed_alloc(qpad_species* sp) {
   if (e != cudaSuccess) { cudaGetLastError(); return set_err(ctx, QPAD_E_NOMEM, "cudaMalloc(mixed pristine)"); }
   e = cudaMalloc(&sp->hist, sizeof(int32_t) * (ctx->g.nr + 4));
   if (e == cudaSuccess) e = cudaMalloc(&sp->cursor, sizeof(int32_t) * (ctx->g.nr + 4));
-  sp->items_cap = (int64_t)(cap / kMinItem) + ctx->g.nr + 2;
+  sp->items_cap = ((int64_t)(cap / kMinItem) + ctx->g.nr + 2 + kItemThreads / 32 - 1) / (kItemThreads / 32) *
+                  (kItemThreads / 32);                  // whole CTAs: every warp may load its item
   if (e == cudaSuccess) e = cudaMalloc(&sp->items, sizeof(int4) * (size_t)sp->items_cap);
   if (e == cudaSuccess) e = cudaMalloc(&sp->d_nitems, sizeof(int) * 2);
   if (e == cudaSuccess) e = cudaMemset(sp->d_nitems, 0, sizeof(int) * 2);
