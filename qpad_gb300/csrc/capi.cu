@@ -1249,8 +1249,10 @@ extern "C" int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* sta
     const std::string key = step_key(ctx);
     if (!ctx->step_exec || ctx->step_key != key) {
       int rb = build_step_graph(ctx);
+      std::string why;
       if (rb && ctx->pdl) {                          // a graph with programmatic edges was refused:
-        cudaGetLastError();                          // build it with plain edges
+        why = ctx->err;                              // build it with plain edges
+        cudaGetLastError();
         ctx->pdl = false;
         rb = build_step_graph(ctx);
       }
@@ -1261,6 +1263,7 @@ extern "C" int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* sta
         cudaGetLastError();
       } else {
         ctx->step_key = step_key(ctx);
+        ctx->graph_status = why.empty() ? "" : "programmatic edges refused, plain edges: " + why;
       }
     }
   }
