@@ -89,7 +89,8 @@ int qpad_launch_count(const qpad_ctx* ctx, int64_t* count);
 int qpad_set_graph(qpad_ctx* ctx, int on);
 /* 1 if the last 3D step ran as a graph. */
 int qpad_graph_active(const qpad_ctx* ctx, int* active);
-/* Why the graph path was switched off ("" while it is on). */
+/* Why the graph path was switched off, or that it runs with plain instead of programmatic
+ * edges ("" while it runs as designed). */
 const char* qpad_graph_status(const qpad_ctx* ctx);
 /* Per-kernel CUDA-event timing on the context's stream: enable/disable, then read the
  * accumulated device time (ms) and launch count of one kernel family by name
@@ -212,7 +213,10 @@ int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* stats);
  * context of the batch by one 3D step (qpad_3d_step semantics for each); the slice loops
  * of all of them, every slice and predictor-corrector iteration, run as ONE CUDA graph
  * launch, each simulation an independent branch with its own device-side loop conditions.
- * The contexts must share a device and must not sort every few slices (sort_freq = 0). */
+ * The contexts must share a device and must not sort every few slices (sort_freq = 0).
+ * The first step of a batch gives every context's iteration kernel the smallest cluster
+ * that fits its grid (a batch is throughput-bound); qpad_autotune afterwards restores a
+ * context's single-simulation shape. */
 typedef struct qpad_batch qpad_batch;
 int qpad_batch_create(qpad_ctx* const* ctxs, int n, qpad_batch** out);
 int qpad_batch_destroy(qpad_batch* batch);
