@@ -30,7 +30,7 @@
 // inside one cluster.  Each group-0 CTA takes its node range's ticket after writing its
 // B-perp; the last of the M+1 CTAs of a range evaluates the record there and folds its
 // maxima into two global words (max on the bit patterns of non-negative doubles, which is
-// exact and order independent); the last range to finish takes the verdict, drives the
+// exact and order independent); the last range to finish takes the decision, drives the
 // loop state and resets the tickets.  No CTA waits on another.
 #include <cooperative_groups.h>
 
@@ -718,7 +718,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
       if (mo) red_max_u64(mx, mo);
       if (mn) red_max_u64(mx + 1, mn);
       a.tickets[rank] = 0u;
-      if (atom_add_acq_rel(&a.tickets[CL], 1u) == (unsigned)(CL - 1)) {   // the last range: the verdict
+      if (atom_add_acq_rel(&a.tickets[CL], 1u) == (unsigned)(CL - 1)) {   // the last range: the decision
         const unsigned long long vo = __ldcg(mx), vn = __ldcg(mx + 1);
         mx[0] = 0ull;
         mx[1] = 0ull;

@@ -331,7 +331,7 @@ __device__ __forceinline__ void conv_node(const GridDev& G, const BF& B, int com
   s_im[i - 1] = nim;
 }
 
-// The verdict from the maxima over nodes: relative and absolute residuals, convergence,
+// The decision from the maxima over nodes: relative and absolute residuals, convergence,
 // and the loop state (iteration count, statistics, WHILE condition).  One thread.
 __device__ inline void conv_decide_at(double mx_old, double mx_new, double reltol, double abstol, double* res,
                                       const ConvLoop& L, int it_prev, int jp) {
