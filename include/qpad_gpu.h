@@ -87,6 +87,12 @@ int qpad_launch_count(const qpad_ctx* ctx, int64_t* count);
  * WHILE node over predictor-corrector iterations, both conditions set on the device) when
  * on != 0 (the default); off, the host drives slices and iterations. */
 int qpad_set_graph(qpad_ctx* ctx, int on);
+/* Binomial (1,2,1) smoothing of the species' charge and current deposits, `order` passes
+ * (0, the default, 1 or 2): the species' smooth_order (sim_plasma_class.f03:139-142), applied
+ * as qdp_species2d / amjdp_species2d do (species2d_class.f03:202, 270-272) with
+ * ufield::smooth_f1 (ufield_class.f03:274-339); the neutralising background is not smoothed.
+ * Orders above 2 are refused (QPAD_E_ARG). */
+int qpad_set_smooth(qpad_ctx* ctx, int order);
 /* 1 if the last 3D step ran as a graph. */
 int qpad_graph_active(const qpad_ctx* ctx, int* active);
 /* Why the graph path was switched off, or that it runs with plain instead of programmatic

@@ -45,7 +45,7 @@ class SimDesc(C.Structure):
                 ("iter_abstol", C.c_double), ("dt3d", C.c_double), ("sp_qbm", C.c_double),
                 ("sp_push_type", C.c_int), ("sp_neutralized", C.c_int), ("sp_npmax", C.c_int64),
                 ("nbeams", C.c_int), ("beam_qbm", C.c_double * 4), ("beam_push_type", C.c_int * 4),
-                ("beam_npmax", C.c_int64 * 4), ("nthreads", C.c_int)]
+                ("beam_npmax", C.c_int64 * 4), ("nthreads", C.c_int), ("smooth_order", C.c_int)]
 
 
 BND_ZERO, BND_OPEN = 2, 3
@@ -82,6 +82,7 @@ def lib():
             "orc_conv_record": (None, [G, D, D, D]),
             "orc_conv_compare": (None, [G, D, D, D, D, D]),
             "orc_qdeposit": (None, [G, C.c_int64, D, D, D, D]),
+            "orc_smooth": (None, [G, C.c_int, D]),
             "orc_amjdeposit": (None, [G, C.c_int, C.c_double, C.c_double, C.c_int64, D, D, D, D, D, D,
                                       D, D, D, D, D, D, D, C.c_int]),
             "orc_push_u": (None, [G, C.c_int, C.c_double, C.c_double, C.c_int64, D, D, D, D, D, D, D,
@@ -230,6 +231,12 @@ def qdeposit(g, pl: Plasma, qf=None):
     return qf
 
 
+def smooth(g, kind, f):
+    """One smoothing pass in place (kind 0 rho, 1 jay, 2 djdxi)."""
+    lib().orc_smooth(C.byref(g), kind, ptr(f))
+    return f
+
+
 def amjdeposit(g, push_type, qbm, dt, pl: Plasma, ef, bf, nthreads=1):
     cu, amu, dcu = field(g, 3), field(g, 3), field(g, 2)
     lib().orc_amjdeposit(C.byref(g), push_type, qbm, dt, pl.n, ptr(pl.x), ptr(pl.y), ptr(pl.px),
@@ -333,7 +340,7 @@ class Sim:
 
     def __init__(self, g: Grid, *, iter_max=50, iter_reltol=1e-6, iter_abstol=0.0, dt3d=10.0,
                  sp_qbm=-1.0, sp_push_type=PUSH_ROBUST, neutralized=True, sp_npmax=1,
-                 beams=(), nthreads=1):
+                 beams=(), nthreads=1, smooth_order=0):
         d = SimDesc()
         d.g = g
         d.iter_max, d.iter_reltol, d.iter_abstol, d.dt3d = iter_max, iter_reltol, iter_abstol, dt3d
@@ -342,6 +349,7 @@ class Sim:
         for k, (qbm, ptype, npmax) in enumerate(beams):
             d.beam_qbm[k], d.beam_push_type[k], d.beam_npmax[k] = qbm, ptype, max(1, npmax)
         d.nthreads = nthreads
+        d.smooth_order = smooth_order
         self.g = g
         self.h = lib().orc_sim_create(C.byref(d))
 

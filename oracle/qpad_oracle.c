@@ -553,6 +553,39 @@ void orc_conv_compare(const orc_grid* g, const double* b, double* s_re, double* 
 /* =============================================================================
  * Plasma charge deposit: part2d_class.f03:231-359 (accumulates into qf)
  * ============================================================================= */
+/* ufield::smooth_f1 (ufield_class.f03:274-339) on every mode part and component of a
+ * deposit field, single rank (idproc = 0, noff = 0): kernel = stencil / sum(stencil) with
+ * stencil (1, 2, 1); node 1 uses the axis form where ax_smooth is set for the mode and
+ * component (else 0), node 2 the near-axis form, nodes j >= 3 the r-weighted form with
+ * r_idx = j - 1; the guard nodes are left as they are.  The ax_smooth switches per mode are
+ * those of field_rho / field_jay / field_djdxi::smooth (field_src_class.f03:114-118,
+ * 181-193, 256-266). */
+void orc_smooth(const orc_grid* g, int kind, double* f) {
+  const int nc = kind == 0 ? 1 : (kind == 1 ? 3 : 2);
+  const double st[3] = {1.0, 2.0, 1.0};
+  const double sum = st[0] + st[1] + st[2];
+  const double km = st[0] / sum, k0 = st[1] / sum, kp = st[2] / sum;
+  double* tmp = (double*)malloc((size_t)(g->nr + 2) * sizeof(double));
+  for (int p = 0; p < nparts(g); ++p) {
+    const int m = (p + 1) / 2;
+    for (int c = 0; c < nc; ++c) {
+      int ax;
+      if (kind == 0) ax = m == 0;
+      else if (kind == 1) ax = m == 0 ? (c == 2) : (m == 1 ? (c < 2) : 0);
+      else ax = m == 1;
+      double* v = &F(f, nc, p, c, 0);
+      tmp[1] = ax ? (k0 + kp) * v[1] + 8.0 * kp * v[2] : 0.0;
+      tmp[2] = k0 * v[2] + 0.125 * km * v[1] + 2.0 * kp * v[3];
+      for (int j = 3; j <= g->nr; ++j) {
+        const double r = (double)(j - 1);
+        tmp[j] = k0 * v[j] + (1.0 - 1.0 / r) * km * v[j - 1] + (1.0 + 1.0 / r) * kp * v[j + 1];
+      }
+      for (int j = 1; j <= g->nr; ++j) v[j] = tmp[j];
+    }
+  }
+  free(tmp);
+}
+
 static void qdeposit_axis_scale(const orc_grid* g, double* qf) {
   const int nr = g->nr, M = g->max_mode;
   F(qf, 1, 0, 0, 0) = 0.0;
@@ -1374,6 +1407,7 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
     memset(s->q_spe, 0, n1 * sizeof(double));
     memset(s->qsp, 0, n1 * sizeof(double));
     orc_qdeposit(g, s->np, s->x, s->y, s->q, s->qsp);
+    for (int k = 0; k < s->d.smooth_order; ++k) orc_smooth(g, 0, s->qsp);   /* q%smooth(), :202 */
     for (size_t i = 0; i < n1; ++i) s->q_spe[i] = s->q_spe[i] + s->qsp[i];
     if (s->d.sp_neutralized) for (size_t i = 0; i < n1; ++i) s->q_spe[i] = s->q_spe[i] + s->qn[i];
     /* :356-360 */
@@ -1393,6 +1427,11 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
       memset(s->amu, 0, 3 * n1 * sizeof(double));
       orc_amjdeposit(g, s->d.sp_push_type, s->d.sp_qbm, dxi, s->np, s->x, s->y, s->px, s->py, s->pz,
                      s->q, s->gamma, s->ppsi, s->e, s->b, s->cu, s->amu, s->acu, nt);
+      for (int k = 0; k < s->d.smooth_order; ++k) {      /* cu, dcu, amu %smooth(), :270-272 */
+        orc_smooth(g, 1, s->cu);
+        orc_smooth(g, 2, s->acu);
+        orc_smooth(g, 1, s->amu);
+      }
       orc_solve_djdxi(g, s->acu, s->amu, s->dcu);
       orc_solve_bt_iter(g, s->dcu, s->cu, s->b_spe);
       orc_solve_bz(g, s->cu, s->b_spe);

@@ -133,8 +133,14 @@ typedef struct orc_sim_desc {
   /* beams */
   int nbeams; double beam_qbm[4]; int beam_push_type[4]; int64_t beam_npmax[4];
   int nthreads;                /* OpenMP threads for particle loops (1 = serial) */
+  int smooth_order;            /* binomial smoothing passes of the species deposits (0 = none) */
 } orc_sim_desc;
 
+/* One binomial (1,2,1) smoothing pass of a deposit field (ufield::smooth_f1,
+ * ufield_class.f03:274-339, with the axis switches of field_rho / field_jay / field_djdxi
+ * ::smooth, field_src_class.f03:102-125, 169-199, 243-271): kind 0 = rho (1 comp),
+ * 1 = jay (3 comps: cu, amu), 2 = djdxi (2 comps: the acu deposit). */
+void orc_smooth(const orc_grid* g, int kind, double* f);
 orc_sim* orc_sim_create(const orc_sim_desc* d);
 void orc_sim_destroy(orc_sim* s);
 /* Load a fresh plasma slice state (species2d::new / renew, species2d_class.f03:75-184):

@@ -74,6 +74,7 @@ _SIGS = {
     "qpad_device_count": (C.c_int, [C.POINTER(C.c_int)]),
     "qpad_launch_count": (C.c_int, [C.c_void_p, I64P]),
     "qpad_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "qpad_set_smooth": (C.c_int, [C.c_void_p, C.c_int]),
     "qpad_graph_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "qpad_graph_status": (C.c_char_p, [C.c_void_p]),
     "qpad_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),

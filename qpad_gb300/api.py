@@ -198,6 +198,11 @@ class Simulation:
         """Run 3D steps as one CUDA graph (default) or drive slices/iterations from the host."""
         self._check(self.lib.qpad_set_graph(self.h, int(on)))
 
+    def set_smooth(self, order: int):
+        """Binomial smoothing passes (0, 1 or 2) of the species' charge and current deposits
+        (the species' smooth_order)."""
+        self._check(self.lib.qpad_set_smooth(self.h, int(order)))
+
     def graph_active(self):
         """(whether the last 3D step ran as a graph, reason when it did not)."""
         a = C.c_int()

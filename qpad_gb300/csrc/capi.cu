@@ -190,7 +190,7 @@ int species_set_background(qpad_species* sp) {
   if (cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess)
     return check_launch(ctx, "memset qraw");
   if (int r = species_qdeposit_raw(sp, ctx->qraw)) return r;
-  if (int r = launch_finish_q(ctx, ctx->qraw, sp->qf, 0)) return r;
+  if (int r = launch_finish_q(ctx, ctx->qraw, sp->qf, 0, 0)) return r;   // qn is not smoothed
   k_neg<<<elem_grid(n1), 256, 0, ctx->stream>>>(sp->qf, sp->qn, n1);
   return check_launch(ctx, "qn");
 }
@@ -294,7 +294,7 @@ extern "C" int qpad_ctx_create(const qpad_grid_desc* d, qpad_ctx** out) {
   if (!ctx) return QPAD_E_NOMEM;
   GridDev& g = ctx->g;
   g.nr = d->nr; g.nz = d->nz; g.M = d->max_mode; g.P = 2 * d->max_mode + 1; g.ld = d->nr + 2; g.bnd = d->bnd;
-  g.dr = d->dr; g.dxi = d->dxi; g.idr = 1.0 / d->dr; g.toff = 0;
+  g.dr = d->dr; g.dxi = d->dxi; g.idr = 1.0 / d->dr; g.toff = 0; g.smooth = 0;
   g.relax_fac = d->relax_fac >= 0.0 ? d->relax_fac : 1.0e-3 * ((d->dr / 0.02) * (d->dr / 0.02));
   ctx->iter_max = d->iter_max; ctx->reltol = d->iter_reltol; ctx->abstol = d->iter_abstol; ctx->dt = d->dt;
   ctx->precision = d->precision; ctx->device = d->device;
@@ -404,6 +404,21 @@ extern "C" int qpad_set_graph(qpad_ctx* ctx, int on) {
 extern "C" int qpad_graph_active(const qpad_ctx* ctx, int* active) {
   if (!ctx || !active) return QPAD_E_ARG;
   *active = (ctx->use_graph && ctx->step_exec != nullptr) ? 1 : 0;
+  return QPAD_OK;
+}
+
+extern "C" int qpad_set_smooth(qpad_ctx* ctx, int order) {
+  if (!ctx) return QPAD_E_ARG;
+  if (order < 0 || order > 2) return set_err(ctx, QPAD_E_ARG, "smooth order: 0, 1 or 2");
+  const int old = ctx->g.smooth;
+  ctx->g.smooth = order;
+  // the iteration kernel's shared memory grows with smoothing: check its shape still fits
+  if (ctx->iter_cl > 0 && iterate_try_cluster(ctx, ctx->iter_cl) != 0) {
+    cudaGetLastError();
+    ctx->g.smooth = old;
+    iterate_try_cluster(ctx, ctx->iter_cl);
+    return set_err(ctx, QPAD_E_CAPACITY, "smoothing scratch does not fit the iteration kernel's shape");
+  }
   return QPAD_OK;
 }
 
@@ -712,7 +727,7 @@ extern "C" int qpad_species_qdp(qpad_species* sp, int q) {
   const size_t n1 = f1_elems(ctx, QPAD_F_Q_SPE);
   if (cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess) return check_launch(ctx, "memset");
   if (int r = is_mixed(sp) ? mixed_qdeposit_raw(sp, ctx->qraw) : species_qdeposit_raw(sp, ctx->qraw)) return r;
-  if (int r = launch_finish_q(ctx, ctx->qraw, sp->qf, 0)) return r;
+  if (int r = launch_finish_q(ctx, ctx->qraw, sp->qf, 0, ctx->g.smooth)) return r;
   k_add2<<<elem_grid(n1), 256, 0, ctx->stream>>>(ctx->f[q], sp->qf, sp->neutralized ? sp->qn : nullptr, n1);
   return check_launch(ctx, "qdp add");
 }
@@ -1133,7 +1148,7 @@ int build_step_graph(qpad_ctx* ctx) {
 std::string step_key(const qpad_ctx* ctx) {
   std::string k = std::to_string(ctx->precision) + "/" + std::to_string(ctx->iter_cl) + "/" +
                   std::to_string(ctx->item_ppl) + "/" + std::to_string(ctx->guess != nullptr) + "/" +
-                  std::to_string(ctx->pdl);
+                  std::to_string(ctx->pdl) + "/" + std::to_string(ctx->g.smooth);
   for (auto* s : ctx->species)
     k += "|" + std::to_string((long long)s->np) + ":" + std::to_string(s->push_type) + ":" +
          std::to_string(s->neutralized) + ":" + std::to_string(s->sort_freq);

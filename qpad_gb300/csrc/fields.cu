@@ -484,9 +484,43 @@ __device__ void op_djdxi(const GridDev& G, int m, const double* __restrict__ acu
 // Raw charge deposit -> density (part2d_class.f03:314-335): axis guard 0, axis x8 for
 // m=0 and 0 for m>0, 1/(j-1) beyond.  out = raw finished (+ qn when add_qn, which is the
 // species2d::qdp accumulation q_spe = 0 + q_species + qn).
+// smooth > 0: the finished charge takes that many binomial smoothing passes before qn is
+// added (qdp_species2d, species2d_class.f03:198-203); sm holds 4 (nr + 2) doubles.
 __device__ void op_finish_q(const GridDev& G, int m, const double* __restrict__ raw, const double* __restrict__ qn,
-                            double* __restrict__ out) {
+                            double* __restrict__ out, int smooth, double* sm) {
   const int np_ = m == 0 ? 1 : 2;
+  if (smooth > 0) {
+    const int ld = G.ld;
+    for (int h = 0; h < np_; ++h) {
+      const int p = h == 0 ? part_re(m) : part_im(m);
+      for (int i = threadIdx.x; i <= G.nr + 1; i += blockDim.x) {
+        const double r = FLD(raw, 1, p, 0, i);
+        sm[h * ld + i] = i == 0 ? 0.0 : (i == 1 ? ((m == 0) ? 8.0 * r : 0.0) : r * G.inv[i]);
+      }
+    }
+    __syncthreads();
+    for (int pass = 0; pass < smooth; ++pass) {
+      for (int h = 0; h < np_; ++h)
+        for (int i = 1 + threadIdx.x; i <= G.nr; i += blockDim.x) {
+          const double* v = sm + h * ld;
+          sm[(2 + h) * ld + i] = smooth_node(G, i, smooth_ax(0, m, 0), v[i - 1], v[i], v[i + 1]);
+        }
+      __syncthreads();
+      for (int h = 0; h < np_; ++h)
+        for (int i = 1 + threadIdx.x; i <= G.nr; i += blockDim.x) sm[h * ld + i] = sm[(2 + h) * ld + i];
+      __syncthreads();
+    }
+    for (int h = 0; h < np_; ++h) {
+      const int p = h == 0 ? part_re(m) : part_im(m);
+      for (int i = threadIdx.x; i <= G.nr + 1; i += blockDim.x) {
+        double v = sm[h * ld + i];
+        if (qn) v = (0.0 + v) + FLD(qn, 1, p, 0, i);
+        FLD(out, 1, p, 0, i) = v;
+      }
+    }
+    __syncthreads();
+    return;
+  }
   for (int h = 0; h < np_; ++h) {
     const int p = h == 0 ? part_re(m) : part_im(m);
     for (int i = threadIdx.x; i <= G.nr + 1; i += blockDim.x) {
@@ -504,8 +538,10 @@ __device__ void op_finish_q(const GridDev& G, int m, const double* __restrict__ 
 
 // Axis fixes and 1/(j-1) scaling of the current, momentum-flux and acceleration deposits,
 // in place (part2d_class.f03:914-1005).
+// smooth > 0: then that many binomial smoothing passes of each of them
+// (amjdp_species2d, species2d_class.f03:270-272); sm holds 4 (nr + 2) doubles.
 __device__ void op_finish_amj(const GridDev& G, int m, double* __restrict__ cu, double* __restrict__ amu,
-                              double* __restrict__ acu) {
+                              double* __restrict__ acu, int smooth, double* sm) {
   const int np_ = m == 0 ? 1 : 2;
   for (int h = 0; h < np_; ++h) {
     const int p = h == 0 ? part_re(m) : part_im(m);
@@ -518,6 +554,26 @@ __device__ void op_finish_amj(const GridDev& G, int m, double* __restrict__ cu, 
     }
   }
   __syncthreads();
+  if (smooth <= 0) return;
+  const int ld = G.ld;
+  for (int h = 0; h < np_; ++h) {
+    const int p = h == 0 ? part_re(m) : part_im(m);
+    for (int row = 0; row < 8; ++row) {              // cu 0..2, amu 0..2, acu 0..1
+      double* f = row < 3 ? &FLD(cu, 3, p, row, 0) : (row < 6 ? &FLD(amu, 3, p, row - 3, 0) : &FLD(acu, 2, p, row - 6, 0));
+      const int kind = row < 6 ? 1 : 2, comp = row < 3 ? row : (row < 6 ? row - 3 : row - 6);
+      for (int i = threadIdx.x; i <= G.nr + 1; i += blockDim.x) sm[i] = f[i];
+      __syncthreads();
+      for (int pass = 0; pass < smooth; ++pass) {
+        for (int i = 1 + threadIdx.x; i <= G.nr; i += blockDim.x)
+          sm[ld + i] = smooth_node(G, i, smooth_ax(kind, m, comp), sm[i - 1], sm[i], sm[i + 1]);
+        __syncthreads();
+        for (int i = 1 + threadIdx.x; i <= G.nr; i += blockDim.x) sm[i] = sm[ld + i];
+        __syncthreads();
+      }
+      for (int i = 1 + threadIdx.x; i <= G.nr; i += blockDim.x) f[i] = sm[i];
+      __syncthreads();
+    }
+  }
 }
 
 // FP32 gather table of the mixed-precision particle path: T[(node*P + part)*6 + c],
@@ -635,7 +691,7 @@ __global__ void __launch_bounds__(kFieldThreads) k_slice_begin(GridDev G, const 
     op_copy(G, m, 1, qs, F.f[QPAD_F_Q_BEAM]);                      // q_beam%copy_slice(j, 2->1)
     op_bt_beam(G, m, fac, sm, sc, F.f[QPAD_F_Q_BEAM], F.f[QPAD_F_B_BEAM]);
   } else if (job == 1) {
-    op_finish_q(G, m, F.qraw, use_qn ? F.qn : nullptr, F.f[QPAD_F_Q_SPE]);
+    op_finish_q(G, m, F.qraw, use_qn ? F.qn : nullptr, F.f[QPAD_F_Q_SPE], G.smooth, sm);
     op_psi(G, m, fac, sm, sc, F.f[QPAD_F_Q_SPE], F.f[QPAD_F_PSI]);
   } else if (job == 2) {
     op_bz(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_B_SPE]);
@@ -711,7 +767,7 @@ __global__ void __launch_bounds__(kFieldThreads) k_iter_b(GridDev G, const doubl
   extern __shared__ double sm[];
   __shared__ double sc[6 * 32 + 8];
   const int m = blockIdx.x;
-  op_finish_amj(G, m, F.f[QPAD_F_CU], F.f[QPAD_F_AMU], F.f[QPAD_F_ACU]);
+  op_finish_amj(G, m, F.f[QPAD_F_CU], F.f[QPAD_F_AMU], F.f[QPAD_F_ACU], G.smooth, sm);
   op_djdxi(G, m, F.f[QPAD_F_ACU], F.f[QPAD_F_AMU], F.f[QPAD_F_DCU]);
   op_bt_iter(G, m, fac, sm, sc, F.f[QPAD_F_DCU], F.f[QPAD_F_CU], F.f[QPAD_F_B_SPE]);
   op_bz(G, m, fac, sm, sc, F.f[QPAD_F_CU], F.f[QPAD_F_B_SPE]);
@@ -777,12 +833,14 @@ __global__ void __launch_bounds__(256) k_store_espe(GridDev G, SliceFields F, co
 }
 
 __global__ void __launch_bounds__(kFieldThreads) k_finish_q(GridDev G, const double* raw, const double* qn,
-                                                            double* out) {
-  op_finish_q(G, blockIdx.x, raw, qn, out);
+                                                            double* out, int smooth) {
+  extern __shared__ double sm[];
+  op_finish_q(G, blockIdx.x, raw, qn, out, smooth, sm);
 }
 
 __global__ void __launch_bounds__(kFieldThreads) k_finish_amj(GridDev G, double* cu, double* amu, double* acu) {
-  op_finish_amj(G, blockIdx.x, cu, amu, acu);
+  extern __shared__ double sm[];
+  op_finish_amj(G, blockIdx.x, cu, amu, acu, G.smooth, sm);
 }
 
 // convergence_tester (simulation_class.f03:522-606) on component `comp` of b:
@@ -856,7 +914,8 @@ int raise_dyn_smem(qpad_ctx* ctx, const void* func, size_t bytes) {
 static int ensure_smem_attr(qpad_ctx* ctx) {
   if (ctx->field_attr_done) return 0;
   const size_t need = field_smem(ctx);
-  const void* ks[] = {(const void*)k_field_op, (const void*)k_slice_begin, (const void*)k_iter_b};
+  const void* ks[] = {(const void*)k_field_op, (const void*)k_slice_begin, (const void*)k_iter_b,
+                      (const void*)k_finish_q, (const void*)k_finish_amj};
   for (const void* k : ks)
     if (int r = raise_dyn_smem(ctx, k, need)) return r;
   ctx->field_attr_done = true;
@@ -930,13 +989,17 @@ int launch_slice_end(qpad_ctx* ctx) {
   return check_launch(ctx, "k_slice_end", 2);
 }
 
-int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn) {
-  k_finish_q<<<ctx->g.M + 1, kFieldThreads, 0, ctx->stream>>>(ctx->g, raw, add_qn ? ctx->qn : nullptr, out);
+int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn, int smooth) {
+  if (int r = ensure_smem_attr(ctx)) return r;
+  k_finish_q<<<ctx->g.M + 1, kFieldThreads, smooth > 0 ? field_smem(ctx) : 0, ctx->stream>>>(
+      ctx->g, raw, add_qn ? ctx->qn : nullptr, out, smooth);
   return check_launch(ctx, "k_finish_q");
 }
 
 int launch_finish_amj(qpad_ctx* ctx, double* cu, double* amu, double* acu) {
-  k_finish_amj<<<ctx->g.M + 1, kFieldThreads, 0, ctx->stream>>>(ctx->g, cu, amu, acu);
+  if (int r = ensure_smem_attr(ctx)) return r;
+  k_finish_amj<<<ctx->g.M + 1, kFieldThreads, ctx->g.smooth > 0 ? field_smem(ctx) : 0, ctx->stream>>>(ctx->g, cu, amu,
+                                                                                                      acu);
   return check_launch(ctx, "k_finish_amj");
 }
 

@@ -139,10 +139,10 @@ struct WinF {
 // Shared-memory staging of one CTA (doubles): the finished deposits on the node window
 // [r0-1, r1+2] (cu 0..2, amu 3..5, acu 6..7), b_spe components 0..1 and b_beam on the owned
 // nodes, psi on the window, the factor rows of the three matrices, the right-hand sides.
-__host__ __device__ inline size_t iterate_smem_doubles(int R, int ld) {
+__host__ __device__ inline size_t iterate_smem_doubles(int R, int ld, int smooth) {
   const size_t W = (size_t)R + 6;                // node window [r0-2, r0+R+4)
   (void)ld;
-  return 30 * W + 21 * (size_t)R;
+  return 30 * W + 21 * (size_t)R + (smooth > 0 ? 12 * W : 0);   // + the smoothing scratch rows
 }
 
 // Bulk (TMA) copy global -> this CTA's shared memory, completing on an mbarrier.
@@ -201,6 +201,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   double* dsm = facs + 9 * R;                    // [kMaxRhs][R]
   double* tab = dsm + kMaxRhs * R;               // node tables ir, inv on the window
   double* djs = tab + 2 * W;                     // dJ/dxi of the owned nodes [4][R]
+  double* sms = djs + 4 * R;                     // smoothing scratch [up to 12 rows][W] (smooth > 0)
   GridDev G = a.G;                               // the node tables read from shared memory
   G.ir = tab;
   G.inv = tab + W;
@@ -342,6 +343,27 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
                                                                 : finish_amj(G, m, 2, c8 - 6, node, v));
   }
   __syncthreads();
+  // binomial smoothing of the finished deposits (amjdp_species2d, species2d_class.f03:270-272):
+  // pass k is exact on window nodes [wb + k, wb + W - 1 - k], which covers the owned nodes and
+  // their neighbours for k <= 2
+  for (int pass = 1; pass <= G.smooth; ++pass) {
+    for (int q = t; q < c8_n * nh * W; q += blockDim.x) {
+      const int row = q / W, x = q % W, c8 = c8_lo + row / nh, node = wb + x;
+      const double* v = win + (c8 * 2 + row % nh) * W;
+      double out = v[x];
+      if (x >= pass && x <= W - 1 - pass && node >= 1 && node <= nr) {
+        const int kind = c8 < 6 ? 1 : 2, comp = c8 < 3 ? c8 : (c8 < 6 ? c8 - 3 : c8 - 6);
+        out = smooth_node(G, node, smooth_ax(kind, m, comp), v[x - 1], v[x], v[x + 1]);
+      }
+      sms[q] = out;
+    }
+    __syncthreads();
+    for (int q = t; q < c8_n * nh * W; q += blockDim.x) {
+      const int row = q / W, c8 = c8_lo + row / nh;
+      win[(c8 * 2 + row % nh) * W + q % W] = sms[q];
+    }
+    __syncthreads();
+  }
   const WinF CU{win, W, wb, pr, 0}, AMU{win, W, wb, pr, 3}, ACU{win, W, wb, pr, 6};
   const WinF PS{psw, W, wb, pr, 0};
   const auto BO = [&](int p, int c, int i) { return bo[(c * 2 + (p == pr ? 0 : 1)) * W + (i - wb)]; };
@@ -417,7 +439,8 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
       double s = 0.0;
       for (int q = 0; q < CL; ++q) s += *cluster.map_shared_rank(&divp, q);
       const RawFin CUg{&a.G, raw_cu, 0, 0, 3};    // nodes nr-2, nr-1 lie outside this window
-      dsm[3 * R + 0] = ez_axis_row(a.G, s, CUg);
+      const auto CUs = [&](int p, int c, int i) { return smoothed_at(a.G, CUg, 1, 0, p, c, i, a.G.smooth); };
+      dsm[3 * R + 0] = ez_axis_row(a.G, s, CUs);
     }
   }
   __syncthreads();
@@ -754,7 +777,7 @@ int iterate_try_cluster(qpad_ctx* ctx, int cl) {
   cudaError_t e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return cuda_check(ctx, e, "cluster attribute");
   const int R = (ctx->g.nr + cl - 1) / cl;
-  const size_t smem = iterate_smem_doubles(R, ctx->g.ld) * sizeof(double);
+  const size_t smem = iterate_smem_doubles(R, ctx->g.ld, ctx->g.smooth) * sizeof(double);
   if (smem > 200 * 1024) return QPAD_E_CAPACITY;
   if (int r = raise_dyn_smem(ctx, (const void*)k_iterate, smem)) return r;
   cudaLaunchConfig_t cfg = {};
@@ -825,7 +848,7 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2 * cl * (ctx->g.M + 1));
   cfg.blockDim = dim3(kIterThreads);
-  cfg.dynamicSmemBytes = iterate_smem_doubles(a.R, ctx->g.ld) * sizeof(double);
+  cfg.dynamicSmemBytes = iterate_smem_doubles(a.R, ctx->g.ld, ctx->g.smooth) * sizeof(double);
   cfg.stream = ctx->stream;
   cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;

@@ -39,6 +39,7 @@ struct GridDev {
   const double* ir;
   const double* inv;
   int toff;
+  int smooth;     // binomial smoothing passes of the species deposits (0..2)
 };
 
 __host__ __device__ inline int part_re(int m) { return m == 0 ? 0 : 2 * m - 1; }
@@ -94,6 +95,7 @@ struct qpad_ctx {
   int iter_cl = 0, iter_rows = 0;              // cluster size and rows per CTA of k_iterate
   int item_ppl = 4;                            // particles per lane of a mixed deposit work item
   bool pdl = true;                             // k_iterate as programmatic dependent of the deposit
+  // (the smoothing order lives in g.smooth)
   struct qpad_guess_state* guess = nullptr;    // learned predictor-corrector guess (learn.cu)
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
   float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
@@ -209,7 +211,7 @@ int launch_slice_begin(qpad_ctx* ctx, int neutralized_any);   // slice index rea
 int launch_iter_e(qpad_ctx* ctx);
 int launch_iter_b(qpad_ctx* ctx);
 int launch_slice_end(qpad_ctx* ctx);
-int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn);
+int launch_finish_q(qpad_ctx* ctx, const double* raw, double* out, int add_qn, int smooth);
 int launch_finish_amj(qpad_ctx* ctx, double* cu, double* amu, double* acu);
 // learned guess of the slice's initial B-perp and J-perp predictor (learn.cu)
 int guess_enqueue(qpad_ctx* ctx);

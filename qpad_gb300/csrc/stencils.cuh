@@ -331,6 +331,41 @@ __device__ __forceinline__ void conv_node(const GridDev& G, const BF& B, int com
   s_im[i - 1] = nim;
 }
 
+// ---- binomial smoothing of the species deposits (ufield::smooth_f1, ufield_class.f03:274-339)
+// Deposit kinds: 0 rho (1 comp), 1 jay (cu and amu, 3 comps), 2 djdxi (the acu deposit, 2).
+// Whether node 1 takes the axis form for mode m and component c (field_src_class.f03:114-118,
+// 181-193, 256-266).
+__host__ __device__ inline bool smooth_ax(int kind, int m, int c) {
+  if (kind == 0) return m == 0;
+  if (kind == 1) return m == 0 ? c == 2 : (m == 1 && c < 2);
+  return m == 1;
+}
+
+// One pass at node i (1..nr) from the values at i-1, i, i+1 (single rank: node 1 the axis
+// form or 0, node 2 the near-axis form, nodes >= 3 the r-weighted form with r = i - 1);
+// kernel = (1, 2, 1) / 4.
+__device__ __forceinline__ double smooth_node(const GridDev& G, int i, bool ax, double vm, double v0, double vp) {
+  const double km = 0.25, k0 = 0.5, kp = 0.25;
+  if (i == 1) return ax ? (k0 + kp) * v0 + 8.0 * kp * vp : 0.0;
+  if (i == 2) return k0 * v0 + 0.125 * km * vm + 2.0 * kp * vp;
+  const double ir = G.inv[(i) - G.toff];
+  return k0 * v0 + (1.0 - ir) * km * vm + (1.0 + ir) * kp * vp;
+}
+
+// A deposit component after `order` (<= 2) smoothing passes, at node i, computed from an
+// unsmoothed accessor F(p, c, i) (guard nodes 0 and nr + 1 are not smoothed).
+template <class FF>
+__device__ double smoothed_at(const GridDev& G, const FF& F, int kind, int m, int p, int c, int i, int order) {
+  const bool ax = smooth_ax(kind, m, c);
+  const auto s1 = [&](int k) {
+    if (k < 1 || k > G.nr) return F(p, c, k);
+    return smooth_node(G, k, ax, F(p, c, k - 1), F(p, c, k), F(p, c, k + 1));
+  };
+  if (order <= 0 || i < 1 || i > G.nr) return F(p, c, i);
+  if (order == 1) return s1(i);
+  return smooth_node(G, i, ax, s1(i - 1), s1(i), s1(i + 1));
+}
+
 // The decision from the maxima over nodes: relative and absolute residuals, convergence,
 // and the loop state (iteration count, statistics, WHILE condition).  One thread.
 __device__ inline void conv_decide_at(double mx_old, double mx_new, double reltol, double abstol, double* res,

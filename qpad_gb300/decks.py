@@ -59,6 +59,7 @@ class Deck:
     iter_abstol: float = 0.0
     dt: float = 10.0
     n_steps: int = 1
+    smooth_order: int = 0
 
     @property
     def np_per_slice(self) -> int:

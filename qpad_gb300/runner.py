@@ -30,6 +30,8 @@ def build_simulation(deck: Deck, precision=K.PREC_FP64, device=0, sort_freq=0, i
     sim = Simulation(deck.nr, deck.nz, deck.max_mode, deck.dr, deck.dxi, iter_max=deck.iter_max,
                      iter_reltol=deck.iter_reltol, iter_abstol=deck.iter_abstol, dt=deck.dt, precision=precision,
                      device=device)
+    if deck.smooth_order:
+        sim.set_smooth(deck.smooth_order)
     pl, beams = inputs if inputs is not None else deck_inputs(deck)
     x, p, g, ps, q = pl
     sim.add_species(x, p, g, ps, q, qbm=-1.0, npmax=max(1, len(q)), sort_freq=sort_freq)

@@ -187,3 +187,34 @@ def test_linear_wake_period():
     period = 2 * float(np.mean(np.diff(zc)))
     assert abs(period - 2 * math.pi) / (2 * math.pi) < 0.03, period
     assert ez[(xi > 1.0) & (xi < 2.5)].max() > 0            # decelerating field inside an electron driver
+
+
+def test_smooth_known_answer():
+    """One binomial smoothing pass (ufield_class.f03:274-339) written out by hand: kernel
+    (1, 2, 1)/4; node 1 the axis form where the mode/component switch is set (else 0), node 2
+    the near-axis form, nodes j >= 3 weighted by (1 -+ 1/(j-1)); guards unchanged.  Switches:
+    rho m=0; jay m=0 comp 2 and m=1 comps 0, 1; djdxi m=1 (field_src_class.f03)."""
+    nr, M = 7, 2
+    g = O.grid(nr, 4, M, 0.1, 0.1)
+    P, ld = 2 * M + 1, nr + 2
+    rng = np.random.default_rng(12)
+    for kind, nc in ((0, 1), (1, 3), (2, 2)):
+        f = rng.standard_normal(P * nc * ld)
+        got = O.smooth(g, kind, f.copy()).reshape(P, nc, ld)
+        v = f.reshape(P, nc, ld)
+        for p in range(P):
+            m = (p + 1) // 2
+            for c in range(nc):
+                ax = {0: m == 0, 1: (c == 2) if m == 0 else (m == 1 and c < 2), 2: m == 1}[kind]
+                w = v[p, c]
+                exp = w.copy()
+                exp[1] = (0.5 + 0.25) * w[1] + 8.0 * 0.25 * w[2] if ax else 0.0
+                exp[2] = 0.5 * w[2] + 0.125 * 0.25 * w[1] + 2.0 * 0.25 * w[3]
+                for j in range(3, nr + 1):
+                    r = float(j - 1)
+                    exp[j] = 0.5 * w[j] + (1.0 - 1.0 / r) * 0.25 * w[j - 1] + (1.0 + 1.0 / r) * 0.25 * w[j + 1]
+                assert np.array_equal(got[p, c], exp), (kind, p, c)
+    # a constant is preserved away from the axis
+    f = np.ones(P * ld)
+    O.smooth(g, 0, f)
+    assert np.all(f.reshape(P, ld)[:, 3:nr + 1] == 1.0)
