@@ -167,6 +167,8 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
+// kSmooth: the instance with the deposit smoothing (the other one carries none of its code)
+template <bool kSmooth>
 __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   extern __shared__ __align__(16) double smem[];
   __shared__ __align__(8) uint64_t mbar;
@@ -346,6 +348,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   // binomial smoothing of the finished deposits (amjdp_species2d, species2d_class.f03:270-272):
   // pass k is exact on window nodes [wb + k, wb + W - 1 - k], which covers the owned nodes and
   // their neighbours for k <= 2
+  if constexpr (kSmooth)
   for (int pass = 1; pass <= G.smooth; ++pass) {
     for (int q = t; q < c8_n * nh * W; q += blockDim.x) {
       const int row = q / W, x = q % W, c8 = c8_lo + row / nh, node = wb + x;
@@ -439,8 +442,12 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
       double s = 0.0;
       for (int q = 0; q < CL; ++q) s += *cluster.map_shared_rank(&divp, q);
       const RawFin CUg{&a.G, raw_cu, 0, 0, 3};    // nodes nr-2, nr-1 lie outside this window
-      const auto CUs = [&](int p, int c, int i) { return smoothed_at(a.G, CUg, 1, 0, p, c, i, a.G.smooth); };
-      dsm[3 * R + 0] = ez_axis_row(a.G, s, CUs);
+      if constexpr (kSmooth) {
+        const auto CUs = [&](int p, int c, int i) { return smoothed_at(a.G, CUg, 1, 0, p, c, i, a.G.smooth); };
+        dsm[3 * R + 0] = ez_axis_row(a.G, s, CUs);
+      } else {
+        dsm[3 * R + 0] = ez_axis_row(a.G, s, CUg);
+      }
     }
   }
   __syncthreads();
@@ -771,15 +778,18 @@ static int solve_lanes(int R) {
 }
 
 // Uses cluster size cl for k_iterate if the kernel can launch with it; nonzero otherwise.
+static void (*iterate_kernel(int smooth))(IterArgs) { return smooth > 0 ? k_iterate<true> : k_iterate<false>; }
+
 int iterate_try_cluster(qpad_ctx* ctx, int cl) {
   if (cl < 1 || cl > 16 || cl > ctx->g.nr) return QPAD_E_ARG;
   if ((ctx->g.nr + cl - 1) / cl > 32 * kMaxRL) return QPAD_E_CAPACITY;      // rows per CTA beyond the solver
-  cudaError_t e = cudaFuncSetAttribute(k_iterate, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  const auto kern = iterate_kernel(ctx->g.smooth);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return cuda_check(ctx, e, "cluster attribute");
   const int R = (ctx->g.nr + cl - 1) / cl;
   const size_t smem = iterate_smem_doubles(R, ctx->g.ld, ctx->g.smooth) * sizeof(double);
   if (smem > 200 * 1024) return QPAD_E_CAPACITY;
-  if (int r = raise_dyn_smem(ctx, (const void*)k_iterate, smem)) return r;
+  if (int r = raise_dyn_smem(ctx, (const void*)kern, smem)) return r;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2 * cl * (ctx->g.M + 1));
   cfg.blockDim = dim3(kIterThreads);
@@ -792,7 +802,7 @@ int iterate_try_cluster(qpad_ctx* ctx, int cl) {
   cfg.attrs = at;
   cfg.numAttrs = 1;
   int ncl = 0;
-  e = cudaOccupancyMaxActiveClusters(&ncl, k_iterate, &cfg);
+  e = cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg);
   if (e != cudaSuccess || ncl < 1) {
     cudaGetLastError();
     return QPAD_E_CAPACITY;
@@ -862,7 +872,7 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   cfg.attrs = at;
   cfg.numAttrs = (after_deposit && ctx->pdl) ? 2 : 1;
   prof_begin(ctx, "iterate");
-  cudaError_t e = cudaLaunchKernelEx(&cfg, k_iterate, a);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, iterate_kernel(ctx->g.smooth), a);
   prof_end(ctx, "iterate");
   if (e != cudaSuccess) return cuda_check(ctx, e, "k_iterate launch");
   return check_launch(ctx, "k_iterate");
