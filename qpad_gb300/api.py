@@ -336,6 +336,7 @@ class Beam3D:
         x, p, q = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, p, q))
         sim._check(sim.lib.qpad_beam_create(sim.h, C.byref(d), _dp(x), _dp(p), _dp(q), n, C.byref(h)))
         self.h = h
+        self.qbm, self.push_type, self.evolution, self.npmax = qbm, push_type, bool(evolution), npmax
 
     def count(self) -> int:
         n = C.c_int64()
