@@ -211,7 +211,9 @@ typedef struct qpad_slice_stats {
  * species and the stored beam charge. */
 int qpad_slice_step(qpad_ctx* ctx, int j, qpad_slice_stats* stats);
 /* One whole 3D step (simulation_class.f03:294-512 without diagnostics): beam deposit,
- * slices 1..nz, beam push; per-slice stats into stats[nz] (may be NULL). */
+ * slices 1..nz, beam push; per-slice stats into stats[nz] (may be NULL).  Returns
+ * QPAD_E_CUDA with a message if the field iteration's bounded wait for its staged inputs
+ * gave up during the step (the step's results are then not valid). */
 int qpad_3d_step(qpad_ctx* ctx, int push_beams, qpad_slice_stats* stats);
 
 /* ---- batches of independent simulations (no counterpart in the reference) -----------
