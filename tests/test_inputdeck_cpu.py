@@ -1,0 +1,86 @@
+"""The reference's JSON input deck (json-fortran dialect) read into this library's setup:
+keys, derived grid quantities, the accepted subset and refusals, and the particle inputs the
+CPU loaders make from it."""
+import copy
+import json
+import os
+
+import numpy as np
+import pytest
+
+from qpad_gb300 import _capi as K
+from qpad_gb300 import inputdeck as ID
+
+DECK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "decks", "two_beams.json")
+
+
+def _raw():
+    with open(DECK) as f:
+        return json.loads(ID.strip_comments(f.read()))
+
+
+def test_comments_stripped_outside_strings():
+    assert ID.strip_comments('{"a" : 1 ! note\n}') == '{"a" : 1 \n}'
+    assert json.loads(ID.strip_comments('{"a" : "x!y" ! c\n}')) == {"a": "x!y"}
+
+
+def test_parse_simulation_species_beams():
+    d = ID.read(DECK)
+    assert (d.nr, d.nz, d.max_mode) == (128, 96, 2)
+    assert d.dr == pytest.approx(0.04) and d.dxi == pytest.approx(0.04)
+    assert d.n_steps == 3 and d.dt == 10.0 and d.seed == 7
+    assert (d.iter_max, d.iter_reltol, d.iter_abstol) == (40, 1e-5, 1e-12)
+    assert d.bnd == K.BND_OPEN and d.relax_fac is None and d.start_step == 1
+    (s,) = d.species
+    assert s["ppc"] == (2, 2) and s["num_theta"] == 8 and s["push_type"] == K.PUSH2_STD
+    assert s["neutralized"] and s["smooth_order"] == 1 and s["qbm"] == -1.0
+    b1, b2 = d.beams
+    assert b1["tot_num"] == 20000 and b1["tot_charge"] == 3.5 and b1["push_type"] == K.PUSH3_REDUCED
+    assert b1["center"] == (0.03, 0.0, 1.2) and b1["range_hi"] == (1.5, 1.5, 3.2)
+    assert b2["qbm"] == -0.5 and b2["push_type"] == K.PUSH3_BORIS and b2["uth"] == (0.0, 0.0, 0.0)
+
+
+def test_restart_start_step():
+    raw = _raw()
+    raw["simulation"]["read_restart"] = True
+    assert ID.parse(raw).start_step == 5      # restart_timestep + 1 (simulation_class.f03:150-155)
+
+
+@pytest.mark.parametrize("path,value", [
+    (("simulation", "nlasers"), 1),
+    (("simulation", "nneutrals"), 2),
+    (("simulation", "interpolation"), "quadratic"),
+    (("beam", 0, "profile_type"), "standard"),
+    (("beam", 1, "profile"), ["gaussian", "gaussian", "uniform"]),
+    (("species", 0, "profile"), ["uniform", "piecewise-linear"]),
+    (("simulation", "box", "z"), [1.0, 4.84]),
+])
+def test_unsupported_features_refused(path, value):
+    raw = copy.deepcopy(_raw())
+    node = raw
+    for k in path[:-1]:
+        node = node[k]
+    node[path[-1]] = value
+    with pytest.raises(NotImplementedError):
+        ID.parse(raw)
+
+
+def test_missing_required_key():
+    raw = _raw()
+    del raw["simulation"]["iter_max"]
+    with pytest.raises(ValueError):
+        ID.parse(raw)
+
+
+def test_inputs_from_the_loaders():
+    d = ID.read(DECK)
+    (pl,), (b1, b2) = ID.inputs(d)
+    x, p, g, ps, q = pl
+    assert len(q) == d.nr * 2 * 2 * 8 and x.shape == (len(q), 2)
+    for (bx, bp, bq), spec in zip((b1, b2), d.beams):
+        assert len(bq) == spec["tot_num"] and bx.shape == (len(bq), 3)
+        lo, hi = np.array(spec["range_lo"]), np.array(spec["range_hi"])
+        assert np.all(bx >= lo - 1e-12) and np.all(bx <= hi + 1e-12)
+    # the same seed gives the same particles
+    (pl2,), _ = ID.inputs(d)
+    assert np.array_equal(pl2[0], x)
