@@ -191,3 +191,20 @@ def build(deck: InputDeck, precision=K.PREC_FP64, device=0) -> Simulation:
         sim.add_beam(x, p, q, qbm=b["qbm"], push_type=b["push_type"], evolution=b["evolution"],
                      npmax=max(1, len(q)))
     return sim
+
+
+def run(deck: InputDeck, sim: Simulation, steps: int | None = None):
+    """Runs the deck's 3D steps (deck.n_steps from deck.start_step, or `steps`): before every
+    step after the first, each species is renewed from that step's loader stream, as the
+    reference re-injects its plasma after each 3D step (species2d::renew,
+    species2d_class.f03:154-184).  Returns the per-step (iterations per slice, rel_res)."""
+    n = deck.n_steps if steps is None else steps
+    out = []
+    for k in range(n):
+        step = deck.start_step + k
+        if k > 0:
+            sp, _ = inputs(deck, step) if deck.species else ([], [])
+            for spec, (x, p, g, ps, q) in zip(sim.species, sp):
+                spec.renew(x, p, g, ps, q)
+        out.append(sim.run_3d_step())
+    return out
