@@ -174,8 +174,10 @@ def inputs(deck: InputDeck, step: int = 1):
     return sp, bm
 
 
-def build(deck: InputDeck, precision=K.PREC_FP64, device=0) -> Simulation:
-    """The simulation the deck describes, with its species and beams on the device."""
+def build(deck: InputDeck, precision=K.PREC_FP64, device=0, restart_root: str = ".") -> Simulation:
+    """The simulation the deck describes, with its species and beams on the device.  With
+    read_restart the beams come from their restart files at restart_timestep under
+    `restart_root` (sim_beams_class.f03:121-128) instead of the loader."""
     sim = Simulation(deck.nr, deck.nz, deck.max_mode, deck.dr, deck.dxi, bnd=deck.bnd, relax_fac=deck.relax_fac,
                      iter_max=deck.iter_max, iter_reltol=deck.iter_reltol, iter_abstol=deck.iter_abstol, dt=deck.dt,
                      precision=precision, device=device)
@@ -187,6 +189,10 @@ def build(deck: InputDeck, precision=K.PREC_FP64, device=0) -> Simulation:
     for s, (x, p, g, ps, q) in zip(deck.species, sp):
         sim.add_species(x, p, g, ps, q, qbm=s["qbm"], push_type=s["push_type"], neutralized=s["neutralized"],
                         npmax=s["npmax"] or max(1, len(q)), sort_freq=s["sort_freq"])
+    if deck.read_restart:
+        from . import restart
+        restart.load_beams(sim, restart_root, deck.start_step - 1, len(deck.beams))
+        return sim
     for b, (x, p, q) in zip(deck.beams, bm):
         sim.add_beam(x, p, q, qbm=b["qbm"], push_type=b["push_type"], evolution=b["evolution"],
                      npmax=max(1, len(q)))
