@@ -84,3 +84,29 @@ def test_inputs_from_the_loaders():
     # the same seed gives the same particles
     (pl2,), _ = ID.inputs(d)
     assert np.array_equal(pl2[0], x)
+
+
+def test_run_renews_plasma_before_later_steps():
+    d = ID.read(DECK)
+
+    class _Sp:
+        def __init__(self):
+            self.renewed = []
+
+        def renew(self, x, p, g, ps, q):
+            self.renewed.append(x.copy())
+
+    class _Sim:
+        def __init__(self):
+            self.species, self.steps = [_Sp()], 0
+
+        def run_3d_step(self):
+            self.steps += 1
+            return np.zeros(d.nz, np.int32), np.zeros(d.nz)
+
+    sim = _Sim()
+    out = ID.run(d, sim)
+    assert sim.steps == d.n_steps == len(out)
+    assert len(sim.species[0].renewed) == d.n_steps - 1
+    (pl2,), _ = ID.inputs(d, d.start_step + 1)
+    assert np.array_equal(sim.species[0].renewed[0], pl2[0])
