@@ -1,21 +1,26 @@
 """Benchmark of the quasi-static slice loop (one JSON line on rank 0).
 
-A step is one 3D step of the c2 deck: beam charge deposit, 1024 xi slices with the full
-B-perp predictor-corrector (iter_reltol 1e-6), beam push, and the plasma renewal that
-the reference performs after every 3D step.  The metric's first half, plasma
-particle-pushes/s, is the headline value (one plasma particle advanced through one
-slice, all of its predictor-corrector deposits included); B-perp iterations per slice
-are reported beside it.  The headline path is the mixed-precision one (FP32 particles,
-FP64 solves); the plain FP64 path runs on the same deck and inputs as the comparison arm
-("compare", "speedup_vs_fp64", "iters_change_vs_fp64").
+A step is one 3D step of the c5 deck (the largest single-GPU shape: M=4, nr=2048, 4096
+slices, 1.05e6 plasma particles per slice, 1e8 beam particles): beam charge deposit, every
+slice with the full B-perp predictor-corrector (iter_reltol 1e-6), beam push, and the
+plasma renewal that the reference performs after every 3D step.  The metric's first half,
+plasma particle-pushes/s, is the headline value (one plasma particle advanced through one
+slice, all of its predictor-corrector deposits included); B-perp iterations per slice are
+reported beside it.  The headline path is the mixed-precision one (FP32 particles, FP64
+solves).  The plain FP64 path runs on the same deck and inputs as the comparison arm
+("compare", "speedup_vs_fp64", "iters_change_vs_fp64"), and the per-mode field error of
+the mixed path against it over one whole 3D step from identical inputs is "max_mode_err"
+(the FP64 path itself matches the FP64 oracle to 1e-9; the oracle is too slow for a whole
+c5 step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--deck c2] [--precision mixed|fp64] [--no-compare]
+                  [--deck c5|c2|c1|c3] [--precision mixed|fp64] [--no-compare]
 
 --impl reference times the reference algorithm's CPU implementation (the project's C
 restatement of it, OpenMP over particles, every host core) on a bounded sample of the
-same deck; the Fortran reference itself cannot be built on these machines.
-Multi-GPU runs are independent replicas (one simulation per GPU, different seeds).
+same deck, with inputs from the oracle's own loaders; the Fortran reference itself cannot
+be built on these machines.  Multi-GPU runs are independent replicas (one simulation per
+GPU, different seeds).
 """
 from __future__ import annotations
 
@@ -92,50 +97,73 @@ class ClockSampler:
 
 
 def _deck(args):
-    from qpad_gb300 import decks
+    from qpad_gb300 import decks          # pure Python: the deck shapes, no library load
     d = decks.DECKS[args.deck]()
+    tags = []
     if args.slices:
         # profiling runs: the same slice workload over fewer slices
         d.nz = args.slices
-        d.name = f"{d.name}_nz{args.slices}"
+        tags.append(f"nz{args.slices}")
+    if args.beam_frac:
+        # profiling runs: fewer beam particles (a few GB on the device at most)
+        for b in d.beams:
+            b.num = max(1, int(b.num * args.beam_frac))
+        tags.append(f"beam{args.beam_frac:g}")
+    if tags:
+        d.name = d.name + "_" + "_".join(tags)
     return d
 
 
-def cpu_sample(deck, nslices, steps=1, nthreads=None):
-    """Times the oracle (C restatement of the reference loop, OpenMP over particles) on the
-    first `nslices` slices of the deck with every plasma particle; the beam charge of the
-    whole deck is deposited before the clock starts.  Returns pushes/s and details."""
-    import numpy as np
-
-    import qpad_gb300 as Q
+def oracle_inputs(deck):
+    """The deck's plasma and beams from the oracle's own loaders (orc_load_plasma /
+    orc_load_beam: the same seeded streams as the product's loaders, which the CPU tests
+    check bit for bit), so that the CPU arm never loads the product library."""
     from oracle import oracle as O
-    nthreads = nthreads or os.cpu_count()
-    pl, beams = Q.deck_inputs(deck)
     g = O.grid(deck.nr, deck.nz, deck.max_mode, deck.dr, deck.dxi)
-    x, p, gam, ps, q = pl
-    opl = O.Plasma(len(q))
-    opl.x[:], opl.y[:], opl.px[:], opl.py[:], opl.pz[:] = x[:, 0], x[:, 1], p[:, 0], p[:, 1], p[:, 2]
-    opl.gamma[:], opl.psi[:], opl.q[:] = gam, ps, q
-    sim = O.Sim(g, iter_max=deck.iter_max, iter_reltol=deck.iter_reltol, iter_abstol=deck.iter_abstol,
-                dt3d=deck.dt, sp_npmax=len(q), beams=[(-1.0, O.PUSH3_REDUCED, len(b[2])) for b in beams],
-                nthreads=nthreads)
-    for k, (bx, bp, bq) in enumerate(beams):
-        bm = O.Beam(len(bq))
-        bm.x[:], bm.y[:], bm.z[:], bm.px[:], bm.py[:], bm.pz[:], bm.q[:] = (bx[:, 0], bx[:, 1], bx[:, 2],
-                                                                               bp[:, 0], bp[:, 1], bp[:, 2], bq)
-        sim.set_beam(k, bm)
-    best, iters = None, []
-    for _ in range(steps):
-        sim.set_plasma(opl)
-        sim.begin_3dstep()
+    pl = O.load_plasma(g, deck.seed * 1000, deck.ppc[0], deck.ppc[1], deck.num_theta,
+                       uth=(deck.uth, deck.uth, deck.uth))
+    beams = []
+    for k, b in enumerate(deck.beams):
+        a = b.load_args(deck.nz, deck.dxi)
+        if a["range_lo"][2] >= a["range_hi"][2]:              # beam entirely behind a shortened box
+            beams.append(O.Beam(0))
+            continue
+        beams.append(O.load_beam(g, deck.seed * 1000 + 999 + k, a["tot_num"], a["tot_charge"], a["qm"], a["gamma"],
+                                 a["center"], a["sigma"], a["range_lo"], a["range_hi"], uth=a["uth"]))
+    return g, pl, beams
+
+
+class CpuSample:
+    """The oracle (C restatement of the reference loop, OpenMP over particles and modes) set up
+    once for a deck; run(n) times its first n slices with every plasma particle, the beam
+    charge of the whole deck deposited before the clock starts."""
+
+    def __init__(self, deck, nthreads=None):
+        from oracle import oracle as O
+        self.deck = deck
+        self.nthreads = nthreads or os.cpu_count()
+        g, self.pl, beams = oracle_inputs(deck)
+        self.sim = O.Sim(g, iter_max=deck.iter_max, iter_reltol=deck.iter_reltol, iter_abstol=deck.iter_abstol,
+                         dt3d=deck.dt, sp_npmax=self.pl.n,
+                         beams=[(spec.qm, O.PUSH3_REDUCED, b.n) for b, spec in zip(beams, deck.beams)],
+                         nthreads=self.nthreads)
+        for k, bm in enumerate(beams):
+            self.sim.set_beam(k, bm)
+
+    def run(self, nslices):
+        import numpy as np
+        self.sim.set_plasma(self.pl)
+        self.sim.begin_3dstep()
         t0 = time.perf_counter()
-        its = [sim.slice(j)[0] for j in range(1, nslices + 1)]
+        its = [self.sim.slice(j)[0] for j in range(1, nslices + 1)]
         t = time.perf_counter() - t0
-        if best is None or t < best:
-            best, iters = t, its
-    pushes = len(q) * nslices
-    return {"value": pushes / best, "seconds": best, "iters_per_slice": float(np.mean(iters)),
-            "cores": nthreads, "slices": nslices, "particles_per_slice": len(q)}
+        return {"value": self.pl.n * nslices / t, "seconds": t, "iters_per_slice": float(np.mean(its)),
+                "cores": self.nthreads, "slices": nslices, "particles_per_slice": self.pl.n}
+
+    def sample_text(self, nslices):
+        return (f"first {nslices} of {self.deck.nz} slices of {self.deck.name}, all {self.pl.n} plasma particles, "
+                f"full predictor-corrector, beam charge of the whole deck deposited before the clock, "
+                f"OpenMP oracle, inputs from the oracle's loaders")
 
 
 def run_reference(args):
@@ -143,31 +171,35 @@ def run_reference(args):
     if rank != 0:
         return 0
     deck = _deck(args)
-    nslices = args.cpu_slices
-    vals = []
-    info = None
+    cs = CpuSample(deck)
+    vals, info = [], None
     for k in range(args.warmup + args.steps):
-        info = cpu_sample(deck, nslices)
+        info = cs.run(args.cpu_slices)
         if k >= args.warmup:
             vals.append(info["value"])
     v = statistics.median(vals)
-    sample = (f"first {info['slices']} of {deck.nz} slices of {deck.name}, all {info['particles_per_slice']} "
-              f"plasma particles, full predictor-corrector, beam charge precomputed")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": deck.name, "sample_slices": info["slices"]},
             "iters_per_slice": info["iters_per_slice"],
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
+                             "sample": cs.sample_text(info["slices"])},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
-    """Times args.steps 3D steps of one simulation (after args.warmup untimed ones) on the
-    library's stream with CUDA events; with `full`, also the end-to-end pass with host
-    buffers and one host-driven step with per-kernel event timing."""
+def _stores(sim, names):
+    from qpad_gb300.diagnostics import ERROR_FIELDS
+    return {n: sim.fields[n].store_all() for n in (names or ERROR_FIELDS)}
+
+
+def _measure(args, deck, inputs, prec, local, dist, steps, warmup, full=True, guess=False, keep_stores=False):
+    """Times `steps` 3D steps of one simulation (after `warmup` untimed ones) on the library's
+    stream with CUDA events; with `full`, also the end-to-end pass with host buffers and one
+    host-driven step with per-kernel event timing.  With keep_stores, the 3D stores of the
+    first step (from the deck's inputs) come back in out["stores"]."""
     import qpad_gb300 as Q
     from qpad_gb300.replicas import reduce_timing
     sim = Q.build_simulation(deck, precision=prec, device=local, inputs=inputs)
@@ -175,9 +207,7 @@ def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
     tune = sim.autotune(reps=20) if not args.no_autotune else None
     if guess:
         from qpad_gb300 import learned as LR
-        from qpad_gb300.train_guess import DEFAULT_OUT
-        nets = LR.load(DEFAULT_OUT, deck.max_mode, device=local)
-        LR.attach(sim, *nets)
+        LR.attach(sim, *LR.load(LR.weights_path(deck.max_mode), deck.max_mode, device=local))
     sp = sim.species[0]
     npl = len(inputs[0][4])
 
@@ -185,9 +215,14 @@ def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
         if dist is not None:
             dist.barrier()
 
-    for _ in range(args.warmup):
+    stores, first_iters = None, None
+    for k in range(warmup):
         sp.reset()
-        sim.run_3d_step()
+        it, _ = sim.run_3d_step()
+        if k == 0:
+            first_iters = it
+            if keep_stores:
+                stores = _stores(sim, None)
     barrier()
     sim.synchronize()
     sim.profile(True)
@@ -195,7 +230,7 @@ def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
     iters_tot = 0
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             sp.reset()
             it, _ = sim.run_3d_step()
             iters_tot += int(it.sum())
@@ -208,11 +243,11 @@ def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
     dev_s = step_ms / 1e3 if nstep else wall
     barrier()
     pushes_step = npl * deck.nz
-    dev_s, total_pushes = reduce_timing(dev_s, float(pushes_step * args.steps), dist)
-    out = {"tune": tune, "value": total_pushes / dev_s, "ms_per_step": dev_s * 1e3 / args.steps,
-           "iters_per_slice": iters_tot / (args.steps * deck.nz), "wall_s": wall, "launches": launches,
+    dev_s, total_pushes = reduce_timing(dev_s, float(pushes_step * steps), dist)
+    out = {"tune": tune, "value": total_pushes / dev_s, "ms_per_step": dev_s * 1e3 / steps,
+           "iters_per_slice": iters_tot / (steps * deck.nz), "wall_s": wall, "launches": launches,
            "graph": {"active": graph_on, "status": graph_why}, "clocks": clk.summary(), "dev_s": dev_s,
-           "pushes_step": pushes_step}
+           "pushes_step": pushes_step, "stores": stores, "first_iters": first_iters}
     if full:
         # kernel timing pass (outside the timed region): one host-driven step with CUDA events
         # bracketing every launch of each kernel family on the library's stream
@@ -225,20 +260,22 @@ def _measure(args, deck, inputs, prec, local, dist, full=True, guess=False):
                                                          "beam_qdeposit", "step")}
         sim.profile(False)
         sim.use_graph(args.graph == "on")
-        # end to end through the C ABI with host buffers: renew from host arrays every step
+        # end to end through the C ABI with host buffers: renew from host arrays every step and
+        # read the per-slice statistics back
         x, p, g, ps, q = inputs[0]
         h2d = sum(a.nbytes for a in (x, p, g, ps, q))
         d2h = 0
+        e2e_steps = max(1, min(steps, args.e2e_steps))
         e2e_t0 = time.perf_counter()
-        for _ in range(max(1, args.steps)):
+        for _ in range(e2e_steps):
             sp.renew(x, p, g, ps, q)
             it, _ = sim.run_3d_step()
-            d2h += int(it.sum()) * 24 + 8
+            d2h += deck.nz * 24
         e2e_s = time.perf_counter() - e2e_t0
-        e2e_steps = max(1, args.steps)
         world = dist.get_world_size() if dist is not None else 1
         out["e2e"] = {"value": world * pushes_step * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                      "d2h_bytes_per_step": d2h // e2e_steps}
+                      "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps,
+                      "timing": "host wall clock around qpad_species_renew + qpad_3d_step"}
     sim.close()
     return out
 
@@ -307,9 +344,21 @@ def run_batch(args):
     return 0
 
 
+def _traffic(deck, precision):
+    """DRAM bytes per launch of the roofline kernels, copied from the committed ncu captures
+    (profiles/dram_traffic_per_launch.json) for this workload, or {} when none was made."""
+    tf = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.json")
+    try:
+        wl = deck.name.split("_nz")[0].split("_beam")[0]
+        return json.load(open(tf))["dram_bytes_per_launch"].get(wl, {}).get(precision, {})
+    except Exception:
+        return {}
+
+
 def run_ours(args):
     import qpad_gb300 as Q
     from qpad_gb300 import _capi as K
+    from qpad_gb300.diagnostics import step_error_report
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -326,40 +375,46 @@ def run_ours(args):
     inputs = Q.deck_inputs(deck)
     npl = len(inputs[0][4])
     nbeam = sum(len(b[2]) for b in inputs[1])
-    r = _measure(args, deck, inputs, prec, local, dist, full=True)
+    want_err = not args.no_compare
+    r = _measure(args, deck, inputs, prec, local, dist, args.steps, args.warmup, full=True, keep_stores=want_err)
     # the other arm of the metric: the plain FP64 path on the same deck and inputs
-    cmp = None
+    cmp, err = None, None
     if not args.no_compare:
         other = K.PREC_FP64 if prec == K.PREC_MIXED else K.PREC_MIXED
-        c = _measure(args, deck, inputs, other, local, dist, full=False)
+        csteps = args.compare_steps or args.steps
+        c = _measure(args, deck, inputs, other, local, dist, csteps, max(1, args.compare_warmup), full=False,
+                     keep_stores=True)
         cmp = {"path": "fp64" if other == K.PREC_FP64 else "mixed", "value": c["value"],
                "ms_per_step": c["ms_per_step"], "iters_per_slice": c["iters_per_slice"],
-               "graph": c["graph"]["active"]}
-    # the learned guess (trained nets for the c2 shape), measured as its own arm
+               "graph": c["graph"]["active"], "steps": csteps, "warmup": max(1, args.compare_warmup)}
+        ref_st, got_st = (c["stores"], r["stores"]) if other == K.PREC_FP64 else (r["stores"], c["stores"])
+        err = step_error_report(got_st or {}, ref_st or {}, deck.max_mode)
+        err["against"] = ("the plain FP64 GPU path on the same inputs, first 3D step (that path matches the FP64 "
+                          "oracle within 1e-9 over whole steps in the parity tests)")
+        ref_it, got_it = (c["first_iters"], r["first_iters"]) if other == K.PREC_FP64 else (r["first_iters"],
+                                                                                          c["first_iters"])
+        if got_it is not None and ref_it is not None:
+            err["iters_per_slice_first_step"] = {"mixed": float(got_it.mean()), "fp64": float(ref_it.mean())}
+        r["stores"] = c["stores"] = None
+    # the learned guess (trained nets for this deck's mode count), measured as its own arm
     learned = None
-    if not args.no_compare and deck.name.startswith("c2") and deck.max_mode == 2:
-        from qpad_gb300.train_guess import DEFAULT_OUT
-        if os.path.exists(DEFAULT_OUT):
-            g = _measure(args, deck, inputs, prec, local, dist, full=False, guess=True)
+    if not args.no_compare and not args.no_learned:
+        from qpad_gb300 import learned as LR
+        wp = LR.weights_path(deck.max_mode)
+        if os.path.exists(wp):
+            lsteps = args.learned_steps or args.steps
+            g = _measure(args, deck, inputs, prec, local, dist, lsteps, args.warmup, full=False, guess=True)
             learned = {"value": g["value"], "ms_per_step": g["ms_per_step"], "iters_per_slice": g["iters_per_slice"],
                        "iters_change": g["iters_per_slice"] / r["iters_per_slice"] - 1.0,
-                       "weights": os.path.relpath(DEFAULT_OUT, ROOT)}
+                       "weights": os.path.relpath(wp, ROOT), "steps": lsteps}
     kern = r["kern"]
     peak, peak_kind = _peaks()
-    traffic = {}
-    tf = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.json")
-    if os.path.exists(tf):
-        try:
-            # captured per workload; the profiling runs shorten the deck (same slice workload)
-            wl = deck.name.split("_nz")[0]
-            traffic = json.load(open(tf))["dram_bytes_per_launch"].get(wl, {}).get(args.precision, {})
-        except Exception:
-            traffic = {}
-    # the dominant kernel, k_iterate: algorithmic bytes of one launch (every mode) -- it reads
-    # the raw deposits (8 components), psi, B_old (2), b_beam (3), the factor rows of its three
-    # matrices and the node tables; it writes the finished deposits (8), zeroes the raw ones
-    # (8), writes dJ/dxi (2), b_spe, b, E (3 each), the convergence record and, on the mixed
-    # path, the FP32 gather table (6 floats per node and part)
+    traffic = _traffic(deck, args.precision)
+    # k_iterate: algorithmic bytes of one launch (every mode) -- it reads the raw deposits
+    # (8 components), psi, B_old (2), b_beam (3), the factor rows of its three matrices and the
+    # node tables; it writes the finished deposits (8), zeroes the raw ones (8), writes dJ/dxi
+    # (2), b_spe, b, E (3 each), the convergence record and, on the mixed path, the FP32
+    # gather table (6 floats per node and part)
     ld, P = deck.nr + 2, 2 * deck.max_mode + 1
     it_bytes = 8 * ((8 + 1 + 2 + 3) * P * ld + 9 * deck.nr * (deck.max_mode + 1) + 2 * ld) \
         + 8 * ((8 + 8 + 2 + 3 + 3 + 3) * P * ld + 2 * deck.nr) + (4 * 6 * P * ld if prec == K.PREC_MIXED else 0)
@@ -368,11 +423,29 @@ def run_ours(args):
     it_ach = it_bytes / it_avg_s / 1e9 if nit else None
     # the deposit: algorithmic bytes per particle of one amjdp pass: FP64 reads x, y, px, py,
     # pz, q and writes gamma, psi (64 B); mixed reads the cell word, two offsets, three
-    # momenta and q (28 B)
+    # momenta, psi and q (28 B; psi only on the standard pusher, counted once here)
     amj_ms, namj = kern["amjdp"]
     bytes_per_particle = 64 if prec == K.PREC_FP64 else 28
     amj_avg_s = (amj_ms / 1e3) / max(namj, 1)
     achieved = bytes_per_particle * npl / amj_avg_s / 1e9 if namj else None
+    it_roof = {"bound": "hbm", "achieved": it_ach, "peak": peak, "unit": "GB/s",
+               "frac": (it_ach / peak) if it_ach else None, "traffic": traffic.get("k_iterate"),
+               "kernel": "k_iterate", "peak_kind": peak_kind, "bytes_per_launch": it_bytes,
+               "avg_launch_us": it_avg_s * 1e6, "device_ms_per_step": it_ms,
+               "limiter": "latency: dependent FP64 chains and CTA/cluster barriers on an L2-resident "
+                          "per-slice working set"}
+    dep_name = "k_amjdp" if prec == K.PREC_FP64 else "k_mamjdp"
+    dep_roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic.get(dep_name),
+                "kernel": dep_name, "peak_kind": peak_kind, "bytes_per_launch": bytes_per_particle * npl,
+                "avg_launch_us": amj_avg_s * 1e6, "device_ms_per_step": amj_ms,
+                "limiter": "FP32 issue and load latency: gather, push and 16 x (M+1) deposit sums per particle"}
+    for rf in (it_roof, dep_roof):
+        rf["traffic_source"] = ("ncu capture of this workload, profiles/dram_traffic_per_launch.json"
+                                if rf["traffic"] is not None else "no capture of this workload")
+    # the dominant kernel of the step (by device time in the host-driven timing pass) is the
+    # roofline line; the other beside it
+    top_dep = amj_ms > it_ms
     dev_s = r["dev_s"]
     line = {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -383,31 +456,25 @@ def run_ours(args):
                    "plasma_particles_per_slice": npl, "beam_particles": nbeam, "path": args.precision,
                    "iter_reltol": deck.iter_reltol, "iter_max": deck.iter_max,
                    "l2": "step working set above L2 (beam arrays and 3D field stores); per-slice data L2-resident",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "cpu_sample": f"first {args.cpu_slices} slices (reference arm and cpu_baseline)"},
         "iters_per_slice": r["iters_per_slice"],
         "slices_per_s": world * deck.nz * args.steps / dev_s,
         "beam_pushes_per_s": world * nbeam * args.steps / dev_s,
         "wall_s": r["wall_s"],
         "e2e": r["e2e"],
         "gpu_launches": r["launches"],
-        "roofline": {"bound": "hbm", "achieved": it_ach, "peak": peak, "unit": "GB/s",
-                     "frac": (it_ach / peak) if it_ach else None, "traffic": traffic.get("k_iterate"),
-                     "kernel": "k_iterate", "peak_kind": peak_kind, "bytes_per_launch": it_bytes,
-                     "avg_launch_us": it_avg_s * 1e6,
-                     "limiter": "latency: dependent FP64 chains and CTA/cluster barriers on an L2-resident "
-                                "per-slice working set"},
-        "roofline_deposit": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": (achieved / peak) if achieved else None,
-                             "traffic": traffic.get("k_amjdp" if prec == K.PREC_FP64 else "k_mamjdp"),
-                             "kernel": "k_amjdp" if prec == K.PREC_FP64 else "k_mamjdp", "peak_kind": peak_kind,
-                             "bytes_per_launch": bytes_per_particle * npl, "avg_launch_us": amj_avg_s * 1e6,
-                             "limiter": "latency: particle and gather-table loads, one warp per cell work item"},
+        "roofline": dep_roof if top_dep else it_roof,
+        "roofline_other": it_roof if top_dep else dep_roof,
         "clocks": r["clocks"],
         "graph": r["graph"],
         "autotune": r["tune"],
         "kernel_ms_per_step": {k: round(v[0], 3) for k, v in kern.items()},
         "kernel_launches_per_step": {k: v[1] for k, v in kern.items()},
     }
+    if err is not None:
+        line["max_mode_err"] = err["max"]
+        line["mode_err"] = err
     if learned is not None:
         line["learned_guess"] = learned
     if cmp is not None:
@@ -415,10 +482,10 @@ def run_ours(args):
         line["speedup_vs_" + cmp["path"]] = r["value"] / cmp["value"]
         line["iters_change_vs_" + cmp["path"]] = r["iters_per_slice"] / cmp["iters_per_slice"] - 1.0
     if rank == 0 and not args.no_cpu_baseline:
-        cb = cpu_sample(deck, args.cpu_slices)
+        cs = CpuSample(deck)
+        cb = max((cs.run(args.cpu_slices) for _ in range(2)), key=lambda x: x["value"])
         line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": "port",
-                                "sample": f"first {cb['slices']} of {deck.nz} slices of {deck.name}, all "
-                                          f"{cb['particles_per_slice']} plasma particles, OpenMP oracle"}
+                                "sample": cs.sample_text(cb["slices"]), "iters_per_slice": cb["iters_per_slice"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -432,13 +499,20 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--deck", default="c2")
+    ap.add_argument("--deck", default="c5")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP64 (or mixed) comparison arm")
+    ap.add_argument("--compare-steps", type=int, default=1,
+                    help="timed steps of the comparison arm (0: as --steps); its first warm-up step gives the error")
+    ap.add_argument("--compare-warmup", type=int, default=1)
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess arm")
+    ap.add_argument("--learned-steps", type=int, default=3, help="timed steps of the learned-guess arm (0: --steps)")
+    ap.add_argument("--e2e-steps", type=int, default=5, help="steps of the end-to-end pass (at most --steps)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
-    ap.add_argument("--cpu-slices", type=int, default=48)
+    ap.add_argument("--cpu-slices", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slices", type=int, default=0, help="override the deck's slice count (profiling runs)")
+    ap.add_argument("--beam-frac", type=float, default=0.0, help="scale the beams' particle counts (profiling runs)")
     ap.add_argument("--graph", default="on", choices=["on", "off"],
                     help="off: host-driven slice loop (one launch per kernel, visible to per-kernel profilers)")
     args = ap.parse_args()

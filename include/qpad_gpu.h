@@ -111,6 +111,11 @@ int qpad_field_download(qpad_ctx* ctx, int field, int part, double* f1);
 /* 3D store f2(dim, 0:nr+1, slice) of one slice and part (slice 1..nz+1) */
 int qpad_store_download(qpad_ctx* ctx, int field, int slice, int part, double* f1);
 int qpad_store_upload(qpad_ctx* ctx, int field, int slice, int part, const double* f1);
+/* Slices slice_lo .. slice_lo+nslices-1 of a 3D store in one copy, in the device layout
+ * host[s][part][component][node] (node 0..nr+1): what the reference's diagnostics read from
+ * ufield%f2 (field_class.f03 write_hdf5, diagnostics_class.f03:822-944), without the
+ * per-part transposition of qpad_store_download. */
+int qpad_store_read(qpad_ctx* ctx, int field, int slice_lo, int nslices, double* host);
 /* field = value (assign_f1, field_class.f03:917-950) and field%as (f2) */
 int qpad_field_fill(qpad_ctx* ctx, int field, double value);
 int qpad_store_fill(qpad_ctx* ctx, int field, double value);
@@ -161,6 +166,11 @@ int qpad_species_reset(qpad_species* sp);
 int qpad_species_count(qpad_species* sp, int64_t* np);
 /* species2d::qdp (species2d_class.f03:186-208): q += deposit (+ qn if neutralized) */
 int qpad_species_qdp(qpad_species* sp, int q);
+/* species2d::cbq (species2d_class.f03:396-410): the species' charge density after the
+ * slice's iteration, rho = (rho - Jz) + Jz, i.e. q(1) += cu(3) over every mode part and node,
+ * then q's slice is stored at `slice` of its 3D store (copy_slice 1to2).  q and cu name the
+ * fields holding this species' own (rho - Jz) and current. */
+int qpad_species_cbq(qpad_species* sp, int q, int cu, int slice);
 /* species2d::amjdp (species2d_class.f03:233-280): cu, amu, dcu += deposits */
 int qpad_species_amjdp(qpad_species* sp, int ef, int bf, int cu, int amu, int dcu, double dt);
 /* No counterpart in the reference.  Same arguments and result as qpad_species_amjdp, but

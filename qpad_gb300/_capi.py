@@ -83,6 +83,7 @@ _SIGS = {
     "qpad_field_upload": (C.c_int, [C.c_void_p, C.c_int, C.c_int, D]),
     "qpad_field_download": (C.c_int, [C.c_void_p, C.c_int, C.c_int, D]),
     "qpad_store_download": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, D]),
+    "qpad_store_read": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, D]),
     "qpad_store_upload": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, D]),
     "qpad_field_fill": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "qpad_store_fill": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
@@ -105,6 +106,7 @@ _SIGS = {
     "qpad_species_download": (C.c_int, [C.c_void_p, D, D, D, D, D, I64P]),
     "qpad_species_count": (C.c_int, [C.c_void_p, I64P]),
     "qpad_species_qdp": (C.c_int, [C.c_void_p, C.c_int]),
+    "qpad_species_cbq": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "qpad_species_amjdp": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]),
     "qpad_species_amjdp_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                              C.c_double]),

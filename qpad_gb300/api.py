@@ -68,6 +68,15 @@ class Field:
             out[p] = buf.T
         return out
 
+    def store_all(self, lo: int = 1, n: int | None = None) -> np.ndarray:
+        """Slices lo .. lo+n-1 of the 3D store (default: 1..nz) in one copy, shaped
+        (n, P, ncomp, nr + 2)."""
+        s = self.sim
+        n = s.nz - lo + 1 if n is None else n
+        out = np.empty((n, s.P, self.ncomp, s.nr + 2))
+        s._check(s.lib.qpad_store_read(s.h, self.id, lo, n, _dp(out)))
+        return out
+
     def store_upload(self, slice_: int, arr: np.ndarray):
         s = self.sim
         arr = np.asarray(arr, dtype=np.float64)
@@ -309,6 +318,10 @@ class Species2D:
 
     def qdp(self, q: Field):
         self.sim._check(self.sim.lib.qpad_species_qdp(self.h, q.id))
+
+    def cbq(self, pos: int, q: Field, cu: Field):
+        """rho = (rho - Jz) + Jz into q, then q's slice `pos` into its 3D store (cbq_species2d)."""
+        self.sim._check(self.sim.lib.qpad_species_cbq(self.h, q.id, cu.id, int(pos)))
 
     def amjdp(self, ef: Field, bf: Field, cu: Field, amu: Field, dcu: Field, dt: float):
         self.sim._check(self.sim.lib.qpad_species_amjdp(self.h, ef.id, bf.id, cu.id, amu.id, dcu.id, dt))

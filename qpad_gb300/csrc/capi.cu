@@ -503,6 +503,19 @@ extern "C" int qpad_store_upload(qpad_ctx* ctx, int field, int slice, int part, 
   return f1_transfer(ctx, dev, nc, const_cast<double*>(f1), true);
 }
 
+extern "C" int qpad_store_read(qpad_ctx* ctx, int field, int slice_lo, int nslices, double* host) {
+  if (!ctx || !valid_field(field) || !has_store(field) || !host || nslices < 0 || slice_lo < 1 ||
+      (int64_t)slice_lo + nslices - 1 > ctx->g.nz + 1)
+    return ctx ? set_err(ctx, QPAD_E_ARG, "bad store range") : QPAD_E_ARG;
+  const size_t per = f1_elems(ctx, field);
+  if (nslices == 0) return 0;
+  if (int r = cuda_check(ctx, cudaMemcpyAsync(host, ctx->f2[field] + (size_t)(slice_lo - 1) * per,
+                                              per * (size_t)nslices * sizeof(double), cudaMemcpyDeviceToHost,
+                                              ctx->stream), "store read"))
+    return r;
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "store read sync");
+}
+
 extern "C" int qpad_field_fill(qpad_ctx* ctx, int field, double v) {
   if (!ctx || !valid_field(field)) return QPAD_E_ARG;
   const size_t n = f1_elems(ctx, field);
@@ -739,6 +752,17 @@ int ensure_scratch(qpad_ctx* ctx) {
   return dmalloc(ctx, (void**)&ctx->scratch, n * sizeof(double), "scratch");
 }
 }  // namespace
+
+extern "C" int qpad_species_cbq(qpad_species* sp, int q, int cu, int slice) {
+  if (!sp) return QPAD_E_ARG;
+  qpad_ctx* ctx = sp->ctx;
+  if (!valid_field(q) || field_ncomp(q) != 1 || !has_store(q) || !valid_field(cu) || field_ncomp(cu) != 3)
+    return set_err(ctx, QPAD_E_ARG, "cbq: q must be a one-component field with a 3D store, cu a three-component one");
+  if (slice < 1 || slice > ctx->g.nz + 1) return set_err(ctx, QPAD_E_ARG, "cbq: slice out of range");
+  const int32_t a = 3, b = 1;
+  if (int r = qpad_field_add_dim(ctx, cu, q, &a, &b, 1)) return r;
+  return qpad_field_copy_slice(ctx, q, slice, QPAD_COPY_1TO2);
+}
 
 extern "C" int qpad_species_amjdp(qpad_species* sp, int ef, int bf, int cu, int amu, int dcu, double dt) {
   if (!sp || !valid_field(ef) || !valid_field(bf) || !valid_field(cu) || !valid_field(amu) || !valid_field(dcu) ||

@@ -16,8 +16,11 @@
 //
 // Staging.  A CTA's inputs are rows on an even-aligned node window; warp 0 issues one
 // bulk copy per row onto an mbarrier when every row is 16-byte aligned (even nr and R),
-// otherwise every thread issues 8-byte cp.async copies.  The wait is bounded; a wait
-// that gives up sets an error word that the host reads after the step.
+// otherwise every thread issues 8-byte cp.async copies.  The wait is bounded; a CTA whose
+// wait gives up sets an error word that the host reads after the step, keeps taking part in
+// the cluster barriers and the convergence tickets (so that nothing else waits on it) but
+// writes no field, deposit or record to global memory, ends the slice's iteration loop, and
+// waits once more, bounded, for its own copies in flight before it retires.
 //
 // Solves.  Both substitutions of a factored tridiagonal system are first-order affine
 // recurrences.  Within a CTA, each right-hand side is taken by a group of gw lanes,
@@ -176,6 +179,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   __shared__ double wpart[kIterThreads / 32];
   __shared__ double divp;
   __shared__ unsigned int s_ticket;
+  __shared__ int s_gaveup;
   cg::cluster_group cluster = cg::this_cluster();
   const int CL = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
@@ -311,15 +315,18 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
           if (bytes) bulk_g2s(dst, src, bytes, &mbar);
         }
     }
-    if (t == 0) s_bulk = ok;
+    if (t == 0) {
+      s_bulk = ok;
+      s_gaveup = 0;
+    }
   }
-  __syncthreads();                                    // s_bulk and the mbarrier are set up
+  __syncthreads();                                    // s_bulk, s_gaveup and the mbarrier are set up
   griddep_wait();                                     // nothing below runs before the deposit is complete
   if (s_bulk) {
     int spins = 0;
     while (!mbar_try_wait(&mbar, 0u))
-      if (++spins > (1 << 20)) {                     // bounded wait: flag the error and go on
-        if (t == 0) atomicExch(a.err, 1);
+      if (++spins > (1 << 20)) {                     // bounded wait: give up (see below)
+        s_gaveup = 1;
         break;
       }
   } else {
@@ -337,6 +344,13 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     cp_async_wait_all();
   }
   __syncthreads();
+  // A wait that gave up: the host reads the error word after the step and reports its
+  // results as invalid.  The CTA still takes part in every cluster barrier and in the
+  // convergence tickets, so that its peers and the loop state finish, but from here on it
+  // writes nothing to global memory except that control state, and before it retires it
+  // waits (again bounded) for its own bulk copies still in flight.
+  const bool gave_up = s_gaveup != 0;
+  if (gave_up && t == 0) atomicExch(a.err, 1u);
   for (int q = t; q < c8_n * nh * W; q += blockDim.x) {   // finish the deposits in place
     const int row = q / W, k = q % W, c8 = c8_lo + row / nh, node = wb + k;
     if (node < 0 || node > nr + 1) continue;
@@ -642,12 +656,12 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     }
   };
   for (int q = t; q < Rc; q += blockDim.x)
-    if (!special(r0 + q + 1)) field_row(q);
+    if (!special(r0 + q + 1) && !gave_up) field_row(q);
   {
     const bool v0 = Rc > 0 && special(r0 + 1), v1 = Rc > 1 && special(r0 + 2), v2 = Rc > 2 && special(r0 + Rc);
     const int ns = (int)v0 + (int)v1 + (int)v2;
     const int sidx = (int)blockDim.x - 1 - t;
-    if (sidx < ns) {
+    if (sidx < ns && !gave_up) {
       int w = sidx, k = -1;
       if (v0) k = w-- == 0 ? 0 : k;
       if (v1 && k < 0) k = w-- == 0 ? 1 : k;
@@ -663,6 +677,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   // cleared raw deposits (every CTA of the cluster staged its window before the forward
   // barrier); threads first, first + stride, ...
   const auto late_stores = [&](int first, int stride) {
+    if (gave_up) return;
     const int i0 = rank == 0 ? 0 : r0 + 1, i1 = rank == CL - 1 ? nr + 1 : r1;
     const int nn = i1 - i0 + 1;
     for (int q = first; q < c8_n * nh * nn; q += stride) {
@@ -724,8 +739,10 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
       };
       double nre, nim, xo = 0.0, xn = 0.0;
       conv_node_v(G, Bc, kCompConv, i, ore, oim, true, nre, nim, xo, xn);
-      s_re[i - 1] = nre;
-      s_im[i - 1] = nim;
+      if (!gave_up) {
+        s_re[i - 1] = nre;
+        s_im[i - 1] = nim;
+      }
       mo = max(mo, (unsigned long long)__double_as_longlong(xo));
       mn = max(mn, (unsigned long long)__double_as_longlong(xn));
     }
@@ -745,16 +762,20 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
         mn = max(mn, rmn[w]);
       }
       unsigned long long* mx = a.maxima;
-      if (mo) red_max_u64(mx, mo);
-      if (mn) red_max_u64(mx + 1, mn);
+      if (mo && !gave_up) red_max_u64(mx, mo);
+      if (mn && !gave_up) red_max_u64(mx + 1, mn);
       a.tickets[rank] = 0u;
       if (atom_add_acq_rel(&a.tickets[CL], 1u) == (unsigned)(CL - 1)) {   // the last range: the decision
+        // (the error word loads with the maxima: no extra latency on the decision)
         const unsigned long long vo = __ldcg(mx), vn = __ldcg(mx + 1);
+        const unsigned ev = __ldcg(a.err);
         mx[0] = 0ull;
         mx[1] = 0ull;
         a.tickets[CL] = 0u;
-        conv_decide_at(__longlong_as_double((long long)vo), __longlong_as_double((long long)vn), a.reltol, a.abstol,
-                       a.conv + 2 * nr, a.L, it_prev, jp);
+        // after a give-up the iteration ends the slice (its results are invalid)
+        const bool failed = gave_up || ev != 0u;
+        conv_decide_at(__longlong_as_double((long long)vo), failed ? 0.0 : __longlong_as_double((long long)vn),
+                       a.reltol, a.abstol, a.conv + 2 * nr, a.L, it_prev, jp);
       }
     }
   }
@@ -762,6 +783,13 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
 
   if (!late_done) late_stores(t, (int)blockDim.x);
   cluster_wait();
+  if (gave_up && s_bulk && t == 0) {
+    // drain: bulk copies into this CTA's shared memory must land before it retires; a copy
+    // that has not completed after this second bounded wait cannot be cancelled
+    int spins = 0;
+    while (!mbar_try_wait(&mbar, 0u) && ++spins <= (1 << 22)) {
+    }
+  }
 }
 
 // ------------------------------------------------------------------------------------

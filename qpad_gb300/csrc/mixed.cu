@@ -8,12 +8,13 @@
 // Gather: E and B are read from an FP32 table [node][part][E0,E1,E2,B0,B1,B2] written by
 // the field kernels after every FP64 solve, so one particle reads two contiguous records.
 //
-// Deposit: each CTA takes a chunk of consecutive (sorted) particles, whose cells span a
-// narrow radial window.  Contributions are reduced across the warp when all 32 lanes sit
-// in the same cell (the common case for sorted particles), accumulated in an FP32
-// shared-memory tile of that window, and the tile is folded into the FP64 global mode
-// arrays with one atomic per entry.  Windows wider than the tile fall back to direct FP64
-// atomics.  The field solves that follow stay FP64.
+// Deposit: the counting sort after every push also writes deposit work items, each at most
+// one warp's worth of particles (32 x PPL, PPL = 1, 2 or 4) of a single radial cell.  A warp
+// takes an item: every particle of it deposits to the same two nodes, so each lane
+// accumulates its particles' contributions to the 2 nodes x Re/Im x 8 quantities of a mode
+// in registers, one transposing butterfly (31 shuffles) leaves each lane one total, and each
+// lane adds that total into the FP64 global mode arrays with one atomic.  The field solves
+// that follow stay FP64.
 //
 // Reference routines: part2d::qdeposit (part2d_class.f03:231-359), amjdeposit_robust /
 // _std (:746-1010, 478-744), push_u_robust / _std (:1879-1965, 1790-1877), push_x

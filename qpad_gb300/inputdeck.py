@@ -99,6 +99,8 @@ def parse(text_or_dict) -> InputDeck:
     _unsupported(int(sim.get("nlasers", 0)) != 0, "simulation.nlasers: lasers (PGC) are not built")
     _unsupported(int(sim.get("nneutrals", 0)) != 0, "simulation.nneutrals: neutrals / ionisation are not built")
     _unsupported(sim.get("interpolation", "linear") != "linear", "simulation.interpolation: only linear")
+    alg = sim.get("algorithm", "standard")
+    _unsupported(alg != "standard", f"simulation.algorithm: only the standard quasi-static loop ({alg})")
     fb = sim.get("field_boundary", "open")
     _unsupported(fb not in ("open", "zero"), f"simulation.field_boundary: {fb}")
     dt = float(_need(sim, "dt", "simulation"))
@@ -138,6 +140,10 @@ def parse(text_or_dict) -> InputDeck:
         _unsupported(prof != ["gaussian"] * 3, f"{w}.profile: only gaussian in all three directions ({prof})")
         _unsupported(b.get("geometry", "cartesian") != "cartesian", f"{w}.geometry: only cartesian")
         _unsupported(bool(b.get("has_spin", False)), f"{w}.has_spin: spin is not built")
+        # beam-shaping keys of fdist3d_rnd (fdist3d_rnd_class.f03:286-314): the Twiss alpha
+        # correlation and the xi-dependent transverse offsets
+        for key in ("alpha", "perp_offset_x", "perp_offset_y"):
+            _unsupported(key in b, f"{w}.{key}: not built")
         pt = b.get("push_type", "reduced")
         _unsupported(pt not in ("reduced", "boris"), f"{w}.push_type: {pt}")
         q, m = float(_need(b, "q", w)), float(b.get("m", 1.0))
@@ -158,17 +164,25 @@ def read(path: str) -> InputDeck:
         return parse(f.read())
 
 
-def inputs(deck: InputDeck, step: int = 1):
-    """Host arrays of every species (for 3D step `step`) and every beam, from the deck's seed
-    (the same stream convention as the synthetic decks: species k at seed*1000 + 100 k + step,
-    beam k at seed*1000 + 999 + k)."""
+def stream_seed(seed: int, kind: int, k: int, step: int = 0) -> int:
+    """Loader seed of one particle stream: species k (kind 0) at 3D step `step`, or beam k
+    (kind 1), mixed from the tuple by numpy's SeedSequence, so that no two streams of a run
+    coincide however many steps or species it has.  (The reference's random_seed 0 asks for
+    an OS-chosen seed; here every seed, 0 included, is reproducible.)"""
+    import numpy as np
+    return int(np.random.SeedSequence([int(seed), int(kind), int(k), int(step)]).generate_state(1, np.uint64)[0])
+
+
+def inputs(deck: InputDeck, step: int = 1, beams: bool = True):
+    """Host arrays of every species (for 3D step `step`) and, with `beams`, every beam, from
+    the deck's seed (one stream per species and step, one per beam: stream_seed)."""
     sp = []
     for k, s in enumerate(deck.species):
-        sp.append(load_plasma(deck.nr, deck.dr, deck.seed * 1000 + 100 * k + step, s["ppc"][0], s["ppc"][1],
+        sp.append(load_plasma(deck.nr, deck.dr, stream_seed(deck.seed, 0, k, step), s["ppc"][0], s["ppc"][1],
                               s["num_theta"], qm=s["q"], density=s["density"], uth=s["uth"]))
     bm = []
-    for k, b in enumerate(deck.beams):
-        bm.append(load_beam(deck.nr, deck.nz, deck.dr, deck.dxi, deck.seed * 1000 + 999 + k, b["tot_num"],
+    for k, b in enumerate(deck.beams if beams else []):
+        bm.append(load_beam(deck.nr, deck.nz, deck.dr, deck.dxi, stream_seed(deck.seed, 1, k), b["tot_num"],
                             b["tot_charge"], b["qm"], b["gamma"], b["center"], b["sigma"], b["range_lo"],
                             b["range_hi"], uth=b["uth"], quiet=b["quiet"]))
     return sp, bm
@@ -185,13 +199,17 @@ def build(deck: InputDeck, precision=K.PREC_FP64, device=0, restart_root: str = 
     _unsupported(len(orders) > 1, "species smooth_order: one order for all species")
     if orders and max(orders) > 0:
         sim.set_smooth(max(orders))
-    sp, bm = inputs(deck, deck.start_step)
+    sp, bm = inputs(deck, deck.start_step, beams=not deck.read_restart)
     for s, (x, p, g, ps, q) in zip(deck.species, sp):
         sim.add_species(x, p, g, ps, q, qbm=s["qbm"], push_type=s["push_type"], neutralized=s["neutralized"],
                         npmax=s["npmax"] or max(1, len(q)), sort_freq=s["sort_freq"])
     if deck.read_restart:
         from . import restart
-        restart.load_beams(sim, restart_root, deck.start_step - 1, len(deck.beams))
+        # the particles come from the files, the beam's parameters from the deck
+        # (sim_beams_class.f03 reads only x, p and q back)
+        restart.load_beams(sim, restart_root, deck.start_step - 1, len(deck.beams),
+                           params=[dict(qbm=b["qbm"], push_type=b["push_type"], evolution=b["evolution"])
+                                   for b in deck.beams])
         return sim
     for b, (x, p, q) in zip(deck.beams, bm):
         sim.add_beam(x, p, q, qbm=b["qbm"], push_type=b["push_type"], evolution=b["evolution"],
@@ -200,11 +218,13 @@ def build(deck: InputDeck, precision=K.PREC_FP64, device=0, restart_root: str = 
 
 
 def run(deck: InputDeck, sim: Simulation, steps: int | None = None):
-    """Runs the deck's 3D steps (deck.n_steps from deck.start_step, or `steps`): before every
-    step after the first, each species is renewed from that step's loader stream, as the
-    reference re-injects its plasma after each 3D step (species2d::renew,
-    species2d_class.f03:154-184).  Returns the per-step (iterations per slice, rel_res)."""
-    n = deck.n_steps if steps is None else steps
+    """Runs the deck's 3D steps start_step .. n_steps (the reference's `do i = start3d,
+    nstep3d`, simulation_class.f03:294; none when a restart is already past the end), or
+    `steps` steps from start_step: before every step after the first, each species is renewed
+    from that step's loader stream, as the reference re-injects its plasma after each 3D step
+    (species2d::renew, species2d_class.f03:154-184).  Returns the per-step (iterations per
+    slice, rel_res)."""
+    n = max(0, deck.n_steps - deck.start_step + 1) if steps is None else steps
     out = []
     for k in range(n):
         step = deck.start_step + k

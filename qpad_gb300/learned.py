@@ -10,6 +10,7 @@ normalisation).  Net ``m0`` serves m = 0 (10 -> 4 channels), net ``m1`` every m 
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -143,6 +144,15 @@ def attach(sim: Simulation, net0: ConvNet | None, net1: ConvNet | None):
 def configure(sim: Simulation, apply_b=True, apply_j=True, weight=1.0):
     """Which parts of the attached guess are used, and the weight of the net's correction."""
     sim._check(sim.lib.qpad_guess_config(sim.h, int(apply_b) | (2 * int(apply_j)), float(weight)))
+
+
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
+
+
+def weights_path(max_mode: int) -> str:
+    """Trained weights for simulations with `max_mode` modes: guess_c2.npz (trained on
+    c2-shaped runs, M = 2) serves M <= 2, guess_c5.npz (c5-shaped runs, M = 4) larger M."""
+    return os.path.join(WEIGHTS, "guess_c2.npz" if max_mode <= 2 else "guess_c5.npz")
 
 
 def save(path, net0: ConvNet, net1: ConvNet | None):

@@ -37,9 +37,11 @@ def save_beams(sim, root: str, timestep: int, rank: int = 0) -> list[str]:
     return paths
 
 
-def load_beams(sim, root: str, timestep: int, nbeams: int, rank: int = 0) -> list:
+def load_beams(sim, root: str, timestep: int, nbeams: int, rank: int = 0, params: list | None = None) -> list:
     """Re-creates beams 1..nbeams on `sim` from their restart files at `timestep` (the
-    reference's read_restart start-up); returns the new beams."""
+    reference's read_restart start-up); returns the new beams.  `params[i]` (qbm, push_type,
+    evolution), when given, overrides what the file recorded: the reference takes them from
+    the input deck and only the particles from the file."""
     out = []
     for i in range(1, nbeams + 1):
         path = rst_path(root, i, timestep, rank)
@@ -48,6 +50,8 @@ def load_beams(sim, root: str, timestep: int, nbeams: int, rank: int = 0) -> lis
         with np.load(path) as d:
             n = int(d["npp"])
             x, p, q = d["x"][:n], d["p"][:n], d["q"][:n]
-            out.append(sim.add_beam(x, p, q, qbm=float(d["qbm"]), push_type=int(d["push_type"]),
-                                    evolution=bool(int(d["evolution"])), npmax=max(int(d["npmax"]), n, 1)))
+            kw = dict(qbm=float(d["qbm"]), push_type=int(d["push_type"]), evolution=bool(int(d["evolution"])))
+            if params is not None:
+                kw.update(params[i - 1])
+            out.append(sim.add_beam(x, p, q, npmax=max(int(d["npmax"]), n, 1), **kw))
     return out

@@ -120,3 +120,38 @@ def test_field_arithmetic_and_slices():
     sim.e.copy_slice(3, Q._capi.COPY_2TO1)
     assert np.array_equal(sim.e.download(), b)
     sim.close()
+
+
+def test_species_cbq():
+    """cbq_species2d (species2d_class.f03:396-410): q(1) += cu(3), then q's slice into its store;
+    the store read in one copy returns the same slices."""
+    import qpad_gb300 as Q
+    rng = np.random.default_rng(12)
+    nr, M, nz = 48, 2, 6
+    g = O.grid(nr, nz, M, 0.05, 0.05)
+    sim = Q.Simulation(nr, nz, M, 0.05, 0.05)
+    x, p, gam, ps, qq = Q.load_plasma(nr, 0.05, 3, 1, 1, 8)
+    sp = sim.add_species(x, p, gam, ps, qq)
+    sim.q_spe.store_fill(0.0)
+    expect = {}
+    for pos in (1, 4, nz):
+        q = smooth_field(rng, g, 1)
+        cu = smooth_field(rng, g, 3, zero_guards=False)
+        sim.q_spe.upload(q)
+        sim.cu.upload(cu)
+        sp.cbq(pos, sim.q_spe, sim.cu)
+        want = q.copy()
+        want[:, 0] += cu[:, 2]
+        assert np.array_equal(sim.q_spe.download(), want)
+        assert np.array_equal(sim.q_spe.store(pos), want)
+        expect[pos] = want
+    allq = sim.q_spe.store_all()
+    assert allq.shape == (nz, 2 * M + 1, 1, nr + 2)
+    for pos, want in expect.items():
+        assert np.array_equal(allq[pos - 1], want)
+    assert np.count_nonzero(allq[1]) == 0
+    with pytest.raises(Q.QpadError):
+        sp.cbq(nz + 2, sim.q_spe, sim.cu)
+    with pytest.raises(Q.QpadError):
+        sp.cbq(1, sim.cu, sim.q_spe)
+    sim.close()

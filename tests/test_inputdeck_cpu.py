@@ -54,6 +54,11 @@ def test_restart_start_step():
     (("beam", 1, "profile"), ["gaussian", "gaussian", "uniform"]),
     (("species", 0, "profile"), ["uniform", "piecewise-linear"]),
     (("simulation", "box", "z"), [1.0, 4.84]),
+    (("simulation", "algorithm"), "subcycling"),
+    (("beam", 0, "alpha"), [0.5, 0.5]),
+    (("beam", 0, "perp_offset_x"), [0.0, 0.1]),
+    (("beam", 1, "perp_offset_y"), [0.0, 0.1]),
+    (("beam", 1, "has_spin"), True),
 ])
 def test_unsupported_features_refused(path, value):
     raw = copy.deepcopy(_raw())
@@ -110,3 +115,38 @@ def test_run_renews_plasma_before_later_steps():
     assert len(sim.species[0].renewed) == d.n_steps - 1
     (pl2,), _ = ID.inputs(d, d.start_step + 1)
     assert np.array_equal(sim.species[0].renewed[0], pl2[0])
+
+
+def _counting_sim(d):
+    class _Sp:
+        def renew(self, *a):
+            pass
+
+    class _Sim:
+        def __init__(self):
+            self.species, self.steps = [_Sp() for _ in d.species], 0
+
+        def run_3d_step(self):
+            self.steps += 1
+            return np.zeros(d.nz, np.int32), np.zeros(d.nz)
+    return _Sim()
+
+
+def test_restart_runs_only_the_remaining_steps():
+    # the reference loops i = start3d .. nstep3d (simulation_class.f03:294)
+    raw = _raw()
+    raw["simulation"]["read_restart"] = True
+    d = ID.parse(raw)
+    for rst, expect in ((0, d.n_steps), (1, d.n_steps - 1), (d.n_steps - 1, 1), (d.n_steps, 0), (d.n_steps + 3, 0)):
+        raw["simulation"]["restart_timestep"] = rst
+        dd = ID.parse(raw)
+        assert dd.start_step == rst + 1
+        sim = _counting_sim(dd)
+        assert len(ID.run(dd, sim)) == expect == sim.steps
+
+
+def test_loader_streams_distinct():
+    seeds = {ID.stream_seed(7, 0, k, s) for k in range(3) for s in range(1, 1200)}
+    seeds |= {ID.stream_seed(7, 1, k) for k in range(4)}
+    assert len(seeds) == 3 * 1199 + 4
+    assert ID.stream_seed(7, 0, 1, 5) == ID.stream_seed(7, 0, 1, 5)
