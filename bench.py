@@ -195,6 +195,17 @@ def _stores(sim, names):
     return {n: sim.fields[n].store_all() for n in (names or ERROR_FIELDS)}
 
 
+def _first_step_stores(args, deck, inputs, prec, local):
+    """The error fields' 3D stores after one 3D step from `inputs` (untimed)."""
+    import qpad_gb300 as Q
+    sim = Q.build_simulation(deck, precision=prec, device=local, inputs=inputs)
+    sim.use_graph(args.graph == "on")
+    sim.run_3d_step()
+    out = _stores(sim, None)
+    sim.close()
+    return out
+
+
 def _measure(args, deck, inputs, prec, local, dist, steps, warmup, full=True, guess=False, keep_stores=False):
     """Times `steps` 3D steps of one simulation (after `warmup` untimed ones) on the library's
     stream with CUDA events; with `full`, also the end-to-end pass with host buffers and one
@@ -395,6 +406,20 @@ def run_ours(args):
                                                                                           c["first_iters"])
         if got_it is not None and ref_it is not None:
             err["iters_per_slice_first_step"] = {"mixed": float(got_it.mean()), "fp64": float(ref_it.mean())}
+        if prec == K.PREC_MIXED and not args.no_sensitivity and ref_st:
+            # how much the deck amplifies round-off: the FP64 path run again from the same
+            # inputs differs from the first run only by the order of its atomic additions
+            # (FP64 round-off); the mixed path's error against FP32 unit round-off amplified
+            # by the same factor says whether it is at the limit of FP32 particle state
+            rep = step_error_report(_first_step_stores(args, deck, inputs, K.PREC_FP64, local), ref_st,
+                                    deck.max_mode)
+            amp = 2.0 ** -24 / 2.0 ** -53
+            ratios = [v / (amp * rep["per_mode"][k]) for k, v in err["per_mode"].items()
+                      if rep["per_mode"].get(k, 0.0) > 0.0]
+            err["fp64_repeat"] = {"max": rep["max"], "worst": rep["worst"], "per_mode": rep["per_mode"],
+                                  "what": "FP64 path run twice from the same inputs (atomic-order round-off), "
+                                          "first step"}
+            err["max_ratio_to_amplified_fp32_roundoff"] = max(ratios) if ratios else None
         r["stores"] = c["stores"] = None
     # the learned guess (trained nets for this deck's mode count), measured as its own arm
     learned = None
@@ -505,6 +530,8 @@ def main():
     ap.add_argument("--compare-steps", type=int, default=1,
                     help="timed steps of the comparison arm (0: as --steps); its first warm-up step gives the error")
     ap.add_argument("--compare-warmup", type=int, default=1)
+    ap.add_argument("--no-sensitivity", action="store_true",
+                    help="skip the repeated FP64 run that measures how much the deck amplifies round-off")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess arm")
     ap.add_argument("--learned-steps", type=int, default=3, help="timed steps of the learned-guess arm (0: --steps)")
     ap.add_argument("--e2e-steps", type=int, default=5, help="steps of the end-to-end pass (at most --steps)")

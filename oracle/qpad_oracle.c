@@ -1296,6 +1296,7 @@ struct orc_sim {
   double *psi, *e, *e_spe, *b, *b_spe, *b_beam, *cu, *amu, *acu, *dcu, *q_spe, *q_beam, *qsp, *qn;
   /* 3D stores */
   double *q_beam2, *e2, *b2, *psi2, *b_spe2, *e_spe2, *cu2, *q_spe2;
+  double *q_beamk;  /* one beam's own charge store (beam3d%q), summed into q_beam2 */
   /* plasma */
   int64_t np;
   double *x, *y, *px, *py, *pz, *gamma, *ppsi, *q;
@@ -1322,6 +1323,7 @@ orc_sim* orc_sim_create(const orc_sim_desc* d) {
   s->q_beam2 = zalloc(s->n2); s->e2 = zalloc(3 * s->n2); s->b2 = zalloc(3 * s->n2);
   s->psi2 = zalloc(s->n2); s->b_spe2 = zalloc(3 * s->n2); s->e_spe2 = zalloc(3 * s->n2);
   s->cu2 = zalloc(3 * s->n2); s->q_spe2 = zalloc(s->n2);
+  s->q_beamk = d->nbeams > 1 ? zalloc(s->n2) : NULL;
   int64_t npm = d->sp_npmax;
   s->x = zalloc(npm); s->y = zalloc(npm); s->px = zalloc(npm); s->py = zalloc(npm);
   s->pz = zalloc(npm); s->gamma = zalloc(npm); s->ppsi = zalloc(npm); s->q = zalloc(npm);
@@ -1340,7 +1342,7 @@ void orc_sim_destroy(orc_sim* s) {
   double* all[] = {s->psi, s->e, s->e_spe, s->b, s->b_spe, s->b_beam, s->cu, s->amu, s->acu, s->dcu,
                    s->q_spe, s->q_beam, s->qsp, s->qn, s->q_beam2, s->e2, s->b2, s->psi2, s->b_spe2,
                    s->e_spe2, s->cu2, s->q_spe2, s->x, s->y, s->px, s->py, s->pz, s->gamma, s->ppsi,
-                   s->q, s->s_re, s->s_im};
+                   s->q, s->s_re, s->s_im, s->q_beamk};
   for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); ++i) free(all[i]);
   for (int k = 0; k < s->d.nbeams; ++k) {
     free(s->bx[k]); free(s->by[k]); free(s->bz[k]); free(s->bpx[k]); free(s->bpy[k]);
@@ -1384,8 +1386,17 @@ void orc_sim_begin_3dstep(orc_sim* s) {
   /* simulation_class.f03:309-317 */
   memset(s->q_beam2, 0, sizeof(double) * s->n2);
   memset(s->q_spe2, 0, sizeof(double) * s->n2);
-  for (int k = 0; k < s->d.nbeams; ++k)
-    orc_beam_qdeposit(g, s->nb[k], s->bx[k], s->by[k], s->bz[k], s->bq[k], s->q_beam2);
+  /* beam3d::qdp (beam3d_class.f03:193-221): each beam deposits into its own zeroed store,
+     which part3d::qdeposit finishes (axis rule, 1/(i-1)), then add_f2 into q_beam */
+  if (s->d.nbeams == 1) {
+    orc_beam_qdeposit(g, s->nb[0], s->bx[0], s->by[0], s->bz[0], s->bq[0], s->q_beam2);
+  } else {
+    for (int k = 0; k < s->d.nbeams; ++k) {
+      memset(s->q_beamk, 0, sizeof(double) * s->n2);
+      orc_beam_qdeposit(g, s->nb[k], s->bx[k], s->by[k], s->bz[k], s->bq[k], s->q_beamk);
+      for (size_t i = 0; i < s->n2; ++i) s->q_beam2[i] = s->q_beam2[i] + s->q_beamk[i];
+    }
+  }
   /* :332-341 */
   memset(s->b, 0, 3 * n1 * sizeof(double)); memset(s->e, 0, 3 * n1 * sizeof(double));
   memset(s->b_spe, 0, 3 * n1 * sizeof(double)); memset(s->e_spe, 0, 3 * n1 * sizeof(double));

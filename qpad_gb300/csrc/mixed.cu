@@ -57,6 +57,42 @@ __device__ __forceinline__ int32_t pack_cell(int ix, int iy) {
   return (int32_t)(((uint32_t)(uint16_t)(int16_t)ix) | ((uint32_t)(uint16_t)(int16_t)iy << 16));
 }
 
+// gamma - u_z of a momentum u with gamma = sqrt(1 + |u|^2), without the cancellation of
+// the difference for u_z > 0: (gamma - u_z)(gamma + u_z) = 1 + u_x^2 + u_y^2.  In FP32 the
+// plain difference loses about log2(2 u_z^2 / (1 + u_perp^2)) bits for a relativistic
+// particle moving forward (sheath electrons of a blowout), which the FP64 reference does
+// not notice but an FP32 push would.
+__device__ __forceinline__ float gamma_minus_uz(float ux, float uy, float uz, float gam) {
+  return uz > 0.0f ? (1.0f + ux * ux + uy * uy) / (gam + uz) : gam - uz;
+}
+
+// Radial cell K = floor(r) and fraction d = r - K of a particle at (ix + fx, iy + fy) cells,
+// to the FP32 precision of d itself.  X = ix + fx rounded to FP32 keeps only
+// 24 - log2|X| bits of the offset (about 1e-5 of a cell at X = 500), so away from the axis
+// r is not formed from X: r - K = (r^2 - K^2) / (r + K), whose numerator splits into the
+// exact integer ix^2 + iy^2 - K^2 and 2 (ix fx + iy fy) + fx^2 + fy^2, both small next to
+// r + K.  Within 4 cells of the axis X and Y are nearly exact and the plain radius is the
+// more precise.  r_est: sqrtf(X^2 + Y^2).
+__device__ __forceinline__ void cell_radius(int ix, int iy, float fx, float fy, float r_est, int& K, float& d) {
+  K = (int)r_est;
+  d = r_est - (float)K;
+  if (r_est < 4.0f) return;
+  const float B = 2.0f * ((float)ix * fx + (float)iy * fy) + (fx * fx + fy * fy);
+  const long long s2 = (long long)ix * ix + (long long)iy * iy;
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    d = ((float)(s2 - (long long)K * K) + B) / (r_est + (float)K);
+    if (d < 0.0f) {
+      --K;
+    } else if (d >= 1.0f) {
+      ++K;
+    } else {
+      return;
+    }
+  }
+  d = fminf(fmaxf(d, 0.0f), 0.99999994f);   // (a third step is never needed: |r_est - r| << 1)
+}
+
 // Radial interpolation data in cell units (FP32).
 struct MInterp {
   float w0, w1, pcos, psin;
@@ -69,14 +105,16 @@ __device__ __forceinline__ MInterp minterp(int32_t c, float fx, float fy, int nr
   unpack_cell(c, ix, iy);
   const float X = (float)ix + fx, Y = (float)iy + fy;
   const float r = sqrtf(X * X + Y * Y);
+  int K;
+  float d;
+  cell_radius(ix, iy, fx, fy, r, K, d);
   MInterp m;
   m.pcos = X / r;
   m.psin = Y / r;
-  m.ok = r >= 0.0f && r < (float)nr;
-  const int ip = m.ok ? (int)r : 0;
-  m.idx = ip + 1;
-  m.w1 = m.ok ? r - (float)ip : 0.0f;
-  m.w0 = m.ok ? 1.0f - m.w1 : 0.0f;
+  m.ok = K >= 0 && K < nr;
+  m.idx = (m.ok ? K : 0) + 1;
+  m.w1 = m.ok ? d : 0.0f;
+  m.w0 = m.ok ? 1.0f - d : 0.0f;
   return m;
 }
 
@@ -218,11 +256,11 @@ __device__ __forceinline__ void mpredict(const GridDev& G, int push_type, float 
   const float psi_in = pv[3];
   if (push_type == QPAD_PUSH2_ROBUST) {
     float gam = sqrtf(1.0f + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
-    const float qtmh1 = qtmh * gam / (gam - u0[2]);
+    const float qtmh1 = qtmh * gam / gamma_minus_uz(u0[0], u0[1], u0[2], gam);
 #pragma unroll
     for (int c = 0; c < 3; ++c) { ep[c] *= qtmh1; ut[c] = u0[c] + ep[c]; }
     gam = sqrtf(1.0f + ut[0] * ut[0] + ut[1] * ut[1] + ut[2] * ut[2]);
-    const float qtmh2 = qtmh / (gam - ut[2]);
+    const float qtmh2 = qtmh / gamma_minus_uz(ut[0], ut[1], ut[2], gam);
 #pragma unroll
     for (int c = 0; c < 3; ++c) bp[c] *= qtmh2;
   } else {
@@ -260,8 +298,12 @@ __device__ __forceinline__ void mpredict(const GridDev& G, int push_type, float 
   const float g = sqrtf(1.0f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
   float ipsi;
   if (push_type == QPAD_PUSH2_ROBUST) {
-    ipsi = 1.0f / (g - u[2]);
-    if (write_back) { A.gam[i] = g; A.psi[i] = (1.0f - 1.0f / ipsi) / qbm; }
+    ipsi = 1.0f / gamma_minus_uz(u[0], u[1], u[2], g);
+    // psi = (1 - gamma + u_z) / qbm with gamma - 1 = |u|^2 / (gamma + 1): no cancellation
+    if (write_back) {
+      A.gam[i] = g;
+      A.psi[i] = (u[2] - (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) / (g + 1.0f)) / qbm;
+    }
   } else {
     ipsi = 1.0f / (1.0f - qbm * psi_in);
     A.gam[i] = g;
@@ -412,7 +454,7 @@ __global__ void __launch_bounds__(kMixThreads) k_mpush(GridDev G, int push_type,
   float qtmh1, qtmh2;
   if (push_type == QPAD_PUSH2_ROBUST) {
     const float gam = sqrtf(1.0f + p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
-    qtmh1 = qtmh / (gam - p[2]);
+    qtmh1 = qtmh / gamma_minus_uz(p[0], p[1], p[2], gam);
     qtmh2 = qtmh1 * gam;
   } else {
     qtmh1 = qtmh / (1.0f - qbm * A.psi[i]);
@@ -438,7 +480,7 @@ __global__ void __launch_bounds__(kMixThreads) k_mpush(GridDev G, int push_type,
   }
   if (!do_x) return;
   // x += p dt / (gamma - pz), in cell units, renormalising the offset into [0,1)
-  const float dtc = dt / (g - p[2]) * (float)G.idr;
+  const float dtc = dt / gamma_minus_uz(p[0], p[1], p[2], g) * (float)G.idr;
   fx += p[0] * dtc;
   fy += p[1] * dtc;
   const float sx = floorf(fx), sy = floorf(fy);
@@ -446,13 +488,16 @@ __global__ void __launch_bounds__(kMixThreads) k_mpush(GridDev G, int push_type,
   iy += (int)sy; fy -= sy;
   if (fx >= 1.0f) { fx -= 1.0f; ix += 1; }
   if (fy >= 1.0f) { fy -= 1.0f; iy += 1; }
+  const bool inside = ix > -32000 && ix < 32000 && iy > -32000 && iy < 32000;
   const float X = (float)ix + fx, Y = (float)iy + fy;
-  const float r = sqrtf(X * X + Y * Y);
-  const bool alive = r < (float)G.nr && ix > -32000 && ix < 32000 && iy > -32000 && iy < 32000;
+  int K = G.nr;
+  float d;
+  if (inside) cell_radius(ix, iy, fx, fy, sqrtf(X * X + Y * Y), K, d);
+  const bool alive = inside && K < G.nr;
   A.cxy[i] = pack_cell(alive ? ix : 0, alive ? iy : 0);
   A.fx[i] = fx;
   A.fy[i] = fy;
-  A.key[i] = alive ? (int)r + 1 : G.nr + 1;
+  A.key[i] = alive ? K + 1 : G.nr + 1;
 }
 
 // ------------------------------------------------------------------------------------
@@ -559,10 +604,12 @@ __global__ void k_to_mixed(GridDev G, const int64_t* __restrict__ n_ptr, const d
   A.px[i] = (float)px[i]; A.py[i] = (float)py[i]; A.pz[i] = (float)pz[i];
   A.gam[i] = (float)gam[i]; A.psi[i] = (float)psi[i]; A.q[i] = (float)q[i];
   const float X = (float)ix + fx, Y = (float)iy + fy;
-  const float r = sqrtf(X * X + Y * Y);
+  int K;
+  float d;
+  cell_radius(ix, iy, fx, fy, sqrtf(X * X + Y * Y), K, d);
   // a particle handed in beyond the edge is kept (the reference removes particles only in
   // update_bound after a push); it sorts into the last cell and deposits nothing
-  A.key[i] = r < (float)G.nr ? (int)r + 1 : G.nr;
+  A.key[i] = K < G.nr ? K + 1 : G.nr;
 }
 
 __global__ void k_to_fp64(GridDev G, const int64_t* __restrict__ n_ptr, MArr A, double* __restrict__ x,

@@ -49,3 +49,22 @@ def step_error_report(got: dict, ref: dict, max_mode: int) -> dict:
     key = max(per, key=lambda k: per[k][0])
     return {"max": per[key][0], "worst": key, "worst_slice": per[key][1],
             "per_mode": {k: float(f"{v[0]:.4g}") for k, v in per.items()}}
+
+
+def fp32_state(pl, dr):
+    """The plasma arrays (x, p, gamma, psi, q) rounded as the mixed path holds them (integer
+    cell + FP32 offset per coordinate, FP32 momenta, gamma, psi and charge), back in FP64.
+    An FP64 run from these inputs differs from one from the originals only by the rounding
+    of the initial state: the deck's own sensitivity to FP32 particle state."""
+    x, p, g, ps, q = pl
+    t = x * (1.0 / dr)
+    s = np.floor(t)
+    f = (t - s).astype(np.float32)
+    up = f >= np.float32(1.0)
+    f[up] -= np.float32(1.0)
+    s[up] += 1.0
+    xr = np.ascontiguousarray((s + f.astype(np.float64)) * dr)
+
+    def r32(a):
+        return np.ascontiguousarray(np.asarray(a).astype(np.float32).astype(np.float64))
+    return xr, r32(p), r32(g), r32(ps), r32(q)

@@ -218,3 +218,27 @@ def test_smooth_known_answer():
     f = np.ones(P * ld)
     O.smooth(g, 0, f)
     assert np.all(f.reshape(P, ld)[:, 3:nr + 1] == 1.0)
+
+
+def test_two_beams_deposit_as_their_sum():
+    """beam3d::qdp (beam3d_class.f03:193-221): every beam deposits into its own zeroed store,
+    finished by part3d::qdeposit (axis rule, 1/(i-1)), then added to q_beam; two beams give
+    the same store as one beam holding both beams' particles."""
+    g = O.grid(32, 16, 2, 0.1, 0.1)
+    b1 = O.load_beam(g, 5, 4000, 3.0, -1.0, 1000.0, (0.05, 0.0, 0.6), (0.3, 0.3, 0.2), (-1.5, -1.5, 0.0),
+                     (1.5, 1.5, 1.6))
+    b2 = O.load_beam(g, 6, 3000, 2.0, -1.0, 1000.0, (0.0, 0.0, 1.0), (0.2, 0.2, 0.2), (-1.0, -1.0, 0.0),
+                     (1.0, 1.0, 1.6))
+    both = O.Beam(b1.n + b2.n)
+    for k in O.Beam.NAMES:
+        setattr(both, k, np.ascontiguousarray(np.concatenate([getattr(b1, k), getattr(b2, k)])))
+    stores = []
+    for beams in ([b1, b2], [both]):
+        sim = O.Sim(g, iter_max=1, sp_npmax=1, beams=[(-1.0, O.PUSH3_REDUCED, b.n) for b in beams])
+        for k, b in enumerate(beams):
+            sim.set_beam(k, b)
+        sim.begin_3dstep()
+        stores.append(sim.store("q_beam"))
+    sep = O.beam_qdeposit(g, b1) + O.beam_qdeposit(g, b2)
+    np.testing.assert_allclose(stores[0], stores[1], rtol=0, atol=1e-12 * np.abs(stores[1]).max())
+    np.testing.assert_allclose(stores[0][:g.nz], sep[:g.nz], rtol=0, atol=1e-12 * np.abs(sep).max())
