@@ -118,9 +118,22 @@ __device__ __forceinline__ MInterp minterp(int32_t c, float fx, float fy, int nr
   return m;
 }
 
+// Instances of the particle kernels: kM >= 0 is the highest azimuthal mode known at compile
+// time (every mode loop unrolls, every table offset is a constant); kM = -1 takes it from
+// the grid at run time (at most QPAD_MAX_MODE).
+template <int kM>
+struct ModeLoop {
+  static constexpr int kLast = kM >= 0 ? kM : QPAD_MAX_MODE;
+  __device__ __forceinline__ static bool past(int m, int M) { return kM < 0 && m > M; }
+  __device__ __forceinline__ static int modes(int M) { return kM >= 0 ? kM : M; }
+};
+
 // E and B gathered from the FP32 table (interp_field, interp_part2d.f03:67-109)
 // t0: the records of node ii.idx (in the table, or a copy of the two nodes' records)
-__device__ __forceinline__ void mgather_at(const float* t0, int P, int M, const MInterp& ii, float ep[3], float bp[3]) {
+template <int kM>
+__device__ __forceinline__ void mgather_at(const float* t0, int Prt, int Mrt, const MInterp& ii, float ep[3],
+                                           float bp[3]) {
+  const int M = ModeLoop<kM>::modes(Mrt), P = kM >= 0 ? 2 * kM + 1 : Prt;
 #pragma unroll
   for (int c = 0; c < 3; ++c) { ep[c] = 0.0f; bp[c] = 0.0f; }
   if (!ii.ok) return;
@@ -131,7 +144,9 @@ __device__ __forceinline__ void mgather_at(const float* t0, int P, int M, const 
     bp[c] = t0[3 + c] * ii.w0 + t1[3 + c] * ii.w1;
   }
   float phr = 1.0f, phi = 0.0f;
-  for (int m = 1; m <= M; ++m) {
+#pragma unroll
+  for (int m = 1; m <= ModeLoop<kM>::kLast; ++m) {
+    if (ModeLoop<kM>::past(m, M)) break;
     const float t = phr * ii.pcos - phi * ii.psin;
     phi = phr * ii.psin + phi * ii.pcos;
     phr = t;
@@ -149,9 +164,43 @@ __device__ __forceinline__ void mgather_at(const float* t0, int P, int M, const 
   }
 }
 
+template <int kM>
 __device__ __forceinline__ void mgather(const float* __restrict__ T, int P, int M, const MInterp& ii, float ep[3],
                                         float bp[3]) {
-  mgather_at(T + (size_t)(ii.ok ? ii.idx : 0) * P * 6, P, M, ii, ep, bp);
+  mgather_at<kM>(T + (size_t)(ii.ok ? ii.idx : 0) * P * 6, P, M, ii, ep, bp);
+}
+
+// The same gather from one cell's records staged as pairs tp[part * 6 + comp] =
+// (value at the inner node, outer minus inner): each value at the particle is one FMA.
+template <int kM>
+__device__ __forceinline__ void mgather_pair(const float2* tp, int Mrt, const MInterp& ii, float ep[3], float bp[3]) {
+  const int M = ModeLoop<kM>::modes(Mrt);
+  const float w1 = ii.w1;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float2 e = tp[c], b = tp[3 + c];
+    ep[c] = ii.ok ? fmaf(w1, e.y, e.x) : 0.0f;
+    bp[c] = ii.ok ? fmaf(w1, b.y, b.x) : 0.0f;
+  }
+  if (!ii.ok) return;
+  float phr = 1.0f, phi = 0.0f;
+#pragma unroll
+  for (int m = 1; m <= ModeLoop<kM>::kLast; ++m) {
+    if (ModeLoop<kM>::past(m, M)) break;
+    const float t = phr * ii.pcos - phi * ii.psin;
+    phi = phr * ii.psin + phi * ii.pcos;
+    phr = t;
+    const float pre = 2.0f * phr, pim = 2.0f * phi;
+    const float2* re = tp + (2 * m - 1) * 6;
+    const float2* im = tp + (2 * m) * 6;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float er = fmaf(w1, re[c].y, re[c].x), ei = fmaf(w1, im[c].y, im[c].x);
+      const float br = fmaf(w1, re[3 + c].y, re[3 + c].x), bi = fmaf(w1, im[3 + c].y, im[3 + c].x);
+      ep[c] = fmaf(er, pre, fmaf(-ei, pim, ep[c]));
+      bp[c] = fmaf(br, pre, fmaf(-bi, pim, bp[c]));
+    }
+  }
 }
 
 // Sum over the 32 lanes of each of 32 values: after the exchange, lane l holds in a[0]
@@ -172,7 +221,7 @@ __device__ __forceinline__ void butterfly32(float (&a)[32], int lane) {
 // ------------------------------------------------------------------------------------
 // charge deposit (rho - Jz), one warp per work item (kItem particles of one cell)
 // ------------------------------------------------------------------------------------
-template <int kPPL>
+template <int kPPL, int kM>
 __global__ void __launch_bounds__(kItemThreads) k_mqdeposit(GridDev G, const int4* __restrict__ items,
                                                             const int* __restrict__ n_items, MArr A,
                                                             double* __restrict__ qraw) {
@@ -203,7 +252,9 @@ __global__ void __launch_bounds__(kItemThreads) k_mqdeposit(GridDev G, const int
   float ph[kPPL][2];
 #pragma unroll
   for (int j = 0; j < kPPL; ++j) { ph[j][0] = 1.0f; ph[j][1] = 0.0f; }
-  for (int m = 0; m <= G.M; ++m) {
+#pragma unroll
+  for (int m = 0; m <= ModeLoop<kM>::kLast; ++m) {
+    if (ModeLoop<kM>::past(m, G.M)) break;
     float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};          // [node 0/1][re, im]
 #pragma unroll
     for (int j = 0; j < kPPL; ++j) {
@@ -238,14 +289,13 @@ __global__ void __launch_bounds__(kItemThreads) k_mqdeposit(GridDev G, const int
 
 // Predictor push of one particle (amjdeposit_robust / _std): the deposit values
 // v = {u0, u1, u2, du0, du1, u0 u0 / (g - u2) .. } and the charge factor qq = q / (g - u2).
-// pv: the particle's px, py, pz, psi, q (loaded by the caller); t0: the gather records of
-// node ii.idx
-__device__ __forceinline__ void mpredict(const GridDev& G, int push_type, float qbm, float dt, const MArr& A,
-                                         const float* t0, int64_t i, int write_back, const MInterp& ii,
+// pv: the particle's px, py, pz, psi, q (loaded by the caller); ep, bp: E and B gathered at
+// the particle (overwritten)
+__device__ __forceinline__ void mpredict(int push_type, float qbm, float dt, const MArr& A, int64_t i,
+                                         int write_back, const MInterp& ii, float ep[3], float bp[3],
                                          const float pv[5], float v[8], float& qq) {
   const float idt = 1.0f / dt, qtmh = 0.5f * qbm * dt;
-  float ep[3], bp[3], wp[3], u0[3], u[3], ut[3];
-  mgather_at(t0, G.P, G.M, ii, ep, bp);
+  float wp[3], u0[3], u[3], ut[3];
   wp[0] = ep[0] - bp[1];
   wp[1] = ep[1] + bp[0];
   wp[2] = ep[2];
@@ -323,7 +373,7 @@ __device__ __forceinline__ void mpredict(const GridDev& G, int push_type, float 
 // [node 0/1][Re/Im][cu 0..2, acu 3..4, amu 5..7] in registers, one butterfly sums them
 // over the warp, and each lane adds one total into the FP64 arrays.
 // ------------------------------------------------------------------------------------
-template <int kPPL>
+template <int kPPL, int kM>
 __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_type, float qbm, float dt,
                                                          const int4* __restrict__ items, const int* __restrict__ n_items,
                                                          MArr A, const float* __restrict__ T, double* __restrict__ cu,
@@ -343,7 +393,9 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
   // key + 1) load with the particles, then go to this warp's shared slot
   constexpr int kTV = (12 * QPAD_MAX_PARTS + 31) / 32;
   __shared__ float tsm[kItemThreads / 32][12 * QPAD_MAX_PARTS];
-  const int nt = 12 * G.P;
+  __shared__ float2 tpair[kItemThreads / 32][6 * QPAD_MAX_PARTS];
+  const int PP = kM >= 0 ? 2 * kM + 1 : G.P;
+  const int nt = 12 * PP;
   const float* tb = T + (size_t)min(key, G.nr) * G.P * 6;
   float tv[kTV];
 #pragma unroll
@@ -368,6 +420,11 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
   for (int q = 0; q < kTV; ++q)
     if (lane + 32 * q < nt) tsm[w][lane + 32 * q] = tv[q];
   __syncwarp();
+  for (int l = lane; l < 6 * PP; l += 32) {
+    const float a = tsm[w][l], b = tsm[w][6 * PP + l];
+    tpair[w][l] = make_float2(a, b - a);
+  }
+  __syncwarp();
   float v[kPPL][8], wq[kPPL][2], pc[kPPL][2];
 #pragma unroll
   for (int j = 0; j < kPPL; ++j) {
@@ -381,9 +438,12 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
       const int i = start + o;
       const MInterp ii = minterp(pcx[j], pf[j][0], pf[j][1], G.nr);
       if (ii.ok) {
-        float qq;
-        const float* t0 = ii.idx == key ? &tsm[w][0] : T + (size_t)ii.idx * G.P * 6;
-        mpredict(G, push_type, qbm, dt, A, t0, i, write_back, ii, pv[j], v[j], qq);
+        float qq, ep[3], bp[3];
+        if (ii.idx == key)
+          mgather_pair<kM>(&tpair[w][0], G.M, ii, ep, bp);
+        else      // (not reached: the sort key and the gather use the same cell_radius)
+          mgather_at<kM>(T + (size_t)ii.idx * G.P * 6, G.P, G.M, ii, ep, bp);
+        mpredict(push_type, qbm, dt, A, i, write_back, ii, ep, bp, pv[j], v[j], qq);
         wq[j][0] = qq * ii.w0;
         wq[j][1] = qq * ii.w1;
         pc[j][0] = ii.pcos;
@@ -397,7 +457,9 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
   const int jn = lane >> 4, h = (lane >> 3) & 1, c = lane & 7;
   double* dst = c < 3 ? cu + (size_t)c * ld : (c < 5 ? acu + (size_t)(c - 3) * ld : amu + (size_t)(c - 5) * ld);
   const int ncomp = c < 3 ? 3 : (c < 5 ? 2 : 3);
-  for (int m = 0; m <= G.M; ++m) {
+#pragma unroll
+  for (int m = 0; m <= ModeLoop<kM>::kLast; ++m) {
+    if (ModeLoop<kM>::past(m, G.M)) break;
     float acc[32];
 #pragma unroll
     for (int k = 0; k < 32; ++k) acc[k] = 0.0f;
@@ -429,6 +491,7 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
 // ------------------------------------------------------------------------------------
 // push_u + push_x + edge test + new cell key
 // ------------------------------------------------------------------------------------
+template <int kM>
 __global__ void __launch_bounds__(kMixThreads) k_mpush(GridDev G, int push_type, float qbm, float dt,
                                                        const int64_t* __restrict__ n_ptr, MArr A,
                                                        const float* __restrict__ T, int do_u, int do_x) {
@@ -444,7 +507,7 @@ __global__ void __launch_bounds__(kMixThreads) k_mpush(GridDev G, int push_type,
   if (do_u) {
   const MInterp ii = minterp(A.cxy[i], fx, fy, G.nr);
   float ep[3], bp[3], ut[3];
-  mgather(T, G.P, G.M, ii, ep, bp);
+  mgather<kM>(T, G.P, G.M, ii, ep, bp);
   float t = ep[0] * ii.pcos - ep[1] * ii.psin;
   ep[1] = ep[0] * ii.psin + ep[1] * ii.pcos;
   ep[0] = t;
@@ -652,6 +715,18 @@ __global__ void __launch_bounds__(kMixThreads) k_minterp_psi(GridDev G, const in
 // ------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------
+// the instance for the grid's highest mode: compile-time M for 0..4, run-time M above
+#define QPAD_MIXED_BY_MODE(M, LAUNCH) \
+  do {                                \
+    switch (M) {                      \
+      case 0: LAUNCH(0); break;       \
+      case 1: LAUNCH(1); break;       \
+      case 2: LAUNCH(2); break;       \
+      case 3: LAUNCH(3); break;       \
+      case 4: LAUNCH(4); break;       \
+      default: LAUNCH(-1); break;     \
+    }                                 \
+  } while (0)
 int mixed_alloc(qpad_species* sp) {
   qpad_ctx* ctx = sp->ctx;
   const size_t cap = (size_t)sp->npmax;
@@ -782,12 +857,13 @@ int mixed_qdeposit_raw(qpad_species* sp, double* qraw) {
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
   prof_begin(ctx, "qdeposit");
-  if (ctx->item_ppl == 1)
-    k_mqdeposit<1><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
-  else if (ctx->item_ppl == 2)
-    k_mqdeposit<2><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
-  else
-    k_mqdeposit<4><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw);
+#define QPAD_MQDEP(PPL, MM) \
+  k_mqdeposit<PPL, MM><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->items, sp->d_nitems, marr(sp, 0), qraw)
+#define QPAD_MQDEP_M(MM) \
+  do { if (ctx->item_ppl == 1) QPAD_MQDEP(1, MM); else if (ctx->item_ppl == 2) QPAD_MQDEP(2, MM); else QPAD_MQDEP(4, MM); } while (0)
+  QPAD_MIXED_BY_MODE(ctx->g.M, QPAD_MQDEP_M);
+#undef QPAD_MQDEP_M
+#undef QPAD_MQDEP
   prof_end(ctx, "qdeposit");
   return check_launch(ctx, "k_mqdeposit");
 }
@@ -796,18 +872,15 @@ int mixed_amjdp_raw(qpad_species* sp, const float* gtab, double* cu, double* amu
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
   prof_begin(ctx, "amjdp");
-  if (ctx->item_ppl == 1)
-    k_mamjdp<1><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
-                                                                   sp->items, sp->d_nitems, marr(sp, 0), gtab, cu, amu,
-                                                                   acu, 0);
-  else if (ctx->item_ppl == 2)
-    k_mamjdp<2><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
-                                                                   sp->items, sp->d_nitems, marr(sp, 0), gtab, cu, amu,
-                                                                   acu, 0);
-  else
-    k_mamjdp<4><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm, (float)dt,
-                                                                   sp->items, sp->d_nitems, marr(sp, 0), gtab, cu, amu,
-                                                                   acu, 0);
+#define QPAD_MAMJ(PPL, MM)                                                                                        \
+  k_mamjdp<PPL, MM><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm,     \
+                                                                      (float)dt, sp->items, sp->d_nitems,         \
+                                                                      marr(sp, 0), gtab, cu, amu, acu, 0)
+#define QPAD_MAMJ_M(MM) \
+  do { if (ctx->item_ppl == 1) QPAD_MAMJ(1, MM); else if (ctx->item_ppl == 2) QPAD_MAMJ(2, MM); else QPAD_MAMJ(4, MM); } while (0)
+  QPAD_MIXED_BY_MODE(ctx->g.M, QPAD_MAMJ_M);
+#undef QPAD_MAMJ_M
+#undef QPAD_MAMJ
   prof_end(ctx, "amjdp");
   return check_launch(ctx, "k_mamjdp");
 }
@@ -816,8 +889,11 @@ int mixed_push(qpad_species* sp, const float* gtab, double dt, int do_u, int do_
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
   prof_begin(ctx, "push");
-  k_mpush<<<mgrid(sp->np, kMixThreads), kMixThreads, 0, ctx->stream>>>(
-      ctx->g, sp->push_type, (float)sp->qbm, (float)dt, sp->d_count, marr(sp, 0), gtab, do_u, do_x);
+#define QPAD_MPUSH(MM)                                                                                 \
+  k_mpush<MM><<<mgrid(sp->np, kMixThreads), kMixThreads, 0, ctx->stream>>>(                            \
+      ctx->g, sp->push_type, (float)sp->qbm, (float)dt, sp->d_count, marr(sp, 0), gtab, do_u, do_x)
+  QPAD_MIXED_BY_MODE(ctx->g.M, QPAD_MPUSH);
+#undef QPAD_MPUSH
   prof_end(ctx, "push");
   if (int r = check_launch(ctx, "k_mpush")) return r;
   return do_x ? mixed_sort(sp) : 0;
