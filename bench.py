@@ -206,7 +206,8 @@ def _first_step_stores(args, deck, inputs, prec, local):
     return out
 
 
-def _measure(args, deck, inputs, prec, local, dist, steps, warmup, full=True, guess=False, keep_stores=False):
+def _measure(args, deck, inputs, prec, local, dist, steps, warmup, full=True, guess=False, keep_stores=False,
+             order=0):
     """Times `steps` 3D steps of one simulation (after `warmup` untimed ones) on the library's
     stream with CUDA events; with `full`, also the end-to-end pass with host buffers and one
     host-driven step with per-kernel event timing.  With keep_stores, the 3D stores of the
@@ -214,6 +215,7 @@ def _measure(args, deck, inputs, prec, local, dist, steps, warmup, full=True, gu
     import qpad_gb300 as Q
     from qpad_gb300.replicas import reduce_timing
     sim = Q.build_simulation(deck, precision=prec, device=local, inputs=inputs)
+    sim.set_guess_extrapolation(order)
     sim.use_graph(args.graph == "on")
     tune = sim.autotune(reps=20) if not args.no_autotune else None
     if guess:
@@ -387,7 +389,8 @@ def run_ours(args):
     npl = len(inputs[0][4])
     nbeam = sum(len(b[2]) for b in inputs[1])
     want_err = not args.no_compare
-    r = _measure(args, deck, inputs, prec, local, dist, args.steps, args.warmup, full=True, keep_stores=want_err)
+    r = _measure(args, deck, inputs, prec, local, dist, args.steps, args.warmup, full=True, keep_stores=want_err,
+                 order=args.guess_order)
     # the other arm of the metric: the plain FP64 path on the same deck and inputs
     cmp, err = None, None
     if not args.no_compare:
@@ -479,6 +482,8 @@ def run_ours(args):
         "data": "synthetic (seeded deck, no dataset)",
         "config": {"workload": deck.name, "nr": deck.nr, "nz": deck.nz, "max_mode": deck.max_mode,
                    "plasma_particles_per_slice": npl, "beam_particles": nbeam, "path": args.precision,
+                   "guess": (f"B-perp extrapolated from the previous slices, order {args.guess_order}"
+                             if args.guess_order else "carried B-perp(j-1), as the reference"),
                    "iter_reltol": deck.iter_reltol, "iter_max": deck.iter_max,
                    "l2": "step working set above L2 (beam arrays and 3D field stores); per-slice data L2-resident",
                    "parallelism": f"replicas x{world}",
@@ -526,6 +531,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--deck", default="c5")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--guess-order", type=int, default=1, choices=[0, 1, 2],
+                    help="initial B-perp guess of the measured arm: 0 carried (the reference), 1 / 2 extrapolated")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP64 (or mixed) comparison arm")
     ap.add_argument("--compare-steps", type=int, default=1,
                     help="timed steps of the comparison arm (0: as --steps); its first warm-up step gives the error")

@@ -88,10 +88,10 @@ int qpad_launch_count(const qpad_ctx* ctx, int64_t* count);
  * on != 0 (the default); off, the host drives slices and iterations. */
 int qpad_set_graph(qpad_ctx* ctx, int on);
 /* Binomial (1,2,1) smoothing of the species' charge and current deposits, `order` passes
- * (0, the default, 1 or 2): the species' smooth_order (sim_plasma_class.f03:139-142), applied
- * as qdp_species2d / amjdp_species2d do (species2d_class.f03:202, 270-272) with
- * ufield::smooth_f1 (ufield_class.f03:274-339); the neutralising background is not smoothed.
- * Orders above 2 are refused (QPAD_E_ARG). */
+ * (0, the default, up to 64): the species' smooth_order (sim_plasma_class.f03:139-142),
+ * applied as qdp_species2d / amjdp_species2d do (species2d_class.f03:202, 270-272) with
+ * ufield::smooth_f1 (ufield_class.f03:274-339) `order` times (field_src_class.f03:114-121);
+ * the neutralising background is not smoothed.  Orders above 64 are refused (QPAD_E_ARG). */
 int qpad_set_smooth(qpad_ctx* ctx, int order);
 /* 1 if the last 3D step ran as a graph. */
 int qpad_graph_active(const qpad_ctx* ctx, int* active);
@@ -295,6 +295,12 @@ int qpad_learn_train(qpad_learn* net, const float* x, const float* t, int64_t ns
  * net0 (10 -> 4 channels) for m = 0, net1 (20 -> 8) for the modes m >= 1.  The iteration
  * still runs to iter_reltol.  Null net0 detaches.  The nets must outlive the attachment. */
 int qpad_guess_attach(qpad_ctx* ctx, qpad_learn* net0, qpad_learn* net1);
+/* Initial B-perp guess of every slice from the stored B-perp of the previous slices, without
+ * a net (no counterpart in the reference, which carries B-perp(j-1), simulation_class.f03:
+ * 324-326, 360): order 0 keeps the carried value (the default), 1 extrapolates linearly from
+ * slices j-1, j-2, 2 quadratically from j-1..j-3.  The iteration still runs to iter_reltol.
+ * Attached nets take precedence. */
+int qpad_set_guess_extrapolation(qpad_ctx* ctx, int order);
 /* Which parts of the guess are applied (bit 0: B-perp, bit 1: the J-perp predictor; both by
  * default) and the weight w in [0, 1] of the net's correction: guess = carried + w (net - carried). */
 int qpad_guess_config(qpad_ctx* ctx, int apply, double weight);

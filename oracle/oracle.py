@@ -45,7 +45,8 @@ class SimDesc(C.Structure):
                 ("iter_abstol", C.c_double), ("dt3d", C.c_double), ("sp_qbm", C.c_double),
                 ("sp_push_type", C.c_int), ("sp_neutralized", C.c_int), ("sp_npmax", C.c_int64),
                 ("nbeams", C.c_int), ("beam_qbm", C.c_double * 4), ("beam_push_type", C.c_int * 4),
-                ("beam_npmax", C.c_int64 * 4), ("nthreads", C.c_int), ("smooth_order", C.c_int)]
+                ("beam_npmax", C.c_int64 * 4), ("nthreads", C.c_int), ("smooth_order", C.c_int),
+                ("extrap", C.c_int)]
 
 
 BND_ZERO, BND_OPEN = 2, 3
@@ -340,7 +341,7 @@ class Sim:
 
     def __init__(self, g: Grid, *, iter_max=50, iter_reltol=1e-6, iter_abstol=0.0, dt3d=10.0,
                  sp_qbm=-1.0, sp_push_type=PUSH_ROBUST, neutralized=True, sp_npmax=1,
-                 beams=(), nthreads=1, smooth_order=0):
+                 beams=(), nthreads=1, smooth_order=0, extrap=0):
         d = SimDesc()
         d.g = g
         d.iter_max, d.iter_reltol, d.iter_abstol, d.dt3d = iter_max, iter_reltol, iter_abstol, dt3d
@@ -350,6 +351,7 @@ class Sim:
             d.beam_qbm[k], d.beam_push_type[k], d.beam_npmax[k] = qbm, ptype, max(1, npmax)
         d.nthreads = nthreads
         d.smooth_order = smooth_order
+        d.extrap = extrap
         self.g = g
         self.h = lib().orc_sim_create(C.byref(d))
 

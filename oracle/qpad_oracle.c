@@ -1410,6 +1410,19 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
   const int nt = s->d.nthreads;
   const double dxi = g->dxi;
   const size_t n1 = s->n1;
+  if (s->d.extrap > 0 && j > s->d.extrap + 1) {
+    /* not in the reference, which carries B-perp(j-1) into slice j: the initial B-perp guess
+       extrapolated from the stored slices j-1, j-2 (order 1) or j-1..j-3 (order 2), every
+       mode part, nodes 1..nr */
+    const int P = s->P;
+    for (int p = 0; p < P; ++p)
+      for (int c = 0; c < 2; ++c)
+        for (int i = 1; i <= g->nr; ++i) {
+          const double b1 = F2(s->b_spe2, 3, j - 1, p, c, i), b2 = F2(s->b_spe2, 3, j - 2, p, c, i);
+          F(s->b_spe, 3, p, c, i) = s->d.extrap == 1 ? 2.0 * b1 - b2
+                                                     : 3.0 * (b1 - b2) + F2(s->b_spe2, 3, j - 3, p, c, i);
+        }
+  }
   {
     /* :344-345 q_beam%copy_slice(j, 2->1); b_beam%solve(q_beam) */
     memcpy(s->q_beam, s->q_beam2 + (size_t)(j - 1) * n1, n1 * sizeof(double));

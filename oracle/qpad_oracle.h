@@ -134,6 +134,9 @@ typedef struct orc_sim_desc {
   int nbeams; double beam_qbm[4]; int beam_push_type[4]; int64_t beam_npmax[4];
   int nthreads;                /* OpenMP threads for particle loops (1 = serial) */
   int smooth_order;            /* binomial smoothing passes of the species deposits (0 = none) */
+  int extrap;                  /* initial B-perp guess of a slice: 0 = carried (the reference),
+                                  1 / 2 = linear / quadratic extrapolation from the stored slices
+                                  (the product's optional guess, restated here to check it) */
 } orc_sim_desc;
 
 /* One binomial (1,2,1) smoothing pass of a deposit field (ufield::smooth_f1,

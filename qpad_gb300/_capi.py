@@ -135,6 +135,7 @@ _SIGS = {
                                    C.c_uint64, D]),
     "qpad_guess_attach": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "qpad_guess_sample": (C.c_int, [C.c_void_p, C.c_int, C.c_int, F, F, F]),
+    "qpad_set_guess_extrapolation": (C.c_int, [C.c_void_p, C.c_int]),
     "qpad_guess_config": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "qpad_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "qpad_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -208,9 +208,14 @@ class Simulation:
         self._check(self.lib.qpad_set_graph(self.h, int(on)))
 
     def set_smooth(self, order: int):
-        """Binomial smoothing passes (0, 1 or 2) of the species' charge and current deposits
+        """Binomial smoothing passes (0 .. 64) of the species' charge and current deposits
         (the species' smooth_order)."""
         self._check(self.lib.qpad_set_smooth(self.h, int(order)))
+
+    def set_guess_extrapolation(self, order: int):
+        """Initial B-perp guess of every slice: 0 carries B-perp(j-1) as the reference does, 1
+        and 2 extrapolate it linearly / quadratically from the previous slices."""
+        self._check(self.lib.qpad_set_guess_extrapolation(self.h, int(order)))
 
     def graph_active(self):
         """(whether the last 3D step ran as a graph, reason when it did not)."""

@@ -409,7 +409,8 @@ extern "C" int qpad_graph_active(const qpad_ctx* ctx, int* active) {
 
 extern "C" int qpad_set_smooth(qpad_ctx* ctx, int order) {
   if (!ctx) return QPAD_E_ARG;
-  if (order < 0 || order > 2) return set_err(ctx, QPAD_E_ARG, "smooth order: 0, 1 or 2");
+  if (order < 0 || order > kMaxSmoothOrder)
+    return set_err(ctx, QPAD_E_ARG, "smooth order: 0 .. " + std::to_string(kMaxSmoothOrder));
   const int old = ctx->g.smooth;
   ctx->g.smooth = order;
   // the iteration kernel's shared memory grows with smoothing: check its shape still fits
@@ -1020,8 +1021,8 @@ int enqueue_slice_prologue(qpad_ctx* ctx, cudaGraphConditionalHandle hi, int use
         return r;
   // the convergence record of B_phi: in the graph the last iteration of the previous slice
   // left it (nothing changes B_phi in between; the step start zeroes both), unless the
-  // learned guess has just replaced b_spe
-  if (use_h && !ctx->guess) return 0;
+  // learned or extrapolated guess has just replaced b_spe
+  if (use_h && !ctx->guess && !ctx->extrap) return 0;
   return launch_conv(ctx, ctx->f[QPAD_F_B_SPE], 1, 0, use_h, hi, use_h);
 }
 
@@ -1039,6 +1040,7 @@ int enqueue_iteration(qpad_ctx* ctx, cudaGraphConditionalHandle h, int use_h) {
                         : species_amjdp_raw(s, ctx->f[QPAD_F_E], ctx->f[QPAD_F_B], rcu, ramu, racu, ctx->g.dxi);
     if (r) return r;
   }
+  if (int r = launch_smooth_raw(ctx)) return r;       // smoothing orders above the window's
   return launch_iterate(ctx, 1, h, use_h, 1);
 }
 
@@ -1172,6 +1174,7 @@ int build_step_graph(qpad_ctx* ctx) {
 std::string step_key(const qpad_ctx* ctx) {
   std::string k = std::to_string(ctx->precision) + "/" + std::to_string(ctx->iter_cl) + "/" +
                   std::to_string(ctx->item_ppl) + "/" + std::to_string(ctx->guess != nullptr) + "/" +
+                  std::to_string(ctx->extrap) + "/" +
                   std::to_string(ctx->pdl) + "/" + std::to_string(ctx->g.smooth);
   for (auto* s : ctx->species)
     k += "|" + std::to_string((long long)s->np) + ":" + std::to_string(s->push_type) + ":" +

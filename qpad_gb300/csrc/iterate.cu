@@ -69,6 +69,7 @@ struct IterArgs {
   int gw;                 // lanes per right-hand side in the solves
   int tma;                // stage with bulk copies (even nr and R: every row 16-byte aligned)
   unsigned int* err;      // device error word: 1 = a bulk-copy wait gave up
+  int prefinished;        // the raw deposits were already finished (and smoothed) by k_smooth_raw
 };
 
 __device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
@@ -91,8 +92,10 @@ struct RawFin {
   const GridDev* G;
   const double* raw;
   int m, which, nc;
+  int prefinished;
   __device__ __forceinline__ double operator()(int p, int c, int i) const {
-    return finish_amj(*G, m, which, c, i, raw[fidx(G->ld, nc, p, c, i)]);
+    const double v = raw[fidx(G->ld, nc, p, c, i)];
+    return prefinished ? v : finish_amj(*G, m, which, c, i, v);
   }
 };
 
@@ -142,10 +145,15 @@ struct WinF {
 // Shared-memory staging of one CTA (doubles): the finished deposits on the node window
 // [r0-1, r1+2] (cu 0..2, amu 3..5, acu 6..7), b_spe components 0..1 and b_beam on the owned
 // nodes, psi on the window, the factor rows of the three matrices, the right-hand sides.
+// Smoothing orders up to this many passes run inside k_iterate's node window (a +-2-node
+// halo); higher orders run as a pass of their own before it (k_smooth_raw).
+static constexpr int kWindowSmooth = 2;
+
 __host__ __device__ inline size_t iterate_smem_doubles(int R, int ld, int smooth) {
   const size_t W = (size_t)R + 6;                // node window [r0-2, r0+R+4)
   (void)ld;
-  return 30 * W + 21 * (size_t)R + (smooth > 0 ? 12 * W : 0);   // + the smoothing scratch rows
+  const bool in_window = smooth > 0 && smooth <= kWindowSmooth;
+  return 30 * W + 21 * (size_t)R + (in_window ? 12 * W : 0);   // + the smoothing scratch rows
 }
 
 // Bulk (TMA) copy global -> this CTA's shared memory, completing on an mbarrier.
@@ -355,6 +363,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     const int row = q / W, k = q % W, c8 = c8_lo + row / nh, node = wb + k;
     if (node < 0 || node > nr + 1) continue;
     double& v = win[(c8 * 2 + row % nh) * W + k];
+    if (a.prefinished) continue;
     v = c8 < 3 ? finish_amj(G, m, 0, c8, node, v) : (c8 < 6 ? finish_amj(G, m, 1, c8 - 3, node, v)
                                                                 : finish_amj(G, m, 2, c8 - 6, node, v));
   }
@@ -455,7 +464,7 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
     if (rank == 0 && t == 0) {
       double s = 0.0;
       for (int q = 0; q < CL; ++q) s += *cluster.map_shared_rank(&divp, q);
-      const RawFin CUg{&a.G, raw_cu, 0, 0, 3};    // nodes nr-2, nr-1 lie outside this window
+      const RawFin CUg{&a.G, raw_cu, 0, 0, 3, a.prefinished};   // nodes nr-2, nr-1 lie outside this window
       if constexpr (kSmooth) {
         const auto CUs = [&](int p, int c, int i) { return smoothed_at(a.G, CUg, 1, 0, p, c, i, a.G.smooth); };
         dsm[3 * R + 0] = ez_axis_row(a.G, s, CUs);
@@ -806,7 +815,46 @@ static int solve_lanes(int R) {
 }
 
 // Uses cluster size cl for k_iterate if the kernel can launch with it; nonzero otherwise.
-static void (*iterate_kernel(int smooth))(IterArgs) { return smooth > 0 ? k_iterate<true> : k_iterate<false>; }
+static void (*iterate_kernel(int smooth))(IterArgs) {
+  return smooth > 0 && smooth <= kWindowSmooth ? k_iterate<true> : k_iterate<false>;
+}
+
+// Smoothing orders above kWindowSmooth (amjdp_species2d's cu / dcu / amu%smooth(),
+// species2d_class.f03:270-272, ufield::smooth_f1 applied smooth_order times,
+// ufield_class.f03:274-339): one CTA per deposit row (8 components) and mode part finishes
+// the raw line, applies every pass and stores the finished, smoothed line in place; the
+// iteration kernel then takes it as it is (IterArgs::prefinished).  (It cannot go back to
+// raw form: the smoothing's axis rule may leave a value on an axis node that the finishing
+// zeroes.)
+__global__ void __launch_bounds__(256) k_smooth_raw(GridDev G, double* __restrict__ raw) {
+  extern __shared__ double sl[];                 // two lines of ld doubles
+  const int row = blockIdx.x % 8, p = blockIdx.x / 8;
+  const int m = (p + 1) / 2, ld = G.ld, nr = G.nr;
+  const size_t P1 = (size_t)G.P * ld;
+  const int which = row < 3 ? 0 : (row < 6 ? 1 : 2), comp = row < 3 ? row : (row < 6 ? row - 3 : row - 6);
+  double* line = raw + (size_t)(row < 6 ? (row < 3 ? 0 : 3) : 6) * P1 +
+                 ((size_t)p * (which == 2 ? 2 : 3) + comp) * ld;
+  double* a = sl;
+  double* b = sl + ld;
+  for (int i = threadIdx.x; i < ld; i += blockDim.x) a[i] = finish_amj(G, m, which, comp, i, line[i]);
+  __syncthreads();
+  const bool ax = smooth_ax(which == 2 ? 2 : 1, m, comp);
+  for (int pass = 0; pass < G.smooth; ++pass) {
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) b[i] = smooth_node(G, i, ax, a[i - 1], a[i], a[i + 1]);
+    __syncthreads();
+    for (int i = 1 + threadIdx.x; i <= nr; i += blockDim.x) a[i] = b[i];
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < ld; i += blockDim.x) line[i] = a[i];
+}
+
+int launch_smooth_raw(qpad_ctx* ctx) {
+  if (ctx->g.smooth <= kWindowSmooth) return 0;
+  const size_t smem = 2 * (size_t)ctx->g.ld * sizeof(double);
+  if (int r = raise_dyn_smem(ctx, (const void*)k_smooth_raw, smem)) return r;
+  k_smooth_raw<<<8 * ctx->g.P, 256, smem, ctx->stream>>>(ctx->g, ctx->raw);
+  return check_launch(ctx, "k_smooth_raw");
+}
 
 int iterate_try_cluster(qpad_ctx* ctx, int cl) {
   if (cl < 1 || cl > 16 || cl > ctx->g.nr) return QPAD_E_ARG;
@@ -882,6 +930,7 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   a.gw = solve_lanes(a.R);
   a.tma = (ctx->g.nr % 2 == 0 && a.R % 2 == 0) ? 1 : 0;
   a.err = ctx->iter_tickets + kIterErrWord;
+  a.prefinished = ctx->g.smooth > kWindowSmooth ? 1 : 0;
   const int cl = ctx->iter_cl;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2 * cl * (ctx->g.M + 1));

@@ -630,9 +630,38 @@ void guess_free(qpad_ctx* ctx) {
   ctx->guess = nullptr;
 }
 
+// Polynomial extrapolation of the initial B-perp guess of slice j (every mode part, nodes
+// 1..nr) from the stored B-perp of slices j-1, j-2 (, j-3): order 1 is 2 B1 - B2, order 2 is
+// 3 B1 - 3 B2 + B3.  Slices without enough history keep the carried value B(j-1).
+__global__ void __launch_bounds__(256) k_guess_extrap(GridDev G, const double* __restrict__ b2,
+                                                      const int* __restrict__ jp, double* __restrict__ b_spe,
+                                                      int order) {
+  const int j = *jp;
+  if (j <= order + 1) return;
+  const int n = G.P * 2 * G.nr;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int p = q / (2 * G.nr), c = (q / G.nr) % 2, i = q % G.nr + 1;
+    const double b1 = st2(G, b2, 3, j - 1, p, c, i), bb = st2(G, b2, 3, j - 2, p, c, i);
+    double v;
+    if (order == 1) {
+      v = 2.0 * b1 - bb;
+    } else {
+      const double b3 = st2(G, b2, 3, j - 3, p, c, i);
+      v = 3.0 * (b1 - bb) + b3;
+    }
+    b_spe[fidx(G.ld, 3, p, c, i)] = v;
+  }
+}
+
 // Graph-capturable: the guess of the slice in ctx->d_j (slices 1 and 2 keep the carried one).
 int guess_enqueue(qpad_ctx* ctx) {
   qpad_guess_state* g = ctx->guess;
+  if (!g && ctx->extrap > 0) {
+    const int n = ctx->g.P * 2 * ctx->g.nr;
+    k_guess_extrap<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->g, ctx->f2[QPAD_F_B_SPE], ctx->d_j,
+                                                             ctx->f[QPAD_F_B_SPE], ctx->extrap);
+    return check_launch(ctx, "k_guess_extrap");
+  }
   if (!g) return 0;
   const GridDev& G = ctx->g;
   const int nr = G.nr, M = G.M;
@@ -690,6 +719,13 @@ extern "C" int qpad_guess_sample(qpad_ctx* ctx, int j, int m, float* x, float* t
   if (!r) r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "guess sample");
   cudaFree(d);
   return r;
+}
+
+extern "C" int qpad_set_guess_extrapolation(qpad_ctx* ctx, int order) {
+  if (!ctx || order < 0 || order > 2)
+    return ctx ? set_err(ctx, QPAD_E_ARG, "guess extrapolation: order 0, 1 or 2") : QPAD_E_ARG;
+  ctx->extrap = order;
+  return 0;
 }
 
 extern "C" int qpad_guess_config(qpad_ctx* ctx, int apply, double weight) {

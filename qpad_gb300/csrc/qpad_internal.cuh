@@ -74,6 +74,7 @@ struct Beam;
 
 }  // namespace qpad
 
+static constexpr int kMaxSmoothOrder = 64;    // smoothing passes of the species deposits, at most
 static constexpr int kIterMaxWords = 64;      // k_iterate's two 64-bit maxima in the ticket buffer
 static constexpr int kIterErrWord = 127;       // k_iterate's error word in the ticket buffer
 
@@ -97,6 +98,7 @@ struct qpad_ctx {
   bool pdl = true;                             // k_iterate as programmatic dependent of the deposit
   // (the smoothing order lives in g.smooth)
   struct qpad_guess_state* guess = nullptr;    // learned predictor-corrector guess (learn.cu)
+  int extrap = 0;                              // polynomial order of the initial B-perp guess (0: carried)
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
   float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
   double* scratch = nullptr;                   // per-call deposit scratch (cu, amu, acu)
@@ -219,6 +221,7 @@ void guess_free(qpad_ctx* ctx);
 // one predictor-corrector iteration after the deposit, as a cluster kernel (iterate.cu)
 int iterate_setup(qpad_ctx* ctx);
 int iterate_try_cluster(qpad_ctx* ctx, int cl);
+int launch_smooth_raw(qpad_ctx* ctx);
 int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, int use_h,
                    int after_deposit = 0);
 

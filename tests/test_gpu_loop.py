@@ -128,3 +128,31 @@ def test_slice_by_slice_api_matches_fused_step():
         assert field_errors(b.e.store(s), a.e.store(s)).max() < 1e-12
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_extrapolated_guess_matches_oracle(order):
+    """The optional initial B-perp guess extrapolated from the previous slices (no counterpart
+    in the reference; restated in the oracle): identical per-slice iteration counts and every
+    store within 1e-9 on the FP64 path."""
+    deck = _deck(2)
+    pl, beams = Q.deck_inputs(deck)
+    g = O.grid(deck.nr, deck.nz, deck.max_mode, deck.dr, deck.dxi)
+    osim = O.Sim(g, iter_max=deck.iter_max, iter_reltol=deck.iter_reltol, dt3d=deck.dt, sp_npmax=len(pl[4]),
+                 beams=[(-1.0, O.PUSH3_REDUCED, len(beams[0][2]))], extrap=order)
+    osim.set_plasma(plasma_to_oracle(*pl))
+    osim.set_beam(0, beam_to_oracle(*beams[0]))
+    oiters, _ = osim.run_3dstep()
+    sim = Q.Simulation(deck.nr, deck.nz, 2, deck.dr, deck.dxi, iter_max=deck.iter_max,
+                       iter_reltol=deck.iter_reltol, dt=deck.dt)
+    sim.set_guess_extrapolation(order)
+    sim.add_species(*pl)
+    sim.add_beam(*beams[0])
+    iters, _ = sim.run_3d_step()
+    assert np.array_equal(iters, oiters), (iters, oiters)
+    worst = {n: float(store_errors(sim.fields[n].store_all(), osim.store(n)[:deck.nz]).max())
+             for n in ("e", "b", "psi", "cu", "b_spe")}
+    assert max(worst.values()) < 1e-9, worst
+    with pytest.raises(Q.QpadError):
+        sim.set_guess_extrapolation(3)
+    sim.close()

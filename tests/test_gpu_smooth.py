@@ -1,5 +1,7 @@
-"""Binomial smoothing of the species deposits (smooth_order 1 and 2) against the CPU oracle:
-the per-op charge and current deposits, and a whole 3D step through the fused loop."""
+"""Binomial smoothing of the species deposits against the CPU oracle, which applies
+ufield::smooth_f1 smooth_order times: the per-op charge and current deposits, and whole 3D
+steps through the fused loop (orders 1-2 inside the iteration kernel's node window, higher
+orders as a pass of their own before it)."""
 import numpy as np
 import pytest
 
@@ -19,7 +21,7 @@ def _plasma(nr, dr, seed):
     return x, p, g, ps, q
 
 
-@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("order", [1, 2, 3])
 @pytest.mark.parametrize("nr,M", [(64, 1), (96, 3)])
 def test_qdp_smoothed(order, nr, M):
     dr = 0.04
@@ -37,7 +39,7 @@ def test_qdp_smoothed(order, nr, M):
     sim.close()
 
 
-@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("order", [1, 2, 4])
 @pytest.mark.parametrize("push_type", [O.PUSH_ROBUST, O.PUSH_STD])
 def test_amjdp_smoothed(order, push_type):
     nr, M, dr, dt = 96, 2, 0.04, 0.04
@@ -68,9 +70,10 @@ def test_amjdp_smoothed(order, push_type):
 def test_smooth_order_limits():
     sim = Q.Simulation(32, 4, 1, 0.04, 0.04)
     with pytest.raises(Q.QpadError):
-        sim.set_smooth(3)
+        sim.set_smooth(65)
     with pytest.raises(Q.QpadError):
         sim.set_smooth(-1)
+    sim.set_smooth(64)
     sim.set_smooth(2)
     sim.set_smooth(0)
     sim.close()
@@ -78,7 +81,8 @@ def test_smooth_order_limits():
 
 # (nr 66: two CTAs of 33 rows, the 8-byte staging path)
 @pytest.mark.parametrize("order,M,push_type,nr", [(1, 2, O.PUSH_ROBUST, 64), (2, 1, O.PUSH_STD, 64),
-                                                  (2, 2, O.PUSH_ROBUST, 66)])
+                                                  (2, 2, O.PUSH_ROBUST, 66), (3, 2, O.PUSH_ROBUST, 64),
+                                                  (5, 1, O.PUSH_STD, 66)])
 def test_3d_step_smoothed_matches_oracle(order, M, push_type, nr):
     deck = Q.decks.Deck("smooth_loop", nr=nr, nz=32, max_mode=M, dr=0.04, dxi=0.04, ppc=(2, 1), num_theta=8,
                         uth=2e-3, seed=5, beams=[Q.decks.BeamSpec(2.0, 0.4, 0.3, 0.6, 20000, x0=0.04)],
