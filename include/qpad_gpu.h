@@ -271,6 +271,52 @@ typedef struct qpad_beam_load_desc {
 int64_t qpad_load_beam(int nr, int nz, double dr, double dxi, qpad_rng* r,
                        const qpad_beam_load_desc* d, double* x, double* p, double* q, int64_t cap);
 
+/* ---- diagnostic and restart files in the reference's HDF5 layout ----------------------
+ * Written and read by this library's own implementation of the HDF5 file format (the
+ * subset libhdf5 produces with default settings; no HDF5 library is needed).  Errors of the
+ * file-level calls are in qpad_h5_last_error(). */
+typedef struct qpad_h5_grid_info {
+  double time;                  /* root attribute TIME (tstep * dt) */
+  int32_t iter;                 /* ITER and the file's 8-digit step number */
+  double dt;                    /* DT */
+  const char* timeunit;         /* TIME UNIT */
+  const char* units;            /* dataset UNITS */
+  const char* label;            /* dataset LONG_NAME */
+  double axis_min[2], axis_max[2];                  /* AXIS/AXIS1 (r), AXIS/AXIS2 (xi) */
+  const char* axis_name[2];
+  const char* axis_label[2];
+  const char* axis_units[2];
+} qpad_h5_grid_info;
+const char* qpad_h5_last_error(void);
+/* One grid file as pwfield_2d writes it (hdf5io_class.f03:398-452, attributes :264-335): root
+ * attributes NAME, TYPE "grid", TIME, ITER, DT, TIME UNIT; group AXIS with AXIS1, AXIS2; the
+ * dataset `dataname` of shape [nz][nr] (data row-major, radial node fastest). */
+int qpad_h5_write_grid(const char* path, const char* dataname, const double* data, int nz, int nr,
+                       const qpad_h5_grid_info* info);
+/* One particle file as wpart writes it (hdf5io_class.f03:1584-1710): root attributes as above
+ * with TYPE "restart" and tp = n; datasets x [n][3], p [n][3], q [n] (none when n = 0). */
+int qpad_h5_write_particles(const char* path, const char* dataname, const double* x, const double* p,
+                            const double* q, int64_t n, int iter, double time, double dt);
+/* A float or integer dataset (path "name" or "group/name") as doubles; count, rank and dims
+ * (up to 8) are returned; out may be null to query them. */
+int qpad_h5_read_dataset(const char* path, const char* name, double* out, int64_t cap, int64_t* count,
+                         int32_t* rank, int64_t* dims);
+/* An attribute of the root ("" object) or of a member: numbers into *value, strings into text. */
+int qpad_h5_read_attr(const char* path, const char* object, const char* attr, double* value, char* text,
+                      int64_t text_cap);
+/* The field diagnostic of one component of a field's 3D store, every mode part
+ * (sim_diag::run, diagnostics_class.f03:822-944, files per part from add_diag_cym :947-1045):
+ * dir/Re0/, dir/Re1/, dir/Im1/, ... each <dataname>_<iter, 8 digits>.h5, dataset [nz][nr]
+ * over nodes 1..nr and slices 1..nz. */
+int qpad_diag_write_field(qpad_ctx* ctx, int field, int comp, const char* dir, const char* dataname,
+                          const char* units, const char* label, int iter, double time, double dt);
+/* beam3d::wrst (part3d_class.f03:827-845): the beam's particles into the restart file `path`
+ * (the reference names it ./RST/Beam<ii>/RST-beam<ii>-<rank, 6 digits>_<step, 8 digits>.h5). */
+int qpad_beam_write_rst(qpad_beam* bm, const char* path, const char* dataname, int iter, double time, double dt);
+/* beam3d::rrst (part3d_class.f03:847-865): a restart file's particles into host arrays
+ * x[n][3], p[n][3], q[n]; with all three null only *n is returned. */
+int qpad_rst_read(const char* path, double* x, double* p, double* q, int64_t cap, int64_t* n);
+
 /* ---- learned predictor-corrector guess (no counterpart in the reference) ------------
  * A radial 1D conv net (layers x conv1d(ksize), width channels, GELU between layers),
  * trained and evaluated by this library's own BF16 tensor-core kernels with FP32
@@ -298,15 +344,18 @@ int qpad_guess_attach(qpad_ctx* ctx, qpad_learn* net0, qpad_learn* net1);
 /* Initial B-perp guess of every slice from the stored B-perp of the previous slices, without
  * a net (no counterpart in the reference, which carries B-perp(j-1), simulation_class.f03:
  * 324-326, 360): order 0 keeps the carried value (the default), 1 extrapolates linearly from
- * slices j-1, j-2, 2 quadratically from j-1..j-3.  The iteration still runs to iter_reltol.
- * Attached nets take precedence. */
-int qpad_set_guess_extrapolation(qpad_ctx* ctx, int order);
+ * slices j-1, j-2, 2 quadratically from j-1..j-3; weight w in [0, 2] applies that fraction of
+ * the extrapolation's change to the carried value (1: the full extrapolation).  The iteration
+ * still runs to iter_reltol.  Attached nets take precedence. */
+int qpad_set_guess_extrapolation(qpad_ctx* ctx, int order, double weight);
 /* Which parts of the guess are applied (bit 0: B-perp, bit 1: the J-perp predictor; both by
  * default) and the weight w in [0, 1] of the net's correction: guess = carried + w (net - carried). */
 int qpad_guess_config(qpad_ctx* ctx, int apply, double weight);
 /* One training sample of mode m at slice j (3 <= j <= nz) from the 3D stores of the last
  * step: inputs x [10 or 20][nr], targets t [4 or 8][nr], both in units of *scale. */
 int qpad_guess_sample(qpad_ctx* ctx, int j, int m, float* x, float* t, float* scale);
+/* The same for slices j_lo .. j_hi in one call: x [n][10 or 20][nr], t [n][4 or 8][nr], scale [n]. */
+int qpad_guess_samples(qpad_ctx* ctx, int j_lo, int j_hi, int m, float* x, float* t, float* scale);
 
 #ifdef __cplusplus
 }

@@ -42,6 +42,13 @@ class TuneResult(C.Structure):
                 ("deposit_us", C.c_double)]
 
 
+class H5GridInfo(C.Structure):
+    _fields_ = [("time", C.c_double), ("iter", C.c_int32), ("dt", C.c_double), ("timeunit", C.c_char_p),
+                ("units", C.c_char_p), ("label", C.c_char_p), ("axis_min", C.c_double * 2),
+                ("axis_max", C.c_double * 2), ("axis_name", C.c_char_p * 2), ("axis_label", C.c_char_p * 2),
+                ("axis_units", C.c_char_p * 2)]
+
+
 class Rng(C.Structure):
     _fields_ = [("s", C.c_uint64), ("have", C.c_int32), ("next", C.c_double)]
 
@@ -135,7 +142,18 @@ _SIGS = {
                                    C.c_uint64, D]),
     "qpad_guess_attach": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "qpad_guess_sample": (C.c_int, [C.c_void_p, C.c_int, C.c_int, F, F, F]),
-    "qpad_set_guess_extrapolation": (C.c_int, [C.c_void_p, C.c_int]),
+    "qpad_h5_last_error": (C.c_char_p, []),
+    "qpad_h5_write_grid": (C.c_int, [C.c_char_p, C.c_char_p, D, C.c_int, C.c_int, C.c_void_p]),
+    "qpad_h5_write_particles": (C.c_int, [C.c_char_p, C.c_char_p, D, D, D, C.c_int64, C.c_int, C.c_double,
+                                          C.c_double]),
+    "qpad_h5_read_dataset": (C.c_int, [C.c_char_p, C.c_char_p, D, C.c_int64, I64P, I32P, I64P]),
+    "qpad_h5_read_attr": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, D, C.c_char_p, C.c_int64]),
+    "qpad_diag_write_field": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_char_p, C.c_char_p,
+                                        C.c_char_p, C.c_int, C.c_double, C.c_double]),
+    "qpad_beam_write_rst": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int, C.c_double, C.c_double]),
+    "qpad_rst_read": (C.c_int, [C.c_char_p, D, D, D, C.c_int64, I64P]),
+    "qpad_set_guess_extrapolation": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "qpad_guess_samples": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, F, F, F]),
     "qpad_guess_config": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "qpad_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "qpad_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -212,10 +212,11 @@ class Simulation:
         (the species' smooth_order)."""
         self._check(self.lib.qpad_set_smooth(self.h, int(order)))
 
-    def set_guess_extrapolation(self, order: int):
+    def set_guess_extrapolation(self, order: int, weight: float = 1.0):
         """Initial B-perp guess of every slice: 0 carries B-perp(j-1) as the reference does, 1
-        and 2 extrapolate it linearly / quadratically from the previous slices."""
-        self._check(self.lib.qpad_set_guess_extrapolation(self.h, int(order)))
+        and 2 extrapolate it linearly / quadratically from the previous slices; `weight` is
+        the fraction of the extrapolation's change to the carried value that is applied."""
+        self._check(self.lib.qpad_set_guess_extrapolation(self.h, int(order), float(weight)))
 
     def graph_active(self):
         """(whether the last 3D step ran as a graph, reason when it did not)."""

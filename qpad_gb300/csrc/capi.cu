@@ -1174,7 +1174,7 @@ int build_step_graph(qpad_ctx* ctx) {
 std::string step_key(const qpad_ctx* ctx) {
   std::string k = std::to_string(ctx->precision) + "/" + std::to_string(ctx->iter_cl) + "/" +
                   std::to_string(ctx->item_ppl) + "/" + std::to_string(ctx->guess != nullptr) + "/" +
-                  std::to_string(ctx->extrap) + "/" +
+                  std::to_string(ctx->extrap) + "/" + std::to_string(ctx->extrap_w) + "/" +
                   std::to_string(ctx->pdl) + "/" + std::to_string(ctx->g.smooth);
   for (auto* s : ctx->species)
     k += "|" + std::to_string((long long)s->np) + ":" + std::to_string(s->push_type) + ":" +

@@ -510,10 +510,11 @@ extern "C" int qpad_learn_train(qpad_learn* L, const float* X, const float* T, i
 // 3D stores (b_spe, cu, q_spe), channel (d-1)*5*nh + q*nh + h for slice j-d, quantity q in
 // {B_r, B_phi, J_r, J_phi, rho-Jz} and part h (Re, Im; m = 0 has Re only), over nodes
 // 1..nr, divided by their root mean square s.  Outputs (and training targets), channel
-// q*nh + h: q in {dB_r, dB_phi} = B-perp(j) - B-perp(j-1) and q in {dJ_r, dJ_phi} =
+// q*nh + h: q in {dB_r, dB_phi} = B-perp(j) - (2 B-perp(j-1) - B-perp(j-2)), what the linear
+// extrapolation from the two previous slices misses, and q in {dJ_r, dJ_phi} =
 // (J-perp(j) - J-perp(j-1)) / dxi, also in units of s.  The guess for slice j is then
-// b_spe = B-perp(j-1) + s dB and J-perp = J-perp(j-1) + dxi s dJ (the latter replaces the
-// carried predictor J-perp(j-1) + dxi dcu(j-1)).
+// b_spe = 2 B-perp(j-1) - B-perp(j-2) + s dB and J-perp = J-perp(j-1) + dxi s dJ (the latter
+// replaces the carried predictor J-perp(j-1) + dxi dcu(j-1); off by default).
 namespace qpad {
 
 struct GuessStores {
@@ -572,7 +573,8 @@ __global__ void __launch_bounds__(256) k_guess_in(GridDev G, GuessStores S, cons
     const int ch = q / nr, x = q % nr, i = x + 1;
     const int qq = ch / nh, h = ch % nh, p = h == 0 ? part_re(m) : part_im(m);
     double v;
-    if (qq < 2) v = st2(G, S.b2, 3, j, p, qq, i) - st2(G, S.b2, 3, j - 1, p, qq, i);
+    if (qq < 2)
+      v = st2(G, S.b2, 3, j, p, qq, i) - (2.0 * st2(G, S.b2, 3, j - 1, p, qq, i) - st2(G, S.b2, 3, j - 2, p, qq, i));
     else v = (st2(G, S.cu2, 3, j, p, qq - 2, i) - st2(G, S.cu2, 3, j - 1, p, qq - 2, i)) / G.dxi;
     T[(size_t)ch * nr + x] = (float)(v * s_inv);
   }
@@ -592,10 +594,12 @@ __global__ void __launch_bounds__(256) k_guess_out(GridDev G, GuessStores S, con
   const double s = (double)scale[m];
   for (int q = threadIdx.x; q < 2 * nh * nr; q += blockDim.x) {
     const int ch = q / nr, x = q % nr, i = x + 1;
-    if (i == 1) continue;                        // the axis node keeps the carried value
     const int c = ch / nh, h = ch % nh, p = h == 0 ? part_re(m) : part_im(m);
+    // the axis node takes the extrapolation alone
     if (apply & 1)
-      b_spe[fidx(G.ld, 3, p, c, i)] = st2(G, S.b2, 3, j - 1, p, c, i) + weight * s * (double)Y[(size_t)ch * ldy + x];
+      b_spe[fidx(G.ld, 3, p, c, i)] = 2.0 * st2(G, S.b2, 3, j - 1, p, c, i) - st2(G, S.b2, 3, j - 2, p, c, i) +
+                                      (i == 1 ? 0.0 : weight * s * (double)Y[(size_t)ch * ldy + x]);
+    if (i == 1) continue;
     if (apply & 2) {     // a blend of the carried predictor and the net's dJ-perp/dxi
       const double carried = cu[fidx(G.ld, 3, p, c, i)];
       const double net = st2(G, S.cu2, 3, j - 1, p, c, i) + G.dxi * s * (double)Y[(size_t)(2 * nh + ch) * ldy + x];
@@ -611,7 +615,7 @@ struct qpad_guess_state {
   qpad_learn* net1 = nullptr;     // m >= 1, all modes as one batch
   LearnBufs b0, b1;
   float* scale = nullptr;         // [M+1]
-  int apply = 3;                  // bit 0: B-perp guess, bit 1: J-perp predictor
+  int apply = 1;                  // bit 0: B-perp guess, bit 1: J-perp predictor
   double weight = 1.0;            // fraction of the net's correction that is applied
 };
 
@@ -635,7 +639,7 @@ void guess_free(qpad_ctx* ctx) {
 // 3 B1 - 3 B2 + B3.  Slices without enough history keep the carried value B(j-1).
 __global__ void __launch_bounds__(256) k_guess_extrap(GridDev G, const double* __restrict__ b2,
                                                       const int* __restrict__ jp, double* __restrict__ b_spe,
-                                                      int order) {
+                                                      int order, double w) {
   const int j = *jp;
   if (j <= order + 1) return;
   const int n = G.P * 2 * G.nr;
@@ -649,7 +653,7 @@ __global__ void __launch_bounds__(256) k_guess_extrap(GridDev G, const double* _
       const double b3 = st2(G, b2, 3, j - 3, p, c, i);
       v = 3.0 * (b1 - bb) + b3;
     }
-    b_spe[fidx(G.ld, 3, p, c, i)] = v;
+    b_spe[fidx(G.ld, 3, p, c, i)] = w == 1.0 ? v : b1 + w * (v - b1);
   }
 }
 
@@ -659,7 +663,7 @@ int guess_enqueue(qpad_ctx* ctx) {
   if (!g && ctx->extrap > 0) {
     const int n = ctx->g.P * 2 * ctx->g.nr;
     k_guess_extrap<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->g, ctx->f2[QPAD_F_B_SPE], ctx->d_j,
-                                                             ctx->f[QPAD_F_B_SPE], ctx->extrap);
+                                                             ctx->f[QPAD_F_B_SPE], ctx->extrap, ctx->extrap_w);
     return check_launch(ctx, "k_guess_extrap");
   }
   if (!g) return 0;
@@ -721,10 +725,37 @@ extern "C" int qpad_guess_sample(qpad_ctx* ctx, int j, int m, float* x, float* t
   return r;
 }
 
-extern "C" int qpad_set_guess_extrapolation(qpad_ctx* ctx, int order) {
-  if (!ctx || order < 0 || order > 2)
-    return ctx ? set_err(ctx, QPAD_E_ARG, "guess extrapolation: order 0, 1 or 2") : QPAD_E_ARG;
+extern "C" int qpad_guess_samples(qpad_ctx* ctx, int j_lo, int j_hi, int m, float* x, float* t, float* scale) {
+  if (!ctx || !x || !t || m < 0 || m > ctx->g.M || j_lo < 3 || j_hi > ctx->g.nz || j_hi < j_lo)
+    return ctx ? set_err(ctx, QPAD_E_ARG, "guess samples: needs 3 <= j_lo <= j_hi <= nz, 0 <= m <= max_mode")
+               : QPAD_E_ARG;
+  const int nr = ctx->g.nr, nh = m == 0 ? 1 : 2, ns = j_hi - j_lo + 1;
+  const size_t nx = (size_t)10 * nh * nr, nt = (size_t)4 * nh * nr;
+  float* d = nullptr;
+  if (int r = cuda_check(ctx, cudaMalloc(&d, sizeof(float) * (nx + nt + 1) * ns), "guess samples buffer")) return r;
+  float* dx = d;
+  float* dt = d + nx * ns;
+  float* ds = dt + nt * ns;
+  int r = 0;
+  for (int k = 0; k < ns && !r; ++k) {
+    k_guess_in<<<1, 256, 0, ctx->stream>>>(ctx->g, guess_stores(ctx), nullptr, j_lo + k, m, dx + nx * k, dx + nx * k,
+                                           nr, ds + k, dt + nt * k);
+    r = check_launch(ctx, "k_guess_in");
+  }
+  if (!r) r = cuda_check(ctx, cudaMemcpyAsync(x, dx, sizeof(float) * nx * ns, cudaMemcpyDeviceToHost, ctx->stream), "x");
+  if (!r) r = cuda_check(ctx, cudaMemcpyAsync(t, dt, sizeof(float) * nt * ns, cudaMemcpyDeviceToHost, ctx->stream), "t");
+  if (!r && scale)
+    r = cuda_check(ctx, cudaMemcpyAsync(scale, ds, sizeof(float) * ns, cudaMemcpyDeviceToHost, ctx->stream), "s");
+  if (!r) r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "guess samples");
+  cudaFree(d);
+  return r;
+}
+
+extern "C" int qpad_set_guess_extrapolation(qpad_ctx* ctx, int order, double weight) {
+  if (!ctx || order < 0 || order > 2 || !(weight >= 0.0 && weight <= 2.0))
+    return ctx ? set_err(ctx, QPAD_E_ARG, "guess extrapolation: order 0, 1 or 2, weight in [0, 2]") : QPAD_E_ARG;
   ctx->extrap = order;
+  ctx->extrap_w = weight;
   return 0;
 }
 

@@ -99,6 +99,7 @@ struct qpad_ctx {
   // (the smoothing order lives in g.smooth)
   struct qpad_guess_state* guess = nullptr;    // learned predictor-corrector guess (learn.cu)
   int extrap = 0;                              // polynomial order of the initial B-perp guess (0: carried)
+  double extrap_w = 1.0;                       // weight of the extrapolation's correction to the carried value
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
   float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
   double* scratch = nullptr;                   // per-call deposit scratch (cu, amu, acu)

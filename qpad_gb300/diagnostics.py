@@ -68,3 +68,81 @@ def fp32_state(pl, dr):
     def r32(a):
         return np.ascontiguousarray(np.asarray(a).astype(np.float32).astype(np.float64))
     return xr, r32(p), r32(g), r32(ps), r32(q)
+
+
+# ---- field dumps in the reference's layout ------------------------------------------------
+# The reference's field diagnostics (field.diag names, diagnostics_class.f03:421-600): diag
+# name -> (field object, component, directory under Fields/, data name, units, label).
+FIELD_DIAGS = {
+    "er_cyl_m": ("e", 0, "Er", "er", "m_ec\\omega_p/e", "E_r"),
+    "ephi_cyl_m": ("e", 1, "Ephi", "ephi", "m_ec\\omega_p/e", "E_\\phi"),
+    "ez_cyl_m": ("e", 2, "Ez", "ez", "m_ec\\omega_p/e", "E_z"),
+    "br_cyl_m": ("b", 0, "Br", "br", "m_e\\omega_p/e", "B_r"),
+    "bphi_cyl_m": ("b", 1, "Bphi", "bphi", "m_e\\omega_p/e", "B_\\phi"),
+    "bz_cyl_m": ("b", 2, "Bz", "bz", "m_e\\omega_p/e", "B_z"),
+    "spec_er_cyl_m": ("e_spe", 0, "Er_spec", "er", "m_ec\\omega_p/e", "E_r"),
+    "spec_ephi_cyl_m": ("e_spe", 1, "Ephi_spec", "ephi", "m_ec\\omega_p/e", "E_\\phi"),
+    "spec_ez_cyl_m": ("e_spe", 2, "Ez_spec", "ez", "m_ec\\omega_p/e", "E_z"),
+    "spec_br_cyl_m": ("b_spe", 0, "Br_spec", "br", "m_e\\omega_p/e", "B_r"),
+    "spec_bphi_cyl_m": ("b_spe", 1, "Bphi_spec", "bphi", "m_e\\omega_p/e", "B_\\phi"),
+    "spec_bz_cyl_m": ("b_spe", 2, "Bz_spec", "bz", "m_e\\omega_p/e", "B_z"),
+    "charge_cyl_m": ("q_spe", 0, "Charge", "charge", "n_0", "\\rho"),
+    "jr_cyl_m": ("cu", 0, "Jr", "jr", "n_0 c", "J_r"),
+    "jphi_cyl_m": ("cu", 1, "Jphi", "jphi", "n_0 c", "J_\\phi"),
+    "jz_cyl_m": ("cu", 2, "Jz", "jz", "n_0 c", "J_z"),
+    "psi_cyl_m": ("psi", 0, "Psi", "psi", "m_ec^2/e", "\\Psi"),
+}
+
+
+def mode_dirs(max_mode: int) -> list:
+    """Per-part directories of a real field dump: Re0, Re1, Im1, ... (add_diag_cym)."""
+    out = ["Re0"]
+    for m in range(1, max_mode + 1):
+        out += [f"Re{m}", f"Im{m}"]
+    return out
+
+
+def write_field_diags(sim, names, root: str, tstep: int) -> list:
+    """The field dumps `names` (keys of FIELD_DIAGS) of the last 3D step into
+    root/Fields/<Name>/<Re0|Re1|Im1|...>/<name>_<tstep, 8 digits>.h5 with TIME = tstep * dt;
+    returns the directories written."""
+    import os
+    out = []
+    for n in names:
+        field, comp, sub, dataname, units, label = FIELD_DIAGS[n]
+        d = os.path.join(root, "Fields", sub) + "/"
+        f = sim.fields[field]
+        sim._check(sim.lib.qpad_diag_write_field(sim.h, f.id, comp, d.encode(), dataname.encode(), units.encode(),
+                                                 label.encode(), int(tstep), float(tstep * sim.dt), float(sim.dt)))
+        out.append(d)
+    return out
+
+
+def read_h5_dataset(path: str, name: str):
+    """A dataset of an HDF5 file (this library's reader) as a float64 array of its shape."""
+    import ctypes as C
+
+    from . import _capi as K
+    L = K.load()
+    n, rank = C.c_int64(), C.c_int32()
+    dims = (C.c_int64 * 8)()
+    if L.qpad_h5_read_dataset(path.encode(), name.encode(), None, 0, C.byref(n), C.byref(rank), dims):
+        raise IOError(L.qpad_h5_last_error().decode())
+    out = np.zeros(max(n.value, 1))
+    if L.qpad_h5_read_dataset(path.encode(), name.encode(), out.ctypes.data_as(K.D), n.value, C.byref(n),
+                              C.byref(rank), dims):
+        raise IOError(L.qpad_h5_last_error().decode())
+    return out[:n.value].reshape([dims[k] for k in range(rank.value)])
+
+
+def read_h5_attr(path: str, attr: str, obj: str = ""):
+    """An attribute (number or string, strings with the trailing padding removed)."""
+    import ctypes as C
+
+    from . import _capi as K
+    L = K.load()
+    v = C.c_double()
+    buf = C.create_string_buffer(512)
+    if L.qpad_h5_read_attr(path.encode(), obj.encode(), attr.encode(), C.byref(v), buf, 512):
+        raise IOError(L.qpad_h5_last_error().decode())
+    return buf.value.decode().rstrip() if buf.value else v.value

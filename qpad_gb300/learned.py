@@ -116,6 +116,9 @@ def samples(sim: Simulation, m: int, j_range=None):
     xs = np.zeros((len(js), cin, sim.nr), np.float32)
     ts = np.zeros((len(js), cout, sim.nr), np.float32)
     sc = np.zeros(len(js), np.float32)
+    if js and js == list(range(js[0], js[-1] + 1)):      # a contiguous range: one call
+        sim._check(lib.qpad_guess_samples(sim.h, js[0], js[-1], m, _fp(xs), _fp(ts), _fp(sc)))
+        return xs, ts, sc
     for k, j in enumerate(js):
         s = C.c_float()
         sim._check(lib.qpad_guess_sample(sim.h, j, m, _fp(xs[k]), _fp(ts[k]), C.byref(s)))

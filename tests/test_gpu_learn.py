@@ -89,8 +89,8 @@ def test_guess_samples_match_stores():
             tr = []
             for qq in range(4):
                 for p in parts:
-                    if qq < 2:
-                        tr.append(b[j - 1, p, qq, 1:-1] - b[j - 2, p, qq, 1:-1])
+                    if qq < 2:      # what the linear extrapolation from slices j-1, j-2 misses
+                        tr.append(b[j - 1, p, qq, 1:-1] - (2 * b[j - 2, p, qq, 1:-1] - b[j - 3, p, qq, 1:-1]))
                     else:
                         tr.append((cu[j - 1, p, qq - 2, 1:-1] - cu[j - 2, p, qq - 2, 1:-1]) / deck.dxi)
             assert rel_l2(t[k], np.array(tr) / scale) < 1e-5
@@ -113,6 +113,26 @@ def test_guess_hook_with_zero_net_keeps_the_answer():
         assert rel_l2(b.b.store(s), a.b.store(s)) < 1e-4
     assert abs(ib.mean() - ia.mean()) < 3.0
     LR.attach(b, None, None)
+    a.close()
+    b.close()
+
+
+def test_zero_residual_net_is_the_linear_extrapolation():
+    """The nets predict what the linear extrapolation of B-perp misses: nets that output zero
+    give exactly the run with the linear extrapolation alone (qpad_set_guess_extrapolation 1)."""
+    deck = _deck()
+    a = Q.build_simulation(deck)
+    a.set_guess_extrapolation(1)
+    ia, _ = a.run_3d_step()
+    b = Q.build_simulation(deck)
+    n0, n1 = LR.ConvNet(*LR.CHANNELS[0]), LR.ConvNet(*LR.CHANNELS[1])
+    n0.set_params(np.zeros(n0.nparam, np.float32))
+    n1.set_params(np.zeros(n1.nparam, np.float32))
+    LR.attach(b, n0, n1)
+    ib, _ = b.run_3d_step()
+    assert np.array_equal(ia, ib)
+    for name in ("e", "b", "psi"):
+        assert rel_l2(b.fields[name].store_all(), a.fields[name].store_all()) < 1e-12
     a.close()
     b.close()
 
