@@ -193,6 +193,34 @@ int qpad_species_interp_psi(qpad_species* sp, int psi);
 /* part2d::sort (part2d_class.f03:2498-2579): exact reference permutation */
 int qpad_species_sort(qpad_species* sp);
 
+/* ---- neutral gas (source/species/neutral_class.f03) ------------------------------ */
+/* An ionising neutral gas: a species with no electrons at the start of every 3D step, whose
+ * gas ionises level by level at the ADK rates of |E| at the cell centres and angles
+ * 2 pi k / num_theta (ionize_neutral, neutral_class.f03:600-753), whose new electrons are
+ * born at rest evenly across each cell (add_particles, :755-837) and then pushed like any
+ * species, and whose ions stay put and join the charge source (ion_deposit_neutral,
+ * :904-930).  The rate of level i is adk[i][0] E^-adk[i][2] exp(-adk[i][1] / E) per second
+ * with E in GV/m (the reference's table of elements gives these numbers per element; the
+ * caller passes them, e.g. from qpad_gb300.neutrals.adk_coefficients).  Uniform gas; the
+ * FP64 path; no deposit smoothing.  The reference's mode sum for |E| reads the Re part of
+ * each mode m >= 1 for both its Re and Im terms (neutral_class.f03:659-660); this does the
+ * same, for identical results. */
+typedef struct qpad_neutral_desc {
+  double qm;             /* charge of the ionised particle (-1: electrons) */
+  double qbm;            /* its charge-to-mass ratio */
+  int32_t push_type;     /* QPAD_PUSH2_* */
+  int32_t levels;        /* ionisation levels followed (the reference's max_e), 1..16 */
+  const double* adk;     /* [levels][3]: p1, p2, p3 */
+  double wp;             /* plasma frequency of n0 (1/s): E is converted with m_e c wp / e */
+  double density;        /* gas density / n0 */
+  int32_t ppc1, ppc2, num_theta;   /* particles per cell as the reference's ppc, num_theta */
+  int64_t npmax;         /* capacity for the step's ionised electrons (exceeding it fails the step) */
+} qpad_neutral_desc;
+int qpad_neutral_create(qpad_ctx* ctx, const qpad_neutral_desc* desc, qpad_species** out);
+/* ionisation state [num_theta][nr][levels + 2]: the fractions in levels 1..levels, the neutral
+ * fraction, and the mean ionisation quantised to the particles per cell */
+int qpad_neutral_state_download(qpad_species* sp, double* state);
+
 /* ---- beams (source/beam/) -------------------------------------------------------- */
 typedef struct qpad_beam_desc {
   double qbm;

@@ -46,7 +46,10 @@ class SimDesc(C.Structure):
                 ("sp_push_type", C.c_int), ("sp_neutralized", C.c_int), ("sp_npmax", C.c_int64),
                 ("nbeams", C.c_int), ("beam_qbm", C.c_double * 4), ("beam_push_type", C.c_int * 4),
                 ("beam_npmax", C.c_int64 * 4), ("nthreads", C.c_int), ("smooth_order", C.c_int),
-                ("extrap", C.c_int)]
+                ("extrap", C.c_int), ("neut_levels", C.c_int), ("neut_adk", C.c_double * 48),
+                ("neut_wp", C.c_double), ("neut_density", C.c_double), ("neut_ppc1", C.c_int),
+                ("neut_ppc2", C.c_int), ("neut_num_theta", C.c_int), ("neut_qm", C.c_double),
+                ("neut_qbm", C.c_double), ("neut_push_type", C.c_int), ("neut_npmax", C.c_int64)]
 
 
 BND_ZERO, BND_OPEN = 2, 3
@@ -114,6 +117,8 @@ def lib():
             "orc_sim_store": (D, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int)]),
             "orc_sim_plasma": (C.c_int64, [C.c_void_p] + [C.POINTER(D)] * 8),
             "orc_sim_beam": (C.c_int64, [C.c_void_p, C.c_int] + [C.POINTER(D)] * 7),
+            "orc_sim_neutral": (C.c_int64, [C.c_void_p] + [C.POINTER(D)] * 8),
+            "orc_sim_multi_ion": (D, [C.c_void_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -341,7 +346,7 @@ class Sim:
 
     def __init__(self, g: Grid, *, iter_max=50, iter_reltol=1e-6, iter_abstol=0.0, dt3d=10.0,
                  sp_qbm=-1.0, sp_push_type=PUSH_ROBUST, neutralized=True, sp_npmax=1,
-                 beams=(), nthreads=1, smooth_order=0, extrap=0):
+                 beams=(), nthreads=1, smooth_order=0, extrap=0, neutral=None):
         d = SimDesc()
         d.g = g
         d.iter_max, d.iter_reltol, d.iter_abstol, d.dt3d = iter_max, iter_reltol, iter_abstol, dt3d
@@ -352,6 +357,19 @@ class Sim:
         d.nthreads = nthreads
         d.smooth_order = smooth_order
         d.extrap = extrap
+        self.neutral = neutral
+        if neutral:
+            # neutral: dict(adk=[(p1, p2, p3), ...], wp, density, ppc=(a, b), num_theta, qm, qbm,
+            #               push_type, npmax)
+            d.neut_levels = len(neutral["adk"])
+            for i, (a, b_, c) in enumerate(neutral["adk"]):
+                d.neut_adk[3 * i], d.neut_adk[3 * i + 1], d.neut_adk[3 * i + 2] = a, b_, c
+            d.neut_wp, d.neut_density = neutral["wp"], neutral["density"]
+            d.neut_ppc1, d.neut_ppc2 = neutral["ppc"]
+            d.neut_num_theta = neutral["num_theta"]
+            d.neut_qm, d.neut_qbm = neutral.get("qm", -1.0), neutral.get("qbm", -1.0)
+            d.neut_push_type = neutral.get("push_type", PUSH_ROBUST)
+            d.neut_npmax = neutral["npmax"]
         self.g = g
         self.h = lib().orc_sim_create(C.byref(d))
 
@@ -404,6 +422,21 @@ class Sim:
         for k, p in zip(Plasma.NAMES, ps):
             setattr(pl, k, np.ctypeslib.as_array(p, shape=(max(n, 1),))[:n].copy())
         return pl
+
+    def neutral_plasma(self) -> Plasma:
+        """The neutral gas's ionised electrons."""
+        ps = [D() for _ in range(8)]
+        n = int(lib().orc_sim_neutral(self.h, *[C.byref(p) for p in ps]))
+        pl = Plasma(n)
+        for k, p in zip(Plasma.NAMES, ps):
+            setattr(pl, k, np.ctypeslib.as_array(p, shape=(max(n, 1),))[:n].copy())
+        return pl
+
+    def multi_ion(self) -> np.ndarray:
+        """Ionisation state [n_theta][nr][levels + 2] (levels, neutral fraction, quantised mean)."""
+        L = len(self.neutral["adk"])
+        p = lib().orc_sim_multi_ion(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.neutral["num_theta"], self.g.nr, L + 2)).copy()
 
     def beam(self, k) -> Beam:
         ps = [D() for _ in range(7)]

@@ -1297,6 +1297,12 @@ struct orc_sim {
   /* 3D stores */
   double *q_beam2, *e2, *b2, *psi2, *b_spe2, *e_spe2, *cu2, *q_spe2;
   double *q_beamk;  /* one beam's own charge store (beam3d%q), summed into q_beam2 */
+  /* neutral gas (neutral_class.f03) */
+  int64_t nnp, na;
+  double *nx, *ny, *npx, *npy, *npz, *ngamma, *npsi, *nq;   /* its electrons */
+  double *ax, *ay, *aq;                                      /* ions born in the last update */
+  double *multi_ion, *ion_old;
+  double *rho_ion, *rho_add, *qneut, *cun, *amun, *acun;
   /* plasma */
   int64_t np;
   double *x, *y, *px, *py, *pz, *gamma, *ppsi, *q;
@@ -1324,6 +1330,16 @@ orc_sim* orc_sim_create(const orc_sim_desc* d) {
   s->psi2 = zalloc(s->n2); s->b_spe2 = zalloc(3 * s->n2); s->e_spe2 = zalloc(3 * s->n2);
   s->cu2 = zalloc(3 * s->n2); s->q_spe2 = zalloc(s->n2);
   s->q_beamk = d->nbeams > 1 ? zalloc(s->n2) : NULL;
+  if (d->neut_levels > 0) {
+    const int64_t nm = d->neut_npmax;
+    s->nx = zalloc(nm); s->ny = zalloc(nm); s->npx = zalloc(nm); s->npy = zalloc(nm); s->npz = zalloc(nm);
+    s->ngamma = zalloc(nm); s->npsi = zalloc(nm); s->nq = zalloc(nm);
+    s->ax = zalloc(nm); s->ay = zalloc(nm); s->aq = zalloc(nm);
+    s->multi_ion = zalloc((size_t)d->neut_num_theta * g->nr * (d->neut_levels + 2));
+    s->ion_old = zalloc((size_t)d->neut_num_theta * g->nr);
+    s->rho_ion = zalloc(s->n1); s->rho_add = zalloc(s->n1); s->qneut = zalloc(s->n1);
+    s->cun = zalloc(3 * s->n1); s->amun = zalloc(3 * s->n1); s->acun = zalloc(2 * s->n1);
+  }
   int64_t npm = d->sp_npmax;
   s->x = zalloc(npm); s->y = zalloc(npm); s->px = zalloc(npm); s->py = zalloc(npm);
   s->pz = zalloc(npm); s->gamma = zalloc(npm); s->ppsi = zalloc(npm); s->q = zalloc(npm);
@@ -1342,7 +1358,9 @@ void orc_sim_destroy(orc_sim* s) {
   double* all[] = {s->psi, s->e, s->e_spe, s->b, s->b_spe, s->b_beam, s->cu, s->amu, s->acu, s->dcu,
                    s->q_spe, s->q_beam, s->qsp, s->qn, s->q_beam2, s->e2, s->b2, s->psi2, s->b_spe2,
                    s->e_spe2, s->cu2, s->q_spe2, s->x, s->y, s->px, s->py, s->pz, s->gamma, s->ppsi,
-                   s->q, s->s_re, s->s_im, s->q_beamk};
+                   s->q, s->s_re, s->s_im, s->q_beamk, s->nx, s->ny, s->npx, s->npy, s->npz, s->ngamma, s->npsi,
+                   s->nq, s->ax, s->ay, s->aq, s->multi_ion, s->ion_old, s->rho_ion, s->rho_add, s->qneut,
+                   s->cun, s->amun, s->acun};
   for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); ++i) free(all[i]);
   for (int k = 0; k < s->d.nbeams; ++k) {
     free(s->bx[k]); free(s->by[k]); free(s->bz[k]); free(s->bpx[k]); free(s->bpy[k]);
@@ -1397,11 +1415,125 @@ void orc_sim_begin_3dstep(orc_sim* s) {
       for (size_t i = 0; i < s->n2; ++i) s->q_beam2[i] = s->q_beam2[i] + s->q_beamk[i];
     }
   }
+  /* renew_neutral (neutral_class.f03:839-878): no electrons, no ions, all gas neutral */
+  if (s->d.neut_levels > 0) {
+    const int L = s->d.neut_levels, ncell = s->d.neut_num_theta * g->nr;
+    s->nnp = 0;
+    s->na = 0;
+    for (int c = 0; c < ncell; ++c) {
+      for (int l = 0; l < L + 2; ++l) s->multi_ion[(size_t)c * (L + 2) + l] = l == L ? 1.0 : 0.0;
+      s->ion_old[c] = 0.0;
+    }
+    memset(s->rho_ion, 0, n1 * sizeof(double));
+  }
   /* :332-341 */
   memset(s->b, 0, 3 * n1 * sizeof(double)); memset(s->e, 0, 3 * n1 * sizeof(double));
   memset(s->b_spe, 0, 3 * n1 * sizeof(double)); memset(s->e_spe, 0, 3 * n1 * sizeof(double));
   memset(s->psi, 0, n1 * sizeof(double)); memset(s->cu, 0, 3 * n1 * sizeof(double));
   memset(s->acu, 0, 2 * n1 * sizeof(double)); memset(s->amu, 0, 3 * n1 * sizeof(double));
+}
+
+/* ---- neutral gas: neutral_class.f03 ---------------------------------------------------
+ * multi_ion[(k * nr + j) * (L + 2) + l]: angle k, cell j (0-based, cell j + 1 of the
+ * reference), level l = 0..L-1 the ionisation levels 1..L, l = L the neutral fraction,
+ * l = L + 1 the mean ionisation quantised to the particles per cell. */
+static double* MI(orc_sim* s, int k, int j) {
+  return s->multi_ion + ((size_t)k * s->d.g.nr + j) * (s->d.neut_levels + 2);
+}
+
+/* ionize_neutral (neutral_class.f03:600-753): ADK rates from |E| at the cell centres at the
+ * angles 2 pi k / n_theta and the level cascade over one slice step.  The mode sum takes the
+ * Re part of mode m for both its Re and its Im term, as the reference does (e_im => rf_re(m)). */
+static void neutral_ionize(orc_sim* s) {
+  const orc_grid* g = &s->d.g;
+  const int L = s->d.neut_levels, nth = s->d.neut_num_theta, nr = g->nr, M = g->max_mode;
+  const int ppc_tot = s->d.neut_ppc1 * s->d.neut_ppc2;
+  const double wp = s->d.neut_wp, dt = g->dxi, pi = 3.14159265358979323846;
+  const double* e = s->e;
+  double w[16];
+  for (int k = 0; k < nth; ++k) {
+    const double theta = 2.0 * pi / (double)nth * (double)k;
+    const double inc_r = cos(theta), inc_i = sin(theta);
+    double ph_r = 1.0, ph_i = 0.0;
+    double* e1 = (double*)malloc(sizeof(double) * 3 * (size_t)nr);
+    for (int j = 1; j <= nr; ++j)
+      for (int c = 0; c < 3; ++c) e1[3 * (j - 1) + c] = 0.5 * (F(e, 3, 0, c, j) + F(e, 3, 0, c, j + 1));
+    for (int m = 1; m <= M; ++m) {
+      const double t = ph_r * inc_r - ph_i * inc_i;
+      ph_i = ph_r * inc_i + ph_i * inc_r;
+      ph_r = t;
+      for (int j = 1; j <= nr; ++j)
+        for (int c = 0; c < 3; ++c) {
+          const double er = F(e, 3, PRE(m), c, j) + F(e, 3, PRE(m), c, j + 1);
+          const double ei = F(e, 3, PRE(m), c, j) + F(e, 3, PRE(m), c, j + 1);
+          e1[3 * (j - 1) + c] = e1[3 * (j - 1) + c] + er * ph_r - ei * ph_i;
+        }
+    }
+    for (int j = 0; j < nr; ++j) {
+      double* mi = MI(s, k, j);
+      const double* v = e1 + 3 * j;
+      const double eij = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * wp * 1.708e-12;
+      if (!(eij > 1.0e-6) || !(mi[L + 1] < (double)L)) continue;
+      for (int i = 0; i < L; ++i)
+        w[i] = s->d.neut_adk[3 * i] * pow(eij, -s->d.neut_adk[3 * i + 2]) * exp(-s->d.neut_adk[3 * i + 1] / eij) / wp;
+      int shoot = 0;
+      double cons = mi[L] * w[0] * dt * (1.0 + 0.5 * w[0] * dt);
+      if (cons > mi[L]) { shoot = 1; cons = mi[L]; }
+      mi[L] = mi[L] - cons;
+      for (int i = 1; i <= L - 1; ++i) {          /* levels i = 1 .. L-1 of the reference */
+        const double inj = cons;
+        double dens = 0.0;
+        if (shoot) { dens = inj * 0.5; shoot = 0; }
+        cons = (mi[i - 1] + dens) * w[i] * dt * (1.0 + 0.5 * w[i] * dt);
+        if (cons > mi[i - 1] + dens) { shoot = 1; cons = mi[i - 1] + dens; }
+        const double nv = mi[i - 1] - cons + inj;
+        mi[i - 1] = nv < 1.0 ? nv : 1.0;
+      }
+      const double top = mi[L - 1] + cons;
+      mi[L - 1] = top < 1.0 ? top : 1.0;
+      double avg = 0.0;
+      for (int i = 1; i <= L; ++i) avg = avg + (double)i * mi[i - 1];
+      mi[L + 1] = (double)L / (double)ppc_tot * (double)(int)(avg * (double)ppc_tot / (double)L + 0.5);
+    }
+    free(e1);
+  }
+}
+
+/* add_particles (neutral_class.f03:755-837): each (angle, cell) whose quantised ionisation
+ * rose gives that many new electrons, evenly spaced in r across the cell at the angle, at
+ * rest; their ions (opposite charge, same places) go to the ion buffer.  Uniform gas. */
+static void neutral_inject(orc_sim* s) {
+  const orc_grid* g = &s->d.g;
+  const int L = s->d.neut_levels, nth = s->d.neut_num_theta, nr = g->nr;
+  const int ppc_tot = s->d.neut_ppc1 * s->d.neut_ppc2;
+  const double pi = 3.14159265358979323846, dth = 2.0 * pi / (double)nth;
+  const double coef = (double)L * (s->d.neut_qm < 0.0 ? -1.0 : 1.0) / ((double)ppc_tot * (double)nth);
+  s->na = 0;
+  for (int k = 0; k < nth; ++k)
+    for (int j = 0; j < nr; ++j) {
+      const double* mi = MI(s, k, j);
+      const int add = (int)((mi[L + 1] - s->ion_old[(size_t)k * nr + j]) / (double)L * (double)ppc_tot + 0.5);
+      for (int i = 1; i <= add; ++i) {
+        if (s->nnp >= s->d.neut_npmax) break;      /* capacity (the reference assumes enough room) */
+        const double rn = (double)j + ((double)i - 0.5) / (double)add;   /* (j + 1) + noff - 1 */
+        const double th = (double)k * dth;
+        const int64_t p = s->nnp++, a = s->na++;
+        s->nx[p] = rn * g->dr * cos(th);
+        s->ny[p] = rn * g->dr * sin(th);
+        s->nq[p] = rn * 1.0 * 1.0 * s->d.neut_density * coef;
+        s->npx[p] = 0.0; s->npy[p] = 0.0; s->npz[p] = 0.0;
+        s->ngamma[p] = 1.0; s->npsi[p] = 0.0;
+        s->ax[a] = s->nx[p]; s->ay[a] = s->ny[p]; s->aq[a] = -s->nq[p];
+      }
+    }
+}
+
+/* update_neutral (neutral_class.f03:576-598) */
+static void neutral_update(orc_sim* s) {
+  const int L = s->d.neut_levels, ncell = s->d.neut_num_theta * s->d.g.nr;
+  for (int c = 0; c < ncell; ++c) s->ion_old[c] = s->multi_ion[(size_t)c * (L + 2) + L + 1];
+  neutral_ionize(s);
+  neutral_inject(s);
 }
 
 /* one xi slice j: simulation_class.f03:342-469 */
@@ -1434,6 +1566,19 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
     for (int k = 0; k < s->d.smooth_order; ++k) orc_smooth(g, 0, s->qsp);   /* q%smooth(), :202 */
     for (size_t i = 0; i < n1; ++i) s->q_spe[i] = s->q_spe[i] + s->qsp[i];
     if (s->d.sp_neutralized) for (size_t i = 0; i < n1; ++i) s->q_spe[i] = s->q_spe[i] + s->qn[i];
+    if (s->d.neut_levels > 0) {
+      /* :351-354 neut%qdp (qdeposit_neutral :880-902) and neut%ion_deposit (:904-930) */
+      memset(s->qneut, 0, n1 * sizeof(double));
+      orc_qdeposit(g, s->nnp, s->nx, s->ny, s->nq, s->qneut);
+      for (int k = 0; k < s->d.smooth_order; ++k) orc_smooth(g, 0, s->qneut);
+      for (size_t i = 0; i < n1; ++i) s->q_spe[i] = s->q_spe[i] + s->qneut[i];
+      memset(s->rho_add, 0, n1 * sizeof(double));
+      orc_qdeposit(g, s->na, s->ax, s->ay, s->aq, s->rho_add);
+      for (int k = 0; k < s->d.smooth_order; ++k) orc_smooth(g, 0, s->rho_add);
+      for (size_t i = 0; i < n1; ++i) s->rho_ion[i] = s->rho_ion[i] + s->rho_add[i];
+      for (size_t i = 0; i < n1; ++i) s->q_spe[i] = s->q_spe[i] + s->rho_ion[i];
+      s->na = 0;
+    }
     /* :356-360 */
     orc_solve_psi(g, s->q_spe, s->psi);
     if (s->d.sp_push_type == ORC_PUSH_STD) orc_interp_psi(g, s->np, s->x, s->y, s->psi, s->ppsi);
@@ -1455,6 +1600,15 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
         orc_smooth(g, 1, s->cu);
         orc_smooth(g, 2, s->acu);
         orc_smooth(g, 1, s->amu);
+      }
+      if (s->d.neut_levels > 0) {                      /* :384-386 neut%amjdp (:932-973), not smoothed */
+        memset(s->cun, 0, 3 * n1 * sizeof(double));
+        memset(s->acun, 0, 2 * n1 * sizeof(double));
+        memset(s->amun, 0, 3 * n1 * sizeof(double));
+        orc_amjdeposit(g, s->d.neut_push_type, s->d.neut_qbm, dxi, s->nnp, s->nx, s->ny, s->npx, s->npy, s->npz,
+                       s->nq, s->ngamma, s->npsi, s->e, s->b, s->cun, s->amun, s->acun, nt);
+        for (size_t i = 0; i < 3 * n1; ++i) { s->cu[i] = s->cu[i] + s->cun[i]; s->amu[i] = s->amu[i] + s->amun[i]; }
+        for (size_t i = 0; i < 2 * n1; ++i) s->acu[i] = s->acu[i] + s->acun[i];
       }
       orc_solve_djdxi(g, s->acu, s->amu, s->dcu);
       orc_solve_bt_iter(g, s->dcu, s->cu, s->b_spe);
@@ -1485,6 +1639,13 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
                s->gamma, s->ppsi, s->e, s->b, nt);
     orc_push_x(s->np, dxi, s->x, s->y, s->px, s->py, s->pz, s->gamma);
     s->np = orc_update_bound(g, s->np, s->x, s->y, s->px, s->py, s->pz, s->gamma, s->ppsi, s->q);
+    if (s->d.neut_levels > 0) {                        /* :443-449 neut%update, push_u, push_x */
+      neutral_update(s);
+      orc_push_u(g, s->d.neut_push_type, s->d.neut_qbm, dxi, s->nnp, s->nx, s->ny, s->npx, s->npy, s->npz,
+                 s->ngamma, s->npsi, s->e, s->b, nt);
+      orc_push_x(s->nnp, dxi, s->nx, s->ny, s->npx, s->npy, s->npz, s->ngamma);
+      s->nnp = orc_update_bound(g, s->nnp, s->nx, s->ny, s->npx, s->npy, s->npz, s->ngamma, s->npsi, s->nq);
+    }
     /* :452-456 copy slices */
     copy_1to2(s, s->e, s->e2, 3, j);
     copy_1to2(s, s->b, s->b2, 3, j);
@@ -1533,6 +1694,14 @@ double* orc_sim_store(orc_sim* s, const char* name, int* nc) {
     if (!strcmp(t[i].n, name)) { if (nc) *nc = t[i].c; return t[i].p; }
   return NULL;
 }
+
+int64_t orc_sim_neutral(orc_sim* s, double** x, double** y, double** px, double** py, double** pz,
+                        double** gamma, double** psi, double** q) {
+  *x = s->nx; *y = s->ny; *px = s->npx; *py = s->npy; *pz = s->npz; *gamma = s->ngamma; *psi = s->npsi; *q = s->nq;
+  return s->nnp;
+}
+
+double* orc_sim_multi_ion(orc_sim* s) { return s->multi_ion; }
 
 int64_t orc_sim_plasma(orc_sim* s, double** x, double** y, double** px, double** py, double** pz,
                        double** gamma, double** psi, double** q) {

@@ -137,6 +137,15 @@ typedef struct orc_sim_desc {
   int extrap;                  /* initial B-perp guess of a slice: 0 = carried (the reference),
                                   1 / 2 = linear / quadratic extrapolation from the stored slices
                                   (the product's optional guess, restated here to check it) */
+  /* an ionising neutral gas (neutral_class.f03), none when neut_levels = 0 */
+  int neut_levels;             /* ionisation levels followed (multi_max), at most 16 */
+  double neut_adk[48];         /* per level: p1, p2, p3 of the rate p1 E^-p3 exp(-p2 / E), E in GV/m */
+  double neut_wp;              /* plasma frequency (1/s) */
+  double neut_density;         /* gas density / n0 (uniform) */
+  int neut_ppc1, neut_ppc2, neut_num_theta;
+  double neut_qm, neut_qbm;    /* charge and charge-to-mass ratio of the ionised electrons */
+  int neut_push_type;
+  int64_t neut_npmax;
 } orc_sim_desc;
 
 /* One binomial (1,2,1) smoothing pass of a deposit field (ufield::smooth_f1,
@@ -166,6 +175,11 @@ double* orc_sim_field(orc_sim* s, const char* name, int* ncomp);   /* f1 */
 double* orc_sim_store(orc_sim* s, const char* name, int* ncomp);   /* f2 */
 int64_t orc_sim_plasma(orc_sim* s, double** x, double** y, double** px, double** py,
                        double** pz, double** gamma, double** psi, double** q);
+/* the neutral's electrons, and its ionisation state [n_theta][nr][levels + 2] (levels 1..L,
+ * then the neutral fraction, then the mean ionisation quantised to the particles per cell) */
+int64_t orc_sim_neutral(orc_sim* s, double** x, double** y, double** px, double** py, double** pz,
+                        double** gamma, double** psi, double** q);
+double* orc_sim_multi_ion(orc_sim* s);
 int64_t orc_sim_beam(orc_sim* s, int k, double** x, double** y, double** z, double** px,
                      double** py, double** pz, double** q);
 

@@ -42,6 +42,12 @@ class TuneResult(C.Structure):
                 ("deposit_us", C.c_double)]
 
 
+class NeutralDesc(C.Structure):
+    _fields_ = [("qm", C.c_double), ("qbm", C.c_double), ("push_type", C.c_int32), ("levels", C.c_int32),
+                ("adk", D), ("wp", C.c_double), ("density", C.c_double), ("ppc1", C.c_int32),
+                ("ppc2", C.c_int32), ("num_theta", C.c_int32), ("npmax", C.c_int64)]
+
+
 class H5GridInfo(C.Structure):
     _fields_ = [("time", C.c_double), ("iter", C.c_int32), ("dt", C.c_double), ("timeunit", C.c_char_p),
                 ("units", C.c_char_p), ("label", C.c_char_p), ("axis_min", C.c_double * 2),
@@ -143,6 +149,8 @@ _SIGS = {
     "qpad_guess_attach": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "qpad_guess_sample": (C.c_int, [C.c_void_p, C.c_int, C.c_int, F, F, F]),
     "qpad_h5_last_error": (C.c_char_p, []),
+    "qpad_neutral_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "qpad_neutral_state_download": (C.c_int, [C.c_void_p, D]),
     "qpad_h5_write_grid": (C.c_int, [C.c_char_p, C.c_char_p, D, C.c_int, C.c_int, C.c_void_p]),
     "qpad_h5_write_particles": (C.c_int, [C.c_char_p, C.c_char_p, D, D, D, C.c_int64, C.c_int, C.c_double,
                                           C.c_double]),

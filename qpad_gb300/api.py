@@ -193,6 +193,27 @@ class Simulation:
         self.species.append(sp)
         return sp
 
+    def add_neutral(self, adk, *, wp, density, ppc=(2, 1), num_theta=8, qm=-1.0, qbm=-1.0,
+                    push_type=K.PUSH2_ROBUST, npmax=None) -> "Species2D":
+        """An ionising neutral gas (neutral_class.f03): `adk` = [(p1, p2, p3)] per ionisation
+        level (see qpad_gb300.neutrals), wp the plasma frequency of n0 in 1/s, density in n0.
+        Its electrons appear during each 3D step; npmax bounds them (default: every level of
+        every cell ionised)."""
+        import numpy as np
+        a = np.ascontiguousarray(np.asarray(adk, np.float64).reshape(-1, 3))
+        levels = len(a)
+        if npmax is None:
+            npmax = self.nr * ppc[0] * ppc[1] * num_theta * levels + 1024
+        d = K.NeutralDesc(qm, qbm, push_type, levels, a.ctypes.data_as(K.D), wp, density, ppc[0], ppc[1],
+                          num_theta, int(npmax))
+        h = C.c_void_p()
+        self._check(self.lib.qpad_neutral_create(self.h, C.byref(d), C.byref(h)))
+        sp = Species2D.__new__(Species2D)
+        sp.sim, sp.h, sp.npmax, sp.qbm, sp.push_type = self, h, int(npmax), qbm, push_type
+        sp.levels, sp.num_theta = levels, num_theta
+        self.species.append(sp)
+        return sp
+
     def add_beam(self, x, p, q, *, qbm=-1.0, push_type=K.PUSH3_REDUCED, evolution=True, npmax=None) -> "Beam3D":
         bm = Beam3D(self, x, p, q, qbm=qbm, push_type=push_type, evolution=evolution, npmax=npmax)
         self.beams.append(bm)
@@ -343,6 +364,13 @@ class Species2D:
 
     def sort(self):
         self.sim._check(self.sim.lib.qpad_species_sort(self.h))
+
+    def ionisation_state(self):
+        """A neutral gas's state [num_theta][nr][levels + 2]: the fractions in each level, the
+        neutral fraction and the mean ionisation quantised to the particles per cell."""
+        out = np.zeros((self.num_theta, self.sim.nr, self.levels + 2))
+        self.sim._check(self.sim.lib.qpad_neutral_state_download(self.h, _dp(out)))
+        return out
 
 
 class Beam3D:

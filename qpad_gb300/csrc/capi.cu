@@ -346,6 +346,8 @@ extern "C" int qpad_ctx_destroy(qpad_ctx* ctx) {
   if (ctx->fac) cudaFree(ctx->fac);
   if (ctx->rtab) cudaFree(ctx->rtab);
   if (ctx->qn) cudaFree(ctx->qn);
+  if (ctx->qbg) cudaFree(ctx->qbg);
+  if (ctx->d_neut_err) cudaFree(ctx->d_neut_err);
   guess_free(ctx);
   if (ctx->qraw) cudaFree(ctx->qraw);
   if (ctx->raw) cudaFree(ctx->raw);
@@ -411,6 +413,7 @@ extern "C" int qpad_set_smooth(qpad_ctx* ctx, int order) {
   if (!ctx) return QPAD_E_ARG;
   if (order < 0 || order > kMaxSmoothOrder)
     return set_err(ctx, QPAD_E_ARG, "smooth order: 0 .. " + std::to_string(kMaxSmoothOrder));
+  if (order > 0 && has_neutrals(ctx)) return set_err(ctx, QPAD_E_ARG, "smoothing with a neutral gas is not built");
   const int old = ctx->g.smooth;
   ctx->g.smooth = order;
   // the iteration kernel's shared memory grows with smoothing: check its shape still fits
@@ -678,6 +681,7 @@ extern "C" int qpad_species_destroy(qpad_species* sp) {
   if (sp->qn) cudaFree(sp->qn);
   if (sp->pristine) cudaFree(sp->pristine);
   mixed_free(sp);
+  neutral_free(sp);
   for (size_t i = 0; i < ctx->species.size(); ++i)
     if (ctx->species[i] == sp) { ctx->species.erase(ctx->species.begin() + i); break; }
   delete sp;
@@ -688,12 +692,14 @@ extern "C" int qpad_species_destroy(qpad_species* sp) {
 extern "C" int qpad_species_renew(qpad_species* sp, const double* x, const double* p, const double* gamma,
                                   const double* psi, const double* q, int64_t np) {
   if (!sp) return QPAD_E_ARG;
+  if (sp->neut) return set_err(sp->ctx, QPAD_E_ARG, "a neutral gas's electrons are born, not loaded");
   return species_load(sp, x, p, gamma, psi, q, np);
 }
 
 extern "C" int qpad_species_reset(qpad_species* sp) {
   if (!sp) return QPAD_E_ARG;
   qpad_ctx* ctx = sp->ctx;
+  if (sp->neut) return neutral_step_begin(ctx);   // (every neutral gas of the context)
   sp->np = sp->np_pristine;
   if (is_mixed(sp)) {
     if (int r = mixed_restore_pristine(sp)) return r;
@@ -714,7 +720,7 @@ extern "C" int qpad_species_reset(qpad_species* sp) {
 extern "C" int qpad_species_count(qpad_species* sp, int64_t* np) {
   if (!sp) return QPAD_E_ARG;
   if (int r = species_sync_count(sp)) return r;
-  if (np) *np = sp->np;
+  if (np) *np = *sp->h_count;
   return QPAD_OK;
 }
 
@@ -724,7 +730,7 @@ extern "C" int qpad_species_download(qpad_species* sp, double* x, double* p, dou
   qpad_ctx* ctx = sp->ctx;
   if (int r = species_sync_count(sp)) return r;
   if (int r = sync_fp64_view(sp)) return r;
-  const int64_t n = sp->np;
+  const int64_t n = *sp->h_count;
   if (np) *np = n;
   double* staging = sp->x[1];
   if (x) if (int r = download_vec(ctx, staging, x, n, 2, sp->x[0], sp->y[0], nullptr)) return r;
@@ -1012,11 +1018,13 @@ int enqueue_slice_prologue(qpad_ctx* ctx, cudaGraphConditionalHandle hi, int use
     return check_launch(ctx, "slice prologue memsets", 0);
   for (auto* s : ctx->species)
     if (int r = mixed ? mixed_qdeposit_raw(s, ctx->qraw) : species_qdeposit_raw(s, ctx->qraw)) return r;
-  if (int r = launch_slice_begin(ctx, any_ntd)) return r;
+  // the ions of any neutral gas join the background (neutral_class.f03:904-930)
+  if (int r = neutral_slice_prologue(ctx)) return r;
+  if (int r = launch_slice_begin(ctx, any_ntd || ctx->qbg != nullptr)) return r;
   // E of the first iteration (later iterations get theirs from k_iterate)
   if (int r = launch_iter_e(ctx)) return r;
   for (auto* s : ctx->species)
-    if (s->push_type == QPAD_PUSH2_STD)
+    if (s->push_type == QPAD_PUSH2_STD && !s->neut)   // (the reference interpolates psi for species only)
       if (int r = mixed ? mixed_interp_psi(s, ctx->f[QPAD_F_PSI]) : species_interp_psi(s, ctx->f[QPAD_F_PSI]))
         return r;
   // the convergence record of B_phi: in the graph the last iteration of the previous slice
@@ -1048,6 +1056,7 @@ int enqueue_iteration(qpad_ctx* ctx, cudaGraphConditionalHandle h, int use_h) {
 int enqueue_slice_epilogue(qpad_ctx* ctx, int sort_now) {
   const bool mixed = ctx->precision == QPAD_PREC_MIXED;
   if (int r = launch_slice_end(ctx)) return r;
+  if (int r = neutral_slice_update(ctx)) return r;   // ionisation and new electrons before the push
   for (auto* s : ctx->species) {
     if (mixed) {
       if (int r = mixed_push(s, ctx->gtab, ctx->g.dxi, 1, 1)) return r;   // sorts by cell every slice
@@ -1235,7 +1244,7 @@ int step_begin(qpad_ctx* ctx) {
   // the convergence record of the zeroed B_phi
   if (cudaMemsetAsync(ctx->conv, 0, 2 * (size_t)ctx->g.nr * sizeof(double), ctx->stream) != cudaSuccess)
     return check_launch(ctx, "zero record");
-  return 0;
+  return neutral_step_begin(ctx);           // every neutral gas starts the step un-ionised
 }
 
 bool graph_ok(const qpad_ctx* ctx) {
@@ -1275,6 +1284,13 @@ int step_end(qpad_ctx* ctx, int push_beams) {
   if (werr) {
     cudaMemsetAsync(ctx->iter_tickets + kIterErrWord, 0, sizeof(werr), ctx->stream);
     return set_err(ctx, QPAD_E_CUDA, "field iteration: a bulk-copy wait gave up (staging incomplete)");
+  }
+  if (ctx->d_neut_err) {
+    unsigned int nerr = 0;
+    if (int r = cuda_check(ctx, cudaMemcpy(&nerr, ctx->d_neut_err, sizeof(nerr), cudaMemcpyDeviceToHost),
+                           "neutral error word"))
+      return r;
+    if (nerr) return set_err(ctx, QPAD_E_CAPACITY, "a neutral gas ionised more electrons than its npmax holds");
   }
   return QPAD_OK;
 }
@@ -1337,7 +1353,7 @@ extern "C" int qpad_batch_create(qpad_ctx* const* ctxs, int n, qpad_batch** out)
   if (!ctxs || n < 1 || !out) return QPAD_E_ARG;
   *out = nullptr;
   for (int i = 0; i < n; ++i)
-    if (!ctxs[i] || ctxs[i]->device != ctxs[0]->device) return QPAD_E_ARG;
+    if (!ctxs[i] || ctxs[i]->device != ctxs[0]->device || has_neutrals(ctxs[i])) return QPAD_E_ARG;
   qpad_batch* b = new (std::nothrow) qpad_batch();
   if (!b) return QPAD_E_NOMEM;
   b->ctxs.assign(ctxs, ctxs + n);

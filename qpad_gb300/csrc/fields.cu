@@ -657,7 +657,7 @@ static SliceFields slice_fields(qpad_ctx* ctx) {
   SliceFields s;
   for (int k = 0; k < QPAD_NFIELDS; ++k) { s.f[k] = ctx->f[k]; s.f2[k] = ctx->f2[k]; }
   s.qraw = ctx->qraw;
-  s.qn = ctx->qn;
+  s.qn = ctx->qbg ? ctx->qbg : ctx->qn;          // with a neutral gas: qn + its ions
   s.gtab = ctx->precision == QPAD_PREC_MIXED ? ctx->gtab : nullptr;
   return s;
 }

@@ -397,6 +397,14 @@ int species_qdeposit_raw(qpad_species* sp, double* qraw) {
   return check_launch(ctx, "k_qdeposit");
 }
 
+// The charge deposit of arbitrary particle arrays (count on the device, at most n_bound).
+int qdeposit_arrays(qpad_ctx* ctx, const int64_t* d_count, int64_t n_bound, const double* x, const double* y,
+                    const double* q, double* qraw) {
+  if (n_bound <= 0) return 0;
+  k_qdeposit<<<grid_for(n_bound, kPartThreads), kPartThreads, 0, ctx->stream>>>(ctx->g, d_count, x, y, q, qraw);
+  return check_launch(ctx, "k_qdeposit (arrays)");
+}
+
 int species_amjdp_raw(qpad_species* sp, const double* ef, const double* bf, double* cu, double* amu, double* acu,
                       double dt) {
   qpad_ctx* ctx = sp->ctx;
@@ -483,7 +491,7 @@ int species_sync_count(qpad_species* sp) {
   if (e != cudaSuccess) return cuda_check(ctx, e, "count readback");
   e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_check(ctx, e, "count sync");
-  sp->np = *sp->h_count;
+  sp->np = sp->neut ? sp->npmax : *sp->h_count;   // (a neutral gas's launches cover its capacity)
   return 0;
 }
 

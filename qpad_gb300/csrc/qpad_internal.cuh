@@ -99,6 +99,8 @@ struct qpad_ctx {
   // (the smoothing order lives in g.smooth)
   struct qpad_guess_state* guess = nullptr;    // learned predictor-corrector guess (learn.cu)
   int extrap = 0;                              // polynomial order of the initial B-perp guess (0: carried)
+  double* qbg = nullptr;                       // qn + the ions of every neutral gas (when there is one)
+  unsigned int* d_neut_err = nullptr;          // set when a neutral's particle buffer overflowed
   double extrap_w = 1.0;                       // weight of the extrapolation's correction to the carried value
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
   float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
@@ -162,6 +164,7 @@ struct qpad_species {
   void* mixed_pristine = nullptr;
   double* qf = nullptr;         // this species' charge density (finished deposit)
   double* qn = nullptr;         // this species' neutralising background
+  struct qpad_neutral_state* neut = nullptr;   // ionisation state when this species is a neutral gas
 };
 
 struct qpad_beam {
@@ -228,6 +231,14 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
 
 // ---- particle kernels (plasma.cu, beam.cu) ---------------------------------------------
 int species_qdeposit_raw(qpad_species* sp, double* qraw);
+int qdeposit_arrays(qpad_ctx* ctx, const int64_t* d_count, int64_t n_bound, const double* x, const double* y,
+                    const double* q, double* qraw);
+// neutral gas species (neutral.cu)
+int neutral_step_begin(qpad_ctx* ctx);
+int neutral_slice_prologue(qpad_ctx* ctx);
+int neutral_slice_update(qpad_ctx* ctx);
+bool has_neutrals(const qpad_ctx* ctx);
+void neutral_free(qpad_species* sp);
 int species_amjdp_raw(qpad_species* sp, const double* ef, const double* bf, double* cu, double* amu,
                       double* acu, double dt);
 int species_push_u(qpad_species* sp, const double* ef, const double* bf, double dt, int fuse_x);
