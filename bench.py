@@ -7,7 +7,10 @@ plasma renewal that the reference performs after every 3D step.  The metric's fi
 plasma particle-pushes/s, is the headline value (one plasma particle advanced through one
 slice, all of its predictor-corrector deposits included); B-perp iterations per slice are
 reported beside it.  The headline path is the mixed-precision one (FP32 particles, FP64
-solves).  The plain FP64 path runs on the same deck and inputs as the comparison arm
+solves); each slice's B-perp iteration starts from the linear extrapolation of the two
+previous slices' converged B-perp (--guess-order 1, not in the reference, which carries
+slice j-1's: --guess-order 0).  The plain FP64 path, with the carried guess, runs on the
+same deck and inputs as the comparison arm
 ("compare", "speedup_vs_fp64", "iters_change_vs_fp64"), and the per-mode field error of
 the mixed path against it over one whole 3D step from identical inputs is "max_mode_err"
 (the FP64 path itself matches the FP64 oracle to 1e-9; the oracle is too slow for a whole

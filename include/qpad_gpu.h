@@ -42,7 +42,8 @@ enum {
 
 /* ---- enums mirroring source/param.f03 ------------------------------------------- */
 enum { QPAD_BND_ZERO = 2, QPAD_BND_OPEN = 3 };                     /* param.f03:72-74 */
-enum { QPAD_PUSH2_STD = 0, QPAD_PUSH2_ROBUST = 1 };                /* param.f03:63-64 */
+enum { QPAD_PUSH2_STD = 0, QPAD_PUSH2_ROBUST = 1,                   /* param.f03:63-64 */
+       QPAD_PUSH2_STD_PGC = 4, QPAD_PUSH2_ROBUST_PGC = 5 };          /* species that see the lasers */
 enum { QPAD_PUSH3_REDUCED = 1, QPAD_PUSH3_BORIS = 2 };             /* param.f03:62 */
 enum { QPAD_COPY_1TO2 = 1, QPAD_COPY_2TO1 = -1 };                  /* param.f03:125 */
 enum { QPAD_PREC_FP64 = 0, QPAD_PREC_MIXED = 1 };
@@ -57,6 +58,7 @@ enum {
 /* ---- context ------------------------------------------------------------------- */
 typedef struct qpad_ctx qpad_ctx;
 typedef struct qpad_species qpad_species;
+typedef struct qpad_laser qpad_laser;
 typedef struct qpad_beam qpad_beam;
 
 typedef struct qpad_grid_desc {
@@ -203,7 +205,7 @@ int qpad_species_sort(qpad_species* sp);
  * with E in GV/m (the reference's table of elements gives these numbers per element; the
  * caller passes them, e.g. from qpad_gb300.neutrals.adk_coefficients).  Uniform gas; the
  * FP64 path; no deposit smoothing.  The reference's mode sum for |E| reads the Re part of
- * each mode m >= 1 for both its Re and Im terms (neutral_class.f03:659-660); this does the
+ * each mode m >= 1 for both its Re and Im terms (neutral_class.f03:652-659); this does the
  * same, for identical results. */
 typedef struct qpad_neutral_desc {
   double qm;             /* charge of the ionised particle (-1: electrons) */
@@ -220,6 +222,36 @@ int qpad_neutral_create(qpad_ctx* ctx, const qpad_neutral_desc* desc, qpad_speci
 /* ionisation state [num_theta][nr][levels + 2]: the fractions in levels 1..levels, the neutral
  * fraction, and the mean ionisation quantised to the particles per cell */
 int qpad_neutral_state_download(qpad_species* sp, double* state);
+
+/* ---- laser envelopes (source/laser/, sim_lasers_class.f03) ------------------------
+ * A laser is the envelope a = a_r + i a_i of its vector potential, held per xi slice in the
+ * azimuthal modes (field_laser_class.f03; the launch profiles of profile_laser_class.f03 are
+ * evaluated by the caller, e.g. qpad_gb300.lasers.launch).  With lasers on the context, every
+ * 3D step gathers per slice the sum of their envelopes and gradients for the species of push
+ * type QPAD_PUSH2_*_PGC (amjdeposit_*_pgc, push_u_*_pgc, part2d_class.f03:1012-1602,
+ * 1967-2219), deposits every species' susceptibility chi into a store after the slice's
+ * iteration (deposit_chi :361-476; its axis factor needs the species' radial particles per
+ * cell, qpad_species_set_radial_ppc), and after the slice loop advances each envelope by the
+ * 3D time step (set_rhs + solve, field_laser_class.f03:393-927, with the penta-diagonal
+ * cyclic reduction of fpcr_penta_class.f03).  FP64 path; nr a power of two; at most 7 modes.
+ * Replaces sim_lasers%new/advance/deposit_chi (sim_lasers_class.f03:83-223). */
+typedef struct qpad_laser_desc {
+  double k0;             /* central wavenumber (laser(i).k0) */
+  int32_t iter;          /* implicit iterations per slice of the advance (laser(i).iteration) */
+} qpad_laser_desc;
+/* ar, ai: the initial envelope [nz][P][nr] (nodes 1..nr; the on-axis values of m >= 1 are
+ * taken as zero, as the advance leaves them) */
+int qpad_laser_create(qpad_ctx* ctx, const qpad_laser_desc* desc, const double* ar, const double* ai,
+                      qpad_laser** out);
+/* the envelope [nz][P][nr + 2] (slices 1..nz) */
+int qpad_laser_download(qpad_laser* laser, double* ar, double* ai);
+/* the susceptibility store of the last 3D step [nz][P][nr + 2] */
+int qpad_laser_chi_download(qpad_ctx* ctx, double* chi);
+/* lasers%advance on its own (qpad_3d_step runs it after the slice loop) */
+int qpad_lasers_advance(qpad_ctx* ctx);
+/* the species' radial particles per cell (pf%ppc(1)): chi's on-axis factor
+ * 12 ppc_r^2 / (1 + 2 ppc_r^2) (get_deposit_ax_corr, part2d_class.f03:2581-2586); default 2 */
+int qpad_species_set_radial_ppc(qpad_species* sp, int32_t ppc_r);
 
 /* ---- beams (source/beam/) -------------------------------------------------------- */
 typedef struct qpad_beam_desc {

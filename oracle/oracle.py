@@ -49,12 +49,20 @@ class SimDesc(C.Structure):
                 ("extrap", C.c_int), ("neut_levels", C.c_int), ("neut_adk", C.c_double * 48),
                 ("neut_wp", C.c_double), ("neut_density", C.c_double), ("neut_ppc1", C.c_int),
                 ("neut_ppc2", C.c_int), ("neut_num_theta", C.c_int), ("neut_qm", C.c_double),
-                ("neut_qbm", C.c_double), ("neut_push_type", C.c_int), ("neut_npmax", C.c_int64)]
+                ("neut_qbm", C.c_double), ("neut_push_type", C.c_int), ("neut_npmax", C.c_int64),
+                ("nlasers", C.c_int), ("laser_k0", C.c_double * 4), ("laser_iter", C.c_int * 4),
+                ("sp_ppc_r", C.c_int)]
+
+
+class LaserF1(C.Structure):
+    _fields_ = [("ar", C.POINTER(C.c_double)), ("ai", C.POINTER(C.c_double)),
+                ("gr", C.POINTER(C.c_double)), ("gi", C.POINTER(C.c_double))]
 
 
 BND_ZERO, BND_OPEN = 2, 3
 FK_PSI, FK_EZ, FK_BZ, FK_BT, FK_BPLUS, FK_BMINUS = range(6)
 PUSH_STD, PUSH_ROBUST = 0, 1
+PUSH_STD_PGC, PUSH_ROBUST_PGC = 4, 5
 PUSH3_REDUCED, PUSH3_BORIS = 1, 2
 
 _lib = None
@@ -119,6 +127,18 @@ def lib():
             "orc_sim_beam": (C.c_int64, [C.c_void_p, C.c_int] + [C.POINTER(D)] * 7),
             "orc_sim_neutral": (C.c_int64, [C.c_void_p] + [C.POINTER(D)] * 8),
             "orc_sim_multi_ion": (D, [C.c_void_p]),
+            "orc_sim_set_laser": (None, [C.c_void_p, C.c_int, D, D]),
+            "orc_sim_laser": (None, [C.c_void_p, C.c_int, C.POINTER(D), C.POINTER(D)]),
+            "orc_pcr_coef": (None, [C.c_int, D, D, D, D, D, D, D, D, D, D]),
+            "orc_pcr_solve": (None, [C.c_int, D, D, D, D, D, D]),
+            "orc_laser_matrix": (None, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        D, D, D, D, D]),
+            "orc_laser_grad": (None, [C.POINTER(Grid), D, D, C.c_int, D, D]),
+            "orc_deposit_chi": (None, [C.POINTER(Grid), C.c_double, C.c_int, C.c_int64, D, D, D, D, D]),
+            "orc_amjdeposit_pgc": (None, [C.POINTER(Grid), C.c_int, C.c_double, C.c_double, C.c_int64] + [D] * 10
+                                   + [C.POINTER(LaserF1), D, D, D]),
+            "orc_push_u_pgc": (None, [C.POINTER(Grid), C.c_double, C.c_double, C.c_int64] + [D] * 9
+                               + [C.POINTER(LaserF1)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -136,6 +156,29 @@ def ptr(a: np.ndarray):
 def iptr(a: np.ndarray):
     assert a.dtype == np.int32 and a.flags.c_contiguous
     return a.ctypes.data_as(I32)
+
+
+def laser_matrix(nr, m, k0, ds, dr, dz):
+    """Rows (a, b, c, d, e) [5][2 nr] of the envelope's penta-diagonal system for mode m."""
+    A = np.zeros((5, 2 * nr))
+    lib().orc_laser_matrix(nr, m, k0, ds, dr, dz, *[ptr(A[k]) for k in range(5)])
+    return A
+
+
+def pcr_coef(A):
+    """PCR tables of a penta-diagonal matrix A [5][n]: (cm1, cm2, cp1, cp2 [steps][n], cfin [n])."""
+    n = A.shape[1]
+    steps = int(np.ceil(np.log2(n)))
+    A = np.ascontiguousarray(A, np.float64)
+    c = [np.zeros((steps, n)) for _ in range(4)] + [np.zeros(n)]
+    lib().orc_pcr_coef(n, *[ptr(A[k]) for k in range(5)], *[ptr(x) for x in c])
+    return c
+
+
+def pcr_solve(coef, rhs):
+    x = np.ascontiguousarray(rhs, np.float64).copy()
+    lib().orc_pcr_solve(len(x), *[ptr(c) for c in coef], ptr(x))
+    return x
 
 
 def grid(nr, nz, max_mode, dr, dxi, relax_fac=None, bnd=BND_OPEN) -> Grid:
@@ -346,7 +389,7 @@ class Sim:
 
     def __init__(self, g: Grid, *, iter_max=50, iter_reltol=1e-6, iter_abstol=0.0, dt3d=10.0,
                  sp_qbm=-1.0, sp_push_type=PUSH_ROBUST, neutralized=True, sp_npmax=1,
-                 beams=(), nthreads=1, smooth_order=0, extrap=0, neutral=None):
+                 beams=(), nthreads=1, smooth_order=0, extrap=0, neutral=None, lasers=(), sp_ppc_r=2):
         d = SimDesc()
         d.g = g
         d.iter_max, d.iter_reltol, d.iter_abstol, d.dt3d = iter_max, iter_reltol, iter_abstol, dt3d
@@ -370,8 +413,18 @@ class Sim:
             d.neut_qm, d.neut_qbm = neutral.get("qm", -1.0), neutral.get("qbm", -1.0)
             d.neut_push_type = neutral.get("push_type", PUSH_ROBUST)
             d.neut_npmax = neutral["npmax"]
+        # lasers: [dict(k0=, iter=, ar=[nz][P][nr], ai=[nz][P][nr])]; nr a power of two
+        d.nlasers = len(lasers)
+        for k, ls in enumerate(lasers):
+            d.laser_k0[k], d.laser_iter[k] = ls["k0"], ls["iter"]
+        d.sp_ppc_r = sp_ppc_r
         self.g = g
+        self.nlasers = len(lasers)
         self.h = lib().orc_sim_create(C.byref(d))
+        for k, ls in enumerate(lasers):
+            ar = np.ascontiguousarray(ls["ar"], np.float64)
+            ai = np.ascontiguousarray(ls["ai"], np.float64)
+            lib().orc_sim_set_laser(self.h, k, ptr(ar), ptr(ai))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -431,6 +484,14 @@ class Sim:
         for k, p in zip(Plasma.NAMES, ps):
             setattr(pl, k, np.ctypeslib.as_array(p, shape=(max(n, 1),))[:n].copy())
         return pl
+
+    def laser(self, k):
+        """Laser k's envelope (a_r, a_i) over slices 1..nz: [nz][P][nr + 2] each."""
+        pr, pi = D(), D()
+        lib().orc_sim_laser(self.h, k, C.byref(pr), C.byref(pi))
+        P = 2 * self.g.max_mode + 1
+        shape = (self.g.nz + 3, P, self.g.nr + 2)
+        return tuple(np.ctypeslib.as_array(p, shape=shape)[2:self.g.nz + 2].copy() for p in (pr, pi))
 
     def multi_ion(self) -> np.ndarray:
         """Ionisation state [n_theta][nr][levels + 2] (levels, neutral fraction, quantised mean)."""

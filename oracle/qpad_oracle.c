@@ -946,6 +946,207 @@ void orc_push_u(const orc_grid* g, int push_type, double qbm, double dt, int64_t
     push_u_one(g, push_type, qbm, qtmh, idr, pp, x, y, px, py, pz, gamma, psi, ef, bf);
 }
 
+/* =============================================================================
+ * PGC (ponderomotive guiding centre) pushers, for species that see a laser envelope
+ *   amjdeposit_robust_pgc part2d_class.f03:1310-1602, amjdeposit_std_pgc :1012-1308,
+ *   push_u_robust_pgc / push_u_std_pgc :1967-2219 (the two push_u variants are the same).
+ * The laser enters through a = a_r + i a_i and the gradients (r, phi, xi components) of
+ * a_r and a_i, all gathered like any field; |a|^2 raises gamma, its gradient adds the
+ * ponderomotive force to E.
+ * ============================================================================= */
+static void amj_one_pgc(const orc_grid* g, int push_type, double qbm, double qtmh, double idt,
+                        double idr, int64_t pp, const double* x, const double* y, const double* px,
+                        const double* py, const double* pz, const double* q, double* gamma, double* psi,
+                        const double* ef, const double* bf, const orc_laser_f1* lf, double* cu,
+                        double* amu, double* dcu) {
+  const int M = g->max_mode;
+  interp_info ii = gen_interp_info(x[pp], y[pp], idr);
+  double ep[3], bp[3], wp[3], u0[3], u[3], utmp[3], du[2], u2[3], gr[3], gi[3];
+  interp_vec(g, ef, &ii, ep);
+  interp_vec(g, bf, &ii, bp);
+  const double apr = interp_scalar(g, lf->ar, &ii), api = interp_scalar(g, lf->ai, &ii);
+  interp_vec(g, lf->gr, &ii, gr);
+  interp_vec(g, lf->gi, &ii, gi);
+  const double gam_corr = 0.5 * (qbm * qbm) * (apr * apr + api * api);
+  u0[0] = px[pp] * ii.pcos + py[pp] * ii.psin;
+  u0[1] = py[pp] * ii.pcos - px[pp] * ii.psin;
+  u0[2] = pz[pp];
+  double gam = sqrt(1.0 + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2] + gam_corr);
+  wp[0] = ep[0] - bp[1];
+  wp[1] = ep[1] + bp[0];
+  wp[2] = ep[2];
+  const double tmp = 0.5 * qbm / gam;          /* effective E: the ponderomotive force */
+  ep[0] = ep[0] - tmp * (apr * gr[0] + api * gi[0]);
+  ep[1] = ep[1] - tmp * (apr * gr[1] + api * gi[1]);
+  ep[2] = ep[2] + tmp * (apr * gr[2] + api * gi[2]);
+  double qtmh_e, qtmh_b = 0.0;
+  if (push_type == ORC_PUSH_ROBUST_PGC) {
+    qtmh_e = qtmh * gam / (gam - u0[2]);
+    for (int c = 0; c < 3; ++c) utmp[c] = u0[c] + ep[c] * qtmh_e;
+    gam = sqrt(1.0 + utmp[0] * utmp[0] + utmp[1] * utmp[1] + utmp[2] * utmp[2] + gam_corr);
+    qtmh_b = qtmh / (gam - utmp[2]);
+    for (int c = 0; c < 3; ++c) bp[c] = bp[c] * qtmh_b;
+  } else {
+    qtmh_b = qtmh / (1.0 - qbm * psi[pp]);
+    qtmh_e = qtmh_b * gam;
+    for (int c = 0; c < 3; ++c) utmp[c] = u0[c] + ep[c] * qtmh_e;
+    for (int c = 0; c < 3; ++c) bp[c] = bp[c] * qtmh_b;
+  }
+  u[0] = utmp[0] + utmp[1] * bp[2] - utmp[2] * bp[1];
+  u[1] = utmp[1] + utmp[2] * bp[0] - utmp[0] * bp[2];
+  u[2] = utmp[2] + utmp[0] * bp[1] - utmp[1] * bp[0];
+  const double ostq = 2.0 / (1.0 + bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2]);
+  for (int c = 0; c < 3; ++c) bp[c] = bp[c] * ostq;
+  {
+    double t0 = utmp[0] + u[1] * bp[2] - u[2] * bp[1];
+    double t1 = utmp[1] + u[2] * bp[0] - u[0] * bp[2];
+    double t2 = utmp[2] + u[0] * bp[1] - u[1] * bp[0];
+    utmp[0] = t0; utmp[1] = t1; utmp[2] = t2;
+  }
+  gam = sqrt(1.0 + utmp[0] * utmp[0] + utmp[1] * utmp[1] + utmp[2] * utmp[2] + gam_corr);
+  qtmh_e = push_type == ORC_PUSH_ROBUST_PGC ? qtmh * gam / (gam - utmp[2]) : qtmh_b * gam;
+  for (int c = 0; c < 3; ++c) u[c] = utmp[c] + ep[c] * qtmh_e;
+  du[0] = idt * (u[0] - u0[0]);
+  du[1] = idt * (u[1] - u0[1]);
+  for (int c = 0; c < 3; ++c) u[c] = 0.5 * (u[c] + u0[c]);
+  gamma[pp] = sqrt(1.0 + u[0] * u[0] + u[1] * u[1] + u[2] * u[2] + gam_corr);
+  double ipsi;
+  if (push_type == ORC_PUSH_ROBUST_PGC) {
+    ipsi = 1.0 / (gamma[pp] - u[2]);
+    psi[pp] = (1.0 - 1.0 / ipsi) / qbm;
+  } else {
+    ipsi = 1.0 / (1.0 - qbm * psi[pp]);
+  }
+  const double dpsi = qbm * (wp[2] - (wp[0] * u[0] + wp[1] * u[1]) * ipsi);
+  du[0] = du[0] + u[0] * dpsi * ipsi;
+  du[1] = du[1] + u[1] * dpsi * ipsi;
+  u2[0] = u[0] * u[0] * ipsi;
+  u2[1] = u[0] * u[1] * ipsi;
+  u2[2] = u[1] * u[1] * ipsi;
+  if (!II_OK(g, ii)) return;
+  const double ph0r = ii.pcos, ph0i = -ii.psin;
+  double phr = q[pp] * ipsi, phi = 0.0;
+  const double wj[2] = {ii.w0, ii.w1};
+  for (int j = 0; j < 2; ++j) {
+    int n = ii.idx + j;
+    double w = wj[j] * phr;
+    for (int c = 0; c < 3; ++c) F(cu, 3, 0, c, n) = F(cu, 3, 0, c, n) + w * u[c];
+    for (int c = 0; c < 2; ++c) F(dcu, 2, 0, c, n) = F(dcu, 2, 0, c, n) + w * du[c];
+    for (int c = 0; c < 3; ++c) F(amu, 3, 0, c, n) = F(amu, 3, 0, c, n) + w * u2[c];
+  }
+  for (int m = 1; m <= M; ++m) {
+    double t = phr * ph0r - phi * ph0i;
+    phi = phr * ph0i + phi * ph0r;
+    phr = t;
+    const int r = PRE(m), s = PIM(m);
+    for (int j = 0; j < 2; ++j) {
+      int n = ii.idx + j;
+      double w = wj[j] * phr;
+      for (int c = 0; c < 3; ++c) F(cu, 3, r, c, n) = F(cu, 3, r, c, n) + w * u[c];
+      for (int c = 0; c < 2; ++c) F(dcu, 2, r, c, n) = F(dcu, 2, r, c, n) + w * du[c];
+      for (int c = 0; c < 3; ++c) F(amu, 3, r, c, n) = F(amu, 3, r, c, n) + w * u2[c];
+      w = wj[j] * phi;
+      for (int c = 0; c < 3; ++c) F(cu, 3, s, c, n) = F(cu, 3, s, c, n) + w * u[c];
+      for (int c = 0; c < 2; ++c) F(dcu, 2, s, c, n) = F(dcu, 2, s, c, n) + w * du[c];
+      for (int c = 0; c < 3; ++c) F(amu, 3, s, c, n) = F(amu, 3, s, c, n) + w * u2[c];
+    }
+  }
+}
+
+void orc_amjdeposit_pgc(const orc_grid* g, int push_type, double qbm, double dt, int64_t np,
+                        const double* x, const double* y, const double* px, const double* py,
+                        const double* pz, const double* q, double* gamma, double* psi, const double* ef,
+                        const double* bf, const orc_laser_f1* lf, double* cu, double* amu, double* dcu) {
+  const double idt = 1.0 / dt, qtmh = 0.5 * qbm * dt, idr = 1.0 / g->dr;
+  for (int64_t pp = 0; pp < np; ++pp)
+    amj_one_pgc(g, push_type, qbm, qtmh, idt, idr, pp, x, y, px, py, pz, q, gamma, psi, ef, bf, lf, cu, amu, dcu);
+  amj_axis_scale(g, cu, amu, dcu);   /* the same finishing as the plain deposits */
+}
+
+void orc_push_u_pgc(const orc_grid* g, double qbm, double dt, int64_t np, const double* x, const double* y,
+                    double* px, double* py, double* pz, double* gamma, const double* psi, const double* ef,
+                    const double* bf, const orc_laser_f1* lf) {
+  const double qtmh = qbm * dt * 0.5, qbm2_hf = (qbm * qbm) * 0.5, idr = 1.0 / g->dr;
+  for (int64_t pp = 0; pp < np; ++pp) {
+    interp_info ii = gen_interp_info(x[pp], y[pp], idr);
+    double ep[3], bp[3], gr[3], gi[3], utmp[3], p[3];
+    interp_vec(g, ef, &ii, ep);
+    interp_vec(g, bf, &ii, bp);
+    const double apr = interp_scalar(g, lf->ar, &ii), api = interp_scalar(g, lf->ai, &ii);
+    interp_vec(g, lf->gr, &ii, gr);
+    interp_vec(g, lf->gi, &ii, gi);
+    double* vs[4] = {ep, bp, gr, gi};          /* transform_to_cartesian, interp_part2d.f03:155-171 */
+    for (int k = 0; k < 4; ++k) {
+      double t = vs[k][0] * ii.pcos - vs[k][1] * ii.psin;
+      vs[k][1] = vs[k][0] * ii.psin + vs[k][1] * ii.pcos;
+      vs[k][0] = t;
+    }
+    double gam_corr = qbm2_hf * (apr * apr + api * api);
+    double tmp = 0.5 * qbm / gamma[pp];
+    ep[0] = ep[0] - tmp * (apr * gr[0] + api * gi[0]);
+    ep[1] = ep[1] - tmp * (apr * gr[1] + api * gi[1]);
+    ep[2] = ep[2] + tmp * (apr * gr[2] + api * gi[2]);
+    const double qtmh_b = qtmh / (1.0 - qbm * psi[pp]);
+    const double qtmh_e = qtmh_b * gamma[pp];
+    p[0] = px[pp]; p[1] = py[pp]; p[2] = pz[pp];
+    for (int c = 0; c < 3; ++c) { ep[c] = ep[c] * qtmh_e; utmp[c] = p[c] + ep[c]; bp[c] = bp[c] * qtmh_b; }
+    p[0] = utmp[0] + utmp[1] * bp[2] - utmp[2] * bp[1];
+    p[1] = utmp[1] + utmp[2] * bp[0] - utmp[0] * bp[2];
+    p[2] = utmp[2] + utmp[0] * bp[1] - utmp[1] * bp[0];
+    const double ostq = 2.0 / (1.0 + bp[0] * bp[0] + bp[1] * bp[1] + bp[2] * bp[2]);
+    for (int c = 0; c < 3; ++c) bp[c] = bp[c] * ostq;
+    {
+      double t0 = utmp[0] + p[1] * bp[2] - p[2] * bp[1];
+      double t1 = utmp[1] + p[2] * bp[0] - p[0] * bp[2];
+      double t2 = utmp[2] + p[0] * bp[1] - p[1] * bp[0];
+      utmp[0] = t0; utmp[1] = t1; utmp[2] = t2;
+    }
+    for (int c = 0; c < 3; ++c) p[c] = utmp[c] + ep[c];
+    /* time-centred gamma for the position push: |a|^2 advanced by half a step in xi */
+    tmp = gr[2] * dt; gam_corr = gam_corr + qbm2_hf * (apr + 0.25 * tmp) * tmp;
+    tmp = gi[2] * dt; gam_corr = gam_corr + qbm2_hf * (api + 0.25 * tmp) * tmp;
+    px[pp] = p[0]; py[pp] = p[1]; pz[pp] = p[2];
+    gamma[pp] = sqrt(1.0 + p[0] * p[0] + p[1] * p[1] + p[2] * p[2] + gam_corr);
+  }
+}
+
+/* deposit_chi (part2d_class.f03:361-476): the plasma susceptibility -qbm q / (1 - qbm psi)
+ * of each particle into the modes of chi, then the axis rule (m = 0 node 1 times
+ * 12 ppc_r^2 / (1 + 2 ppc_r^2), get_deposit_ax_corr :2581-2586; m >= 1 node 1 zero) and
+ * 1/(i-1) on nodes 2..nr+1.  The finishing scales the whole array, so a second species
+ * finishes the first one's contribution again, as in the reference. */
+void orc_deposit_chi(const orc_grid* g, double qbm, int ppc_r, int64_t np, const double* x, const double* y,
+                     const double* q, const double* psi, double* chi) {
+  const int M = g->max_mode, nr = g->nr;
+  const double idr = 1.0 / g->dr;
+  for (int64_t pp = 0; pp < np; ++pp) {
+    double pos = sqrt(x[pp] * x[pp] + y[pp] * y[pp]) * idr;
+    const double p0r = x[pp] / pos * idr, p0i = -y[pp] / pos * idr;
+    if (!(pos >= 0.0 && pos < (double)nr)) continue;   /* beyond the outer edge: nothing */
+    const int nn0 = (int)floor(pos);
+    pos = pos - (double)nn0;
+    const int nn = nn0 + 1;
+    const double wt[2] = {1.0 - pos, pos};
+    double phr = -(qbm * q[pp] / (1.0 - qbm * psi[pp])), phi = 0.0;
+    for (int j = 0; j < 2; ++j) F(chi, 1, 0, 0, nn + j) = F(chi, 1, 0, 0, nn + j) + wt[j] * phr;
+    for (int m = 1; m <= M; ++m) {
+      const double t = phr * p0r - phi * p0i;
+      phi = phr * p0i + phi * p0r;
+      phr = t;
+      for (int j = 0; j < 2; ++j) {
+        F(chi, 1, PRE(m), 0, nn + j) = F(chi, 1, PRE(m), 0, nn + j) + wt[j] * phr;
+        F(chi, 1, PIM(m), 0, nn + j) = F(chi, 1, PIM(m), 0, nn + j) + wt[j] * phi;
+      }
+    }
+  }
+  const double corr = (12.0 * (double)(ppc_r * ppc_r)) / (1.0 + 2.0 * (double)(ppc_r * ppc_r));
+  for (int p = 0; p < nparts(g); ++p) {
+    F(chi, 1, p, 0, 0) = 0.0;
+    F(chi, 1, p, 0, 1) = p == 0 ? F(chi, 1, p, 0, 1) * corr : 0.0;
+    for (int j = 2; j <= nr + 1; ++j) F(chi, 1, p, 0, j) = F(chi, 1, p, 0, j) * (1.0 / (double)(j - 1));
+  }
+}
+
 void orc_push_x(int64_t np, double dt, double* x, double* y, const double* px, const double* py,
                 const double* pz, const double* gamma) {                  /* :2221-2262 */
   for (int64_t pp = 0; pp < np; ++pp) {
@@ -1310,6 +1511,12 @@ struct orc_sim {
   int64_t nb[4];
   double *bx[4], *by[4], *bz[4], *bpx[4], *bpy[4], *bpz[4], *bq[4];
   double *s_re, *s_im;
+  /* lasers */
+  double *lr2[4], *li2[4], *lsr[4], *lsi[4];   /* envelope stores, explicit right-hand sides */
+  double **lcoef[4];                           /* per mode: PCR tables */
+  double *lgr, *lgi;                           /* one laser's gradients of a slice */
+  double *la_r, *la_i, *la_gr, *la_gi;         /* all lasers' sum of a slice (laser_all) */
+  double *chi, *chi2;
 };
 
 static double* zalloc(size_t n) { return (double*)calloc(n ? n : 1, sizeof(double)); }
@@ -1350,6 +1557,29 @@ orc_sim* orc_sim_create(const orc_sim_desc* d) {
   }
   s->s_re = zalloc((size_t)g->nr);
   s->s_im = zalloc((size_t)g->nr);
+  if (d->nlasers > 0) {
+    const size_t nls = (size_t)(g->nz + 3) * s->n1;
+    const int n = 2 * g->nr;
+    int steps = 0;
+    while ((1 << steps) < n) ++steps;
+    double* A = zalloc(5 * (size_t)n);
+    for (int k = 0; k < d->nlasers; ++k) {
+      s->lr2[k] = zalloc(nls); s->li2[k] = zalloc(nls);
+      s->lsr[k] = zalloc(s->n2); s->lsi[k] = zalloc(s->n2);
+      s->lcoef[k] = (double**)calloc((size_t)g->max_mode + 1, sizeof(double*));
+      for (int m = 0; m <= g->max_mode; ++m) {
+        double* c = zalloc((4 * (size_t)steps + 1) * n);
+        orc_laser_matrix(g->nr, m, d->laser_k0[k], d->dt3d, g->dr, g->dxi, A, A + n, A + 2 * n, A + 3 * n, A + 4 * n);
+        orc_pcr_coef(n, A, A + n, A + 2 * n, A + 3 * n, A + 4 * n, c, c + (size_t)steps * n, c + 2 * (size_t)steps * n,
+                     c + 3 * (size_t)steps * n, c + 4 * (size_t)steps * n);
+        s->lcoef[k][m] = c;
+      }
+    }
+    free(A);
+    s->lgr = zalloc(3 * s->n1); s->lgi = zalloc(3 * s->n1);
+    s->la_r = zalloc(s->n1); s->la_i = zalloc(s->n1); s->la_gr = zalloc(3 * s->n1); s->la_gi = zalloc(3 * s->n1);
+    s->chi = zalloc(s->n1); s->chi2 = zalloc(s->n2);
+  }
   return s;
 }
 
@@ -1362,6 +1592,13 @@ void orc_sim_destroy(orc_sim* s) {
                    s->nq, s->ax, s->ay, s->aq, s->multi_ion, s->ion_old, s->rho_ion, s->rho_add, s->qneut,
                    s->cun, s->amun, s->acun};
   for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); ++i) free(all[i]);
+  for (int k = 0; k < s->d.nlasers; ++k) {
+    free(s->lr2[k]); free(s->li2[k]); free(s->lsr[k]); free(s->lsi[k]);
+    for (int m = 0; m <= s->d.g.max_mode; ++m) free(s->lcoef[k][m]);
+    free(s->lcoef[k]);
+  }
+  free(s->lgr); free(s->lgi); free(s->la_r); free(s->la_i); free(s->la_gr); free(s->la_gi);
+  free(s->chi); free(s->chi2);
   for (int k = 0; k < s->d.nbeams; ++k) {
     free(s->bx[k]); free(s->by[k]); free(s->bz[k]); free(s->bpx[k]); free(s->bpy[k]);
     free(s->bpz[k]); free(s->bq[k]);
@@ -1536,6 +1773,364 @@ static void neutral_update(orc_sim* s) {
   neutral_inject(s);
 }
 
+/* =============================================================================
+ * Laser envelope: field_laser_class.f03 (init_solver :269-391, set_rhs :393-635,
+ * set_grad :637-750, solve :752-927, gather :929-946) and the parallel cyclic
+ * reduction of its penta-diagonal systems (fpcr_penta_class.f03).
+ *
+ * Per laser the envelope a = a_r + i a_i is stored per xi slice like a 1-component field
+ * (parts: m = 0, Re m, Im m), slices -1..nz+1 (the two slices ahead of the box stay zero):
+ *   LS(f, j, p, i) = f[((j + 1) * P + p) * (nr + 2) + i].
+ * In the reference's names, cfr_re(m) / cfr_im(m) are parts Re m / Im m of a_r and
+ * cfi_re(m) / cfi_im(m) those of a_i.
+ * ============================================================================= */
+#define LS(f, j, p, i) ((f)[(((size_t)(j) + 1) * (size_t)P + (size_t)(p)) * (size_t)NR2 + (size_t)(i)])
+#define SL(f, j, p, i) ((f)[(((size_t)(j) - 1) * (size_t)P + (size_t)(p)) * (size_t)NR2 + (size_t)(i)])
+
+static inline int part_of(int m, int im) { return m == 0 ? 0 : (im ? PIM(m) : PRE(m)); }
+
+/* generate_cr_coef (fpcr_penta_class.f03:288-527) on one rank: rows 1..n (index i-1) of a
+ * penta-diagonal matrix, (a, b, c, d, e) multiplying x(i-2) .. x(i+2); steps = log2(n)
+ * reductions with strides 1, 2, 4, ...; rows outside 1..n read as (0, 1, 2, 1, 0).  Writes
+ * the coefficients cm1, cm2, cp1, cp2 [step][n] and the final diagonal cfin[n]. */
+void orc_pcr_coef(int n, const double* a_in, const double* b_in, const double* c_in, const double* d_in,
+                  const double* e_in, double* cm1, double* cm2, double* cp1, double* cp2, double* cfin) {
+  int steps = 0;
+  while ((1 << steps) < n) ++steps;
+  double* A = (double*)malloc(sizeof(double) * 10 * (size_t)n);
+  double *a = A, *b = A + n, *c = A + 2 * n, *d = A + 3 * n, *e = A + 4 * n;
+  double *na = A + 5 * n, *nb = A + 6 * n, *nc = A + 7 * n, *nd = A + 8 * n, *ne = A + 9 * n;
+  memcpy(a, a_in, sizeof(double) * n); memcpy(b, b_in, sizeof(double) * n); memcpy(c, c_in, sizeof(double) * n);
+  memcpy(d, d_in, sizeof(double) * n); memcpy(e, e_in, sizeof(double) * n);
+#define ROW(arr, k, pad) ((k) >= 1 && (k) <= n ? (arr)[(k) - 1] : (pad))
+  for (int s = 1; s <= steps; ++s) {
+    const int cs = 1 << (s - 1);
+    double* m1 = cm1 + (size_t)(s - 1) * n;
+    double* m2 = cm2 + (size_t)(s - 1) * n;
+    double* p1 = cp1 + (size_t)(s - 1) * n;
+    double* p2 = cp2 + (size_t)(s - 1) * n;
+    for (int i = 1; i <= n; ++i) {
+      const int im1 = i - cs, ip1 = i + cs, im2 = i - 2 * cs, ip2 = i + 2 * cs;
+      const double am1 = ROW(a, im1, 0.0), bm1 = ROW(b, im1, 1.0), cm1v = ROW(c, im1, 2.0), dm1 = ROW(d, im1, 1.0),
+                   em1 = ROW(e, im1, 0.0);
+      const double am2 = ROW(a, im2, 0.0), bm2 = ROW(b, im2, 1.0), cm2v = ROW(c, im2, 2.0), dm2 = ROW(d, im2, 1.0),
+                   em2 = ROW(e, im2, 0.0);
+      const double ap1 = ROW(a, ip1, 0.0), bp1 = ROW(b, ip1, 1.0), cp1v = ROW(c, ip1, 2.0), dp1 = ROW(d, ip1, 1.0),
+                   ep1 = ROW(e, ip1, 0.0);
+      const double ap2 = ROW(a, ip2, 0.0), bp2 = ROW(b, ip2, 1.0), cp2v = ROW(c, ip2, 2.0), dp2 = ROW(d, ip2, 1.0),
+                   ep2 = ROW(e, ip2, 0.0);
+      const double a0 = a[i - 1], b0 = b[i - 1], c0 = c[i - 1], d0 = d[i - 1], e0 = e[i - 1];
+      double tmp = am1 * cp1v * dm2 * dp2 - am1 * bp2 * dm2 * ep1 + ap1 * bm2 * dp2 * em1 + bm2 * bp2 * cm1v * ep1 -
+                   bm2 * cm1v * cp1v * dp2;
+      double km2 = 0.0, km1 = 0.0, kp1 = 0.0, kp2 = 0.0;
+      if (fabs(tmp) > 1e-40) {
+        tmp = 1.0 / tmp;
+        km2 = am1 * (ap1 * d0 * dp2 + b0 * bp2 * ep1 - b0 * cp1v * dp2) * tmp;
+        km1 = -(bm2 * (ap1 * d0 * dp2 + b0 * bp2 * ep1 - b0 * cp1v * dp2) * tmp);
+        kp1 = -(dp2 * (am1 * d0 * dm2 + b0 * bm2 * em1 - d0 * bm2 * cm1v) * tmp);
+        kp2 = ep1 * (am1 * d0 * dm2 + b0 * bm2 * em1 - d0 * bm2 * cm1v) * tmp;
+      }
+      m2[i - 1] = km2; m1[i - 1] = km1; p1[i - 1] = kp1; p2[i - 1] = kp2;
+      na[i - 1] = km2 * am2;
+      nb[i - 1] = km2 * cm2v + km1 * bm1 + a0;
+      nc[i - 1] = km2 * em2 + km1 * dm1 + c0 + kp1 * bp1 + kp2 * ap2;
+      nd[i - 1] = e0 + kp1 * dp1 + kp2 * cp2v;
+      ne[i - 1] = kp2 * ep2;
+    }
+    memcpy(a, na, sizeof(double) * n); memcpy(b, nb, sizeof(double) * n); memcpy(c, nc, sizeof(double) * n);
+    memcpy(d, nd, sizeof(double) * n); memcpy(e, ne, sizeof(double) * n);
+  }
+#undef ROW
+  memcpy(cfin, c, sizeof(double) * n);
+  free(A);
+}
+
+/* solve_fpcr_penta (:129-286) on one rank: rhs in, solution out (rows outside 1..n are 0) */
+void orc_pcr_solve(int n, const double* cm1, const double* cm2, const double* cp1, const double* cp2,
+                   const double* cfin, double* rhs) {
+  int steps = 0;
+  while ((1 << steps) < n) ++steps;
+  double* x = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int s = 1; s <= steps; ++s) {
+    const int cs = 1 << (s - 1);
+    const size_t o = (size_t)(s - 1) * n;
+    for (int i = 1; i <= n; ++i) {
+      const int im1 = i - cs, ip1 = i + cs, im2 = i - 2 * cs, ip2 = i + 2 * cs;
+      double v = rhs[i - 1];
+      v = v + cm1[o + i - 1] * (im1 >= 1 ? rhs[im1 - 1] : 0.0);
+      v = v + cm2[o + i - 1] * (im2 >= 1 ? rhs[im2 - 1] : 0.0);
+      v = v + cp1[o + i - 1] * (ip1 <= n ? rhs[ip1 - 1] : 0.0);
+      v = v + cp2[o + i - 1] * (ip2 <= n ? rhs[ip2 - 1] : 0.0);
+      x[i - 1] = v;
+    }
+    memcpy(rhs, x, sizeof(double) * n);
+  }
+  for (int i = 0; i < n; ++i) rhs[i] = rhs[i] / cfin[i];
+  free(x);
+}
+
+/* init_solver (field_laser_class.f03:269-391) on one rank: the 2 nr rows of mode m, rows
+ * 2i-1 / 2i for a_r / a_i at node i, with set_values_matrix_byrow's boundary entries
+ * (fpcr_penta_class.f03:570-595: a, b of row 1 and a of row 2, d, e of row n and e of row
+ * n-1 set to the machine epsilon). */
+void orc_laser_matrix(int nr, int m, double k0, double ds, double dr, double dz, double* a, double* b, double* c,
+                      double* d, double* e) {
+  const int n = 2 * nr;
+  const double eps = 2.220446049250313e-16;     /* epsilon(1.0) of the 8-byte default real */
+  const double ds_qtr = 0.25 * ds, dr2_idz_1hf = 1.5 * (dr * dr) / dz, kap = k0 * (dr * dr);
+  const double m2 = (double)(m * m);
+#define SETROW(r, A_, B_, C_, D_, E_)                       \
+  do {                                                      \
+    a[(r) - 1] = (A_); b[(r) - 1] = (B_); c[(r) - 1] = (C_); \
+    d[(r) - 1] = (D_); e[(r) - 1] = (E_);                  \
+    if ((r) == 1) { a[0] = eps; b[0] = eps; }               \
+    else if ((r) == 2) a[1] = eps;                          \
+    if ((r) == n) { e[n - 1] = eps; d[n - 1] = eps; }       \
+    else if ((r) == n - 1) e[n - 2] = eps;                  \
+  } while (0)
+  for (int i = 3; i <= n - 1; i += 2) {          /* node j + 1 = (i + 1) / 2; row pair 1-2 is the axis */
+    const int j = (i + 1) / 2 - 1;
+    const double j2 = (double)(j * j);
+    const double av = -(ds_qtr * (1.0 - 0.5 / (double)j));
+    const double cv = ds_qtr * (2.0 + m2 / j2) + dr2_idz_1hf;
+    const double ev = -(ds_qtr * (1.0 + 0.5 / (double)j));
+    SETROW(i, av, 0.0, cv, -kap, ev);
+    SETROW(i + 1, av, kap, cv, 0.0, ev);
+  }
+  if (m == 0) {
+    SETROW(1, 0.0, eps, ds + dr2_idz_1hf, -kap, -ds);
+    SETROW(2, eps, kap, ds + dr2_idz_1hf, 0.0, -ds);
+  } else {
+    SETROW(1, eps, eps, 1.0, eps, eps);
+    SETROW(2, eps, eps, 1.0, eps, eps);
+  }
+  {
+    const int j = nr - 1;
+    const double j2 = (double)(j * j);
+    const double av = -(ds_qtr * (1.0 - 0.5 / (double)j));
+    const double cv = ds_qtr * (2.0 + m2 / j2) + dr2_idz_1hf;
+    SETROW(n - 1, av, 0.0, cv, -kap, 0.0);
+    SETROW(n, av, kap, cv, 0.0, 0.0);
+  }
+#undef SETROW
+}
+
+/* the plasma-susceptibility coupling of mode m at node i and slice j (set_rhs :558-631,
+ * solve :795-862): t[0..3] += the terms of a_r Re, a_i Re, a_r Im, a_i Im */
+static void laser_chi_terms(const orc_grid* g, const double* chi2, const double* lr, const double* li, int j, int m,
+                            int i, double cq, double t[4]) {
+  const int M = g->max_mode, P = nparts(g);
+  for (int k = m - M; k <= M; ++k) {
+    const int ak = abs(k), amk = abs(m - k);
+    const double sg = (k >= 0 && k <= m) ? 1.0 : -1.0;
+    const double cr = SL(chi2, j, part_of(ak, 0), i);
+    t[0] = t[0] + cq * cr * LS(lr, j, part_of(amk, 0), i);
+    t[1] = t[1] + cq * cr * LS(li, j, part_of(amk, 0), i);
+    if (k == 0 || k == m) continue;
+    const double ci = SL(chi2, j, PIM(ak), i);
+    t[0] = t[0] - cq * sg * ci * LS(lr, j, PIM(amk), i);
+    t[1] = t[1] - cq * sg * ci * LS(li, j, PIM(amk), i);
+  }
+  if (m == 0) return;
+  for (int k = m - M; k <= M; ++k) {
+    const int ak = abs(k), amk = abs(m - k);
+    if (k != 0) {
+      const double sg = k < 0 ? -1.0 : 1.0;
+      const double ci = SL(chi2, j, PIM(ak), i);
+      t[2] = t[2] + cq * sg * ci * LS(lr, j, part_of(amk, 0), i);
+      t[3] = t[3] + cq * sg * ci * LS(li, j, part_of(amk, 0), i);
+    }
+    if (k != m) {
+      const double sg = k > m ? -1.0 : 1.0;
+      const double cr = SL(chi2, j, part_of(ak, 0), i);
+      t[2] = t[2] + cq * sg * cr * LS(lr, j, PIM(amk), i);
+      t[3] = t[3] + cq * sg * cr * LS(li, j, PIM(amk), i);
+    }
+  }
+}
+
+/* set_rhs (:393-635): for every slice the explicit half of the envelope equation from the
+ * envelope before the step, plus the susceptibility coupling.  sr / si like chi2 (slices 1..nz). */
+void orc_laser_rhs(const orc_grid* g, double k0, double ds, const double* chi2, const double* lr, const double* li,
+                   double* sr, double* si) {
+  const int M = g->max_mode, P = nparts(g), nr = g->nr;
+  const double dr = g->dr, dz = g->dxi;
+  const double dr2_idzh = 0.5 * (dr * dr) / dz, kap = k0 * (dr * dr), ds_qtr = 0.25 * ds,
+               cq = ds_qtr * (dr * dr);
+  for (int j = 1; j <= g->nz; ++j)
+    for (int m = 0; m <= M; ++m) {
+      const double m2 = (double)(m * m);
+      for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
+        const int p = part_of(m, h);
+        for (int i = 1; i <= nr; ++i) {
+          double bm, bp, al;
+          if (i == 1) {
+            if (m > 0) { SL(sr, j, p, i) = 0.0; SL(si, j, p, i) = 0.0; continue; }
+            bm = 0.0; bp = ds; al = -ds;
+          } else {
+            const double ik = 1.0 / (double)(i - 1);
+            bm = ds_qtr * (1.0 - 0.5 * ik);
+            bp = i == nr ? 0.0 : ds_qtr * (1.0 + 0.5 * ik);
+            al = m == 0 ? -ds_qtr * 2.0 : -(ds_qtr * (2.0 + m2 * ik * ik));
+          }
+          SL(sr, j, p, i) = dr2_idzh * (3.0 * LS(lr, j, p, i) - 4.0 * LS(lr, j - 1, p, i) + LS(lr, j - 2, p, i)) -
+                            kap * LS(li, j, p, i) + bm * LS(lr, j, p, i - 1) + al * LS(lr, j, p, i) +
+                            bp * LS(lr, j, p, i + 1);
+          SL(si, j, p, i) = dr2_idzh * (3.0 * LS(li, j, p, i) - 4.0 * LS(li, j - 1, p, i) + LS(li, j - 2, p, i)) +
+                            kap * LS(lr, j, p, i) + bm * LS(li, j, p, i - 1) + al * LS(li, j, p, i) +
+                            bp * LS(li, j, p, i + 1);
+        }
+      }
+      for (int i = 1; i <= nr; ++i) {
+        double t[4] = {SL(sr, j, part_of(m, 0), i), SL(si, j, part_of(m, 0), i), 0.0, 0.0};
+        if (m > 0) { t[2] = SL(sr, j, PIM(m), i); t[3] = SL(si, j, PIM(m), i); }
+        laser_chi_terms(g, chi2, lr, li, j, m, i, cq, t);
+        SL(sr, j, part_of(m, 0), i) = t[0];
+        SL(si, j, part_of(m, 0), i) = t[1];
+        if (m > 0) { SL(sr, j, PIM(m), i) = t[2]; SL(si, j, PIM(m), i) = t[3]; }
+      }
+    }
+}
+
+/* solve (:752-927): slice by slice from the front of the box, `iter` times each, the
+ * implicit half: coupling with the current envelope, then one penta-diagonal solve per mode
+ * and Re / Im part; m >= 1 axis values zero.  coef: per mode m the PCR tables
+ * [cm1 | cm2 | cp1 | cp2 ([steps][2nr] each) | cfin (2nr)]. */
+void orc_laser_solve(const orc_grid* g, int iter, double ds, const double* const* coef, const double* chi2,
+                     const double* sr, const double* si, double* lr, double* li) {
+  const int M = g->max_mode, P = nparts(g), nr = g->nr, n = 2 * nr;
+  int steps = 0;
+  while ((1 << steps) < n) ++steps;
+  const double dr = g->dr, dz = g->dxi;
+  const double dr2_idzh = 0.5 * (dr * dr) / dz, cq = 0.25 * ds * (dr * dr);
+  double* t = (double*)malloc(sizeof(double) * 4 * (size_t)(M + 1) * nr);
+  double* x = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int j = 1; j <= g->nz; ++j)
+    for (int l = 1; l <= iter; ++l) {
+      for (int m = 0; m <= M; ++m)
+        for (int i = 1; i <= nr; ++i) {
+          double* tt = t + 4 * ((size_t)m * nr + (i - 1));
+          tt[0] = tt[1] = tt[2] = tt[3] = 0.0;
+          laser_chi_terms(g, chi2, lr, li, j, m, i, cq, tt);
+        }
+      for (int m = 0; m <= M; ++m) {
+        const double* cm1 = coef[m];
+        const double* cm2 = cm1 + (size_t)steps * n;
+        const double* cp1 = cm2 + (size_t)steps * n;
+        const double* cp2 = cp1 + (size_t)steps * n;
+        const double* cf = cp2 + (size_t)steps * n;
+        for (int h = 0; h < (m == 0 ? 1 : 2); ++h) {
+          const int p = part_of(m, h);
+          for (int i = 1; i <= nr; ++i) {
+            const double* tt = t + 4 * ((size_t)m * nr + (i - 1));
+            x[2 * i - 2] = SL(sr, j, p, i) + tt[2 * h] + dr2_idzh * (4.0 * LS(lr, j - 1, p, i) - LS(lr, j - 2, p, i));
+            x[2 * i - 1] = SL(si, j, p, i) + tt[2 * h + 1] + dr2_idzh * (4.0 * LS(li, j - 1, p, i) - LS(li, j - 2, p, i));
+          }
+          orc_pcr_solve(n, cm1, cm2, cp1, cp2, cf, x);
+          for (int i = 1; i <= nr; ++i) {
+            LS(lr, j, p, i) = x[2 * i - 2];
+            LS(li, j, p, i) = x[2 * i - 1];
+          }
+        }
+        if (m > 0) {
+          LS(lr, j, PRE(m), 1) = 0.0; LS(li, j, PRE(m), 1) = 0.0;
+          LS(lr, j, PIM(m), 1) = 0.0; LS(li, j, PIM(m), 1) = 0.0;
+        }
+      }
+    }
+  free(t);
+  free(x);
+}
+
+/* set_grad (:637-750) for slice j: gradients [P][3][nr+2] (r, phi, xi) of a_r (gr) and a_i
+ * (gi), every other entry zero (as left by the zeroing at the 3D step start).  For m >= 1 the
+ * reference's axis branch runs with the loop index left at nr + 1 after its loop, so it
+ * writes the upper guard node, not node 1 (node 1 keeps r and phi components zero);
+ * kept for identical results. */
+void orc_laser_grad(const orc_grid* g, const double* lr, const double* li, int j, double* gr, double* gi) {
+  const int M = g->max_mode, P = nparts(g), nr = g->nr;
+  const double idrh = 0.5 / g->dr, idzh = 0.5 / g->dxi;
+  memset(gr, 0, sizeof(double) * 3 * (size_t)P * NR2);
+  memset(gi, 0, sizeof(double) * 3 * (size_t)P * NR2);
+  const double* src[2] = {lr, li};
+  double* dst[2] = {gr, gi};
+  for (int h = 0; h < 2; ++h) {
+    const double* a = src[h];
+    double* gg = dst[h];
+    for (int p = 0; p < P; ++p)
+      for (int i = 1; i <= nr; ++i)
+        F(gg, 3, p, 2, i) = idzh * (3.0 * LS(a, j, p, i) - 4.0 * LS(a, j - 1, p, i) + LS(a, j - 2, p, i));
+    for (int i = 2; i <= nr; ++i) {
+      F(gg, 3, 0, 0, i) = idrh * (LS(a, j, 0, i + 1) - LS(a, j, 0, i - 1));
+      F(gg, 3, 0, 1, i) = 0.0;
+    }
+    for (int m = 1; m <= M; ++m) {
+      const int pr = PRE(m), pi = PIM(m);
+      for (int i = 2; i <= nr; ++i) {
+        const double ir = 1.0 / ((double)(i - 1) * g->dr);
+        F(gg, 3, pr, 0, i) = idrh * (LS(a, j, pr, i + 1) - LS(a, j, pr, i - 1));
+        F(gg, 3, pi, 0, i) = idrh * (LS(a, j, pi, i + 1) - LS(a, j, pi, i - 1));
+        F(gg, 3, pr, 1, i) = -ir * (double)m * LS(a, j, pi, i);
+        F(gg, 3, pi, 1, i) = ir * (double)m * LS(a, j, pr, i);
+      }
+      const int ig = nr + 1;
+      if (m % 2 == 1) {
+        F(gg, 3, pr, 0, ig) = 2.0 * idrh * LS(a, j, pr, 2);
+        F(gg, 3, pi, 0, ig) = 2.0 * idrh * LS(a, j, pi, 2);
+        F(gg, 3, pr, 1, ig) = -((double)m * F(gg, 3, pi, 0, ig));
+        F(gg, 3, pi, 1, ig) = (double)m * F(gg, 3, pr, 0, ig);
+      }
+    }
+  }
+}
+
+void orc_sim_set_laser(orc_sim* s, int k, const double* ar, const double* ai) {
+  const orc_grid* g = &s->d.g;
+  const int P = s->P, nr = g->nr;
+  for (int j = 1; j <= g->nz; ++j)
+    for (int p = 0; p < P; ++p)
+      for (int i = 1; i <= nr; ++i) {
+        const size_t o = ((size_t)(j - 1) * P + p) * nr + (i - 1);
+        LS(s->lr2[k], j, p, i) = ar[o];
+        LS(s->li2[k], j, p, i) = ai[o];
+      }
+}
+
+void orc_sim_laser(orc_sim* s, int k, double** ar, double** ai) { *ar = s->lr2[k]; *ai = s->li2[k]; }
+
+/* :362-367 laser_all = sum over the lasers of slice j's envelope (copy_slice) and gradients (set_grad) */
+static void lasers_slice(orc_sim* s, int j) {
+  const orc_grid* g = &s->d.g;
+  const int P = s->P;
+  const size_t n1 = s->n1;
+  memset(s->la_r, 0, n1 * sizeof(double)); memset(s->la_i, 0, n1 * sizeof(double));
+  memset(s->la_gr, 0, 3 * n1 * sizeof(double)); memset(s->la_gi, 0, 3 * n1 * sizeof(double));
+  for (int k = 0; k < s->d.nlasers; ++k) {
+    orc_laser_grad(g, s->lr2[k], s->li2[k], j, s->lgr, s->lgi);
+    for (int p = 0; p < P; ++p)
+      for (int i = 0; i < NR2; ++i) {
+        F(s->la_r, 1, p, 0, i) = F(s->la_r, 1, p, 0, i) + LS(s->lr2[k], j, p, i);
+        F(s->la_i, 1, p, 0, i) = F(s->la_i, 1, p, 0, i) + LS(s->li2[k], j, p, i);
+      }
+    for (size_t i = 0; i < 3 * n1; ++i) {
+      s->la_gr[i] = s->la_gr[i] + s->lgr[i];
+      s->la_gi[i] = s->la_gi[i] + s->lgi[i];
+    }
+  }
+}
+
+/* :485-486 lasers%advance (sim_lasers_class.f03:202-223): set_rhs, then solve */
+static void lasers_advance(orc_sim* s) {
+  const orc_grid* g = &s->d.g;
+  for (int k = 0; k < s->d.nlasers; ++k) {
+    orc_laser_rhs(g, s->d.laser_k0[k], s->d.dt3d, s->chi2, s->lr2[k], s->li2[k], s->lsr[k], s->lsi[k]);
+    orc_laser_solve(g, s->d.laser_iter[k], s->d.dt3d, (const double* const*)s->lcoef[k], s->chi2, s->lsr[k],
+                    s->lsi[k], s->lr2[k], s->li2[k]);
+  }
+}
+
+static int is_pgc(int push_type) { return push_type == ORC_PUSH_STD_PGC || push_type == ORC_PUSH_ROBUST_PGC; }
+
 /* one xi slice j: simulation_class.f03:342-469 */
 void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
   const orc_grid* g = &s->d.g;
@@ -1581,8 +2176,11 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
     }
     /* :356-360 */
     orc_solve_psi(g, s->q_spe, s->psi);
-    if (s->d.sp_push_type == ORC_PUSH_STD) orc_interp_psi(g, s->np, s->x, s->y, s->psi, s->ppsi);
+    if (s->d.sp_push_type == ORC_PUSH_STD || s->d.sp_push_type == ORC_PUSH_STD_PGC)
+      orc_interp_psi(g, s->np, s->x, s->y, s->psi, s->ppsi);
     orc_solve_bz(g, s->cu, s->b_spe);
+    if (s->d.nlasers > 0) lasers_slice(s, j);
+    const orc_laser_f1 lf = {s->la_r, s->la_i, s->la_gr, s->la_gi};
     /* :370-398 predictor-corrector */
     int l;
     double rel_res = 0.0, abs_res = 0.0;
@@ -1594,8 +2192,12 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
       memset(s->cu, 0, 3 * n1 * sizeof(double));
       memset(s->acu, 0, 2 * n1 * sizeof(double));
       memset(s->amu, 0, 3 * n1 * sizeof(double));
-      orc_amjdeposit(g, s->d.sp_push_type, s->d.sp_qbm, dxi, s->np, s->x, s->y, s->px, s->py, s->pz,
-                     s->q, s->gamma, s->ppsi, s->e, s->b, s->cu, s->amu, s->acu, nt);
+      if (is_pgc(s->d.sp_push_type))
+        orc_amjdeposit_pgc(g, s->d.sp_push_type, s->d.sp_qbm, dxi, s->np, s->x, s->y, s->px, s->py, s->pz,
+                           s->q, s->gamma, s->ppsi, s->e, s->b, &lf, s->cu, s->amu, s->acu);
+      else
+        orc_amjdeposit(g, s->d.sp_push_type, s->d.sp_qbm, dxi, s->np, s->x, s->y, s->px, s->py, s->pz,
+                       s->q, s->gamma, s->ppsi, s->e, s->b, s->cu, s->amu, s->acu, nt);
       for (int k = 0; k < s->d.smooth_order; ++k) {      /* cu, dcu, amu %smooth(), :270-272 */
         orc_smooth(g, 1, s->cu);
         orc_smooth(g, 2, s->acu);
@@ -1618,6 +2220,12 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
     }
     if (iters) *iters = l > s->d.iter_max ? s->d.iter_max : l;
     if (rel) *rel = rel_res;
+    /* :400-401 lasers%deposit_chi (sim_lasers_class.f03:176-200): chi of slice j into its store */
+    if (s->d.nlasers > 0) {
+      memset(s->chi, 0, n1 * sizeof(double));
+      orc_deposit_chi(g, s->d.sp_qbm, s->d.sp_ppc_r, s->np, s->x, s->y, s->q, s->ppsi, s->chi);
+      memcpy(s->chi2 + (size_t)(j - 1) * n1, s->chi, n1 * sizeof(double));
+    }
     /* :403-416 cbq, stores */
     copy_1to2(s, s->cu, s->cu2, 3, j);
     for (int i = 0; i < NR2 * s->P; ++i) {
@@ -1635,8 +2243,11 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
       for (int c = 0; c < 2; ++c)
         for (int n = 0; n < NR2; ++n) F(s->cu, 3, p, c, n) = F(s->cu, 3, p, c, n) + F(s->dcu, 2, p, c, n);
     /* :437-441 push_u, push_x (+update_bound) */
-    orc_push_u(g, s->d.sp_push_type, s->d.sp_qbm, dxi, s->np, s->x, s->y, s->px, s->py, s->pz,
-               s->gamma, s->ppsi, s->e, s->b, nt);
+    if (is_pgc(s->d.sp_push_type))
+      orc_push_u_pgc(g, s->d.sp_qbm, dxi, s->np, s->x, s->y, s->px, s->py, s->pz, s->gamma, s->ppsi, s->e, s->b, &lf);
+    else
+      orc_push_u(g, s->d.sp_push_type, s->d.sp_qbm, dxi, s->np, s->x, s->y, s->px, s->py, s->pz,
+                 s->gamma, s->ppsi, s->e, s->b, nt);
     orc_push_x(s->np, dxi, s->x, s->y, s->px, s->py, s->pz, s->gamma);
     s->np = orc_update_bound(g, s->np, s->x, s->y, s->px, s->py, s->pz, s->gamma, s->ppsi, s->q);
     if (s->d.neut_levels > 0) {                        /* :443-449 neut%update, push_u, push_x */
@@ -1659,6 +2270,7 @@ void orc_sim_slice(orc_sim* s, int j, int* iters, double* rel) {
 void orc_sim_end_3dstep(orc_sim* s, int push_beams) {
   const orc_grid* g = &s->d.g;
   const int nt = s->d.nthreads;
+  if (s->d.nlasers > 0) lasers_advance(s);
   if (push_beams) {
     for (int k = 0; k < s->d.nbeams; ++k) {
       orc_beam_push(g, s->d.beam_push_type[k], s->d.beam_qbm[k], s->d.dt3d, s->nb[k], s->bx[k], s->by[k],
@@ -1689,7 +2301,7 @@ double* orc_sim_field(orc_sim* s, const char* name, int* nc) {
 double* orc_sim_store(orc_sim* s, const char* name, int* nc) {
   struct { const char* n; double* p; int c; } t[] = {
       {"q_beam", s->q_beam2, 1}, {"e", s->e2, 3}, {"b", s->b2, 3}, {"psi", s->psi2, 1},
-      {"b_spe", s->b_spe2, 3}, {"e_spe", s->e_spe2, 3}, {"cu", s->cu2, 3}, {"q_spe", s->q_spe2, 1}};
+      {"b_spe", s->b_spe2, 3}, {"e_spe", s->e_spe2, 3}, {"cu", s->cu2, 3}, {"q_spe", s->q_spe2, 1}, {"chi", s->chi2, 1}};
   for (size_t i = 0; i < sizeof(t) / sizeof(t[0]); ++i)
     if (!strcmp(t[i].n, name)) { if (nc) *nc = t[i].c; return t[i].p; }
   return NULL;

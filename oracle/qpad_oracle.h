@@ -38,7 +38,7 @@ extern "C" {
 enum { ORC_BND_ZERO = 2, ORC_BND_OPEN = 3 };                  /* param.f03:72-74 */
 enum { ORC_FK_PSI = 0, ORC_FK_EZ = 1, ORC_FK_BZ = 2, ORC_FK_BT = 3,
        ORC_FK_BPLUS = 4, ORC_FK_BMINUS = 5 };                   /* param.f03:76-84 */
-enum { ORC_PUSH_STD = 0, ORC_PUSH_ROBUST = 1 };                 /* param.f03:63-64 */
+enum { ORC_PUSH_STD = 0, ORC_PUSH_ROBUST = 1, ORC_PUSH_STD_PGC = 4, ORC_PUSH_ROBUST_PGC = 5 };  /* param.f03:63-64 */
 enum { ORC_PUSH3_REDUCED = 1, ORC_PUSH3_BORIS = 2 };            /* param.f03:62 */
 
 typedef struct orc_grid {
@@ -77,6 +77,26 @@ void orc_amjdeposit(const orc_grid* g, int push_type, double qbm, double dt, int
                     const double* pz, const double* q, double* gamma, double* psi,
                     const double* ef, const double* bf, double* cu, double* amu,
                     double* dcu, int nthreads);                                  /* :478-1010 */
+/* a laser envelope's slice fields as the PGC pushers gather them: a_r, a_i ([P][nr+2]) and
+ * their gradients ([P][3][nr+2], r / phi / xi) */
+typedef struct orc_laser_f1 { const double *ar, *ai, *gr, *gi; } orc_laser_f1;
+void orc_amjdeposit_pgc(const orc_grid* g, int push_type, double qbm, double dt, int64_t np,
+                        const double* x, const double* y, const double* px, const double* py,
+                        const double* pz, const double* q, double* gamma, double* psi, const double* ef,
+                        const double* bf, const orc_laser_f1* lf, double* cu, double* amu, double* dcu);
+void orc_push_u_pgc(const orc_grid* g, double qbm, double dt, int64_t np, const double* x, const double* y,
+                    double* px, double* py, double* pz, double* gamma, const double* psi, const double* ef,
+                    const double* bf, const orc_laser_f1* lf);
+void orc_deposit_chi(const orc_grid* g, double qbm, int ppc_r, int64_t np, const double* x, const double* y,
+                     const double* q, const double* psi, double* chi);
+/* ---- laser envelope (laser/field_laser_class.f03) and its PCR penta-diagonal solver -- */
+void orc_pcr_coef(int n, const double* a, const double* b, const double* c, const double* d, const double* e,
+                  double* cm1, double* cm2, double* cp1, double* cp2, double* cfin);
+void orc_pcr_solve(int n, const double* cm1, const double* cm2, const double* cp1, const double* cp2,
+                   const double* cfin, double* rhs);
+void orc_laser_matrix(int nr, int m, double k0, double ds, double dr, double dz, double* a, double* b, double* c,
+                      double* d, double* e);
+void orc_laser_grad(const orc_grid* g, const double* lr, const double* li, int j, double* gr, double* gi);
 void orc_push_u(const orc_grid* g, int push_type, double qbm, double dt, int64_t np,
                 const double* x, const double* y, double* px, double* py, double* pz,
                 double* gamma, const double* psi, const double* ef, const double* bf,
@@ -146,6 +166,12 @@ typedef struct orc_sim_desc {
   double neut_qm, neut_qbm;    /* charge and charge-to-mass ratio of the ionised electrons */
   int neut_push_type;
   int64_t neut_npmax;
+  /* laser envelopes (field_laser_class.f03), none when nlasers = 0; the initial envelopes
+     come from orc_sim_set_laser.  nr must be a power of two (the PCR solver's size 2 nr). */
+  int nlasers;
+  double laser_k0[4];          /* central wavenumber */
+  int laser_iter[4];           /* implicit iterations per slice of the envelope advance */
+  int sp_ppc_r;                /* the species' radial particles per cell (chi's axis factor) */
 } orc_sim_desc;
 
 /* One binomial (1,2,1) smoothing pass of a deposit field (ufield::smooth_f1,
@@ -180,6 +206,10 @@ int64_t orc_sim_plasma(orc_sim* s, double** x, double** y, double** px, double**
 int64_t orc_sim_neutral(orc_sim* s, double** x, double** y, double** px, double** py, double** pz,
                         double** gamma, double** psi, double** q);
 double* orc_sim_multi_ion(orc_sim* s);
+/* laser k's envelope initial values: ar, ai [nz][P][nr] (nodes 1..nr) */
+void orc_sim_set_laser(orc_sim* s, int k, const double* ar, const double* ai);
+/* laser k's envelope store, slices -1..nz+1: [(nz + 3)][P][nr + 2] */
+void orc_sim_laser(orc_sim* s, int k, double** ar, double** ai);
 int64_t orc_sim_beam(orc_sim* s, int k, double** x, double** y, double** z, double** px,
                      double** py, double** pz, double** q);
 

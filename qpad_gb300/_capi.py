@@ -42,6 +42,10 @@ class TuneResult(C.Structure):
                 ("deposit_us", C.c_double)]
 
 
+class LaserDesc(C.Structure):
+    _fields_ = [("k0", C.c_double), ("iter", C.c_int32)]
+
+
 class NeutralDesc(C.Structure):
     _fields_ = [("qm", C.c_double), ("qbm", C.c_double), ("push_type", C.c_int32), ("levels", C.c_int32),
                 ("adk", D), ("wp", C.c_double), ("density", C.c_double), ("ppc1", C.c_int32),
@@ -70,6 +74,7 @@ class BeamLoadDesc(C.Structure):
 OK, E_ARG, E_CUDA, E_NOMEM, E_CAPACITY, E_STATE = range(6)
 BND_ZERO, BND_OPEN = 2, 3
 PUSH2_STD, PUSH2_ROBUST = 0, 1
+PUSH2_STD_PGC, PUSH2_ROBUST_PGC = 4, 5
 PUSH3_REDUCED, PUSH3_BORIS = 1, 2
 COPY_1TO2, COPY_2TO1 = 1, -1
 PREC_FP64, PREC_MIXED = 0, 1
@@ -151,6 +156,11 @@ _SIGS = {
     "qpad_h5_last_error": (C.c_char_p, []),
     "qpad_neutral_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "qpad_neutral_state_download": (C.c_int, [C.c_void_p, D]),
+    "qpad_laser_create": (C.c_int, [C.c_void_p, C.c_void_p, D, D, C.POINTER(C.c_void_p)]),
+    "qpad_laser_download": (C.c_int, [C.c_void_p, D, D]),
+    "qpad_laser_chi_download": (C.c_int, [C.c_void_p, D]),
+    "qpad_lasers_advance": (C.c_int, [C.c_void_p]),
+    "qpad_species_set_radial_ppc": (C.c_int, [C.c_void_p, C.c_int32]),
     "qpad_h5_write_grid": (C.c_int, [C.c_char_p, C.c_char_p, D, C.c_int, C.c_int, C.c_void_p]),
     "qpad_h5_write_particles": (C.c_int, [C.c_char_p, C.c_char_p, D, D, D, C.c_int64, C.c_int, C.c_double,
                                           C.c_double]),

@@ -138,6 +138,21 @@ class SliceStats:
     abs_res: float
 
 
+class Laser:
+    """A laser envelope on the device (advanced by every 3D step)."""
+
+    def __init__(self, sim, h):
+        self.sim, self.h = sim, h
+
+    def download(self):
+        """(a_r, a_i), each [nz][P][nr + 2] over slices 1..nz."""
+        s = self.sim
+        ar = np.zeros((s.nz, s.P, s.nr + 2))
+        ai = np.zeros((s.nz, s.P, s.nr + 2))
+        s._check(s.lib.qpad_laser_download(self.h, _dp(ar), _dp(ai)))
+        return ar, ai
+
+
 class Simulation:
     """Context: grid + field set + species + beams on one GPU (one CUDA stream)."""
 
@@ -157,6 +172,7 @@ class Simulation:
         self.fields = {n: Field(self, n) for n in K.FIELDS}
         self.species: list[Species2D] = []
         self.beams: list[Beam3D] = []
+        self.lasers: list[Laser] = []
 
     def __getattr__(self, name):
         f = self.__dict__.get("fields")
@@ -187,11 +203,33 @@ class Simulation:
         self._check(self.lib.qpad_synchronize(self.h))
 
     def add_species(self, x, p, gamma, psi, q, *, qbm=-1.0, push_type=K.PUSH2_ROBUST, neutralized=True,
-                    npmax=None, sort_freq=0) -> "Species2D":
+                    npmax=None, sort_freq=0, ppc_r=None) -> "Species2D":
+        """A plasma species from particle arrays; push_type PUSH2_*_PGC makes it see the lasers,
+        ppc_r (its radial particles per cell) sets the on-axis factor of its susceptibility."""
         sp = Species2D(self, x, p, gamma, psi, q, qbm=qbm, push_type=push_type, neutralized=neutralized,
                        npmax=npmax, sort_freq=sort_freq)
         self.species.append(sp)
+        if ppc_r is not None:
+            self._check(self.lib.qpad_species_set_radial_ppc(sp.h, int(ppc_r)))
         return sp
+
+    def add_laser(self, ar, ai, *, k0, iteration=1) -> "Laser":
+        """A laser envelope (field_laser_class.f03) from its initial a_r, a_i [nz][P][nr]
+        (qpad_gb300.lasers.launch evaluates the reference's profiles)."""
+        ar = np.ascontiguousarray(ar, np.float64).reshape(self.nz, self.P, self.nr)
+        ai = np.ascontiguousarray(ai, np.float64).reshape(self.nz, self.P, self.nr)
+        d = K.LaserDesc(float(k0), int(iteration))
+        h = C.c_void_p()
+        self._check(self.lib.qpad_laser_create(self.h, C.byref(d), _dp(ar), _dp(ai), C.byref(h)))
+        lz = Laser(self, h)
+        self.lasers.append(lz)
+        return lz
+
+    def chi_store(self) -> np.ndarray:
+        """The plasma susceptibility of the last 3D step, [nz][P][nr + 2]."""
+        out = np.zeros((self.nz, self.P, self.nr + 2))
+        self._check(self.lib.qpad_laser_chi_download(self.h, _dp(out)))
+        return out
 
     def add_neutral(self, adk, *, wp, density, ppc=(2, 1), num_theta=8, qm=-1.0, qbm=-1.0,
                     push_type=K.PUSH2_ROBUST, npmax=None) -> "Species2D":

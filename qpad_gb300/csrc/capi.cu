@@ -348,6 +348,7 @@ extern "C" int qpad_ctx_destroy(qpad_ctx* ctx) {
   if (ctx->qn) cudaFree(ctx->qn);
   if (ctx->qbg) cudaFree(ctx->qbg);
   if (ctx->d_neut_err) cudaFree(ctx->d_neut_err);
+  lasers_free(ctx);
   guess_free(ctx);
   if (ctx->qraw) cudaFree(ctx->qraw);
   if (ctx->raw) cudaFree(ctx->raw);
@@ -624,8 +625,13 @@ extern "C" int qpad_species_create(qpad_ctx* ctx, const qpad_species_desc* d, co
   if (!ctx || !d || !out) return QPAD_E_ARG;
   *out = nullptr;
   if (d->npmax < 1 || d->npmax > (int64_t)1 << 30 || np > d->npmax || np < 0 ||
-      (d->push_type != QPAD_PUSH2_STD && d->push_type != QPAD_PUSH2_ROBUST) || d->qbm == 0.0)
+      (d->push_type != QPAD_PUSH2_STD && d->push_type != QPAD_PUSH2_ROBUST && !is_pgc(d->push_type)) ||
+      d->qbm == 0.0)
     return set_err(ctx, QPAD_E_ARG, "invalid species descriptor");
+  if (is_pgc(d->push_type)) {
+    if (ctx->precision != QPAD_PREC_FP64) return set_err(ctx, QPAD_E_ARG, "PGC species: built on the FP64 path only");
+    if (int r = laser_state_ensure(ctx)) return r;   // (zero envelope until a laser is added)
+  }
   qpad_species* sp = new (std::nothrow) qpad_species();
   if (!sp) return set_err(ctx, QPAD_E_NOMEM, "species");
   sp->ctx = ctx;
@@ -1023,8 +1029,11 @@ int enqueue_slice_prologue(qpad_ctx* ctx, cudaGraphConditionalHandle hi, int use
   if (int r = launch_slice_begin(ctx, any_ntd || ctx->qbg != nullptr)) return r;
   // E of the first iteration (later iterations get theirs from k_iterate)
   if (int r = launch_iter_e(ctx)) return r;
+  // the lasers' envelope and gradients of this slice (simulation_class.f03:362-367)
+  if (int r = laser_slice_prologue(ctx)) return r;
   for (auto* s : ctx->species)
-    if (s->push_type == QPAD_PUSH2_STD && !s->neut)   // (the reference interpolates psi for species only)
+    if ((s->push_type == QPAD_PUSH2_STD || s->push_type == QPAD_PUSH2_STD_PGC) &&
+        !s->neut)   // (the reference interpolates psi for species only)
       if (int r = mixed ? mixed_interp_psi(s, ctx->f[QPAD_F_PSI]) : species_interp_psi(s, ctx->f[QPAD_F_PSI]))
         return r;
   // the convergence record of B_phi: in the graph the last iteration of the previous slice
@@ -1055,6 +1064,7 @@ int enqueue_iteration(qpad_ctx* ctx, cudaGraphConditionalHandle h, int use_h) {
 // Epilogue (simulation_class.f03:403-456): stores, final fields, J-perp predictor, push.
 int enqueue_slice_epilogue(qpad_ctx* ctx, int sort_now) {
   const bool mixed = ctx->precision == QPAD_PREC_MIXED;
+  if (int r = laser_deposit_chi(ctx)) return r;       // (simulation_class.f03:400-401)
   if (int r = launch_slice_end(ctx)) return r;
   if (int r = neutral_slice_update(ctx)) return r;   // ionisation and new electrons before the push
   for (auto* s : ctx->species) {
@@ -1184,7 +1194,8 @@ std::string step_key(const qpad_ctx* ctx) {
   std::string k = std::to_string(ctx->precision) + "/" + std::to_string(ctx->iter_cl) + "/" +
                   std::to_string(ctx->item_ppl) + "/" + std::to_string(ctx->guess != nullptr) + "/" +
                   std::to_string(ctx->extrap) + "/" + std::to_string(ctx->extrap_w) + "/" +
-                  std::to_string(ctx->pdl) + "/" + std::to_string(ctx->g.smooth);
+                  std::to_string(ctx->pdl) + "/" + std::to_string(ctx->g.smooth) + "/" +
+                  std::to_string(ctx->lasers.size());
   for (auto* s : ctx->species)
     k += "|" + std::to_string((long long)s->np) + ":" + std::to_string(s->push_type) + ":" +
          std::to_string(s->neutralized) + ":" + std::to_string(s->sort_freq);
@@ -1270,6 +1281,7 @@ int step_graph_stats(qpad_ctx* ctx, qpad_slice_stats* stats) {
 
 // 3D-step work after the slice loop (simulation_class.f03:487-492): beam push, counts.
 int step_end(qpad_ctx* ctx, int push_beams) {
+  if (int r = lasers_advance(ctx)) return r;          // (simulation_class.f03:485-486)
   if (push_beams)
     for (auto* b : ctx->beams)
       if (int r = beam_push(b, ctx->f2[QPAD_F_E], ctx->f2[QPAD_F_B])) return r;
@@ -1353,7 +1365,9 @@ extern "C" int qpad_batch_create(qpad_ctx* const* ctxs, int n, qpad_batch** out)
   if (!ctxs || n < 1 || !out) return QPAD_E_ARG;
   *out = nullptr;
   for (int i = 0; i < n; ++i)
-    if (!ctxs[i] || ctxs[i]->device != ctxs[0]->device || has_neutrals(ctxs[i])) return QPAD_E_ARG;
+    if (!ctxs[i] || ctxs[i]->device != ctxs[0]->device || has_neutrals(ctxs[i]) || !ctxs[i]->lasers.empty() ||
+        ctxs[i]->la)
+      return QPAD_E_ARG;   // (neutral gases and lasers run in single 3D steps only)
   qpad_batch* b = new (std::nothrow) qpad_batch();
   if (!b) return QPAD_E_NOMEM;
   b->ctxs.assign(ctxs, ctxs + n);

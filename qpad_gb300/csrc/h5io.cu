@@ -1,4 +1,4 @@
-// h5io.cpp -- the reference's diagnostic and restart files, written and read without an HDF5
+// h5io.cu -- the reference's diagnostic and restart files, written and read without an HDF5
 // library (none exists on these machines).
 //
 // The reference writes its field dumps and beam restart files through libhdf5 with default

@@ -286,6 +286,7 @@ extern "C" int qpad_neutral_create(qpad_ctx* ctx, const qpad_neutral_desc* d, qp
   *out = nullptr;
   if (ctx->precision != QPAD_PREC_FP64) return set_err(ctx, QPAD_E_ARG, "neutral gas: built on the FP64 path only");
   if (ctx->g.smooth != 0) return set_err(ctx, QPAD_E_ARG, "neutral gas: needs smooth_order 0");
+  if (is_pgc(d->push_type)) return set_err(ctx, QPAD_E_ARG, "neutral gas: the reference pushes its electrons without lasers");
   if (d->levels < 1 || d->levels > 16 || !d->adk || !(d->wp > 0.0) || !(d->density > 0.0) || d->ppc1 < 1 ||
       d->ppc2 < 1 || d->num_theta < 1 || d->npmax < 1 || d->qm == 0.0 || d->qbm == 0.0)
     return set_err(ctx, QPAD_E_ARG, "invalid neutral gas descriptor");

@@ -409,6 +409,7 @@ int species_amjdp_raw(qpad_species* sp, const double* ef, const double* bf, doub
                       double dt) {
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
+  if (is_pgc(sp->push_type)) return laser_amjdp_raw(sp, ef, bf, cu, amu, acu, dt);
   prof_begin(ctx, "amjdp");
   k_amjdp<<<grid_for(sp->np, kPartThreads), kPartThreads, 0, ctx->stream>>>(
       ctx->g, sp->push_type, sp->qbm, dt, sp->d_count, sp->x[0], sp->y[0], sp->px[0], sp->py[0], sp->pz[0], sp->q[0],
@@ -420,6 +421,7 @@ int species_amjdp_raw(qpad_species* sp, const double* ef, const double* bf, doub
 int species_push_u(qpad_species* sp, const double* ef, const double* bf, double dt, int fuse_x) {
   qpad_ctx* ctx = sp->ctx;
   if (sp->np == 0) return 0;
+  if (is_pgc(sp->push_type)) return laser_push_u(sp, ef, bf, dt, fuse_x);
   const double edge = (double)ctx->g.nr * ctx->g.dr;
   prof_begin(ctx, "push");
   k_push<<<grid_for(sp->np, kPartThreads), kPartThreads, 0, ctx->stream>>>(

@@ -101,6 +101,11 @@ struct qpad_ctx {
   int extrap = 0;                              // polynomial order of the initial B-perp guess (0: carried)
   double* qbg = nullptr;                       // qn + the ions of every neutral gas (when there is one)
   unsigned int* d_neut_err = nullptr;          // set when a neutral's particle buffer overflowed
+  std::vector<struct qpad_laser*> lasers;      // laser envelopes (laser.cu)
+  double* la = nullptr;                        // the lasers' sum of a slice: a_r, a_i, their gradients
+  double* chi = nullptr;                       // susceptibility of a slice, and its store
+  double* chi2 = nullptr;
+  double* ltbuf = nullptr;                     // the envelope solve's coupling terms
   double extrap_w = 1.0;                       // weight of the extrapolation's correction to the carried value
   double* conv = nullptr;                      // s_re[nr], s_im[nr], res[8]
   float* gtab = nullptr;                       // FP32 gather table [node][part][E0..2,B0..2] (mixed)
@@ -165,6 +170,7 @@ struct qpad_species {
   double* qf = nullptr;         // this species' charge density (finished deposit)
   double* qn = nullptr;         // this species' neutralising background
   struct qpad_neutral_state* neut = nullptr;   // ionisation state when this species is a neutral gas
+  int ppc_r = 2;                               // radial particles per cell (chi's axis factor)
 };
 
 struct qpad_beam {
@@ -239,6 +245,16 @@ int neutral_slice_prologue(qpad_ctx* ctx);
 int neutral_slice_update(qpad_ctx* ctx);
 bool has_neutrals(const qpad_ctx* ctx);
 void neutral_free(qpad_species* sp);
+// laser envelopes and the species that see them (laser.cu)
+int laser_state_ensure(qpad_ctx* ctx);
+int laser_slice_prologue(qpad_ctx* ctx);
+int laser_amjdp_raw(qpad_species* sp, const double* ef, const double* bf, double* cu, double* amu, double* acu,
+                    double dt);
+int laser_push_u(qpad_species* sp, const double* ef, const double* bf, double dt, int fuse_x);
+int laser_deposit_chi(qpad_ctx* ctx);
+int lasers_advance(qpad_ctx* ctx);
+void lasers_free(qpad_ctx* ctx);
+inline bool is_pgc(int push_type) { return push_type == QPAD_PUSH2_STD_PGC || push_type == QPAD_PUSH2_ROBUST_PGC; }
 int species_amjdp_raw(qpad_species* sp, const double* ef, const double* bf, double* cu, double* amu,
                       double* acu, double dt);
 int species_push_u(qpad_species* sp, const double* ef, const double* bf, double dt, int fuse_x);
