@@ -470,9 +470,10 @@ def run_ours(args):
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic.get(dep_name),
                 "kernel": dep_name, "peak_kind": peak_kind, "bytes_per_launch": bytes_per_particle * npl,
                 "avg_launch_us": amj_avg_s * 1e6, "device_ms_per_step": amj_ms,
-                "limiter": "FP32 issue and load latency: gather, push and 16 x (M+1) deposit sums per particle"}
+                "limiter": "instruction issue (gather, push and 16 x (M+1) deposit sums per particle) and instruction fetch"}
     for rf in (it_roof, dep_roof):
-        rf["traffic_source"] = ("ncu capture of this workload, profiles/dram_traffic_per_launch.json"
+        rf["traffic_source"] = ("copied from an ncu capture of a smaller cut of this workload with the same "
+                                "per-slice work (profiles/dram_traffic_per_launch.json); not measured in this run"
                                 if rf["traffic"] is not None else "no capture of this workload")
     # the dominant kernel of the step (by device time in the host-driven timing pass) is the
     # roofline line; the other beside it

@@ -5,7 +5,9 @@
 * Plasma: a Gaussian pulse drives a wake in a cold uniform plasma of PGC species (robust and
   standard pushers; M = 1 and 2).  Over two 3D steps (the second sees the advanced envelope):
   identical per-slice iteration counts, every 3D store and the susceptibility store within
-  1e-9, the advanced envelope within 1e-9, the plasma particles as a multiset.
+  1e-9 in m = 0 (the m >= 1 parts, round-off noise the wake amplifies, within 20 times the
+  oracle's own sensitivity to a 1e-15 perturbation), the advanced envelope likewise, the plasma
+  particles as a multiset.
 * Refusals: the mixed path, nr not a power of two.
 """
 import numpy as np
@@ -15,7 +17,7 @@ import qpad_gb300 as Q
 from oracle import oracle as O
 from qpad_gb300 import _capi as K
 from qpad_gb300 import lasers as LZ
-from tests.helpers import plasma_to_oracle, sorted_rows, store_errors
+from tests.helpers import plasma_to_oracle, store_errors
 
 pytestmark = pytest.mark.gpu
 
@@ -42,6 +44,7 @@ def test_envelope_advance_in_vacuum_matches_oracle():
     # a mode-2 part too, so that every mode's reduction runs
     ar[:, 3] = 0.3 * ar[:, 0]
     ai[:, 4] = -0.2 * ar[:, 0]
+    ar[:, 1:, 0] = ai[:, 1:, 0] = 0.0      # m >= 1 vanish on the axis (the reference's profiles do)
     g = O.grid(deck.nr, deck.nz, deck.max_mode, deck.dr, deck.dxi)
     osim = O.Sim(g, iter_max=5, dt3d=deck.dt, sp_npmax=1, lasers=[dict(k0=K0, iter=2, ar=ar, ai=ai)])
     osim.set_plasma(O.Plasma(0))
@@ -57,43 +60,70 @@ def test_envelope_advance_in_vacuum_matches_oracle():
     sim.close()
 
 
+def _oracle(deck, pl, ar, ai, push_type, perturb=0.0):
+    g = O.grid(deck.nr, deck.nz, deck.max_mode, deck.dr, deck.dxi)
+    osim = O.Sim(g, iter_max=deck.iter_max, iter_reltol=deck.iter_reltol, dt3d=deck.dt, sp_push_type=push_type,
+                 sp_npmax=len(pl[4]), lasers=[dict(k0=K0, iter=1, ar=ar, ai=ai)], sp_ppc_r=deck.ppc[0])
+    x = pl[0] * (1.0 + perturb * np.random.default_rng(1).standard_normal(pl[0].shape))
+    return osim, (x,) + tuple(pl[1:])
+
+
 @pytest.mark.parametrize("M,push_type", [(1, O.PUSH_ROBUST_PGC), (2, O.PUSH_ROBUST_PGC), (1, O.PUSH_STD_PGC)])
 def test_laser_wake_matches_oracle(M, push_type):
+    """The m >= 1 parts of this deck hold only the particles' round-off noise (an axisymmetric
+    pulse in a plasma loaded at evenly spaced angles), which the wake amplifies: the oracle
+    itself, rerun with positions perturbed by 1e-15 relative, moves them by up to ~1e-7 of
+    their size (~1e-13 of the store).  Each part is therefore held to 1e-9 or to 20 times that
+    measured sensitivity, whichever is larger; the m = 0 parts meet 1e-9."""
     deck = _deck(M)
     pl, _ = Q.deck_inputs(deck)
     ar, ai = _envelope(deck)
-    g = O.grid(deck.nr, deck.nz, M, deck.dr, deck.dxi)
-    osim = O.Sim(g, iter_max=deck.iter_max, iter_reltol=deck.iter_reltol, dt3d=deck.dt, sp_push_type=push_type,
-                 sp_npmax=len(pl[4]), lasers=[dict(k0=K0, iter=1, ar=ar, ai=ai)], sp_ppc_r=deck.ppc[0])
+    osim, pl0 = _oracle(deck, pl, ar, ai, push_type)
+    psim, pl1 = _oracle(deck, pl, ar, ai, push_type, perturb=1e-15)
     sim = Q.Simulation(deck.nr, deck.nz, M, deck.dr, deck.dxi, iter_max=deck.iter_max,
                        iter_reltol=deck.iter_reltol, dt=deck.dt)
     sim.add_species(*pl, push_type=push_type, ppc_r=deck.ppc[0])
     lz = sim.add_laser(ar, ai, k0=K0, iteration=1)
     for step in range(2):
-        osim.set_plasma(plasma_to_oracle(*pl))
+        osim.set_plasma(plasma_to_oracle(*pl0))
+        psim.set_plasma(plasma_to_oracle(*pl1))
         oit, _ = osim.run_3dstep(push_beams=False)
+        psim.run_3dstep(push_beams=False)
         if step:
             sim.species[0].reset()
         it, _ = sim.run_3d_step(push_beams=False)
         assert np.array_equal(it, oit), (step, it, oit)
-        worst = {}
         for name in ("e", "b", "psi", "cu", "q_spe", "b_spe"):
             ref = osim.store(name)[:deck.nz]
+            sens = store_errors(psim.store(name)[:deck.nz], ref)
             got = np.stack([sim.fields[name].store(s) for s in range(1, deck.nz + 1)])
-            worst[name] = store_errors(got, ref).max()
-        assert max(worst.values()) < 1e-9, (step, worst)
-        ochi = osim.store("chi")[:deck.nz, :, 0]
-        assert _rel(sim.chi_store(), ochi) < 1e-9
+            err = store_errors(got, ref)
+            assert err[0].max() < 1e-9, (step, name, err[0])
+            assert np.all(err <= np.maximum(1e-9, 20.0 * sens)), (step, name, err, sens)
+        ochi = osim.store("chi")[:deck.nz, :, :1]
+        chi_sens = store_errors(psim.store("chi")[:deck.nz, :, :1], ochi)
+        chi_err = store_errors(sim.chi_store()[:, :, None], ochi)
+        assert chi_err[0].max() < 1e-9 and np.all(chi_err <= np.maximum(1e-9, 20.0 * chi_sens)), (chi_err, chi_sens)
         olr, oli = osim.laser(0)
+        plr, pli = psim.laser(0)
         glr, gli = lz.download()
-        assert _rel(glr, olr) < 1e-9 and _rel(gli, oli) < 1e-9
+        for got, ref, pert in ((glr, olr, plr), (gli, oli, pli)):
+            e = store_errors(got[:, :, None], ref[:, :, None])
+            sens = store_errors(pert[:, :, None], ref[:, :, None])
+            assert e[0].max() < 1e-9 and np.all(e <= np.maximum(1e-9, 20.0 * sens)), (step, e, sens)
     assert np.abs(osim.store("e")[:deck.nz, 0, 2, 1]).max() > 1e-3      # a wake
     opl = osim.plasma()
     x, p, gm, ps, q = sim.species[0].download()
     assert len(q) == opl.n
-    np.testing.assert_allclose(sorted_rows(q, x[:, 0], x[:, 1]), sorted_rows(opl.q, opl.x, opl.y), rtol=1e-9,
-                               atol=1e-11)
+    # (the cold plasma is loaded at evenly spaced angles: many particles share x up to
+    # round-off, so the rows are ordered by positions rounded to 1e-9)
+    np.testing.assert_allclose(_rows(q, x[:, 0], x[:, 1]), _rows(opl.q, opl.x, opl.y), rtol=1e-9, atol=1e-11)
     sim.close()
+
+
+def _rows(q, x, y):
+    k = np.lexsort((np.round(y, 9), np.round(x, 9), q))
+    return np.stack([q[k], x[k], y[k]], axis=1)
 
 
 def test_laser_refusals():
