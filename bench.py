@@ -221,6 +221,10 @@ def _measure(args, deck, inputs, prec, local, dist, steps, warmup, full=True, gu
     sim.set_guess_extrapolation(order)
     sim.use_graph(args.graph == "on")
     tune = sim.autotune(reps=20) if not args.no_autotune else None
+    if args.item_ppl:
+        sim.set_launch_shapes(item_ppl=args.item_ppl)
+        if tune is not None:
+            tune["item_ppl"] = args.item_ppl
     if guess:
         from qpad_gb300 import learned as LR
         LR.attach(sim, *LR.load(LR.weights_path(deck.max_mode), deck.max_mode, device=local))
@@ -547,6 +551,8 @@ def main():
     ap.add_argument("--learned-steps", type=int, default=3, help="timed steps of the learned-guess arm (0: --steps)")
     ap.add_argument("--e2e-steps", type=int, default=5, help="steps of the end-to-end pass (at most --steps)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--item-ppl", type=int, default=0, choices=[0, 1, 2, 4],
+                    help="particles per lane of the mixed deposit's work items (0: the autotuner's choice)")
     ap.add_argument("--cpu-slices", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slices", type=int, default=0, help="override the deck's slice count (profiling runs)")

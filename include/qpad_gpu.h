@@ -314,6 +314,9 @@ typedef struct qpad_tune_result {
   double deposit_us;          /* the mixed deposit's time per launch (0 on the FP64 path) */
 } qpad_tune_result;
 int qpad_autotune(qpad_ctx* ctx, int reps, qpad_tune_result* out);
+/* Sets the launch shapes by hand (0 keeps one): the iteration kernel's CTAs per mode (1, 2, 4,
+ * 8, 16) and the mixed deposit's particles per lane (1, 2, 4). */
+int qpad_set_launch_shapes(qpad_ctx* ctx, int iter_cluster, int item_ppl);
 
 /* ---- loaders (host; project RNG substituting gfortran random_number) ------------- */
 typedef struct qpad_rng { uint64_t s; int32_t have; double next; } qpad_rng;

@@ -315,6 +315,10 @@ class Simulation:
         return {"iter_cluster": r.iter_cluster, "iter_us": r.iter_us, "item_ppl": r.item_ppl,
                 "deposit_us": r.deposit_us}
 
+    def set_launch_shapes(self, iter_cluster=0, item_ppl=0):
+        """Launch shapes by hand (0 keeps one): iteration CTAs per mode, deposit particles per lane."""
+        self._check(self.lib.qpad_set_launch_shapes(self.h, int(iter_cluster), int(item_ppl)))
+
 
 class Batch:
     """Independent simulations on one GPU advanced together: one 3D step of all of them is

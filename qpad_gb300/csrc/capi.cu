@@ -1487,6 +1487,23 @@ extern "C" int qpad_batch_step(qpad_batch* b, int push_beams, qpad_slice_stats* 
 // =====================================================================================
 // autotuner
 // =====================================================================================
+extern "C" int qpad_set_launch_shapes(qpad_ctx* ctx, int iter_cluster, int item_ppl) {
+  if (!ctx) return QPAD_E_ARG;
+  if (iter_cluster != 0 && (iter_cluster < 1 || iter_cluster > 16 || (iter_cluster & (iter_cluster - 1)) != 0))
+    return set_err(ctx, QPAD_E_ARG, "iteration cluster size must be 1, 2, 4, 8 or 16");
+  if (item_ppl != 0 && item_ppl != 1 && item_ppl != 2 && item_ppl != 4)
+    return set_err(ctx, QPAD_E_ARG, "particles per lane must be 1, 2 or 4");
+  if (iter_cluster)
+    if (int r = iterate_try_cluster(ctx, iter_cluster)) return r;
+  if (item_ppl && item_ppl != ctx->item_ppl) {
+    ctx->item_ppl = item_ppl;
+    if (ctx->precision == QPAD_PREC_MIXED)
+      for (auto* s : ctx->species)
+        if (int r = mixed_index(s)) return r;
+  }
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "launch shapes");
+}
+
 extern "C" int qpad_autotune(qpad_ctx* ctx, int reps, qpad_tune_result* out) {
   if (!ctx || reps < 1) return QPAD_E_ARG;
   // the slice fields are scratch for the timing runs (a 3D step zeroes them anyway)

@@ -457,9 +457,12 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
   const int jn = lane >> 4, h = (lane >> 3) & 1, c = lane & 7;
   double* dst = c < 3 ? cu + (size_t)c * ld : (c < 5 ? acu + (size_t)(c - 3) * ld : amu + (size_t)(c - 5) * ld);
   const int ncomp = c < 3 ? 3 : (c < 5 ? 2 : 3);
-#pragma unroll
-  for (int m = 0; m <= ModeLoop<kM>::kLast; ++m) {
-    if (ModeLoop<kM>::past(m, G.M)) break;
+  // the mode loop is not unrolled: one copy of the accumulation and butterfly keeps the
+  // kernel's code small enough for the instruction cache (measured on the c5 shape: 3.5 %
+  // shorter 3D step with two particles per lane, whose tuning this makes the fastest)
+  const int mlast = kM >= 0 ? kM : G.M;
+#pragma unroll 1
+  for (int m = 0; m <= mlast; ++m) {
     float acc[32];
 #pragma unroll
     for (int k = 0; k < 32; ++k) acc[k] = 0.0f;
