@@ -349,6 +349,8 @@ typedef struct qpad_h5_grid_info {
   const char* axis_name[2];
   const char* axis_label[2];
   const char* axis_units[2];
+  const char* type;             /* root attribute TYPE: null or "grid" (with the AXIS group), else e.g.
+                                   "restart" (no AXIS group, as wrattr_file, hdf5io_class.f03:264-300) */
 } qpad_h5_grid_info;
 const char* qpad_h5_last_error(void);
 /* One grid file as pwfield_2d writes it (hdf5io_class.f03:398-452, attributes :264-335): root

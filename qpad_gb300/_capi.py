@@ -56,7 +56,7 @@ class H5GridInfo(C.Structure):
     _fields_ = [("time", C.c_double), ("iter", C.c_int32), ("dt", C.c_double), ("timeunit", C.c_char_p),
                 ("units", C.c_char_p), ("label", C.c_char_p), ("axis_min", C.c_double * 2),
                 ("axis_max", C.c_double * 2), ("axis_name", C.c_char_p * 2), ("axis_label", C.c_char_p * 2),
-                ("axis_units", C.c_char_p * 2)]
+                ("axis_units", C.c_char_p * 2), ("type", C.c_char_p)]
 
 
 class Rng(C.Structure):

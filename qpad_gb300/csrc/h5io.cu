@@ -529,11 +529,13 @@ extern "C" int qpad_h5_write_grid(const char* path, const char* dataname, const 
   }
   h5::Obj root;
   root.group = true;
-  file_attrs(root, dataname, "grid", info->time, info->iter, info->dt, info->timeunit);
+  const bool grid = !info->type || std::string(info->type) == "grid";
+  file_attrs(root, dataname, grid ? "grid" : info->type, info->time, info->iter, info->dt, info->timeunit);
+  std::vector<std::vector<double>> ax(2);          // (outlives the objects that point into it)
+  if (grid) {
   h5::Obj axis;
   axis.name = "AXIS";
   axis.group = true;
-  std::vector<std::vector<double>> ax(2);
   for (int k = 0; k < 2; ++k) {
     ax[k] = {info->axis_min[k], info->axis_max[k]};
     h5::Obj a;
@@ -549,6 +551,7 @@ extern "C" int qpad_h5_write_grid(const char* path, const char* dataname, const 
     axis.kids.push_back(a);
   }
   root.kids.push_back(axis);
+  }
   h5::Obj d;
   d.name = dataname;
   d.dims = {(uint64_t)nz, (uint64_t)nr};

@@ -10,6 +10,8 @@ reported beside each figure.
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 
 # the fields whose 3D stores the step writes and the error covers: psi, E, B, J, rho
@@ -146,3 +148,59 @@ def read_h5_attr(path: str, attr: str, obj: str = ""):
     if L.qpad_h5_read_attr(path.encode(), obj.encode(), attr.encode(), C.byref(v), buf, 512):
         raise IOError(L.qpad_h5_last_error().decode())
     return buf.value.decode().rstrip() if buf.value else v.value
+
+
+def laser_dirs(max_mode: int) -> list:
+    """(directory, 0 for a_r / 1 for a_i, mode part) of a complex field dump (add_diag_cym,
+    diagnostics_class.f03:1001-1015): Re_Re0, Im_Re0, then per mode Re_Re, Re_Im, Im_Re, Im_Im."""
+    out = [("Re_Re0", 0, 0), ("Im_Re0", 1, 0)]
+    for m in range(1, max_mode + 1):
+        out += [(f"Re_Re{m}", 0, 2 * m - 1), (f"Re_Im{m}", 0, 2 * m), (f"Im_Re{m}", 1, 2 * m - 1),
+                (f"Im_Im{m}", 1, 2 * m)]
+    return out
+
+
+def _grid_info(sim, tstep, units, label):
+    from . import _capi as K
+    info = K.H5GridInfo()
+    info.time, info.iter, info.dt = float(tstep * sim.dt), int(tstep), float(sim.dt)
+    info.timeunit, info.units, info.label = b"1 / \\omega_p", units.encode(), label.encode()
+    info.axis_min[0], info.axis_max[0] = 0.0, sim.nr * sim.dr
+    info.axis_min[1], info.axis_max[1] = 0.0, sim.nz * sim.dxi
+    for k, n in enumerate((b"r", b"\\xi")):
+        info.axis_name[k] = n
+        info.axis_label[k] = n
+        info.axis_units[k] = b"c / \\omega_p"
+    return info
+
+
+def write_laser_diags(sim, root: str, tstep: int, envelope: bool = True, chi: bool = True) -> list:
+    """The laser dumps of the last 3D step (init_diag_lasers, diagnostics_class.f03:608-694):
+    'a_cyl_m' of every laser i into root/Lasers<i>/A_laser/<Re_Re0|Im_Re0|...>/a_laser_<tstep>.h5
+    and 'chi_cyl_m' into root/Fields/Chi/<Re0|Re1|Im1|...>/chi_<tstep>.h5; returns the files."""
+    import os
+    from . import _capi as K
+    L = K.load()
+    out = []
+
+    def write(path, name, data, info):
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        data = np.ascontiguousarray(data)
+        if L.qpad_h5_write_grid(path.encode(), name.encode(), data.ctypes.data_as(K.D), sim.nz, sim.nr,
+                                C.byref(info)):
+            raise IOError(L.qpad_h5_last_error().decode())
+        out.append(path)
+
+    if envelope:
+        info = _grid_info(sim, tstep, "m_ec^2/e", "a")
+        for i, lz in enumerate(sim.lasers, start=1):
+            arrs = lz.download()
+            for d, h, p in laser_dirs(sim.max_mode):
+                write(os.path.join(root, f"Lasers{i}", "A_laser", d, f"a_laser_{tstep:08d}.h5"), "a_laser",
+                      arrs[h][:, p, 1:sim.nr + 1], info)
+    if chi:
+        info = _grid_info(sim, tstep, "n_0", "\\chi")
+        c = sim.chi_store()
+        for p, d in enumerate(mode_dirs(sim.max_mode)):
+            write(os.path.join(root, "Fields", "Chi", d, f"chi_{tstep:08d}.h5"), "chi", c[:, p, 1:sim.nr + 1], info)
+    return out

@@ -10,6 +10,8 @@
   particles as a multiset.
 * Refusals: the mixed path, nr not a power of two.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -17,6 +19,9 @@ import qpad_gb300 as Q
 from oracle import oracle as O
 from qpad_gb300 import _capi as K
 from qpad_gb300 import lasers as LZ
+from qpad_gb300 import restart
+from qpad_gb300.diagnostics import laser_dirs, mode_dirs, write_laser_diags
+from tests import h5_parse
 from tests.helpers import plasma_to_oracle, store_errors
 
 pytestmark = pytest.mark.gpu
@@ -140,3 +145,47 @@ def test_laser_refusals():
     with pytest.raises(Q.api.QpadError):
         odd.add_laser(np.zeros((deck.nz, 3, 48)), np.zeros((deck.nz, 3, 48)), k0=K0)
     odd.close()
+
+
+def test_laser_restart_and_dumps(tmp_path):
+    """The advanced envelope written as the reference's laser restart files comes back on a
+    new context unchanged, and the next 3D step from it equals the original's next step; the
+    laser and chi dumps hold the device's envelope and susceptibility store."""
+    deck = _deck(1)
+    pl, _ = Q.deck_inputs(deck)
+    ar, ai = _envelope(deck)
+
+    def make(lz_from=None):
+        s = Q.Simulation(deck.nr, deck.nz, 1, deck.dr, deck.dxi, iter_max=deck.iter_max,
+                         iter_reltol=deck.iter_reltol, dt=deck.dt)
+        s.add_species(*pl, push_type=K.PUSH2_ROBUST_PGC, ppc_r=deck.ppc[0])
+        return s
+
+    a = make()
+    la = a.add_laser(ar, ai, k0=K0, iteration=1)
+    a.run_3d_step(push_beams=False)
+    restart.save_lasers(a, str(tmp_path), timestep=1)
+    b = make()
+    (lb,) = restart.load_lasers(b, str(tmp_path), timestep=1, nlasers=1, params=[dict(k0=K0, iteration=1)])
+    for u, v in zip(la.download(), lb.download()):
+        assert np.array_equal(u[:, :, 1:deck.nr + 1], v[:, :, 1:deck.nr + 1])
+    a.species[0].reset()
+    ia, _ = a.run_3d_step(push_beams=False)
+    ib, _ = b.run_3d_step(push_beams=False)
+    assert np.array_equal(ia, ib)
+    for u, v in zip(la.download(), lb.download()):
+        assert np.abs(u - v).max() <= 1e-12 * np.abs(u).max()
+    # dumps
+    files = write_laser_diags(a, str(tmp_path), tstep=2)
+    assert len(files) == len(laser_dirs(1)) + len(mode_dirs(1))
+    lr, li = la.download()
+    for d, h, p in laser_dirs(1):
+        f = h5_parse.File(os.path.join(str(tmp_path), "Lasers1", "A_laser", d, "a_laser_00000002.h5"))
+        assert f.members() == ["AXIS", "a_laser"]
+        assert np.array_equal(f.dataset("a_laser"), (lr, li)[h][:, p, 1:deck.nr + 1])
+    chi = a.chi_store()
+    for p, d in enumerate(mode_dirs(1)):
+        f = h5_parse.File(os.path.join(str(tmp_path), "Fields", "Chi", d, "chi_00000002.h5"))
+        assert np.array_equal(f.dataset("chi"), chi[:, p, 1:deck.nr + 1])
+    a.close()
+    b.close()

@@ -50,6 +50,23 @@ def test_grid_file_layout(tmp_path):
     assert read_h5_attr(path, "LONG_NAME", "ez") == "E_z"
 
 
+def test_restart_grid_file_layout(tmp_path):
+    """A grid restart file (a laser envelope part): TYPE "restart", no AXIS group
+    (wrattr_file, hdf5io_class.f03:264-300)."""
+    L = K.load()
+    data = np.ascontiguousarray(np.arange(12.0).reshape(3, 4))
+    path = os.path.join(str(tmp_path), "RST", "Laser01", "RST-laser01-re_re0_00000004.h5")
+    info = _grid_info(it=4)
+    info.type = b"restart"
+    assert L.qpad_h5_write_grid(path.encode(), b"RST-laser01-re_re0", data.ctypes.data_as(K.D), 3, 4,
+                                C.byref(info)) == 0
+    f = h5_parse.File(path)
+    assert f.members() == ["RST-laser01-re_re0"]
+    assert f.attrs["TYPE"].rstrip() == "restart" and f.attrs["ITER"] == [4]
+    assert np.array_equal(f.dataset("RST-laser01-re_re0"), data)
+    assert np.array_equal(read_h5_dataset(path, "RST-laser01-re_re0").reshape(3, 4), data)
+
+
 def test_particle_file_layout(tmp_path):
     L = K.load()
     rng = np.random.default_rng(1)
