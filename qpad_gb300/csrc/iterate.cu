@@ -359,14 +359,27 @@ __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
   // waits (again bounded) for its own bulk copies still in flight.
   const bool gave_up = s_gaveup != 0;
   if (gave_up && t == 0) atomicExch(a.err, 1u);
-  for (int q = t; q < c8_n * nh * W; q += blockDim.x) {   // finish the deposits in place
-    const int row = q / W, k = q % W, c8 = c8_lo + row / nh, node = wb + k;
-    if (node < 0 || node > nr + 1) continue;
-    double& v = win[(c8 * 2 + row % nh) * W + k];
-    if (a.prefinished) continue;
-    v = c8 < 3 ? finish_amj(G, m, 0, c8, node, v) : (c8 < 6 ? finish_amj(G, m, 1, c8 - 3, node, v)
-                                                                : finish_amj(G, m, 2, c8 - 6, node, v));
-  }
+  // finish the deposits in place, one window node per thread (W <= blockDim.x for the
+  // row counts the host allows; the loop covers any W): every row of a node from the
+  // second on takes the same factor 1/(i-1)
+  if (!a.prefinished)
+    for (int x = t; x < W; x += blockDim.x) {
+      const int node = wb + x;
+      if (node < 0 || node > nr + 1) continue;
+      if (node >= 2) {
+        const double f = G.inv[node - G.toff];
+        for (int c = 0; c < c8_n; ++c)
+          for (int h = 0; h < nh; ++h) win[((c8_lo + c) * 2 + h) * W + x] *= f;
+        continue;
+      }
+      for (int c = 0; c < c8_n; ++c)
+        for (int h = 0; h < nh; ++h) {
+          const int c8 = c8_lo + c;
+          double& v = win[(c8 * 2 + h) * W + x];
+          v = c8 < 3 ? finish_amj(G, m, 0, c8, node, v) : (c8 < 6 ? finish_amj(G, m, 1, c8 - 3, node, v)
+                                                                      : finish_amj(G, m, 2, c8 - 6, node, v));
+        }
+    }
   __syncthreads();
   // binomial smoothing of the finished deposits (amjdp_species2d, species2d_class.f03:270-272):
   // pass k is exact on window nodes [wb + k, wb + W - 1 - k], which covers the owned nodes and
