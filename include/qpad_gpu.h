@@ -317,6 +317,12 @@ int qpad_autotune(qpad_ctx* ctx, int reps, qpad_tune_result* out);
 /* Sets the launch shapes by hand (0 keeps one): the iteration kernel's CTAs per mode (1, 2, 4,
  * 8, 16) and the mixed deposit's particles per lane (1, 2, 4). */
 int qpad_set_launch_shapes(qpad_ctx* ctx, int iter_cluster, int item_ppl);
+/* Predictor-corrector iterations per body of the step graph's iteration loop (1 .. 4,
+ * default 2; no counterpart in the reference, whose loop is `do while` on the host,
+ * simulation_class.f03:370-398).  Each WHILE-node round trip of the graph costs several
+ * microseconds; the iterations after the first in a body return at once when the loop has
+ * ended before them, so results and iteration counts do not depend on this setting. */
+int qpad_set_graph_unroll(qpad_ctx* ctx, int iterations);
 
 /* ---- loaders (host; project RNG substituting gfortran random_number) ------------- */
 typedef struct qpad_rng { uint64_t s; int32_t have; double next; } qpad_rng;

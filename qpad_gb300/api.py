@@ -319,6 +319,10 @@ class Simulation:
         """Launch shapes by hand (0 keeps one): iteration CTAs per mode, deposit particles per lane."""
         self._check(self.lib.qpad_set_launch_shapes(self.h, int(iter_cluster), int(item_ppl)))
 
+    def set_graph_unroll(self, iterations: int):
+        """Predictor-corrector iterations per body of the step graph's iteration loop (1 .. 4)."""
+        self._check(self.lib.qpad_set_graph_unroll(self.h, int(iterations)))
+
 
 class Batch:
     """Independent simulations on one GPU advanced together: one 3D step of all of them is

@@ -310,7 +310,7 @@ extern "C" int qpad_ctx_create(const qpad_grid_desc* d, qpad_ctx** out) {
   if (!r && ctx->precision == QPAD_PREC_MIXED)
     r = dmalloc(ctx, (void**)&ctx->gtab, (size_t)g.ld * g.P * 6 * sizeof(float), "gather table");
   if (!r) r = dmalloc(ctx, (void**)&ctx->d_j, 2 * sizeof(int), "slice index");
-  if (!r) r = dmalloc(ctx, (void**)&ctx->d_iter, 2 * sizeof(int), "iteration counter");
+  if (!r) r = dmalloc(ctx, (void**)&ctx->d_iter, (1 + kMaxUnroll) * sizeof(int), "iteration counter");
   if (!r) r = dmalloc(ctx, (void**)&ctx->d_stats, (size_t)g.nz * sizeof(qpad_slice_stats), "slice stats");
   if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->h_j, 2 * sizeof(int)), "pinned slice index");
   if (!r) r = cuda_check(ctx, cudaMallocHost((void**)&ctx->h_res, 8 * sizeof(double)), "pinned");
@@ -1019,7 +1019,7 @@ int enqueue_slice_prologue(qpad_ctx* ctx, cudaGraphConditionalHandle hi, int use
   for (auto* s : ctx->species) any_ntd |= s->neutralized;
   const bool mixed = ctx->precision == QPAD_PREC_MIXED;
   if (int r = guess_enqueue(ctx)) return r;          // before anything reads b_spe or cu
-  if (cudaMemsetAsync(ctx->d_iter, 0, sizeof(int), ctx->stream) != cudaSuccess ||
+  if (cudaMemsetAsync(ctx->d_iter, 0, (1 + kMaxUnroll) * sizeof(int), ctx->stream) != cudaSuccess ||
       cudaMemsetAsync(ctx->qraw, 0, n1 * sizeof(double), ctx->stream) != cudaSuccess)
     return check_launch(ctx, "slice prologue memsets", 0);
   for (auto* s : ctx->species)
@@ -1156,8 +1156,16 @@ int add_slice_loop(qpad_ctx* ctx, cudaGraph_t top) {
   if (!r) r = cuda_check(ctx, cudaStreamBeginCaptureToGraph(ctx->stream, ibody, nullptr, nullptr, 0,
                                                             cudaStreamCaptureModeThreadLocal), "capture iteration");
   if (!r) {
+    // the loop body holds `unroll` iterations: a WHILE-node round trip costs several times a
+    // kernel-to-kernel dependency, and the parts after the first return at once when the
+    // loop ended before them (iter_guard)
     const int64_t l2b = ctx->launches;
-    r = enqueue_iteration(ctx, hi, 1);
+    const int U = std::max(1, std::min(kMaxUnroll, ctx->unroll));
+    for (int u = 0; u < U && !r; ++u) {
+      ctx->iter_part = U > 1 ? u : -1;
+      r = enqueue_iteration(ctx, hi, 1);
+    }
+    ctx->iter_part = -1;
     l3 = l2 + (ctx->launches - l2b);
     cudaGraph_t out = nullptr;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &out);
@@ -1195,7 +1203,7 @@ std::string step_key(const qpad_ctx* ctx) {
                   std::to_string(ctx->item_ppl) + "/" + std::to_string(ctx->guess != nullptr) + "/" +
                   std::to_string(ctx->extrap) + "/" + std::to_string(ctx->extrap_w) + "/" +
                   std::to_string(ctx->pdl) + "/" + std::to_string(ctx->g.smooth) + "/" +
-                  std::to_string(ctx->lasers.size());
+                  std::to_string(ctx->lasers.size()) + "/" + std::to_string(ctx->unroll);
   for (auto* s : ctx->species)
     k += "|" + std::to_string((long long)s->np) + ":" + std::to_string(s->push_type) + ":" +
          std::to_string(s->neutralized) + ":" + std::to_string(s->sort_freq);
@@ -1271,10 +1279,12 @@ int step_graph_stats(qpad_ctx* ctx, qpad_slice_stats* stats) {
                                               cudaMemcpyDeviceToHost, ctx->stream), "stats"))
     return r;
   if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "graph step")) return r;
-  // kernels the graph ran: per slice the prologue and epilogue, per iteration the body
-  int64_t iters = 0;
-  for (const auto& s : ctx->h_stats) iters += s.iters;
-  ctx->launches += ctx->g_once + (int64_t)ctx->g.nz * (ctx->g_pro + ctx->g_epi) + iters * ctx->g_it;
+  // kernels the graph ran: per slice the prologue and epilogue, per execution of the
+  // iteration loop's body (ceil(iterations / unroll) of them) the body's launches
+  const int64_t U = std::max(1, std::min(kMaxUnroll, ctx->unroll));
+  int64_t bodies = 0;
+  for (const auto& s : ctx->h_stats) bodies += (s.iters + U - 1) / U;
+  ctx->launches += ctx->g_once + (int64_t)ctx->g.nz * (ctx->g_pro + ctx->g_epi) + bodies * ctx->g_it;
   if (stats) std::copy(ctx->h_stats.begin(), ctx->h_stats.end(), stats);
   return 0;
 }
@@ -1502,6 +1512,14 @@ extern "C" int qpad_set_launch_shapes(qpad_ctx* ctx, int iter_cluster, int item_
         if (int r = mixed_index(s)) return r;
   }
   return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "launch shapes");
+}
+
+extern "C" int qpad_set_graph_unroll(qpad_ctx* ctx, int iterations) {
+  if (!ctx) return QPAD_E_ARG;
+  if (iterations < 1 || iterations > kMaxUnroll)
+    return set_err(ctx, QPAD_E_ARG, "iterations per loop body must be 1 .. " + std::to_string(kMaxUnroll));
+  ctx->unroll = iterations;
+  return QPAD_OK;
 }
 
 extern "C" int qpad_autotune(qpad_ctx* ctx, int reps, qpad_tune_result* out) {

@@ -70,6 +70,8 @@ struct IterArgs {
   int tma;                // stage with bulk copies (even nr and R: every row 16-byte aligned)
   unsigned int* err;      // device error word: 1 = a bulk-copy wait gave up
   int prefinished;        // the raw deposits were already finished (and smoothed) by k_smooth_raw
+  const int* guard;       // part of an unrolled loop body: return at once if *guard (the loop has ended)
+  int* skip_out;          // ... and then set this part's flag for the part after it
 };
 
 __device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
@@ -181,6 +183,13 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // kSmooth: the instance with the deposit smoothing (the other one carries none of its code)
 template <bool kSmooth>
 __global__ void __launch_bounds__(kIterThreads) k_iterate(IterArgs a) {
+  // a later part of an unrolled loop body after the loop has ended: nothing to do (every CTA
+  // reads the flag, written by a kernel that completed before this one began, and leaves
+  // before any barrier)
+  if (a.guard && __ldcg(a.guard) != 0) {
+    if (a.skip_out && blockIdx.x == 0 && threadIdx.x == 0) *a.skip_out = 1;
+    return;
+  }
   extern __shared__ __align__(16) double smem[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ double fwd[kMaxRhs][2], bwd[kMaxRhs][2];
@@ -839,7 +848,8 @@ static void (*iterate_kernel(int smooth))(IterArgs) {
 // iteration kernel then takes it as it is (IterArgs::prefinished).  (It cannot go back to
 // raw form: the smoothing's axis rule may leave a value on an axis node that the finishing
 // zeroes.)
-__global__ void __launch_bounds__(256) k_smooth_raw(GridDev G, double* __restrict__ raw) {
+__global__ void __launch_bounds__(256) k_smooth_raw(GridDev G, double* __restrict__ raw, const int* __restrict__ guard) {
+  if (guard && *guard) return;                   // a part of an unrolled loop body after the loop ended
   extern __shared__ double sl[];                 // two lines of ld doubles
   const int row = blockIdx.x % 8, p = blockIdx.x / 8;
   const int m = (p + 1) / 2, ld = G.ld, nr = G.nr;
@@ -865,7 +875,7 @@ int launch_smooth_raw(qpad_ctx* ctx) {
   if (ctx->g.smooth <= kWindowSmooth) return 0;
   const size_t smem = 2 * (size_t)ctx->g.ld * sizeof(double);
   if (int r = raise_dyn_smem(ctx, (const void*)k_smooth_raw, smem)) return r;
-  k_smooth_raw<<<8 * ctx->g.P, 256, smem, ctx->stream>>>(ctx->g, ctx->raw);
+  k_smooth_raw<<<8 * ctx->g.P, 256, smem, ctx->stream>>>(ctx->g, ctx->raw, iter_guard(ctx));
   return check_launch(ctx, "k_smooth_raw");
 }
 
@@ -936,6 +946,7 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
     a.L.iter_max = ctx->iter_max;
     a.L.h = h;
     a.L.use_h = use_h;
+    a.L.stop = iter_stop_out(ctx);
   }
   a.reltol = ctx->reltol;
   a.abstol = ctx->abstol;
@@ -944,6 +955,8 @@ int launch_iterate(qpad_ctx* ctx, int loop_state, cudaGraphConditionalHandle h, 
   a.tma = (ctx->g.nr % 2 == 0 && a.R % 2 == 0) ? 1 : 0;
   a.err = ctx->iter_tickets + kIterErrWord;
   a.prefinished = ctx->g.smooth > kWindowSmooth ? 1 : 0;
+  a.guard = iter_guard(ctx);
+  a.skip_out = loop_state ? iter_stop_out(ctx) : nullptr;
   const int cl = ctx->iter_cl;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2 * cl * (ctx->g.M + 1));

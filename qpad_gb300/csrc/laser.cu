@@ -232,7 +232,8 @@ __global__ void __launch_bounds__(kPartThreads) k_amjdp_pgc(GridDev G, int push_
                                                             double* __restrict__ gamma, double* __restrict__ psi,
                                                             const double* __restrict__ ef, const double* __restrict__ bf,
                                                             LaserF1 L, double* __restrict__ cu, double* __restrict__ amu,
-                                                            double* __restrict__ acu) {
+                                                            double* __restrict__ acu, const int* __restrict__ guard) {
+  if (guard && *guard) return;                 // a part of an unrolled loop body after the loop ended
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   const int64_t n = *n_ptr;
   const int64_t pp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -673,7 +674,7 @@ int laser_amjdp_raw(qpad_species* sp, const double* ef, const double* bf, double
   if (sp->np == 0) return 0;
   k_amjdp_pgc<<<blocks_for(sp->np, kPartThreads), kPartThreads, 0, ctx->stream>>>(
       ctx->g, sp->push_type, sp->qbm, dt, sp->d_count, sp->x[0], sp->y[0], sp->px[0], sp->py[0], sp->pz[0], sp->q[0],
-      sp->gamma[0], sp->psi[0], ef, bf, laser_f1(ctx->la, ctx->g), cu, amu, acu);
+      sp->gamma[0], sp->psi[0], ef, bf, laser_f1(ctx->la, ctx->g), cu, amu, acu, iter_guard(ctx));
   return check_launch(ctx, "k_amjdp_pgc");
 }
 

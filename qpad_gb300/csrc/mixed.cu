@@ -378,7 +378,8 @@ __global__ void __launch_bounds__(kItemThreads) k_mamjdp(GridDev G, int push_typ
                                                          const int4* __restrict__ items, const int* __restrict__ n_items,
                                                          MArr A, const float* __restrict__ T, double* __restrict__ cu,
                                                          double* __restrict__ amu, double* __restrict__ acu,
-                                                         int write_back) {
+                                                         int write_back, const int* __restrict__ guard) {
+  if (guard && *guard) return;                         // a part of an unrolled loop body after the loop ended
   // the field iteration launched after this kernel may start its own staging now
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -878,7 +879,8 @@ int mixed_amjdp_raw(qpad_species* sp, const float* gtab, double* cu, double* amu
 #define QPAD_MAMJ(PPL, MM)                                                                                        \
   k_mamjdp<PPL, MM><<<item_blocks(sp), kItemThreads, 0, ctx->stream>>>(ctx->g, sp->push_type, (float)sp->qbm,     \
                                                                       (float)dt, sp->items, sp->d_nitems,         \
-                                                                      marr(sp, 0), gtab, cu, amu, acu, 0)
+                                                                      marr(sp, 0), gtab, cu, amu, acu, 0,         \
+                                                                      iter_guard(ctx))
 #define QPAD_MAMJ_M(MM) \
   do { if (ctx->item_ppl == 1) QPAD_MAMJ(1, MM); else if (ctx->item_ppl == 2) QPAD_MAMJ(2, MM); else QPAD_MAMJ(4, MM); } while (0)
   QPAD_MIXED_BY_MODE(ctx->g.M, QPAD_MAMJ_M);

@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(kPartThreads) k_amjdp(GridDev G, int push_type
                                                         double* __restrict__ gamma, double* __restrict__ psi,
                                                         const double* __restrict__ ef, const double* __restrict__ bf,
                                                         double* __restrict__ cu, double* __restrict__ amu,
-                                                        double* __restrict__ acu) {
+                                                        double* __restrict__ acu, const int* __restrict__ guard) {
+  if (guard && *guard) return;                 // a part of an unrolled loop body after the loop ended
   // the field iteration launched after this kernel may start its own staging now
   asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
   const int64_t n = *n_ptr;
@@ -413,7 +414,7 @@ int species_amjdp_raw(qpad_species* sp, const double* ef, const double* bf, doub
   prof_begin(ctx, "amjdp");
   k_amjdp<<<grid_for(sp->np, kPartThreads), kPartThreads, 0, ctx->stream>>>(
       ctx->g, sp->push_type, sp->qbm, dt, sp->d_count, sp->x[0], sp->y[0], sp->px[0], sp->py[0], sp->pz[0], sp->q[0],
-      sp->gamma[0], sp->psi[0], ef, bf, cu, amu, acu);
+      sp->gamma[0], sp->psi[0], ef, bf, cu, amu, acu, iter_guard(ctx));
   prof_end(ctx, "amjdp");
   return check_launch(ctx, "k_amjdp");
 }

@@ -67,6 +67,7 @@ struct ConvLoop {
   int iter_max;
   cudaGraphConditionalHandle h;  // WHILE-node handle
   int use_h;
+  int* stop;                     // unrolled graph bodies: set to 1 when the loop has ended, else 0
 };
 
 struct Species;
@@ -77,6 +78,7 @@ struct Beam;
 static constexpr int kMaxSmoothOrder = 64;    // smoothing passes of the species deposits, at most
 static constexpr int kIterMaxWords = 64;      // k_iterate's two 64-bit maxima in the ticket buffer
 static constexpr int kIterErrWord = 127;       // k_iterate's error word in the ticket buffer
+static constexpr int kMaxUnroll = 4;          // iterations per body of the graph's iteration loop, at most
 
 struct qpad_ctx {
   qpad::GridDev g;
@@ -119,7 +121,10 @@ struct qpad_ctx {
   bool field_attr_done = false;
   // device-side loop state of the slice driver
   int* d_j = nullptr;                          // current slice (1-based)
-  int* d_iter = nullptr;                       // predictor-corrector iterations in this slice
+  int* d_iter = nullptr;                       // [0] predictor-corrector iterations in this slice,
+                                               // [1 + u] loop ended after part u of an unrolled body
+  int unroll = 2;                              // iterations per body of the graph's iteration loop
+  int iter_part = -1;                          // part of the unrolled body being captured (-1: none)
   qpad_slice_stats* d_stats = nullptr;         // per-slice statistics [nz]
   int* h_j = nullptr;                          // pinned staging of the slice index
   // CUDA graph of the whole slice loop (WHILE over slices, WHILE over iterations)
@@ -189,6 +194,18 @@ struct qpad_beam {
 };
 
 namespace qpad {
+
+// ---- unrolled iteration loop of the step graph ------------------------------------------
+// A body of the graph's iteration loop holds `unroll` iterations.  Part u > 0 runs only if
+// the loop had not ended after part u - 1: its kernels read that part's flag d_iter[u] (1 =
+// ended) and return at once if it is set.  A part's convergence decision writes its own flag
+// d_iter[1 + u]; a part that returned at once sets it to 1 for the part after it.
+inline const int* iter_guard(const qpad_ctx* ctx) {
+  return ctx->iter_part > 0 ? ctx->d_iter + ctx->iter_part : nullptr;
+}
+inline int* iter_stop_out(const qpad_ctx* ctx) {
+  return ctx->iter_part >= 0 && ctx->unroll > 1 ? ctx->d_iter + 1 + ctx->iter_part : nullptr;
+}
 
 // ---- status helpers (capi.cu) -----------------------------------------------------------
 int set_err(qpad_ctx* ctx, int code, const std::string& msg);

@@ -386,7 +386,9 @@ __device__ inline void conv_decide_at(double mx_old, double mx_new, double relto
       s.abs_res = abs_res;
       L.stats[jp - 1] = s;
     }
-    if (L.use_h) cudaGraphSetConditional(L.h, (!converged && it < L.iter_max) ? 1u : 0u);
+    const bool more = !converged && it < L.iter_max;
+    if (L.use_h) cudaGraphSetConditional(L.h, more ? 1u : 0u);
+    if (L.stop) *L.stop = more ? 0 : 1;
   }
 }
 

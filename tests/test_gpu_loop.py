@@ -156,3 +156,50 @@ def test_extrapolated_guess_matches_oracle(order):
     with pytest.raises(Q.QpadError):
         sim.set_guess_extrapolation(3)
     sim.close()
+
+
+@pytest.mark.parametrize("unroll,iter_max", [(1, 30), (3, 30), (4, 30), (2, 3), (3, 4)])
+def test_graph_unroll_matches_oracle(unroll, iter_max):
+    """Iterations per body of the graph's iteration loop (the later ones return at once when
+    the loop ended before them): identical per-slice iteration counts and stores within 1e-9
+    of the oracle, also when the loop stops at iter_max inside a body."""
+    deck = _deck(2)
+    deck.iter_max = iter_max
+    pl, beams = Q.deck_inputs(deck)
+    osim, oiters, _ = _oracle_run(deck, pl, beams, O.PUSH_ROBUST)
+    sim = Q.Simulation(deck.nr, deck.nz, 2, deck.dr, deck.dxi, iter_max=deck.iter_max,
+                       iter_reltol=deck.iter_reltol, dt=deck.dt)
+    sim.set_graph_unroll(unroll)
+    sim.add_species(*pl)
+    sim.add_beam(*beams[0])
+    iters, _ = sim.run_3d_step()
+    assert sim.graph_active()[0]
+    assert np.array_equal(iters, oiters), (iters, oiters)
+    worst = {n: float(store_errors(sim.fields[n].store_all(), osim.store(n)[:deck.nz]).max())
+             for n in ("e", "b", "psi", "cu", "b_spe")}
+    assert max(worst.values()) < 1e-9, worst
+    with pytest.raises(Q.QpadError):
+        sim.set_graph_unroll(5)
+    sim.close()
+
+
+def test_graph_unroll_mixed_path():
+    """The mixed path with 1 and 3 iterations per loop body: the same iteration counts to
+    within the FP32 atomics' summation order, fields within 1e-4."""
+    deck = _deck(2)
+    pl, beams = Q.deck_inputs(deck)
+    runs = []
+    for unroll in (1, 3):
+        s = Q.Simulation(deck.nr, deck.nz, 2, deck.dr, deck.dxi, iter_max=deck.iter_max, dt=deck.dt,
+                         precision=Q._capi.PREC_MIXED)
+        s.set_graph_unroll(unroll)
+        s.add_species(*pl)
+        s.add_beam(*beams[0])
+        it, _ = s.run_3d_step()
+        runs.append((it, [s.e.store(j) for j in (1, deck.nz // 2, deck.nz)], s))
+    (ia, ea, sa), (ib, eb, sb) = runs
+    assert abs(float(ia.mean()) - float(ib.mean())) < 0.5
+    for x, y in zip(ea, eb):
+        assert field_errors(x, y, floor_rel=1e-3).max() < 1e-4
+    sa.close()
+    sb.close()
