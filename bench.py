@@ -512,6 +512,7 @@ def run_ours(args):
     }
     if err is not None:
         line["max_mode_err"] = err["max"]
+        line["max_mode_err_vs_field"] = err.get("max_vs_field")
         line["mode_err"] = err
     if learned is not None:
         line["learned_guess"] = learned

@@ -422,6 +422,10 @@ int qpad_set_guess_extrapolation(qpad_ctx* ctx, int order, double weight);
 /* Which parts of the guess are applied (bit 0: B-perp, bit 1: the J-perp predictor; both by
  * default) and the weight w in [0, 1] of the net's correction: guess = carried + w (net - carried). */
 int qpad_guess_config(qpad_ctx* ctx, int apply, double weight);
+/* Runs the configured initial guess of slice j (3 <= j <= nz) from the 3D stores of the
+ * step before, as the slice loop does at the start of slice j, and leaves it in the b_spe and
+ * cu slice fields (no counterpart in the reference; for tests and diagnostics). */
+int qpad_guess_apply(qpad_ctx* ctx, int j);
 /* One training sample of mode m at slice j (3 <= j <= nz) from the 3D stores of the last
  * step: inputs x [10 or 20][nr], targets t [4 or 8][nr], both in units of *scale. */
 int qpad_guess_sample(qpad_ctx* ctx, int j, int m, float* x, float* t, float* scale);

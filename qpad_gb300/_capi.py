@@ -162,6 +162,7 @@ _SIGS = {
     "qpad_lasers_advance": (C.c_int, [C.c_void_p]),
     "qpad_set_launch_shapes": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "qpad_set_graph_unroll": (C.c_int, [C.c_void_p, C.c_int]),
+    "qpad_guess_apply": (C.c_int, [C.c_void_p, C.c_int]),
     "qpad_species_set_radial_ppc": (C.c_int, [C.c_void_p, C.c_int32]),
     "qpad_h5_write_grid": (C.c_int, [C.c_char_p, C.c_char_p, D, C.c_int, C.c_int, C.c_void_p]),
     "qpad_h5_write_particles": (C.c_int, [C.c_char_p, C.c_char_p, D, D, D, C.c_int64, C.c_int, C.c_double,

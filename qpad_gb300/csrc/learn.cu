@@ -608,6 +608,271 @@ __global__ void __launch_bounds__(256) k_guess_out(GridDev G, GuessStores S, con
   }
 }
 
+// Inputs of the fused guess: every mode's raw (unnormalised) input channels X[ch][x], one
+// CTA per (mode, channel, block of kInNodes nodes) with four nodes per thread, and per CTA
+// the partial sum of squares of its inputs (the RMS scale of a mode is formed from its
+// 20 x nxb partials, in order, where the net reads them; m = 0 has 10 channels and the
+// CTAs of channels 10..19 write a zero partial).
+static constexpr int kInNodes = 1024;
+__global__ void __launch_bounds__(256) k_guess_in_raw(GridDev G, GuessStores S, const int* __restrict__ jp, int nxb,
+                                                      float* __restrict__ X0, float* __restrict__ X1, int ldx1,
+                                                      double* __restrict__ part) {
+  const int j = *jp;
+  if (j < 3) return;
+  const int xb = blockIdx.x % nxb, ch = (blockIdx.x / nxb) % 20, m = blockIdx.x / (20 * nxb);
+  const int nr = G.nr, nh = m == 0 ? 1 : 2, cin = 10 * nh;
+  double ss = 0.0;
+  if (ch < cin) {
+    float* X = m == 0 ? X0 : X1 + (size_t)(m - 1) * nr;
+    const int ldx = m == 0 ? nr : ldx1;
+    double v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int x = xb * kInNodes + k * 256 + (int)threadIdx.x;
+      v[k] = x < nr ? guess_raw_in(G, S, j, m, ch, x + 1) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int x = xb * kInNodes + k * 256 + (int)threadIdx.x;
+      if (x < nr) X[(size_t)ch * ldx + x] = (float)v[k];
+      ss += v[k] * v[k];
+    }
+  }
+  __shared__ double red[8];
+  for (int off = 16; off > 0; off >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    part[blockIdx.x] = tot;
+  }
+}
+
+// ---- fused inference: the whole net over one radial tile in shared memory ---------------
+// One CTA takes a tile of kNetTile output nodes of one mode at a time (net0 for m = 0, net1
+// for m >= 1, each CTA staging one net's weights once) and keeps every layer's activations
+// in shared memory: the input channels on the tile and a halo of 2 nodes per layer on each
+// side (rows outside the radial grid are zero, as the zero padding of every convolution),
+// four BF16 tensor-core GEMMs (mma.sync m16n8k16, FP32 accumulation) with bias and GELU in
+// their epilogues, and the guess applied to b_spe / cu as k_guess_out does.  The weights are
+// BF16 copies of the FP32 master weights, packed once per attach (k_pack_net) as
+// [co][tap * cin_pad + ci], so that a 16-wide K step is 16 channels of one tap.
+static constexpr int kNetTile = 64;                 // output nodes per tile
+static constexpr int kNetRows = kNetTile + 32;      // rows each layer computes (12 n8 tiles)
+static constexpr int kNetBuf = kNetTile + 40;       // rows of an activation buffer
+static constexpr int kNetWidth = 64, kNetLayers = 4, kNetK = 5;
+static constexpr int kActStride = kNetWidth + 8;    // BF16 per activation row (+8: banks spread)
+static constexpr int kNetThreads = 512;
+static constexpr int kNetPairs = (4 * (kNetRows / 8) + kNetThreads / 32 - 1) / (kNetThreads / 32);   // MMA tiles per warp
+static constexpr int kNetInPer = (kNetBuf * 32 + kNetThreads - 1) / kNetThreads;   // input loads per thread
+static constexpr int kMaxGuessParts = 256;                                      // k_guess_in_raw CTAs per mode
+
+struct NetBlock {                   // one net's packed weights
+  const __nv_bfloat16* w[kNetLayers];  // [co_pad][kp], k = tap * cin_pad + ci
+  const float* b[kNetLayers];          // [co_pad]
+  int cin_pad[kNetLayers], co_pad[kNetLayers], kp[kNetLayers];
+  int cin, cout;
+};
+
+__host__ __device__ inline int net_cin_pad(int c) { return (c + 15) / 16 * 16; }
+
+// packs layer l of an FP32 parameter block (W [co][ci * K + tap], then b [co]) into the
+// BF16 layout of NetBlock (zero in the padding), with the rounding of the unfused GEMMs
+__global__ void k_pack_net(const float* __restrict__ W, const float* __restrict__ bias, int ci, int co, int K,
+                           int cin_pad, int co_pad, int kp, __nv_bfloat16* __restrict__ w16, float* __restrict__ b32) {
+  const int n = co_pad * kp;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int o = q / kp, k = q % kp, tap = k / cin_pad, c = k % cin_pad;
+    const float v = (o < co && tap < K && c < ci) ? W[(size_t)o * ci * K + c * K + tap] : 0.0f;
+    w16[q] = __float2bfloat16_rn(v);
+  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < co_pad; q += gridDim.x * blockDim.x)
+    b32[q] = q < co ? bias[q] : 0.0f;
+}
+
+__device__ __forceinline__ uint32_t lds32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// n8 row tiles layer l computes: the rows the layers after it read (kNetTile + 4 (3 - l)),
+// rounded up to whole tiles.  Rows past them hold values of an earlier tile (finite), which
+// reach only rows the next layer does not need.
+__host__ __device__ constexpr int net_tiles(int l) { return (kNetTile + 4 * (kNetLayers - 1 - l) + 7) / 8; }
+
+// One layer: out rows r (0 .. kNetRows) from in rows r .. r + 4.  The (m16 channel tile, n8
+// row tile) pairs go round-robin to the warps; with 1 or 4 channel tiles and 16 warps a warp
+// keeps one channel tile (its A fragments serve all its pairs).
+template <bool kLast>
+__device__ __forceinline__ void net_layer(const __nv_bfloat16* in, const __nv_bfloat16* w, const float* bias,
+                                          int cin_pad, int co_pad, int kp, int cout, __nv_bfloat16* out,
+                                          float* ys, int row_node0, int nr, int nnt) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, q = lane & 3;
+  const int nmt = co_pad / 16;
+  const int npair = nmt * nnt, nw = kNetThreads / 32;
+  const int mt = warp % nmt;
+  // this warp's row tiles and their B-fragment rows (fixed for the layer)
+  int np = 0;
+  const __nv_bfloat16* brow[kNetPairs];
+  int ntile[kNetPairs];
+#pragma unroll
+  for (int k = 0; k < kNetPairs; ++k) {
+    const int pr = warp + k * nw;
+    ntile[k] = pr < npair ? pr / nmt : 0;
+    np += pr < npair ? 1 : 0;
+    brow[k] = in + (size_t)(ntile[k] * 8 + g) * kActStride + 2 * q;
+  }
+  float acc[kNetPairs][4];
+#pragma unroll
+  for (int k = 0; k < kNetPairs; ++k)
+#pragma unroll
+    for (int h = 0; h < 4; ++h) acc[k][h] = 0.0f;
+  const __nv_bfloat16* wr0 = w + (size_t)(mt * 16 + g) * kp + 2 * q;
+  const __nv_bfloat16* wr1 = wr0 + 8 * kp;
+  for (int tap = 0; tap < kNetK; ++tap) {
+#pragma unroll 2
+    for (int c0 = 0; c0 < cin_pad; c0 += 16) {
+      const int k0 = tap * cin_pad + c0, boff = tap * kActStride + c0;
+      uint32_t af[4];
+      af[0] = lds32(wr0 + k0);
+      af[1] = lds32(wr1 + k0);
+      af[2] = lds32(wr0 + k0 + 8);
+      af[3] = lds32(wr1 + k0 + 8);
+#pragma unroll
+      for (int k = 0; k < kNetPairs; ++k) {
+        if (k >= np) break;
+        uint32_t bf[2];
+        bf[0] = lds32(brow[k] + boff);
+        bf[1] = lds32(brow[k] + boff + 8);
+        mma_bf16(acc[k], af, bf);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kNetPairs; ++k) {
+    if (k >= np) break;
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const int co = mt * 16 + g + (h >= 2 ? 8 : 0), r = ntile[k] * 8 + 2 * q + (h & 1);
+      const float v = acc[k][h] + bias[co];
+      if (kLast) {
+        if (co < cout && r < kNetTile) ys[co * kNetTile + r] = v;
+      } else {
+        const int x = row_node0 + r;                     // radial node (0-based) of this row
+        out[(size_t)r * kActStride + co] = __float2bfloat16_rn((x >= 0 && x < nr) ? gelu(v) : 0.0f);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kNetThreads, 1) k_guess_net(GridDev G, GuessStores S, const int* __restrict__ jp,
+                                                             NetBlock n0, NetBlock n1, int g0,
+                                                             const float* __restrict__ X0, const float* __restrict__ X1,
+                                                             int ldx1, const double* __restrict__ part, int nb,
+                                                             double* __restrict__ b_spe, double* __restrict__ cu,
+                                                             int apply, double weight) {
+  const int j = *jp;
+  if (j < 3) return;
+  extern __shared__ __align__(16) unsigned char nsm[];
+  const bool first = (int)blockIdx.x < g0;
+  const NetBlock& N = first ? n0 : n1;
+  const int nr = G.nr, T = (nr + kNetTile - 1) / kNetTile;
+  const int ntiles = first ? T : G.M * T;
+  const int cta = first ? (int)blockIdx.x : (int)blockIdx.x - g0, ncta = first ? g0 : (int)gridDim.x - g0;
+  // shared memory: the layers' weights and biases, two activation buffers, the outputs
+  __nv_bfloat16* wl[kNetLayers];
+  float* bl[kNetLayers];
+  size_t off = 0;
+#pragma unroll
+  for (int l = 0; l < kNetLayers; ++l) {
+    wl[l] = reinterpret_cast<__nv_bfloat16*>(nsm + off);
+    off += (size_t)N.co_pad[l] * N.kp[l] * 2;
+    bl[l] = reinterpret_cast<float*>(nsm + off);
+    off += (size_t)N.co_pad[l] * 4;
+  }
+  __nv_bfloat16* act[2];
+  act[0] = reinterpret_cast<__nv_bfloat16*>(nsm + off);
+  off += (size_t)kNetBuf * kActStride * 2;
+  act[1] = reinterpret_cast<__nv_bfloat16*>(nsm + off);
+  off += (size_t)kNetBuf * kActStride * 2;
+  float* ys = reinterpret_cast<float*>(nsm + off);   // [cout][kNetTile]
+  __shared__ double s_part[kMaxGuessParts];
+  // the weights by 16-byte asynchronous copies, all in flight together (every block is a
+  // multiple of 16 bytes at a 16-byte aligned offset)
+#pragma unroll
+  for (int l = 0; l < kNetLayers; ++l) {
+    const int nv = N.co_pad[l] * N.kp[l] / 8;
+    const char* src = reinterpret_cast<const char*>(N.w[l]);
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(wl[l]);
+    for (int v = threadIdx.x; v < nv; v += blockDim.x)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst + 16u * v), "l"(src + 16 * (size_t)v)
+                   : "memory");
+    for (int v = threadIdx.x; v < N.co_pad[l]; v += blockDim.x) bl[l][v] = N.b[l][v];
+  }
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+  for (int v = threadIdx.x; v < 2 * kNetBuf * kActStride / 8; v += blockDim.x)   // rows never written stay 0
+    reinterpret_cast<uint4*>(act[0])[v] = make_uint4(0u, 0u, 0u, 0u);
+  __syncthreads();
+  for (int tile = cta; tile < ntiles; tile += ncta) {
+    const int m = first ? 0 : 1 + tile / T, x0 = (tile % T) * kNetTile;
+    const int nh = m == 0 ? 1 : 2;
+    const float* X = m == 0 ? X0 : X1 + (size_t)(m - 1) * nr;
+    const int ldx = m == 0 ? nr : ldx1;
+    // the inputs' RMS over the mode (k_guess_in's scale, from the partial sums, loaded
+    // together and added in order)
+    if ((int)threadIdx.x < nb) s_part[threadIdx.x] = part[m * nb + threadIdx.x];
+    // input rows r <-> node x0 - 8 + r, channels ci < cin (zero beyond, and off the grid):
+    // every thread's loads in flight together
+    const int cp0 = N.cin_pad[0], nin = kNetBuf * cp0;
+    float xin[kNetInPer];
+#pragma unroll
+    for (int k = 0; k < kNetInPer; ++k) {
+      const int q = (int)threadIdx.x + k * kNetThreads, r = q / cp0, c = q % cp0, x = x0 - 8 + r;
+      xin[k] = (q < nin && c < N.cin && x >= 0 && x < nr) ? X[(size_t)c * ldx + x] : 0.0f;
+    }
+    __syncthreads();
+    double tot = 0.0;
+    for (int b = 0; b < nb; ++b) tot += s_part[b];
+    const double scd = sqrt(tot / (double)(10 * nh * nr)) + 1e-30;
+    const float s_inv = (float)(1.0 / scd);
+#pragma unroll
+    for (int k = 0; k < kNetInPer; ++k) {
+      const int q = (int)threadIdx.x + k * kNetThreads;
+      if (q < nin) act[0][(size_t)(q / cp0) * kActStride + q % cp0] = __float2bfloat16_rn(xin[k] * s_inv);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int l = 0; l < kNetLayers - 1; ++l) {
+      net_layer<false>(act[l & 1], wl[l], bl[l], N.cin_pad[l], N.co_pad[l], N.kp[l], N.co_pad[l], act[(l + 1) & 1],
+                       nullptr, x0 - 8 + 2 * (l + 1), nr, net_tiles(l));
+      __syncthreads();
+    }
+    net_layer<true>(act[1], wl[3], bl[3], N.cin_pad[3], N.co_pad[3], N.kp[3], N.cout, nullptr, ys, x0, nr, net_tiles(3));
+    __syncthreads();
+    // the guess of slice j on this tile's nodes (k_guess_out's rule)
+    const double sc = (double)(float)scd;
+    for (int q = threadIdx.x; q < 2 * nh * kNetTile; q += blockDim.x) {
+      const int ch = q / kNetTile, xl = q % kNetTile, x = x0 + xl, i = x + 1;
+      if (x >= nr) continue;
+      const int c = ch / nh, h = ch % nh, p = h == 0 ? part_re(m) : part_im(m);
+      if (apply & 1)
+        b_spe[fidx(G.ld, 3, p, c, i)] = 2.0 * st2(G, S.b2, 3, j - 1, p, c, i) - st2(G, S.b2, 3, j - 2, p, c, i) +
+                                        (i == 1 ? 0.0 : weight * sc * (double)ys[ch * kNetTile + xl]);
+      if (i == 1) continue;
+      if (apply & 2) {
+        const double carried = cu[fidx(G.ld, 3, p, c, i)];
+        const double net = st2(G, S.cu2, 3, j - 1, p, c, i) + G.dxi * sc * (double)ys[(2 * nh + ch) * kNetTile + xl];
+        cu[fidx(G.ld, 3, p, c, i)] = carried + weight * (net - carried);
+      }
+    }
+    __syncthreads();                                 // before the next tile overwrites the buffers
+  }
+}
+
+size_t net_smem_bytes(const NetBlock& N) {
+  size_t off = 0;
+  for (int l = 0; l < kNetLayers; ++l) off += (size_t)N.co_pad[l] * N.kp[l] * 2 + (size_t)N.co_pad[l] * 4;
+  return off + 2 * (size_t)kNetBuf * kActStride * 2 + (size_t)N.cout * kNetTile * 4;
+}
+
 }  // namespace qpad
 
 struct qpad_guess_state {
@@ -617,6 +882,13 @@ struct qpad_guess_state {
   float* scale = nullptr;         // [M+1]
   int apply = 1;                  // bit 0: B-perp guess, bit 1: J-perp predictor
   double weight = 1.0;            // fraction of the net's correction that is applied
+  bool fused = false;             // nets of the fused kernel's shape: one k_guess_net launch
+  void* packed = nullptr;         // both nets' BF16 weights and biases (NetBlock layout)
+  qpad::NetBlock nets[2];
+  size_t smem = 0;                // k_guess_net's dynamic shared memory
+  int nsm = 0;                    // SMs of the device
+  double* part = nullptr;         // k_guess_in_raw's partial sums [M+1][nb]
+  int nb = 1;                     // its CTAs per mode
 };
 
 namespace qpad {
@@ -630,6 +902,8 @@ void guess_free(qpad_ctx* ctx) {
   free_bufs(ctx->guess->b0);
   free_bufs(ctx->guess->b1);
   if (ctx->guess->scale) cudaFree(ctx->guess->scale);
+  if (ctx->guess->packed) cudaFree(ctx->guess->packed);
+  if (ctx->guess->part) cudaFree(ctx->guess->part);
   delete ctx->guess;
   ctx->guess = nullptr;
 }
@@ -669,6 +943,25 @@ int guess_enqueue(qpad_ctx* ctx) {
   if (!g) return 0;
   const GridDev& G = ctx->g;
   const int nr = G.nr, M = G.M;
+  if (g->fused) {
+    prof_begin(ctx, "guess_in");
+    k_guess_in_raw<<<(M + 1) * g->nb, 256, 0, ctx->stream>>>(G, guess_stores(ctx), ctx->d_j, g->nb / 20, g->b0.act,
+                                                              g->b1.act, M * nr, g->part);
+    prof_end(ctx, "guess_in");
+    // net0's tiles and net1's (M per radial tile) over at most one CTA per SM, split in
+    // proportion to their tile counts
+    const int T = (nr + kNetTile - 1) / kNetTile, tot = T * (M + 1);
+    const int nsm = g->nsm;
+    const int grid = std::max(2, std::min(tot, std::max(nsm, 2)));
+    int g0 = M >= 1 ? std::max(1, std::min(T, (int)((int64_t)grid * T / tot))) : grid;
+    if (M >= 1 && g0 >= grid) g0 = grid - 1;
+    prof_begin(ctx, "guess_net");
+    k_guess_net<<<M >= 1 ? grid : g0, kNetThreads, g->smem, ctx->stream>>>(
+        G, guess_stores(ctx), ctx->d_j, g->nets[0], g->nets[M >= 1 ? 1 : 0], g0, g->b0.act, g->b1.act, M * nr,
+        g->part, g->nb, ctx->f[QPAD_F_B_SPE], ctx->f[QPAD_F_CU], g->apply, g->weight);
+    prof_end(ctx, "guess_net");
+    return check_launch(ctx, "guess", 2);
+  }
   k_guess_in<<<M + 1, 256, 0, ctx->stream>>>(G, guess_stores(ctx), ctx->d_j, 0, -1, g->b0.act, g->b1.act,
                                              M * nr, g->scale, nullptr);
   int n = 1;
@@ -682,6 +975,62 @@ int guess_enqueue(qpad_ctx* ctx) {
 }
 
 }  // namespace qpad
+
+namespace {
+// BF16 copies of the attached nets for k_guess_net when both have its shape (width 64, 4
+// layers, kernel 5); otherwise the guess runs the per-layer kernels.
+int pack_nets(qpad_ctx* ctx, qpad_guess_state* g) {
+  const qpad_learn* nets[2] = {g->net0, g->net1 ? g->net1 : g->net0};
+  for (const qpad_learn* L : nets)
+    if (L->width != kNetWidth || L->layers != kNetLayers || L->ksize != kNetK || L->cout > 16) return 0;
+  size_t bytes = 0;
+  for (int k = 0; k < 2; ++k) {
+    NetBlock& N = g->nets[k];
+    N.cin = nets[k]->cin;
+    N.cout = nets[k]->cout;
+    for (int l = 0; l < kNetLayers; ++l) {
+      N.cin_pad[l] = net_cin_pad(nets[k]->ci[l]);
+      N.co_pad[l] = nets[k]->co[l] > 16 ? net_cin_pad(nets[k]->co[l]) : 16;
+      N.kp[l] = kNetK * N.cin_pad[l] + 8;
+      if (N.co_pad[l] != 16 && N.co_pad[l] != 64) return 0;
+      bytes += (size_t)N.co_pad[l] * N.kp[l] * 2 + (size_t)N.co_pad[l] * 4;
+    }
+  }
+  if (int r = cuda_check(ctx, cudaMalloc(&g->packed, bytes), "packed guess nets")) return r;
+  g->nb = 20 * ((ctx->g.nr + kInNodes - 1) / kInNodes);       // k_guess_in_raw's partials per mode
+  if (g->nb > kMaxGuessParts) {                                 // (radial grids above 12800 nodes)
+    cudaFree(g->packed);
+    g->packed = nullptr;
+    return 0;
+  }
+  if (int r = cuda_check(ctx, cudaMalloc(&g->part, sizeof(double) * (ctx->g.M + 1) * g->nb), "guess partials"))
+    return r;
+  size_t off = 0;
+  for (int k = 0; k < 2; ++k) {
+    NetBlock& N = g->nets[k];
+    for (int l = 0; l < kNetLayers; ++l) {
+      __nv_bfloat16* w = reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(g->packed) + off);
+      off += (size_t)N.co_pad[l] * N.kp[l] * 2;
+      float* b = reinterpret_cast<float*>(static_cast<char*>(g->packed) + off);
+      off += (size_t)N.co_pad[l] * 4;
+      k_pack_net<<<64, 256, 0, ctx->stream>>>(nets[k]->param + nets[k]->woff[l], nets[k]->param + nets[k]->boff[l],
+                                                nets[k]->ci[l], nets[k]->co[l], kNetK, N.cin_pad[l], N.co_pad[l],
+                                                N.kp[l], w, b);
+      N.w[l] = w;
+      N.b[l] = b;
+    }
+  }
+  if (int r = check_launch(ctx, "k_pack_net", 2 * kNetLayers)) return r;
+  g->smem = std::max(net_smem_bytes(g->nets[0]), net_smem_bytes(g->nets[1]));
+  if (int r = raise_dyn_smem(ctx, (const void*)k_guess_net, g->smem)) return r;
+  if (int r = cuda_check(ctx, cudaDeviceGetAttribute(&g->nsm, cudaDevAttrMultiProcessorCount, ctx->device), "SMs"))
+    return r;
+  // the nets' parameters are read on their own streams: finish the copies before returning
+  if (int r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "pack guess nets")) return r;
+  g->fused = true;
+  return 0;
+}
+}  // namespace
 
 extern "C" int qpad_guess_attach(qpad_ctx* ctx, qpad_learn* net0, qpad_learn* net1) {
   if (!ctx) return QPAD_E_ARG;
@@ -703,6 +1052,7 @@ extern "C" int qpad_guess_attach(qpad_ctx* ctx, qpad_learn* net0, qpad_learn* ne
   int r = alloc_bufs(net0, g->b0, nr, false) ? set_err(ctx, QPAD_E_NOMEM, "guess buffers") : 0;
   if (!r && M >= 1 && alloc_bufs(net1, g->b1, (int64_t)M * nr, false)) r = set_err(ctx, QPAD_E_NOMEM, "guess buffers");
   if (!r) r = cuda_check(ctx, cudaMalloc(&g->scale, sizeof(float) * (M + 1)), "guess scale");
+  if (!r) r = pack_nets(ctx, g);
   if (r) guess_free(ctx);
   return r;
 }
@@ -749,6 +1099,15 @@ extern "C" int qpad_guess_samples(qpad_ctx* ctx, int j_lo, int j_hi, int m, floa
   if (!r) r = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "guess samples");
   cudaFree(d);
   return r;
+}
+
+extern "C" int qpad_guess_apply(qpad_ctx* ctx, int j) {
+  if (!ctx || j < 3 || j > ctx->g.nz)
+    return ctx ? set_err(ctx, QPAD_E_ARG, "guess apply: needs 3 <= j <= nz") : QPAD_E_ARG;
+  if (!ctx->guess && ctx->extrap == 0) return set_err(ctx, QPAD_E_STATE, "guess apply: no guess configured");
+  if (int r = launch_set_slice(ctx, j)) return r;
+  if (int r = guess_enqueue(ctx)) return r;
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "guess apply");
 }
 
 extern "C" int qpad_set_guess_extrapolation(qpad_ctx* ctx, int order, double weight) {

@@ -6,7 +6,9 @@ field, azimuthal mode m and component, the relative L2 norm of the difference ov
 together as one complex amplitude.  Modes whose reference norm is below 1e-6 of the
 component's norm over all modes hold round-off only (for instance the odd modes of an axially
 symmetric case) and are not rated.  The slice contributing most to the squared error is
-reported beside each figure.
+reported beside each figure.  Beside the per-mode figure, the same error relative to the
+component's norm over all modes says how large it is in the field itself: a mode that holds
+only particle noise can carry an O(1) relative error that is a tiny part of the field.
 """
 from __future__ import annotations
 
@@ -20,20 +22,23 @@ ERROR_FIELDS = ("psi", "e", "b", "cu", "q_spe")
 
 def mode_errors(got: np.ndarray, ref: np.ndarray, max_mode: int, floor: float = 1e-6) -> dict:
     """{(m, component): (relative L2 error, worst slice 1-based, its share of the squared
-    error)} for two stores shaped (nz, P, ncomp, nr+2)."""
+    error, the error relative to the component's norm over all modes)} for two stores
+    shaped (nz, P, ncomp, nr+2)."""
     out = {}
     for m in range(max_mode + 1):
         parts = [0] if m == 0 else [2 * m - 1, 2 * m]
         for c in range(ref.shape[2]):
             r = ref[:, parts, c, 1:]
             nrm = float(np.linalg.norm(r))
-            if not nrm > floor * float(np.linalg.norm(ref[:, :, c, 1:])):
+            nrm_all = float(np.linalg.norm(ref[:, :, c, 1:]))
+            if not nrm > floor * nrm_all:
                 continue
             d = got[:, parts, c, 1:] - r
             per = np.einsum("spi,spi->s", d, d)
             tot = float(per.sum())
             s = int(np.argmax(per))
-            out[(m, c)] = (float(np.sqrt(tot)) / nrm, s + 1, float(per[s] / tot) if tot > 0 else 0.0)
+            out[(m, c)] = (float(np.sqrt(tot)) / nrm, s + 1, float(per[s] / tot) if tot > 0 else 0.0,
+                           float(np.sqrt(tot)) / nrm_all)
     return out
 
 
@@ -47,10 +52,14 @@ def step_error_report(got: dict, ref: dict, max_mode: int) -> dict:
         for (m, c), v in mode_errors(got[name], ref[name], max_mode).items():
             per[f"{name}[{c}] m={m}"] = v
     if not per:
-        return {"max": None, "worst": None, "worst_slice": None, "per_mode": {}}
+        return {"max": None, "worst": None, "worst_slice": None, "per_mode": {}, "max_vs_field": None,
+                "worst_vs_field": None}
     key = max(per, key=lambda k: per[k][0])
+    kf = max(per, key=lambda k: per[k][3])
     return {"max": per[key][0], "worst": key, "worst_slice": per[key][1],
-            "per_mode": {k: float(f"{v[0]:.4g}") for k, v in per.items()}}
+            "per_mode": {k: float(f"{v[0]:.4g}") for k, v in per.items()},
+            "max_vs_field": per[kf][3], "worst_vs_field": kf,
+            "per_mode_vs_field": {k: float(f"{v[3]:.4g}") for k, v in per.items()}}
 
 
 def fp32_state(pl, dr):

@@ -153,9 +153,11 @@ WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
 
 
 def weights_path(max_mode: int) -> str:
-    """Trained weights for simulations with `max_mode` modes: guess_c2.npz (trained on
-    c2-shaped runs, M = 2) serves M <= 2, guess_c5.npz (c5-shaped runs, M = 4) larger M."""
-    return os.path.join(WEIGHTS, "guess_c2.npz" if max_mode <= 2 else "guess_c5.npz")
+    """Trained weights for simulations with `max_mode` modes: guess_c5.npz (trained on
+    c5-shaped runs, M = 4) for M > 2 when it exists, else guess_c2.npz (trained on c2-shaped
+    runs, M = 2).  The m >= 1 net takes one mode at a time, so it serves any number of modes."""
+    c5 = os.path.join(WEIGHTS, "guess_c5.npz")
+    return c5 if max_mode > 2 and os.path.exists(c5) else os.path.join(WEIGHTS, "guess_c2.npz")
 
 
 def save(path, net0: ConvNet, net1: ConvNet | None):

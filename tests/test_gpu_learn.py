@@ -159,3 +159,47 @@ def test_trained_guess_effect_on_iterations(record_property):
     assert ib.max() <= d.iter_max
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("nr,M", [(150, 2), (64, 1), (40, 0)])
+def test_fused_guess_matches_the_per_layer_forward(nr, M):
+    """The guess kernel (the whole net of a radial tile in shared memory, one launch for every
+    mode) against the nets' per-layer forward (qpad_learn_predict) on the same inputs: the
+    extrapolated part to round-off, the nets' correction within the BF16 rounding of the
+    activations; on ragged tiles (nr = 150 is two full tiles and a partial one)."""
+    import ctypes as C
+    d = Q.decks.Deck("guess_fused", nr=nr, nz=12, max_mode=M, dr=0.04, dxi=0.04, ppc=(2, 1), num_theta=8,
+                     uth=2e-3, seed=4, beams=[Q.decks.BeamSpec(3.0, 0.4, 0.3, 0.4, 20000, x0=0.05)],
+                     iter_max=30, iter_reltol=1e-6)
+    sim = Q.build_simulation(d)
+    sim.run_3d_step()
+    nets = [LR.ConvNet(*LR.CHANNELS[0], seed=11), LR.ConvNet(*LR.CHANNELS[1], seed=12) if M >= 1 else None]
+    for n in nets:                      # last layers at full scale, so the correction is not small
+        if n is not None:
+            p = n.get_params()
+            n.set_params(p * np.float32(3.0))
+    LR.attach(sim, *nets)
+    LR.configure(sim, apply_b=True, apply_j=True)
+    j = 7
+    cu_before = sim.cu.download().copy()
+    l0 = sim.launch_count()
+    sim._check(sim.lib.qpad_guess_apply(sim.h, j))
+    assert sim.launch_count() - l0 == 3        # slice index, inputs, the fused net
+    b_got, cu_got = sim.b_spe.download(), sim.cu.download()
+    b1, b2, cu1 = sim.b_spe.store(j - 1), sim.b_spe.store(j - 2), sim.cu.store(j - 1)
+    for m in range(M + 1):
+        parts = [0] if m == 0 else [2 * m - 1, 2 * m]
+        nh = len(parts)
+        x, _, sc = LR.samples(sim, m, [j])
+        y = nets[0 if m == 0 else 1].predict(x)[0].astype(np.float64) * float(sc[0])
+        for h, p in enumerate(parts):
+            for c in range(2):
+                ext = 2 * b1[p, c, 1:-1] - b2[p, c, 1:-1]
+                want = ext + np.where(np.arange(nr) == 0, 0.0, y[c * nh + h])
+                got = b_got[p, c, 1:-1]
+                assert rel_l2(got[:1], ext[:1]) < 1e-12 or abs(got[0] - ext[0]) < 1e-14
+                assert rel_l2(got - ext, want - ext) < 1e-2, (m, p, c)
+                cj = cu1[p, c, 2:-1] + d.dxi * y[2 * nh + c * nh + h][1:]
+                assert rel_l2(cu_got[p, c, 2:-1] - cu_before[p, c, 2:-1], cj - cu_before[p, c, 2:-1]) < 1e-2
+    LR.attach(sim, None, None)
+    sim.close()
