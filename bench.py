@@ -317,6 +317,7 @@ def run_batch(args):
     tune = [s.autotune(reps=10) for s in sims]
     pushes = sum(s.species[0].count() * d.nz for s, d in zip(sims, decks))
     batch = Q.Batch(sims)
+    btune = batch.autotune(reps=1) if not args.no_autotune else None
     for _ in range(args.warmup):
         for s in sims:
             s.species[0].reset()
@@ -352,7 +353,7 @@ def run_batch(args):
         "iters_per_slice": float(np.mean(iters)),
         "timing": "host wall clock around qpad_batch_step, which synchronises every simulation",
         "autotune": {"iter_cluster": sorted({t["iter_cluster"] for t in tune}),
-                     "item_ppl": sorted({t["item_ppl"] for t in tune})},
+                     "item_ppl": sorted({t["item_ppl"] for t in tune}), "batch": btune},
         "clocks": clk.summary(),
     }
     if seq is not None:

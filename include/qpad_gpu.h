@@ -301,6 +301,18 @@ int qpad_batch_destroy(qpad_batch* batch);
 const char* qpad_batch_last_error(const qpad_batch* batch);
 /* stats[i] receives context i's nz per-slice statistics (stats or stats[i] may be null) */
 int qpad_batch_step(qpad_batch* batch, int push_beams, qpad_slice_stats* const* stats);
+/* Autotuner of a batch's launch shapes (no counterpart in the reference): times `reps` whole
+ * batch steps (beams not pushed; every species renewed from its uploaded particles before
+ * each step and at the end) for each cluster policy of the iteration kernels (0: the smallest
+ * cluster that fits each grid, the default of qpad_batch_step; c = 4, 8, 16: each
+ * simulation's own shape capped at c CTAs) and iterations per loop body (1, 2, 4), and keeps
+ * the fastest.  The 3D stores hold the last timed step's fields afterwards. */
+typedef struct qpad_batch_tune_result {
+  int32_t policy;             /* 0 or the cluster cap */
+  int32_t unroll;             /* iterations per body of the iteration loops */
+  double step_ms;             /* the fastest batch step (host clock, milliseconds) */
+} qpad_batch_tune_result;
+int qpad_batch_autotune(qpad_batch* batch, int reps, qpad_batch_tune_result* out);
 
 /* ---- autotuner (no counterpart in the reference) ---------------------------------------
  * Times the launch shapes this context can use on this GPU and keeps the fastest: the

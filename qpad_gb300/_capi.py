@@ -42,6 +42,10 @@ class TuneResult(C.Structure):
                 ("deposit_us", C.c_double)]
 
 
+class BatchTuneResult(C.Structure):
+    _fields_ = [("policy", C.c_int32), ("unroll", C.c_int32), ("step_ms", C.c_double)]
+
+
 class LaserDesc(C.Structure):
     _fields_ = [("k0", C.c_double), ("iter", C.c_int32)]
 
@@ -181,6 +185,7 @@ _SIGS = {
     "qpad_batch_last_error": (C.c_char_p, [C.c_void_p]),
     "qpad_batch_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.POINTER(SliceStats))]),
     "qpad_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(TuneResult)]),
+    "qpad_batch_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(BatchTuneResult)]),
     "qpad_rng_seed": (None, [C.POINTER(Rng), C.c_uint64]),
     "qpad_load_plasma": (C.c_int64, [C.c_int, C.c_double, C.POINTER(Rng), C.c_int, C.c_int, C.c_int, C.c_double,
                                      C.c_double, D, D, D, D, D, D, C.c_int64]),

@@ -347,6 +347,16 @@ class Batch:
             raise QpadError(f"qpad_batch_step failed ({r}): {self.lib.qpad_batch_last_error(self.h).decode()}")
         return [np.array([s.iters for s in b], np.int32) for b in bufs]
 
+    def autotune(self, reps=1) -> dict:
+        """Times whole batch steps under each cluster policy of the iteration kernels and
+        iterations per loop body, and keeps the fastest (qpad_batch_autotune)."""
+        r = K.BatchTuneResult()
+        e = self.lib.qpad_batch_autotune(self.h, int(reps), C.byref(r))
+        if e != 0:
+            raise QpadError(f"qpad_batch_autotune failed ({e}): {self.lib.qpad_batch_last_error(self.h).decode()}")
+        return {"policy": "smallest cluster that fits" if r.policy == 0 else f"own shape capped at {r.policy} CTAs",
+                "unroll": r.unroll, "step_ms": r.step_ms}
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.qpad_batch_destroy(self.h)

@@ -1,6 +1,7 @@
 // capi.cu -- the C ABI (include/qpad_gpu.h): contexts, fields, species, beams and the
 // fused slice / 3D-step drivers of run_simulation (simulation_class.f03:294-512).
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -1422,6 +1423,7 @@ extern "C" int qpad_batch_step(qpad_batch* b, int push_beams, qpad_slice_stats* 
   // a batch is throughput-bound: every simulation's iteration kernel takes the smallest
   // cluster that fits its grid (the most rows per CTA, the fewest CTAs), which the
   // single-simulation autotuner, tuning for latency, does not choose
+  // (qpad_batch_autotune times the other policies and keeps the fastest)
   if (!b->shaped) {
     for (auto* c : b->ctxs) {
       int r = QPAD_E_CUDA;
@@ -1492,6 +1494,79 @@ extern "C" int qpad_batch_step(qpad_batch* b, int push_beams, qpad_slice_stats* 
     }
   }
   return QPAD_OK;
+}
+
+// Launch shapes of a batch: policy 0 gives every simulation's iteration kernel the smallest
+// cluster that fits its grid; policy c > 0 the single-simulation shape (up to 16 CTAs, 32
+// rows each) capped at c CTAs.  `unroll` iterations per body of every iteration loop.
+static int batch_shape(qpad_batch* b, int policy, int unroll) {
+  for (auto* c : b->ctxs) {
+    int r = QPAD_E_CUDA;
+    if (policy == 0) {
+      for (int cl = 1; cl <= 16 && r; cl *= 2) r = iterate_try_cluster(c, cl);
+    } else {
+      const int top = std::min(policy, std::max(1, std::min(16, c->g.nr / 32)));
+      for (int cl = top; cl >= 1 && r; cl /= 2) r = iterate_try_cluster(c, cl);
+    }
+    cudaGetLastError();
+    if (r) {
+      b->err = "no cluster shape of the iteration kernel fits: " + c->err;
+      return r;
+    }
+    c->unroll = unroll;
+  }
+  b->shaped = true;
+  return 0;
+}
+
+// Times whole batch steps (beams not pushed, every species renewed from its uploaded state
+// before each step, so the simulations end where they began) under the cluster policies
+// {smallest fitting, capped at 4, 8, 16} with two iterations per loop body, then 1 and 4
+// iterations per body with the fastest policy, and keeps the fastest.
+extern "C" int qpad_batch_autotune(qpad_batch* b, int reps, qpad_batch_tune_result* out) {
+  if (!b || reps < 1) return QPAD_E_ARG;
+  const auto renew = [&]() -> int {
+    for (auto* c : b->ctxs)
+      for (auto* s : c->species)
+        if (s->np_pristine > 0 || s->neut)
+          if (int r = qpad_species_reset(s)) return r;
+    return 0;
+  };
+  const auto timed = [&](int policy, int unroll, double* ms) -> int {
+    if (int r = batch_shape(b, policy, unroll)) return r;
+    if (int r = renew()) return r;
+    if (int r = qpad_batch_step(b, 0, nullptr)) return r;            // graph build and warm-up
+    double best = 1e300;
+    for (int k = 0; k < reps; ++k) {
+      if (int r = renew()) return r;
+      for (auto* c : b->ctxs)
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) return QPAD_E_CUDA;
+      const auto t0 = std::chrono::steady_clock::now();
+      if (int r = qpad_batch_step(b, 0, nullptr)) return r;            // (synchronises every simulation)
+      best = std::min(best, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+    }
+    *ms = best;
+    return 0;
+  };
+  int best_p = 0, best_u = 2;
+  double best_ms = 1e300;
+  for (int policy : {0, 4, 8, 16}) {
+    double ms = 0.0;
+    if (int r = timed(policy, 2, &ms)) return r;
+    if (ms < best_ms) { best_ms = ms; best_p = policy; }
+  }
+  for (int unroll : {1, 4}) {
+    double ms = 0.0;
+    if (int r = timed(best_p, unroll, &ms)) return r;
+    if (ms < best_ms) { best_ms = ms; best_u = unroll; }
+  }
+  if (int r = batch_shape(b, best_p, best_u)) return r;
+  if (out) {
+    out->policy = best_p;
+    out->unroll = best_u;
+    out->step_ms = best_ms;
+  }
+  return renew();
 }
 
 // =====================================================================================

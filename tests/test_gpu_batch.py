@@ -64,3 +64,24 @@ def test_autotune_keeps_results(precision):
         assert store_errors(gb, ga).max() < tol
     a.close()
     b.close()
+
+
+def test_batch_autotune_keeps_results():
+    """The batch autotuner (cluster policy and iterations per loop body, timed on whole batch
+    steps) leaves the simulations where they were: a batch step after it equals single steps
+    of the same simulations (FP64: identical iteration counts, fields within 1e-9)."""
+    decks = _decks()
+    single = [Q.build_simulation(d) for d in decks]
+    its_single = [s.run_3d_step()[0] for s in single]
+    sims = [Q.build_simulation(d) for d in decks]
+    batch = Q.Batch(sims)
+    tune = batch.autotune(reps=1)
+    assert tune["unroll"] in (1, 2, 4) and tune["step_ms"] > 0.0
+    its_batch = batch.step()
+    for d, a, b, ia, ib in zip(decks, single, sims, its_single, its_batch):
+        assert np.array_equal(ia, ib), (d.name, ia, ib)
+        for f in ("e", "b", "psi"):
+            assert store_errors(b.fields[f].store_all(), a.fields[f].store_all()).max() < 1e-9, (d.name, f)
+    batch.close()
+    for s in single + sims:
+        s.close()
