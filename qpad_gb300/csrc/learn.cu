@@ -795,6 +795,7 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_guess_net(GridDev G, GuessSt
   off += (size_t)kNetBuf * kActStride * 2;
   float* ys = reinterpret_cast<float*>(nsm + off);   // [cout][kNetTile]
   __shared__ double s_part[kMaxGuessParts];
+  __shared__ float s_scale[2];                        // 1 / RMS and RMS of the current tile's mode
   // the weights by 16-byte asynchronous copies, all in flight together (every block is a
   // multiple of 16 bytes at a 16-byte aligned offset)
 #pragma unroll
@@ -829,10 +830,21 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_guess_net(GridDev G, GuessSt
       xin[k] = (q < nin && c < N.cin && x >= 0 && x < nr) ? X[(size_t)c * ldx + x] : 0.0f;
     }
     __syncthreads();
-    double tot = 0.0;
-    for (int b = 0; b < nb; ++b) tot += s_part[b];
-    const double scd = sqrt(tot / (double)(10 * nh * nr)) + 1e-30;
-    const float s_inv = (float)(1.0 / scd);
+    // one warp folds the partials (a fixed order: lane-strided sums, then a shuffle tree) and
+    // forms the scale once; FP64 work repeated by every thread would occupy the SM's few
+    // FP64 units for microseconds
+    if (threadIdx.x < 32) {
+      double tot = 0.0;
+      for (int b = (int)threadIdx.x; b < nb; b += 32) tot += s_part[b];
+      for (int off = 16; off > 0; off >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, off);
+      if (threadIdx.x == 0) {
+        const double scd = sqrt(tot / (double)(10 * nh * nr)) + 1e-30;
+        s_scale[0] = (float)(1.0 / scd);
+        s_scale[1] = (float)scd;
+      }
+    }
+    __syncthreads();
+    const float s_inv = s_scale[0];
 #pragma unroll
     for (int k = 0; k < kNetInPer; ++k) {
       const int q = (int)threadIdx.x + k * kNetThreads;
@@ -848,7 +860,7 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_guess_net(GridDev G, GuessSt
     net_layer<true>(act[1], wl[3], bl[3], N.cin_pad[3], N.co_pad[3], N.kp[3], N.cout, nullptr, ys, x0, nr, net_tiles(3));
     __syncthreads();
     // the guess of slice j on this tile's nodes (k_guess_out's rule)
-    const double sc = (double)(float)scd;
+    const double sc = (double)s_scale[1];
     for (int q = threadIdx.x; q < 2 * nh * kNetTile; q += blockDim.x) {
       const int ch = q / kNetTile, xl = q % kNetTile, x = x0 + xl, i = x + 1;
       if (x >= nr) continue;
