@@ -422,7 +422,9 @@ int qpad_learn_train(qpad_learn* net, const float* x, const float* t, int64_t ns
 /* Replaces the carried initial b_spe (simulation_class.f03:324-326, 360) and the J-perp
  * predictor (:425-426) of every slice j >= 3 by the nets' guess from slices j-1, j-2:
  * net0 (10 -> 4 channels) for m = 0, net1 (20 -> 8) for the modes m >= 1.  The iteration
- * still runs to iter_reltol.  Null net0 detaches.  The nets must outlive the attachment. */
+ * still runs to iter_reltol.  Null net0 detaches.  The nets must outlive the attachment.
+ * Nets of width 64, 4 layers, kernel 5 run as one fused kernel per slice from BF16 copies of
+ * their weights taken here: attach again after changing the weights. */
 int qpad_guess_attach(qpad_ctx* ctx, qpad_learn* net0, qpad_learn* net1);
 /* Initial B-perp guess of every slice from the stored B-perp of the previous slices, without
  * a net (no counterpart in the reference, which carries B-perp(j-1), simulation_class.f03:
