@@ -89,3 +89,24 @@ def test_deck_inputs_skip_beam_behind_short_box():
     deck = Q.decks.c2().scaled(nz=48)
     pl, beams = Q.deck_inputs(deck)
     assert len(beams) == 2 and len(beams[1][2]) == 0 and len(beams[0][2]) > 0
+
+
+def _prototypes():
+    """{name: argument count} of every function the header declares."""
+    txt = open(os.path.join(ROOT, "include", "qpad_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = re.sub(r"//[^\n]*", "", txt)
+    out = {}
+    for m in re.finditer(r"\b(qpad_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_python_bindings_match_header_arity():
+    """Every ctypes declaration takes as many arguments as the header's prototype."""
+    from qpad_gb300 import _capi
+    protos = _prototypes()
+    assert set(protos) == set(_capi.EXPORTED)
+    bad = {n: (protos[n], len(_capi._SIGS[n][1])) for n in protos if protos[n] != len(_capi._SIGS[n][1])}
+    assert not bad, bad
