@@ -659,7 +659,7 @@ __global__ void __launch_bounds__(256) k_guess_in_raw(GridDev G, GuessStores S, 
 // BF16 copies of the FP32 master weights, packed once per attach (k_pack_net) as
 // [co][tap * cin_pad + ci], so that a 16-wide K step is 16 channels of one tap.
 static constexpr int kNetTile = 64;                 // output nodes per tile
-static constexpr int kNetRows = kNetTile + 32;      // rows each layer computes (12 n8 tiles)
+static constexpr int kNetRows = kNetTile + 32;      // bound on the rows a layer computes (net_tiles)
 static constexpr int kNetBuf = kNetTile + 40;       // rows of an activation buffer
 static constexpr int kNetWidth = 64, kNetLayers = 4, kNetK = 5;
 static constexpr int kActStride = kNetWidth + 8;    // BF16 per activation row (+8: banks spread)
