@@ -186,6 +186,10 @@ def run_reference(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": deck.name, "sample_slices": info["slices"]},
             "iters_per_slice": info["iters_per_slice"],
+            # the same work counted per predictor-corrector iteration (a plasma particle through
+            # one iteration of one slice), which does not depend on how many iterations the
+            # sampled slices take
+            "iteration_pushes_per_s": v * info["iters_per_slice"],
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
                              "sample": cs.sample_text(info["slices"])},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -498,6 +502,7 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}",
                    "cpu_sample": f"first {args.cpu_slices} slices (reference arm and cpu_baseline)"},
         "iters_per_slice": r["iters_per_slice"],
+        "iteration_pushes_per_s": r["value"] * r["iters_per_slice"],
         "slices_per_s": world * deck.nz * args.steps / dev_s,
         "beam_pushes_per_s": world * nbeam * args.steps / dev_s,
         "wall_s": r["wall_s"],
@@ -525,6 +530,7 @@ def run_ours(args):
         cs = CpuSample(deck)
         cb = max((cs.run(args.cpu_slices) for _ in range(2)), key=lambda x: x["value"])
         line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": cb["cores"], "kind": "port",
+                                "iteration_pushes_per_s": cb["value"] * cb["iters_per_slice"],
                                 "sample": cs.sample_text(cb["slices"]), "iters_per_slice": cb["iters_per_slice"]}
     if rank == 0:
         print(json.dumps(line), flush=True)

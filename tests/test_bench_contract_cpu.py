@@ -21,6 +21,7 @@ def test_reference_arm_json_line():
               "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in d, k
     assert d["value"] > 0 and d["higher_is_better"] is True and d["config"]["workload"].startswith("c1")
+    assert abs(d["iteration_pushes_per_s"] - d["value"] * d["iters_per_slice"]) <= 1e-9 * d["iteration_pushes_per_s"]
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
