@@ -1533,7 +1533,8 @@ extern "C" int qpad_batch_autotune(qpad_batch* b, int reps, qpad_batch_tune_resu
     return 0;
   };
   const auto timed = [&](int policy, int unroll, double* ms) -> int {
-    if (int r = batch_shape(b, policy, unroll)) return r;
+    *ms = 1e300;
+    if (batch_shape(b, policy, unroll)) return 0;                  // a policy no shape of which fits: skipped
     if (int r = renew()) return r;
     if (int r = qpad_batch_step(b, 0, nullptr)) return r;            // graph build and warm-up
     double best = 1e300;
